@@ -1,0 +1,240 @@
+/*
+ * gcm.h - C ABI of the GB300-native implicit-geometry meshing engine.
+ *
+ * Drop-in boundary for the field -> mesh path of DESIGN4ADDITIVE/GPUCADforAM.
+ * The reference exposes that path as C++ classes (MarchingCubeCuda,
+ * Isosurface, Modelling, Fft_lattice, Gratings, File_output); every entry
+ * point below names the reference member it replaces (path:line inside the
+ * reference project).
+ *
+ * Conventions shared by every call:
+ *  - Grids hold nx*ny*nz FP32 samples, x fastest (index x + nx*(y + ny*z)).
+ *    Voxel (x,y,z) spans samples x..x+1, y..y+1, z..z+1; voxels are numbered
+ *    x fastest over (nx-1)*(ny-1)*(nz-1)  (calcGridPos,
+ *    src/MarchingCubes_kernel.cu:121-136).
+ *  - Meshes are unshared triangles: vertex i has position pos[4i..4i+3] =
+ *    (x, y, z, 1) and normal norm[4i..4i+3] = (n, 0), triangle t = vertices
+ *    3t..3t+2, in the reference's order (vertex index = exclusive scan of the
+ *    per-voxel vertex counts in voxel order, then the triangle-table order).
+ *  - Pointers named d_* are device pointers; h_* are host pointers.  The
+ *    caller owns inputs and outputs.  Scratch is owned by the context.
+ *  - `stream` is a cudaStream_t (NULL = the legacy default stream).  Calls
+ *    that return host-side counts synchronise that stream; *_async calls do
+ *    not and write their counts to device memory.
+ *  - Every call returns a gcm_status; nothing exits or aborts.  On
+ *    GCM_ERR_OUTPUT_OVERFLOW the true counts are still reported and only the
+ *    triangles that fit were written.
+ *  - A context is not thread-safe; use one context per host thread.
+ */
+#ifndef GCM_H_
+#define GCM_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GCM_ABI_VERSION 1
+
+typedef enum gcm_status {
+  GCM_OK = 0,
+  GCM_ERR_INVALID_ARGUMENT = 1,
+  GCM_ERR_OUTPUT_OVERFLOW = 2, /* capacity too small; counts are the true ones */
+  GCM_ERR_DEVICE_TIMEOUT = 3,  /* a bounded device-side wait gave up */
+  GCM_ERR_CUDA = 4,            /* a CUDA runtime call failed; see gcm_ctx_last_error */
+  GCM_ERR_OUT_OF_MEMORY = 5,
+  GCM_ERR_NOT_SUPPORTED = 6,
+  GCM_ERR_IO = 7,
+  GCM_ERR_REJECTED = 8,  /* server admission refused the request */
+  GCM_ERR_CANCELLED = 9, /* server request cancelled before completion */
+  GCM_ERR_BUSY = 10      /* server queue full */
+} gcm_status;
+
+typedef struct gcm_ctx gcm_ctx;
+typedef void* gcm_stream; /* cudaStream_t */
+
+/* Grid geometry.  Vertex positions are (gridPos - grid_center) * voxel_size,
+ * as in generateTriangles_* (src/MarchingCubes_kernel.cu:3061-3064). */
+typedef struct gcm_grid {
+  uint32_t nx, ny, nz;
+  float voxel_size[3];  /* reference: voxelSize  */
+  float grid_center[3]; /* reference: gridcenter, in voxel units */
+} gcm_grid;
+
+/* Counts of one extraction (reference: *activeVoxels, *totalVerts,
+ * src/Isosurface.cu:80,114). */
+typedef struct gcm_counts {
+  uint64_t active_voxels;
+  uint64_t total_verts;
+  uint32_t status; /* gcm_status of the device work (0 = ok) */
+  uint32_t reserved;
+} gcm_counts;
+
+/* ---------------------------------------------------------------- context */
+
+/* Creates a context on `device` (replaces the reference's global state:
+ * texture objects src/MarchingCubes_kernel.cu:20-21 and the caller-side
+ * scratch of src/main.cu:2141-2151). */
+gcm_status gcm_ctx_create(int device, gcm_ctx** out);
+gcm_status gcm_ctx_destroy(gcm_ctx* ctx);
+const char* gcm_status_string(gcm_status s);
+/* Text of the last error raised on this context ("" if none). */
+const char* gcm_ctx_last_error(const gcm_ctx* ctx);
+/* Grows the context's scratch so that meshing grids of up to max_points
+ * samples allocates nothing afterwards (needed before stream capture). */
+gcm_status gcm_ctx_reserve(gcm_ctx* ctx, uint64_t max_points);
+/* Upper bound, in nanoseconds, on every device-side wait (decoupled
+ * look-back).  Default 2e9.  A wait that runs out sets
+ * GCM_ERR_DEVICE_TIMEOUT and the kernel returns. */
+gcm_status gcm_ctx_set_wait_limit(gcm_ctx* ctx, uint64_t ns);
+/* Number of kernel launches this context has issued (for accounting). */
+uint64_t gcm_ctx_launch_count(const gcm_ctx* ctx);
+int gcm_abi_version(void);
+
+/* ------------------------------------------------- marching cubes, fed field */
+
+/* One fused pass over a caller-supplied FP32 field: classify, decoupled
+ * look-back scan, and triangle emission.  Replaces
+ * Isosurface::computeIsosurface_lattice / computeIsosurface_latticeone
+ * (src/Isosurface.cu:401-572) in their plain form (cube index
+ * classifyVoxel_new :3207-3249, interpolation vertexInterp4 :1619-1629,
+ * normal calcNormal(v0,v1,v2) :1631-1637).  Host counts; syncs `stream`. */
+gcm_status gcm_mesh_field(gcm_ctx* ctx, const float* d_field, const gcm_grid* grid, float iso, float* d_pos,
+                          float* d_norm, uint64_t capacity_verts, gcm_counts* h_counts, gcm_stream stream);
+/* Same, stream-ordered: counts land in d_counts (device), nothing syncs. */
+gcm_status gcm_mesh_field_async(gcm_ctx* ctx, const float* d_field, const gcm_grid* grid, float iso, float* d_pos,
+                                float* d_norm, uint64_t capacity_verts, gcm_counts* d_counts, gcm_stream stream);
+/* Counting pass only (exact vertex total for admission / sizing). */
+gcm_status gcm_count_field(gcm_ctx* ctx, const float* d_field, const gcm_grid* grid, float iso,
+                           gcm_counts* h_counts, gcm_stream stream);
+
+/* ---------------------------------- staged form (the reference's own steps) */
+
+/* classifyVoxel_new (src/MarchingCubes_kernel.cu:3207-3249): per voxel vertex
+ * count and occupancy flag; d_cube_index (optional) gets the 8-bit case. */
+gcm_status gcm_mc_classify(gcm_ctx* ctx, const float* d_field, const gcm_grid* grid, float iso,
+                           uint32_t* d_voxel_verts, uint32_t* d_voxel_occupied, uint8_t* d_cube_index,
+                           gcm_stream stream);
+/* ThrustScanWrapper_lattice (src/MarchingCubes_kernel.cu:3198-3203): exclusive
+ * scan of n uint32 values (32-bit wrap-around, like thrust on uint), single
+ * pass with decoupled look-back.  h_total (optional, syncs) gets the 64-bit sum. */
+gcm_status gcm_scan_exclusive_u32(gcm_ctx* ctx, const uint32_t* d_in, uint32_t* d_out, uint64_t n,
+                                  uint64_t* h_total, gcm_stream stream);
+/* compactVoxels (src/MarchingCubes_kernel.cu:1594-1608). */
+gcm_status gcm_mc_compact(gcm_ctx* ctx, const uint32_t* d_voxel_occupied, const uint32_t* d_occupied_scan, uint64_t n,
+                          uint32_t* d_compacted, gcm_stream stream);
+/* generateTriangles_lattice_kernel_3 (src/MarchingCubes_kernel.cu:3041-3170)
+ * with the classify cube index. */
+gcm_status gcm_mc_generate(gcm_ctx* ctx, const float* d_field, const gcm_grid* grid, float iso,
+                           const uint32_t* d_compacted, uint64_t active_voxels, const uint32_t* d_verts_scan,
+                           float* d_pos, float* d_norm, uint64_t capacity_verts, gcm_stream stream);
+
+/* --------------------------------------------------------------- band mode */
+
+/* GPU_buffer_normalise_four (src/lattice_files/Gratings.cu:1579-1617):
+ * min/max (the range always includes 0, as the reference's reduction starts
+ * from {0,0}), k = (v-min)/(max-min), label 1 where lo <= k <= hi, boundary
+ * samples forced to k = 0, label 0.  h_minmax (optional, syncs) gets min,max. */
+gcm_status gcm_normalise_band(gcm_ctx* ctx, const float* d_field, uint32_t nx, uint32_t ny, uint32_t nz, float band_lo,
+                              float band_hi, float* d_label, float* d_norm_field, float* h_minmax, gcm_stream stream);
+/* Band extraction: cube index from the label field (< iso), vertices from the
+ * normalised field at the band edges with the reference's 0.0005 endpoint
+ * snapping.  Replaces computeIsosurface_lattice / _latticeone with
+ * generateTriangles_lattice_kernel_new / _newone
+ * (src/MarchingCubes_kernel.cu:3424-3817). */
+gcm_status gcm_mesh_band(gcm_ctx* ctx, const float* d_label, const float* d_norm_field, const gcm_grid* grid, float iso,
+                         float band_lo, float band_hi, float* d_pos, float* d_norm, uint64_t capacity_verts,
+                         gcm_counts* h_counts, gcm_stream stream);
+
+/* ------------------------------------------------------------------ fields */
+
+/* TPMS types: the reference's lattice_index_type values
+ * (src/lattice_files/Fft_lattice.cu:59-85; names src/ImguiApp.cpp:2571). */
+typedef enum gcm_tpms {
+  GCM_TPMS_GYROID = 0,
+  GCM_TPMS_SCHWARZ_P = 1,
+  GCM_TPMS_FRD = 2,
+  GCM_TPMS_IWP = 3,
+  GCM_TPMS_CROSS_CUBE = 4, /* unit cell only */
+  GCM_TPMS_SCHWARZ_D = 5   /* "diamond" */
+} gcm_tpms;
+
+/* create_lattice_kernel (src/lattice_files/Fft_lattice.cu:11-93): unit cell on
+ * [-1,1]^3 (literal 3.14 as in the reference). */
+gcm_status gcm_field_unit_cell(gcm_ctx* ctx, uint32_t type, uint32_t nx, uint32_t ny, uint32_t nz, float* d_out,
+                               gcm_stream stream);
+
+typedef enum gcm_grade_mode {
+  /* period, Euler angles and thickness trilinear from the control grid, type
+   * of the nearest control point, phase about `origin` */
+  GCM_GRADE_PARAMS = 0,
+  /* each control point anchors its own uniform lattice at its position; the
+   * field is the trilinear blend of the 8 surrounding lattices */
+  GCM_GRADE_BLEND = 1
+} gcm_grade_mode;
+
+/* Spatially graded TPMS lattice (the reference grades period, rotation and
+ * thickness through Interpolations / Gratings: src/lattice_files/Gratings.cu:
+ * 345-379 period, :260-341 rotation, :1089-1134 thickness band, trilinear
+ * lookup src/Interpolations.cu:79-107).  Control arrays are device arrays of
+ * cx*cy*cz values, x fastest; control point (i,j,k) sits at voxel position
+ * (i*(nx-1)/(cx-1), ...).  Field = TPMS(R(euler) (p - origin) * 2pi/period)
+ * - thickness, where R uses the Euler basis of src/Modelling.cu:401-407. */
+typedef struct gcm_lattice {
+  uint32_t mode; /* gcm_grade_mode */
+  uint32_t cx, cy, cz;
+  const float* d_period;    /* voxels */
+  const float* d_euler;     /* [3][cx*cy*cz] radians (x, y, z), or NULL */
+  const float* d_thickness; /* or NULL */
+  const uint8_t* d_type;    /* gcm_tpms per control point (not CROSS_CUBE) */
+  float origin[3];          /* GCM_GRADE_PARAMS phase origin (voxel units) */
+} gcm_lattice;
+
+gcm_status gcm_field_lattice(gcm_ctx* ctx, const gcm_lattice* lattice, uint32_t nx, uint32_t ny, uint32_t nz,
+                             float* d_out, gcm_stream stream);
+/* Field evaluation + marching cubes (iso usually 0). */
+gcm_status gcm_mesh_lattice(gcm_ctx* ctx, const gcm_lattice* lattice, const gcm_grid* grid, float iso, float* d_pos,
+                            float* d_norm, uint64_t capacity_verts, gcm_counts* h_counts, gcm_stream stream);
+
+/* Primitive kinds (src/Modelling.cu): 0 sphere / sphere shell (flag) :314-361,
+ * 1 capped cylinder / disc (flag) :244-302, 2 cuboid :375-421, 3 cuboid shell
+ * :435-487, 4 torus :569-616, 5 cone :631-683, 6 cone frustum :698-750,
+ * 7 pyramid frustum :501-557.  Parameters p[] in the reference's order:
+ * sphere (radius, thickness); cylinder (radius, thickness_radial,
+ * thickness_axial) with v3 = axis; cuboid (x_width, y_width, z_width) with
+ * v3 = Euler angles; cuboid shell (+thickness); torus (R, r); cone
+ * (base_radius, height); cone frustum (top_radius, bottom_radius, height);
+ * pyramid frustum (x_base, x_top, y_height, z_base, z_top). */
+typedef enum gcm_csg_op { GCM_CSG_UNION = 0, GCM_CSG_SUBTRACT = 1, GCM_CSG_INTERSECT = 2 } gcm_csg_op;
+typedef struct gcm_primitive {
+  uint32_t kind;
+  uint32_t op;   /* gcm_csg_op applied to the running field */
+  uint32_t flag; /* shell (sphere) / disc (cylinder) selector */
+  uint32_t reserved;
+  float center[3];
+  float v3[3];
+  float p[6];
+} gcm_primitive;
+
+/* Scene frame: sample i sits at (i - origin) * spacing (the reference uses
+ * origin = (N-1)/2, spacing = dx; src/Modelling.cu:259-261). */
+typedef struct gcm_frame {
+  float origin[3];
+  float spacing[3];
+} gcm_frame;
+
+/* CSG field: f = op_n(... op_0(+inf, g_0) ..., g_n) with union = min,
+ * subtract = max(f, -g), intersect = max(f, g).  d_prims is a device array. */
+gcm_status gcm_field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
+                         uint32_t nx, uint32_t ny, uint32_t nz, float* d_out, gcm_stream stream);
+gcm_status gcm_mesh_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
+                        const gcm_grid* grid, float iso, float* d_pos, float* d_norm, uint64_t capacity_verts,
+                        gcm_counts* h_counts, gcm_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GCM_H_ */

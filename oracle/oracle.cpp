@@ -1,0 +1,835 @@
+// CPU oracle for the field -> mesh path.  TEST INFRASTRUCTURE ONLY (see oracle.h).
+//
+// Built with -ffp-contract=off so that every floating-point operation rounds
+// exactly where the code says; the places where the reference's nvcc build fuses
+// a multiply and an add are written as explicit std::fma, selected by the
+// `arith` pattern code (the pattern the reference's compiled kernels follow is
+// pinned by the fixtures in tests/golden/, produced by running those kernels).
+#include "oracle.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <map>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../gpucadforam_gb300/csrc/mc_tables.h"
+
+namespace {
+
+constexpr unsigned kNumVerts(unsigned ci) { return gcm::row_verts(gcm::kTriRows[ci]); }
+
+struct Arith {
+  bool fuse_corner, fuse_delta;
+  int lerp, cross;
+};
+
+Arith decode(uint32_t a) {
+  Arith r;
+  r.fuse_corner = (a & 1u) != 0;
+  r.fuse_delta = (a & 2u) != 0;
+  r.lerp = (int)((a >> 2) & 3u);
+  r.cross = (int)((a >> 4) & 3u);
+  return r;
+}
+
+int set_threads(int threads) {
+#ifdef _OPENMP
+  int t = threads > 0 ? threads : omp_get_max_threads();
+  return t;
+#else
+  (void)threads;
+  return 1;
+#endif
+}
+
+inline uint64_t pidx(uint32_t x, uint32_t y, uint32_t z, uint32_t nx, uint32_t ny) {
+  return (uint64_t)x + (uint64_t)nx * ((uint64_t)y + (uint64_t)ny * z);
+}
+
+// Voxel number -> (x,y,z): calcGridPos, src/MarchingCubes_kernel.cu:121-136.
+inline void voxel_pos(uint64_t v, uint32_t nx, uint32_t ny, uint32_t& x, uint32_t& y, uint32_t& z) {
+  uint64_t mx = nx - 1, my = ny - 1;
+  z = (uint32_t)(v / (mx * my));
+  uint64_t rem = v % (mx * my);
+  y = (uint32_t)(rem / mx);
+  x = (uint32_t)(rem % mx);
+}
+
+inline void corners(const float* f, uint32_t x, uint32_t y, uint32_t z, uint32_t nx, uint32_t ny, float c[8]) {
+  for (int k = 0; k < 8; ++k)
+    c[k] = f[pidx(x + gcm::kCornerX[k], y + gcm::kCornerY[k], z + gcm::kCornerZ[k], nx, ny)];
+}
+
+// Cube index: bit k set when corner k lies below the isovalue
+// (classifyVoxel_new, src/MarchingCubes_kernel.cu:3230-3238).
+inline unsigned cube_index(const float c[8], float iso) {
+  unsigned ci = 0;
+  for (int k = 0; k < 8; ++k) ci |= (unsigned)(c[k] < iso) << k;
+  return ci;
+}
+
+// One coordinate of an edge point.  The reference forms the voxel origin as
+// p = (gridPos - gridcenter) * voxelSize, each corner as p + offset, and the
+// point as lerp(v_a, v_b, t) = v_a + t*(v_b - v_a)
+// (src/MarchingCubes_kernel.cu:3061-3075, :1619-1629; helper_math.h:1145-1148).
+// d = gridPos - gridcenter along this axis; oa/ob = corner offsets (0 or 1).
+inline float corner_coord(float d, float vs, float P, int off, const Arith& A) {
+  if (!off) return P;
+  return A.fuse_corner ? std::fma(d, vs, vs) : P + vs;
+}
+
+inline float lerp_axis(float d, float vs, int oa, int ob, float t, const Arith& A) {
+  const float P = d * vs;
+  const float a = corner_coord(d, vs, P, oa, A);
+  const float b = corner_coord(d, vs, P, ob, A);
+  float B;
+  if (A.fuse_delta && oa == 0) B = std::fma(-d, vs, b);
+  else if (A.fuse_delta && ob == 0) B = std::fma(d, vs, -a);
+  else B = b - a;
+  switch (A.lerp) {
+    case 1: return std::fma(t, B, a);
+    case 2: return oa == 0 ? std::fma(d, vs, t * B) : std::fma(t, B, a);
+    default: return a + t * B;
+  }
+}
+
+// calcNormal(v0, v1, v2) = cross(v1 - v0, v2 - v0)
+// (src/MarchingCubes_kernel.cu:1631-1637, helper_math.h:1427-1430).
+inline float cross_term(float a, float b, float c, float d, int form) {  // a*b - c*d
+  switch (form) {
+    case 1: return std::fma(a, b, -(c * d));
+    case 2: return std::fma(-c, d, a * b);
+    default: return a * b - c * d;
+  }
+}
+
+inline void normal_of(const float* v0, const float* v1, const float* v2, int form, float n[3]) {
+  float e0[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
+  float e1[3] = {v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2]};
+  n[0] = cross_term(e0[1], e1[2], e0[2], e1[1], form);
+  n[1] = cross_term(e0[2], e1[0], e0[0], e1[2], form);
+  n[2] = cross_term(e0[0], e1[1], e0[1], e1[0], form);
+}
+
+// Plain edge point: t = (iso - f_a) / (f_b - f_a) (vertexInterp4, :1619-1629).
+inline void edge_point_plain(const uint32_t g[3], const float* vs, const float* gc, int e, const float c[8], float iso,
+                             const Arith& A, float out[3]) {
+  const int ka = gcm::kEdgeA[e], kb = gcm::kEdgeB[e];
+  const float t = (iso - c[ka]) / (c[kb] - c[ka]);
+  const int oa[3] = {gcm::kCornerX[ka], gcm::kCornerY[ka], gcm::kCornerZ[ka]};
+  const int ob[3] = {gcm::kCornerX[kb], gcm::kCornerY[kb], gcm::kCornerZ[kb]};
+  for (int ax = 0; ax < 3; ++ax) {
+    const float d = (float)g[ax] - gc[ax];
+    out[ax] = lerp_axis(d, vs[ax], oa[ax], ob[ax], t, A);
+  }
+}
+
+// Band edge point (vertexInterp2_new, src/MarchingCubes_kernel.cu:3593-3674): only
+// edges whose endpoint labels are {0,1} are interpolated; the endpoints are ordered
+// so that f0 <= f1; the point snaps to an endpoint when it is within 0.0005 of a
+// band edge, and otherwise lerps at the band edge crossed.  Where the reference
+// leaves t unset (no branch taken) this restatement uses t = 0.
+inline void edge_point_band(const uint32_t g[3], const float* vs, const float* gc, int e, const float lab[8],
+                            const float fv[8], float lo, float hi, const Arith& A, float out[3]) {
+  int ka = gcm::kEdgeA[e], kb = gcm::kEdgeB[e];
+  const float id0 = lab[ka], id1 = lab[kb];
+  float f0 = fv[ka], f1 = fv[kb];
+  const bool crossing = (id0 == 1 && id1 == 0) || (id0 == 0 && id1 == 1);
+  if (crossing && f1 < f0) {
+    std::swap(ka, kb);
+    std::swap(f0, f1);
+  }
+  const int oa[3] = {gcm::kCornerX[ka], gcm::kCornerY[ka], gcm::kCornerZ[ka]};
+  const int ob[3] = {gcm::kCornerX[kb], gcm::kCornerY[kb], gcm::kCornerZ[kb]};
+  float pa[3], pb[3];
+  for (int ax = 0; ax < 3; ++ax) {
+    const float d = (float)g[ax] - gc[ax];
+    const float P = d * vs[ax];
+    pa[ax] = corner_coord(d, vs[ax], P, oa[ax], A);
+    pb[ax] = corner_coord(d, vs[ax], P, ob[ax], A);
+  }
+  float t = 0.0f;  // the reference leaves t unset when no branch applies
+  if (crossing) {
+    for (int side = 0; side < 2; ++side) {
+      const float lev = side ? hi : lo;
+      if ((f1 >= lev) && (f0 <= lev)) {
+        if (std::fabs(lev - f0) < 0.0005) { std::memcpy(out, pa, sizeof(pa)); return; }
+        if (std::fabs(lev - f1) < 0.0005) { std::memcpy(out, pb, sizeof(pb)); return; }
+        if (std::fabs(f1 - f0) < 0.0005) { std::memcpy(out, pa, sizeof(pa)); return; }
+        t = (lev - f0) / (f1 - f0);
+        goto interpolate;
+      }
+    }
+    if ((f1 == f0) && (pa[2] == 0.0)) t = 1.0f;
+    else if (f1 == f0) t = 0.0f;
+  }
+interpolate:
+  for (int ax = 0; ax < 3; ++ax) {
+    const float d = (float)g[ax] - gc[ax];
+    out[ax] = lerp_axis(d, vs[ax], oa[ax], ob[ax], t, A);
+  }
+}
+
+template <class EdgeFn>
+void emit_voxel(uint64_t voxel, unsigned ci, uint64_t base, uint64_t capacity, float* pos, float* norm, int cross_form,
+                EdgeFn&& edge) {
+  const uint64_t row = gcm::kTriRows[ci];
+  const unsigned nv = kNumVerts(ci);
+  (void)voxel;
+  for (unsigned j = 0; j < nv; j += 3) {
+    const uint64_t idx = base + j;
+    float v[3][3];
+    for (int m = 0; m < 3; ++m) edge((int)gcm::tri_edge(row, j + m), v[m]);
+    float n[3];
+    normal_of(v[0], v[1], v[2], cross_form, n);
+    if (idx + 3 > capacity) continue;
+    for (int m = 0; m < 3; ++m) {
+      float* P = pos + 4 * (idx + m);
+      float* N = norm + 4 * (idx + m);
+      P[0] = v[m][0]; P[1] = v[m][1]; P[2] = v[m][2]; P[3] = 1.0f;
+      N[0] = n[0]; N[1] = n[1]; N[2] = n[2]; N[3] = 0.0f;
+    }
+  }
+}
+
+// ---- fields ---------------------------------------------------------------------
+
+// Euler basis rows, ZYX convention of src/Modelling.cu:401-407 (angles.x, .y, .z).
+template <class T>
+void euler_rows(T ax, T ay, T az, T R[9]) {
+  using std::cos;
+  using std::sin;
+  const T sx = sin(ax), cx = cos(ax), sy = sin(ay), cy = cos(ay), sz = sin(az), cz = cos(az);
+  R[0] = cz * cy; R[1] = cz * sy * sx - sz * cx; R[2] = cz * sy * cx + sz * sx;
+  R[3] = sz * cy; R[4] = sz * sy * sx + cz * cx; R[5] = sz * sy * cx - cz * sx;
+  R[6] = -sy;     R[7] = cy * sx;                R[8] = cy * cx;
+}
+
+inline void sincospi32(float x, float& s, float& c) {
+  // Reference sin(pi x) / cos(pi x) of an FP32 argument, rounded from FP64.
+  const double a = M_PI * (double)x;
+  s = (float)std::sin(a);
+  c = (float)std::cos(a);
+}
+inline void sincospi64(double x, double& s, double& c) {
+  // Exact reduction of x to [-1, 1] half-turns before the FP64 trig.
+  double r = x - 2.0 * std::nearbyint(x * 0.5);
+  s = std::sin(M_PI * r);
+  c = std::cos(M_PI * r);
+}
+
+// TPMS of phase (X,Y,Z) given in half-turns.  0 gyroid, 1 Schwarz-P, 2 FRD,
+// 3 IWP, 5 Schwarz-D (diamond); formulas after create_lattice_kernel,
+// src/lattice_files/Fft_lattice.cu:59-85, with the phase supplied by the caller.
+template <class T>
+T tpms_from_sc(unsigned type, T sX, T cX, T sY, T cY, T sZ, T cZ) {
+  switch (type) {
+    case 0: return sX * cY + sY * cZ + sZ * cX;
+    case 1: return cX + cY + cZ;
+    case 2: {
+      const T c2X = 2 * cX * cX - 1, c2Y = 2 * cY * cY - 1, c2Z = 2 * cZ * cZ - 1;
+      return 4 * (cX * cY * cZ) - (c2X * c2Y + c2Y * c2Z + c2Z * c2X);
+    }
+    case 3: {
+      const T c2X = 2 * cX * cX - 1, c2Y = 2 * cY * cY - 1, c2Z = 2 * cZ * cZ - 1;
+      return 2 * (cX * cY + cY * cZ + cZ * cX) - (c2X + c2Y + c2Z);
+    }
+    default: return cX * cY * cZ - sX * sY * sZ;
+  }
+}
+
+struct Cell {
+  int i0[3];
+  float f[3];  // FP32 fractions (the discrete decisions are shared by both precisions)
+  int nearest[3];
+};
+
+inline float ctrl_scale(uint32_t c, uint32_t n) {
+  return (c > 1 && n > 1) ? (float)(c - 1) / (float)(n - 1) : 0.0f;
+}
+
+inline Cell locate(const uint32_t p[3], const uint32_t c[3], const float s[3]) {
+  Cell k;
+  for (int a = 0; a < 3; ++a) {
+    const float cu = (float)p[a] * s[a];
+    int i0 = (int)cu;
+    if (c[a] == 1) i0 = 0;
+    else if (i0 > (int)c[a] - 2) i0 = (int)c[a] - 2;
+    k.i0[a] = i0;
+    k.f[a] = c[a] == 1 ? 0.0f : cu - (float)i0;
+    int nn = (int)(cu + 0.5f);
+    if (nn > (int)c[a] - 1) nn = (int)c[a] - 1;
+    k.nearest[a] = nn;
+  }
+  return k;
+}
+
+inline uint64_t cidx(int x, int y, int z, const uint32_t c[3]) {
+  return (uint64_t)x + (uint64_t)c[0] * ((uint64_t)y + (uint64_t)c[1] * z);
+}
+
+template <class T>
+T ctrl_at(const float* a, int x, int y, int z, const uint32_t c[3]) {
+  return a ? (T)a[cidx(x, y, z, c)] : (T)0;
+}
+
+// Trilinear interpolation of one control array, x then y then z, each step
+// lerp(a, b, t) = a + t*(b - a) (FP32: fma(t, b - a, a)).
+float trilinear32(const float* a, const Cell& k, const uint32_t c[3]) {
+  if (!a) return 0.0f;
+  const int x1 = c[0] > 1 ? k.i0[0] + 1 : 0, y1 = c[1] > 1 ? k.i0[1] + 1 : 0, z1 = c[2] > 1 ? k.i0[2] + 1 : 0;
+  auto L = [](float u, float v, float t) { return std::fma(t, v - u, u); };
+  const int x0 = k.i0[0], y0 = k.i0[1], z0 = k.i0[2];
+  const float c00 = L(a[cidx(x0, y0, z0, c)], a[cidx(x1, y0, z0, c)], k.f[0]);
+  const float c10 = L(a[cidx(x0, y1, z0, c)], a[cidx(x1, y1, z0, c)], k.f[0]);
+  const float c01 = L(a[cidx(x0, y0, z1, c)], a[cidx(x1, y0, z1, c)], k.f[0]);
+  const float c11 = L(a[cidx(x0, y1, z1, c)], a[cidx(x1, y1, z1, c)], k.f[0]);
+  return L(L(c00, c10, k.f[1]), L(c01, c11, k.f[1]), k.f[2]);
+}
+
+double trilinear64(const float* a, const Cell& k, const uint32_t c[3]) {
+  if (!a) return 0.0;
+  const int x1 = c[0] > 1 ? k.i0[0] + 1 : 0, y1 = c[1] > 1 ? k.i0[1] + 1 : 0, z1 = c[2] > 1 ? k.i0[2] + 1 : 0;
+  auto L = [](double u, double v, double t) { return u + t * (v - u); };
+  const int x0 = k.i0[0], y0 = k.i0[1], z0 = k.i0[2];
+  const double f0 = k.f[0], f1 = k.f[1], f2 = k.f[2];
+  const double c00 = L(a[cidx(x0, y0, z0, c)], a[cidx(x1, y0, z0, c)], f0);
+  const double c10 = L(a[cidx(x0, y1, z0, c)], a[cidx(x1, y1, z0, c)], f0);
+  const double c01 = L(a[cidx(x0, y0, z1, c)], a[cidx(x1, y0, z1, c)], f0);
+  const double c11 = L(a[cidx(x0, y1, z1, c)], a[cidx(x1, y1, z1, c)], f0);
+  return L(L(c00, c10, f1), L(c01, c11, f1), f2);
+}
+
+// Phase of one lattice in half-turns: X = R q * (2 / period).
+float lattice_value32(unsigned type, const float R[9], float h, const float q[3], float thick) {
+  float X[3];
+  for (int r = 0; r < 3; ++r) X[r] = std::fma(R[3 * r + 2], q[2], std::fma(R[3 * r + 1], q[1], R[3 * r] * q[0])) * h;
+  float s[3], c[3];
+  for (int r = 0; r < 3; ++r) sincospi32(X[r], s[r], c[r]);
+  return tpms_from_sc<float>(type, s[0], c[0], s[1], c[1], s[2], c[2]) - thick;
+}
+
+double lattice_value64(unsigned type, const double R[9], double h, const double q[3], double thick) {
+  double X[3];
+  for (int r = 0; r < 3; ++r) X[r] = (R[3 * r] * q[0] + R[3 * r + 1] * q[1] + R[3 * r + 2] * q[2]) * h;
+  double s[3], c[3];
+  for (int r = 0; r < 3; ++r) sincospi64(X[r], s[r], c[r]);
+  return tpms_from_sc<double>(type, s[0], c[0], s[1], c[1], s[2], c[2]) - thick;
+}
+
+template <bool F64, class Out>
+void lattice_field_impl(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, Out* out, int threads) {
+  const uint32_t c[3] = {L->cx, L->cy, L->cz};
+  const uint32_t n[3] = {nx, ny, nz};
+  const float s[3] = {ctrl_scale(c[0], nx), ctrl_scale(c[1], ny), ctrl_scale(c[2], nz)};
+  const uint64_t nctrl = (uint64_t)c[0] * c[1] * c[2];
+  // Per-control-point rotation rows (blend mode), from the control Euler angles.
+  std::vector<float> R32(9 * nctrl);
+  std::vector<double> R64(9 * nctrl);
+  for (uint64_t i = 0; i < nctrl; ++i) {
+    const float ax = L->euler ? L->euler[i] : 0.f, ay = L->euler ? L->euler[nctrl + i] : 0.f,
+                az = L->euler ? L->euler[2 * nctrl + i] : 0.f;
+    euler_rows<float>(ax, ay, az, &R32[9 * i]);
+    euler_rows<double>(ax, ay, az, &R64[9 * i]);
+  }
+  const int nt = set_threads(threads);
+  const uint64_t total = (uint64_t)nx * ny * nz;
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (int64_t ii = 0; ii < (int64_t)total; ++ii) {
+    const uint64_t i = (uint64_t)ii;
+    const uint32_t p[3] = {(uint32_t)(i % nx), (uint32_t)((i / nx) % ny), (uint32_t)(i / ((uint64_t)nx * ny))};
+    const Cell k = locate(p, c, s);
+    if (L->mode == 0) {
+      const uint64_t ni = cidx(k.nearest[0], k.nearest[1], k.nearest[2], c);
+      const unsigned type = L->type[ni];
+      if (!F64) {
+        const float P = trilinear32(L->period, k, c);
+        const float ax = trilinear32(L->euler, k, c);
+        const float ay = trilinear32(L->euler ? L->euler + nctrl : nullptr, k, c);
+        const float az = trilinear32(L->euler ? L->euler + 2 * nctrl : nullptr, k, c);
+        const float th = trilinear32(L->thickness, k, c);
+        float R[9];
+        euler_rows<float>(ax, ay, az, R);
+        const float q[3] = {(float)p[0] - L->origin[0], (float)p[1] - L->origin[1], (float)p[2] - L->origin[2]};
+        out[i] = (Out)lattice_value32(type, R, 2.0f / P, q, th);
+      } else {
+        const double P = trilinear64(L->period, k, c);
+        const double ax = trilinear64(L->euler, k, c);
+        const double ay = trilinear64(L->euler ? L->euler + nctrl : nullptr, k, c);
+        const double az = trilinear64(L->euler ? L->euler + 2 * nctrl : nullptr, k, c);
+        const double th = trilinear64(L->thickness, k, c);
+        double R[9];
+        euler_rows<double>(ax, ay, az, R);
+        const double q[3] = {(double)p[0] - (double)L->origin[0], (double)p[1] - (double)L->origin[1],
+                             (double)p[2] - (double)L->origin[2]};
+        out[i] = (Out)lattice_value64(type, R, 2.0 / P, q, th);
+      }
+    } else {
+      // Blend: every control point anchors its own uniform lattice at its position;
+      // the field is the trilinear blend of the 8 surrounding lattices.
+      if (!F64) {
+        float acc = 0.0f;
+        for (int corner = 0; corner < 8; ++corner) {
+          const int d[3] = {corner & 1, (corner >> 1) & 1, (corner >> 2) & 1};
+          int g[3];
+          float w = 1.0f, q[3];
+          for (int a = 0; a < 3; ++a) {
+            g[a] = c[a] > 1 ? k.i0[a] + d[a] : 0;
+            const float wa = d[a] ? k.f[a] : 1.0f - k.f[a];
+            w = (c[a] > 1) ? w * wa : (d[a] ? 0.0f : w);
+            const float anchor = c[a] > 1 ? (float)g[a] * ((float)(n[a] - 1) / (float)(c[a] - 1)) : 0.0f;
+            q[a] = (float)p[a] - anchor;
+          }
+          if (w == 0.0f) continue;
+          const uint64_t ci = cidx(g[0], g[1], g[2], c);
+          const float v = lattice_value32(L->type[ci], &R32[9 * ci], 2.0f / L->period[ci], q,
+                                          L->thickness ? L->thickness[ci] : 0.0f);
+          acc = std::fma(w, v, acc);
+        }
+        out[i] = (Out)acc;
+      } else {
+        double acc = 0.0;
+        for (int corner = 0; corner < 8; ++corner) {
+          const int d[3] = {corner & 1, (corner >> 1) & 1, (corner >> 2) & 1};
+          int g[3];
+          double w = 1.0, q[3];
+          for (int a = 0; a < 3; ++a) {
+            g[a] = c[a] > 1 ? k.i0[a] + d[a] : 0;
+            const double wa = d[a] ? (double)k.f[a] : 1.0 - (double)k.f[a];
+            w = (c[a] > 1) ? w * wa : (d[a] ? 0.0 : w);
+            const double anchor = c[a] > 1 ? (double)g[a] * ((double)(n[a] - 1) / (double)(c[a] - 1)) : 0.0;
+            q[a] = (double)p[a] - anchor;
+          }
+          if (w == 0.0) continue;
+          const uint64_t ci = cidx(g[0], g[1], g[2], c);
+          acc += w * lattice_value64(L->type[ci], &R64[9 * ci], 2.0 / (double)L->period[ci], q,
+                                     L->thickness ? L->thickness[ci] : 0.0);
+        }
+        out[i] = (Out)acc;
+      }
+    }
+  }
+}
+
+// ---- primitives (src/Modelling.cu) -----------------------------------------------------
+
+template <class T>
+T sq(T x) { return x * x; }
+
+// Field of one primitive at a point given in the scene frame.  Float promotions
+// follow the reference kernels (literals such as 2.0 promote to double).
+template <class T>
+T primitive_at(uint32_t kind, uint32_t flag, const float* center, const float* v3, const float* p, T X, T Y, T Z) {
+  using std::fabs;
+  using std::sqrt;
+  const T cxv = center[0], cyv = center[1], czv = center[2];
+  switch (kind) {
+    case 0: {  // implicit_sphere_kernel :314-361
+      const T x = X - cxv, y = Y - cyv, z = Z - czv;
+      const T r = p[0], t = (T)(p[1] / 2.0);
+      const T d2 = sq(x) + sq(y) + sq(z);
+      if (flag) {
+        const T f1 = d2 - sq(r - t), f2 = d2 - sq(r + t);
+        return (T)std::max((double)(f1 * -1.0), (double)f2);
+      }
+      return d2 - sq(r);
+    }
+    case 1: {  // distance_from_line_kernel :244-302 (capped cylinder / disc)
+      const T r = p[0], td = (T)(p[1] / 2.0), tda = (T)(p[2] / 2.0);
+      const T am = sqrt(sq((T)v3[0]) + sq((T)v3[1]) + sq((T)v3[2]));
+      const T ax = v3[0] / am, ay = v3[1] / am, az = v3[2] / am;
+      const T ex = ax + cxv, ey = ay + cyv, ez = az + czv;
+      const T w1x = X - cxv, w1y = Y - cyv, w1z = Z - czv;
+      const T w2x = X - ex, w2y = Y - ey, w2z = Z - ez;
+      const T w3x = ex - cxv, w3y = ey - cyv, w3z = ez - czv;
+      const T dx = w1y * w2z - w1z * w2y, dy = w1z * w2x - w1x * w2z, dz = w1x * w2y - w1y * w2x;
+      const T e = sqrt(sq(dx) + sq(dy) + sq(dz));
+      const T dis = sqrt(sq(w3x) + sq(w3y) + sq(w3z));
+      const T f = e / dis;
+      const T g = (X - cxv) * ax + (Y - cyv) * ay + (Z - czv) * az;
+      const T fld1 = std::max(g - tda, (g + tda) * (T)-1);
+      T fld2;
+      if (flag) fld2 = (T)std::max((double)(f - (r + td)), (double)(f - (r - td)) * -1.0);
+      else fld2 = f - r;
+      return std::max(fld1, fld2);
+    }
+    default: {
+      const T x = X - cxv, y = Y - cyv, z = Z - czv;
+      T R[9];
+      euler_rows<T>((T)v3[0], (T)v3[1], (T)v3[2], R);
+      const T a = x * R[0] + y * R[1] + z * R[2];
+      const T b = x * R[3] + y * R[4] + z * R[5];
+      const T c = x * R[6] + y * R[7] + z * R[8];
+      switch (kind) {
+        case 2: {  // implicit_cuboid_kernel :375-421
+          const T wx = (T)(p[0] / 2.0), wy = (T)(p[1] / 2.0), wz = (T)(p[2] / 2.0);
+          return std::max(std::max(fabs(a) - wx, fabs(b) - wy), fabs(c) - wz);
+        }
+        case 3: {  // implicit_cuboid_shell_kernel :435-487
+          const T wx = (T)(p[0] / 2.0), wy = (T)(p[1] / 2.0), wz = (T)(p[2] / 2.0), th = p[3];
+          const T f11 = fabs(a) - wx, f12 = fabs(a) - (wx - th);
+          const T f21 = fabs(b) - wy, f22 = fabs(b) - (wy - th);
+          const T f3 = fabs(c) - wz;
+          const T inner = (T)((double)std::max(f12, f22) * -1.0);
+          return std::max(std::max(std::max(f11, f21), inner), f3);
+        }
+        case 4: {  // implicit_torus_kernel :569-616
+          const T side = (T)p[0] - sqrt(sq(a) + sq(b));
+          return sq(c) - sq((T)p[1]) + sq(side);
+        }
+        case 5: {  // implicit_cone_kernel :631-683
+          const T br = p[0], hgt = p[1];
+          const T k2 = sq(hgt / br);
+          const T g = (T)(b - hgt / 2.0);
+          const T h = (T)std::max((double)(g - hgt / 2.0) * 100, (double)(g + hgt / 2.0) * 100 * -1.0);
+          const T f1 = ((sq(a) + sq(c)) * k2) - sq(b - hgt);
+          return std::max(f1, h);
+        }
+        case 6: {  // implicit_cone_frustum_kernel :698-750
+          const T tr = p[0], br = p[1], hgt = p[2];
+          const T rd = ((hgt - b) / hgt) * (br - tr);
+          const T g = (T)(b - hgt / 2.0);
+          const T h = (T)std::max((double)(g - hgt / 2.0) * 100, (double)(g + hgt / 2.0) * 100 * -1.0);
+          const T f1 = (T)((double)(sq(a) + sq(c)) - sq((double)(rd + tr)));
+          return std::max(f1, h);
+        }
+        default: {  // 7: implicit_pyramid_frustum_kernel :501-557
+          const T xwb = (T)(p[0] / 2.0), xwt = (T)(p[1] / 2.0), yh = p[2];
+          const T zwb = (T)(p[3] / 2.0), zwt = (T)(p[4] / 2.0);
+          const T ratio = (yh - b) / yh;
+          const T xw = (ratio * (xwb - xwt)) + xwt;
+          const T f1 = fabs(a) - xw;
+          const T f2 = (T)(fabs(b - yh / 2) - yh / 2);
+          const T zw = (ratio * (zwb - zwt)) + zwt;
+          const T f3 = fabs(c) - zw;
+          return std::max(std::max(f1, f2), f3);
+        }
+      }
+    }
+  }
+}
+
+template <class T>
+T csg_apply(T f, T g, uint32_t op) {
+  switch (op) {
+    case 1: return std::max(f, -g);
+    case 2: return std::max(f, g);
+    default: return std::min(f, g);
+  }
+}
+
+// CSG scene: coordinates x = (i - origin) * spacing in the scene frame; the
+// primitive formulas are those of src/Modelling.cu; the combination is a running
+// min / max(f, -g) / max over the list, starting from +inf.
+template <class T, class Out>
+void csg_impl(const orc_prim* prims, uint32_t n, const float* origin, const float* spacing, uint32_t nx,
+                     uint32_t ny, uint32_t nz, Out* out, int threads) {
+  const int nt = set_threads(threads);
+  const uint64_t total = (uint64_t)nx * ny * nz;
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (int64_t ii = 0; ii < (int64_t)total; ++ii) {
+    const uint64_t i = (uint64_t)ii;
+    const uint32_t px = (uint32_t)(i % nx), py = (uint32_t)((i / nx) % ny), pz = (uint32_t)(i / ((uint64_t)nx * ny));
+    const T X = (T)(((float)px - origin[0]) * spacing[0]);
+    const T Y = (T)(((float)py - origin[1]) * spacing[1]);
+    const T Z = (T)(((float)pz - origin[2]) * spacing[2]);
+    T f = std::numeric_limits<T>::infinity();
+    for (uint32_t k = 0; k < n; ++k) {
+      const orc_prim& P = prims[k];
+      f = csg_apply<T>(f, primitive_at<T>(P.kind, P.flag, P.center, P.v3, P.p, X, Y, Z), P.op);
+    }
+    out[i] = (Out)f;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// Pattern of the reference kernels as nvcc builds them (pinned by
+// tests/golden/golden_mc.npz): corners p + vs (no fusion), edge delta b - a,
+// lerp fma(t, b - a, a), cross terms fma(a, b, -(c*d)).
+uint32_t orc_default_arith(void) { return 4u | (1u << 4); }
+
+void orc_mc_classify(const float* field, uint32_t nx, uint32_t ny, uint32_t nz, float iso, uint32_t* voxel_verts,
+                     uint32_t* voxel_occupied, uint8_t* cube) {
+  const uint64_t nv = (uint64_t)(nx - 1) * (ny - 1) * (nz - 1);
+#pragma omp parallel for schedule(static)
+  for (int64_t vv = 0; vv < (int64_t)nv; ++vv) {
+    uint32_t x, y, z;
+    voxel_pos((uint64_t)vv, nx, ny, x, y, z);
+    float c[8];
+    corners(field, x, y, z, nx, ny, c);
+    const unsigned ci = cube_index(c, iso);
+    const unsigned n = kNumVerts(ci);
+    if (voxel_verts) voxel_verts[vv] = n;
+    if (voxel_occupied) voxel_occupied[vv] = n > 0;
+    if (cube) cube[vv] = (uint8_t)ci;
+  }
+}
+
+// thrust::exclusive_scan over uint (src/MarchingCubes_kernel.cu:3198-3203): 32-bit
+// wrap-around sums; the 64-bit total is returned.
+uint64_t orc_scan_exclusive_u32(const uint32_t* in, uint32_t* out, uint64_t n) {
+  uint64_t acc = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    out[i] = (uint32_t)acc;
+    acc += in[i];
+  }
+  return acc;
+}
+
+// compactVoxels (src/MarchingCubes_kernel.cu:1594-1608).
+void orc_mc_compact(const uint32_t* occ, const uint32_t* occ_scan, uint64_t n, uint32_t* out) {
+  for (uint64_t i = 0; i < n; ++i)
+    if (occ[i]) out[occ_scan[i]] = (uint32_t)i;
+}
+
+// generateTriangles_lattice_kernel_3 (src/MarchingCubes_kernel.cu:3041-3170) with
+// the classify cube index; a triangle is written only when all three of its
+// vertices fit below capacity_verts.
+void orc_mc_generate(const float* field, uint32_t nx, uint32_t ny, uint32_t nz, const float* vs, const float* gc,
+                     float iso, const uint32_t* compacted, uint64_t active, const uint32_t* verts_scan,
+                     uint64_t capacity, float* pos, float* norm, uint32_t arith) {
+  (void)nz;
+  const Arith A = decode(arith);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t a = 0; a < (int64_t)active; ++a) {
+    const uint64_t voxel = compacted[a];
+    uint32_t g[3];
+    voxel_pos(voxel, nx, ny, g[0], g[1], g[2]);
+    float c[8];
+    corners(field, g[0], g[1], g[2], nx, ny, c);
+    const unsigned ci = cube_index(c, iso);
+    emit_voxel(voxel, ci, verts_scan[voxel], capacity, pos, norm, A.cross,
+               [&](int e, float* out) { edge_point_plain(g, vs, gc, e, c, iso, A, out); });
+  }
+}
+
+// generateTriangles_lattice_kernel_newone (src/MarchingCubes_kernel.cu:3678-3817):
+// cube index from the label field, vertices from the normalised field.
+void orc_mc_generate_band(const float* label, const float* nf, uint32_t nx, uint32_t ny, uint32_t nz, const float* vs,
+                          const float* gc, float iso, float lo, float hi, const uint32_t* compacted, uint64_t active,
+                          const uint32_t* verts_scan, uint64_t capacity, float* pos, float* norm, uint32_t arith) {
+  (void)nz;
+  const Arith A = decode(arith);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t a = 0; a < (int64_t)active; ++a) {
+    const uint64_t voxel = compacted[a];
+    uint32_t g[3];
+    voxel_pos(voxel, nx, ny, g[0], g[1], g[2]);
+    float lab[8], fv[8];
+    corners(label, g[0], g[1], g[2], nx, ny, lab);
+    corners(nf, g[0], g[1], g[2], nx, ny, fv);
+    const unsigned ci = cube_index(lab, iso);
+    emit_voxel(voxel, ci, verts_scan[voxel], capacity, pos, norm, A.cross,
+               [&](int e, float* out) { edge_point_band(g, vs, gc, e, lab, fv, lo, hi, A, out); });
+  }
+}
+
+uint64_t orc_mesh_field(const float* field, uint32_t nx, uint32_t ny, uint32_t nz, const float* vs, const float* gc,
+                        float iso, float* pos, float* norm, uint64_t capacity, uint64_t* active_out, int threads) {
+  const uint64_t nv = (uint64_t)(nx - 1) * (ny - 1) * (nz - 1);
+  const int nt = set_threads(threads);
+  std::vector<uint32_t> verts(nv);
+#pragma omp parallel for schedule(static) num_threads(nt)
+  for (int64_t vv = 0; vv < (int64_t)nv; ++vv) {
+    uint32_t x, y, z;
+    voxel_pos((uint64_t)vv, nx, ny, x, y, z);
+    float c[8];
+    corners(field, x, y, z, nx, ny, c);
+    verts[vv] = kNumVerts(cube_index(c, iso));
+  }
+  // Two-level exclusive scan over the per-voxel counts.
+  std::vector<uint64_t> chunk_sum(nt + 1, 0), chunk_act(nt + 1, 0);
+  std::vector<uint64_t> scan(nv);
+#pragma omp parallel num_threads(nt)
+  {
+#ifdef _OPENMP
+    const int t = omp_get_thread_num(), T = omp_get_num_threads();
+#else
+    const int t = 0, T = 1;
+#endif
+    const uint64_t b = nv * t / T, e = nv * (t + 1) / T;
+    uint64_t s = 0, a = 0;
+    for (uint64_t i = b; i < e; ++i) { s += verts[i]; a += verts[i] > 0; }
+    chunk_sum[t + 1] = s;
+    chunk_act[t + 1] = a;
+#pragma omp barrier
+#pragma omp single
+    for (int i = 1; i <= T; ++i) { chunk_sum[i] += chunk_sum[i - 1]; chunk_act[i] += chunk_act[i - 1]; }
+    uint64_t acc = chunk_sum[t];
+    for (uint64_t i = b; i < e; ++i) { scan[i] = acc; acc += verts[i]; }
+  }
+  const uint64_t total = chunk_sum[nt];
+  if (active_out) *active_out = chunk_act[nt];
+  const Arith A = decode(orc_default_arith());
+#pragma omp parallel for schedule(dynamic, 4096) num_threads(nt)
+  for (int64_t vv = 0; vv < (int64_t)nv; ++vv) {
+    if (!verts[vv]) continue;
+    uint32_t g[3];
+    voxel_pos((uint64_t)vv, nx, ny, g[0], g[1], g[2]);
+    float c[8];
+    corners(field, g[0], g[1], g[2], nx, ny, c);
+    const unsigned ci = cube_index(c, iso);
+    emit_voxel((uint64_t)vv, ci, scan[vv], capacity, pos, norm, A.cross,
+               [&](int e, float* out) { edge_point_plain(g, vs, gc, e, c, iso, A, out); });
+  }
+  return total;
+}
+
+// create_lattice_kernel (src/lattice_files/Fft_lattice.cu:11-93): unit cell on
+// [-1, 1]^3 with the literal 3.14; the coordinate is formed in double and
+// rounded to float, and the products with 3.14 are double, rounded to float at
+// the call of cosf/sinf.
+void orc_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t nz, float* out) {
+  for (uint32_t z = 0; z < nz; ++z)
+    for (uint32_t y = 0; y < ny; ++y)
+      for (uint32_t x = 0; x < nx; ++x) {
+        const float xx = (float)((((x * 1.0) / (nx - 1)) - 0.5) / 0.5);
+        const float yy = (float)((((y * 1.0) / (ny - 1)) - 0.5) / 0.5);
+        const float zz = (float)((((z * 1.0) / (nz - 1)) - 0.5) / 0.5);
+        float aa = 0.0f;
+        auto C = [](double v) { return cosf((float)v); };
+        auto S = [](double v) { return sinf((float)v); };
+        switch (type) {
+          case 0: aa = C(3.14 * xx) * S(3.14 * yy) + C(3.14 * yy) * S(3.14 * zz) + C(3.14 * zz) * S(3.14 * xx); break;
+          case 1: aa = C(3.14 * xx) + C(3.14 * yy) + C(3.14 * zz); break;
+          case 2:
+            aa = 4 * (cosf(xx) * cosf(yy) * cosf(zz)) -
+                 (cosf(2 * xx) * cosf(2 * yy) + cosf(2 * yy) * cosf(2 * zz) + cosf(2 * zz) * cosf(2 * xx));
+            break;
+          case 3:
+            aa = 2 * (C(3.14 * xx) * C(3.14 * yy) + C(3.14 * yy) * C(3.14 * zz) + C(3.14 * zz) * C(3.14 * xx)) -
+                 (C(2 * 3.14 * xx) + C(2 * 3.14 * yy) + C(2 * 3.14 * zz));
+            break;
+          case 4:
+            aa = (float)std::min(std::min((double)(powf(xx, 2)) + std::pow((double)yy, 2),
+                                          std::pow((double)yy, 2) + std::pow((double)zz, 2)),
+                                 std::pow((double)zz, 2) + std::pow((double)xx, 2));
+            break;
+          case 5:
+            aa = (float)(std::cos(3.14 * xx) * C(3.14 * yy) * C(3.14 * zz) -
+                         (double)(S(3.14 * xx) * S(3.14 * yy) * S(3.14 * zz)));
+            break;
+          default: aa = 0.0f;
+        }
+        out[pidx(x, y, z, nx, ny)] = aa;
+      }
+}
+
+// One primitive on an Nx*Ny*Nz grid with the reference's centred coordinates
+// x = (i - (N-1)/2) * dx (src/Modelling.cu:259-261 and the other kernels).
+void orc_primitive(uint32_t kind, int nx, int ny, int nz, float dx, float dy, float dz, const float* center,
+                   const float* v3, const float* p, uint32_t flag, float* out) {
+  const float mx = (float)((nx - 1) / 2.0), my = (float)((ny - 1) / 2.0), mz = (float)((nz - 1) / 2.0);
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        const float X = (x - mx) * dx, Y = (y - my) * dy, Z = (z - mz) * dz;
+        out[pidx(x, y, z, nx, ny)] = primitive_at<float>(kind, flag, center, v3, p, X, Y, Z);
+      }
+}
+
+void orc_lattice_field(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, float* out, int threads) {
+  lattice_field_impl<false>(L, nx, ny, nz, out, threads);
+}
+void orc_lattice_field64(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, double* out, int threads) {
+  lattice_field_impl<true>(L, nx, ny, nz, out, threads);
+}
+
+void orc_csg_field(const orc_prim* prims, uint32_t n, const float* origin, const float* spacing, uint32_t nx,
+                   uint32_t ny, uint32_t nz, float* out, int threads) {
+  csg_impl<float>(prims, n, origin, spacing, nx, ny, nz, out, threads);
+}
+void orc_csg_field64(const orc_prim* prims, uint32_t n, const float* origin, const float* spacing, uint32_t nx,
+                     uint32_t ny, uint32_t nz, double* out, int threads) {
+  csg_impl<double>(prims, n, origin, spacing, nx, ny, nz, out, threads);
+}
+
+// GPU_buffer_normalise_four (src/lattice_files/Gratings.cu:1579-1617): the
+// reference's final min/max reduction starts from {0, 0}
+// (Min_reduction_lattice, :1439-1495), so the range always includes 0; then
+// device_bufferfour (:1089-1134) maps k = (v - min) / (max - min), labels the
+// band lo <= k <= hi with 1, and forces boundary samples to k = 0, label 0.
+void orc_normalise_band(const float* field, int nx, int ny, int nz, float lo, float hi, float* label, float* nf,
+                        float* minmax) {
+  const uint64_t total = (uint64_t)nx * ny * nz;
+  float a = 0.0f, b = 0.0f;
+  for (uint64_t i = 0; i < total; ++i) {
+    a = std::min(a, field[i]);
+    b = std::max(b, field[i]);
+  }
+  if (minmax) { minmax[0] = a; minmax[1] = b; }
+  for (uint64_t i = 0; i < total; ++i) {
+    const int xx = (int)(i % nx), yy = (int)((i / nx) % ny), zz = (int)(i / ((uint64_t)nx * ny));
+    float k = (field[i] - a) / (b - a), m;
+    if (xx == 0 || xx == nx - 1 || yy == 0 || yy == ny - 1 || zz == 0 || zz == nz - 1) {
+      m = 0.0f;
+      k = 0.0f;
+    } else {
+      m = (k >= lo && k <= hi) ? 1.0f : 0.0f;
+    }
+    label[i] = m;
+    nf[i] = k;
+  }
+}
+
+// File_output::file_write_obj (src/File_output.cu:5-81): positions truncated to a
+// 0.001 grid (int(x*1000)*0.001, rounded back to float), welded on first
+// occurrence with 1-based indices, faces with a repeated index dropped,
+// identical ordered faces written once, winding written as (a, c, b).
+int orc_write_obj(const float* pos, uint64_t nverts, const char* path, uint64_t* nv_out, uint64_t* nf_out) {
+  std::ofstream f(path, std::ios::out);
+  if (!f) return 1;
+  f << "##Sample latttice new Obj \n";
+  f << "o Solid \n";
+  std::map<std::vector<float>, int> vmap;
+  std::vector<uint32_t> faces;
+  faces.reserve(nverts);
+  int index = 0;
+  for (uint64_t i = 0; i < nverts; ++i) {
+    const float vx = (float)(int(pos[4 * i + 0] * 1000) * 0.001);
+    const float vy = (float)(int(pos[4 * i + 1] * 1000) * 0.001);
+    const float vz = (float)(int(pos[4 * i + 2] * 1000) * 0.001);
+    std::vector<float> key = {vx, vy, vz};
+    auto it = vmap.find(key);
+    if (it == vmap.end()) {
+      ++index;
+      vmap.emplace(key, index);
+      faces.push_back((uint32_t)index);
+      f << "v " << vx << " " << vy << " " << vz << "\n";
+    } else {
+      faces.push_back((uint32_t)it->second);
+    }
+  }
+  f << "\n";
+  f << "\n";
+  std::map<std::vector<uint32_t>, int> fmap;
+  uint64_t nfaces = 0;
+  for (uint64_t i = 0; i + 2 < faces.size(); i += 3) {
+    const uint32_t a = faces[i], b = faces[i + 1], c = faces[i + 2];
+    if (a != b && a != c && b != c) {
+      std::vector<uint32_t> key = {a, b, c};
+      if (fmap.count(key) == 0) {
+        fmap[key] = 1;
+        f << " f  " << a << " " << c << " " << b << "\n";
+        ++nfaces;
+      }
+    }
+  }
+  if (nv_out) *nv_out = (uint64_t)index;
+  if (nf_out) *nf_out = nfaces;
+  return f.good() ? 0 : 2;
+}
+
+}  // extern "C"

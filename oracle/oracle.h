@@ -1,0 +1,87 @@
+// CPU oracle for the field -> mesh path.  TEST INFRASTRUCTURE ONLY: the tests,
+// the smoke check and bench.py's CPU-baseline leg call it as the checker; the
+// product never links, loads or falls back to it.
+//
+// Each function restates one piece of the reference (DESIGN4ADDITIVE/GPUCADforAM)
+// and cites the file:line it follows.  Grid conventions are the reference's:
+// nx*ny*nz FP32 samples with x fastest; voxel (x,y,z) spans samples x..x+1,
+// y..y+1, z..z+1; voxels are numbered x fastest over (nx-1)(ny-1)(nz-1)
+// (calcGridPos, src/MarchingCubes_kernel.cu:121-136).
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+// Floating-point contraction pattern of the vertex arithmetic (see oracle.cpp).
+// bit 0     : corner at offset 1 computed as fma(d, vs, vs) instead of d*vs + vs
+// bit 1     : edge delta fused with the corner product
+// bits 2..3 : lerp form (0 unfused, 1 fma(t, B, a), 2 fma(d, vs, t*B))
+// bits 4..5 : cross-product form (0 unfused, 1 fma(a, b, -(c*d)), 2 fma(-c, d, a*b))
+uint32_t orc_default_arith(void);
+
+// ---- marching cubes on a fed field -------------------------------------------------
+void orc_mc_classify(const float* field, uint32_t nx, uint32_t ny, uint32_t nz, float iso,
+                     uint32_t* voxel_verts, uint32_t* voxel_occupied, uint8_t* cube_index);
+uint64_t orc_scan_exclusive_u32(const uint32_t* in, uint32_t* out, uint64_t n);
+void orc_mc_compact(const uint32_t* occupied, const uint32_t* occupied_scan, uint64_t n,
+                    uint32_t* compacted);
+void orc_mc_generate(const float* field, uint32_t nx, uint32_t ny, uint32_t nz, const float* voxel_size,
+                     const float* grid_center, float iso, const uint32_t* compacted, uint64_t active,
+                     const uint32_t* verts_scan, uint64_t capacity_verts, float* pos, float* norm,
+                     uint32_t arith);
+void orc_mc_generate_band(const float* label, const float* norm_field, uint32_t nx, uint32_t ny, uint32_t nz,
+                          const float* voxel_size, const float* grid_center, float iso, float band_lo,
+                          float band_hi, const uint32_t* compacted, uint64_t active,
+                          const uint32_t* verts_scan, uint64_t capacity_verts, float* pos, float* norm,
+                          uint32_t arith);
+// Whole pipeline (classify, scans, compact, generate), OpenMP-parallel.  Returns the
+// vertex total; writes at most capacity_verts vertices.  band: label/norm_field mode.
+uint64_t orc_mesh_field(const float* field, uint32_t nx, uint32_t ny, uint32_t nz, const float* voxel_size,
+                        const float* grid_center, float iso, float* pos, float* norm, uint64_t capacity_verts,
+                        uint64_t* active_out, int threads);
+
+// ---- fields -----------------------------------------------------------------------
+void orc_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t nz, float* out);
+void orc_primitive(uint32_t kind, int nx, int ny, int nz, float dx, float dy, float dz, const float* center,
+                   const float* v3, const float* p, uint32_t flag, float* out);
+
+// Graded lattice, see oracle.cpp for the exact formulation.
+typedef struct orc_lattice {
+  uint32_t mode;  // 0 = trilinear parameters, 1 = trilinear blend of per-control-point fields
+  uint32_t cx, cy, cz;
+  const float* period;     // [cz*cy*cx], voxels
+  const float* euler;      // [3][cz*cy*cx] radians, or NULL
+  const float* thickness;  // [cz*cy*cx] or NULL
+  const uint8_t* type;     // [cz*cy*cx]
+  float origin[3];         // phase origin (voxel units), mode 0 only
+} orc_lattice;
+void orc_lattice_field(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, float* out, int threads);
+void orc_lattice_field64(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, double* out, int threads);
+
+// CSG scene of primitives: f = op_n(...op_1(op_0(+inf, g_0), g_1)..., g_n).
+typedef struct orc_prim {
+  uint32_t kind;  // see orc_primitive
+  uint32_t op;    // 0 union (min), 1 subtract (max(f,-g)), 2 intersect (max)
+  uint32_t flag;  // shell / disc selector
+  uint32_t pad;
+  float center[3];
+  float v3[3];
+  float p[6];
+} orc_prim;
+void orc_csg_field(const orc_prim* prims, uint32_t n, const float* origin, const float* spacing, uint32_t nx,
+                   uint32_t ny, uint32_t nz, float* out, int threads);
+void orc_csg_field64(const orc_prim* prims, uint32_t n, const float* origin, const float* spacing, uint32_t nx,
+                     uint32_t ny, uint32_t nz, double* out, int threads);
+
+// ---- band normalisation -------------------------------------------------------------
+void orc_normalise_band(const float* field, int nx, int ny, int nz, float band_lo, float band_hi, float* label,
+                        float* norm_field, float* minmax);
+
+// ---- .obj -----------------------------------------------------------------------------
+int orc_write_obj(const float* pos, uint64_t nverts, const char* path, uint64_t* nv_out, uint64_t* nf_out);
+
+#ifdef __cplusplus
+}
+#endif

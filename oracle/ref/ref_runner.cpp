@@ -1,0 +1,480 @@
+// Parity harness: runs the reference's own CUDA kernels (device code compiled by
+// oracle/ref/build_ref.py into oracle/_ref/*.fatbin) on inputs fed from a job
+// file and writes their raw outputs, so fixtures can pin the oracle and this
+// project's kernels to what the reference computes on a GB300.
+//
+// Test infrastructure only.  Host orchestration follows the reference's
+// Isosurface::computeIsosurface_lattice (src/Isosurface.cu:401-486): classify,
+// exclusive scan of the occupancy flags, compaction, exclusive scan of the vertex
+// counts, generate.  Two differences, both deliberate:
+//   * the scans are done on the host (plain integer prefix sums, exact); the
+//     reference calls thrust::exclusive_scan (src/MarchingCubes_kernel.cu:3198-3203),
+//     whose kernels cannot be launched by name;
+//   * classify is launched as a plain 1-D grid; the reference's 2-D split
+//     (src/Isosurface.cu:53-60) drops voxels above 65535 blocks.
+// Texture objects for the tables are built from the reference's own tables.h
+// data (tests/golden/ref_tables.bin), as allocateTextures_s does
+// (src/MarchingCubes_kernel.cu:24-68).
+//
+// Build (on the GPU machine):
+//   g++ -O2 -std=c++17 oracle/ref/ref_runner.cpp -I/usr/local/cuda/include -lcuda
+//       -o oracle/_ref/ref_runner
+// Use:  ref_runner <fatbin-dir> <variant sm103a|ptx89> <tables.bin> <job.bin> <out.bin>
+#include <cuda.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+struct U3 { uint32_t x, y, z; };
+struct F3 { float x, y, z; };
+
+[[noreturn]] void die(const char* what) {
+  std::fprintf(stderr, "ref_runner: %s\n", what);
+  std::exit(3);
+}
+
+void ck(CUresult r, const char* what) {
+  if (r != CUDA_SUCCESS) {
+    const char* s = nullptr;
+    cuGetErrorString(r, &s);
+    std::fprintf(stderr, "ref_runner: %s failed: %s\n", what, s ? s : "?");
+    std::exit(4);
+  }
+}
+
+std::vector<uint8_t> slurp(const std::string& path) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) die(("cannot open " + path).c_str());
+  std::fseek(f, 0, SEEK_END);
+  long n = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  std::vector<uint8_t> b((size_t)n);
+  if (n > 0 && std::fread(b.data(), 1, (size_t)n, f) != (size_t)n) die("short read");
+  std::fclose(f);
+  return b;
+}
+
+struct Reader {
+  const std::vector<uint8_t>& b;
+  size_t off = 0;
+  template <class T> T get() {
+    if (off + sizeof(T) > b.size()) die("job file truncated");
+    T v;
+    std::memcpy(&v, b.data() + off, sizeof(T));
+    off += sizeof(T);
+    return v;
+  }
+  template <class T> std::vector<T> arr(size_t n) {
+    if (off + n * sizeof(T) > b.size()) die("job file truncated (array)");
+    std::vector<T> v(n);
+    if (n) std::memcpy(v.data(), b.data() + off, n * sizeof(T));
+    off += n * sizeof(T);
+    return v;
+  }
+};
+
+struct Writer {
+  FILE* f;
+  template <class T> void put(T v) { std::fwrite(&v, sizeof(T), 1, f); }
+  template <class T> void arr(const std::vector<T>& v) {
+    if (!v.empty()) std::fwrite(v.data(), sizeof(T), v.size(), f);
+  }
+};
+
+// Finds a kernel by its unmangled name inside a loaded module: the Itanium
+// mangling of a free function starts with _Z<len><name>.
+CUfunction find_kernel(CUmodule mod, const char* name) {
+  unsigned n = 0;
+  ck(cuModuleGetFunctionCount(&n, mod), "cuModuleGetFunctionCount");
+  std::vector<CUfunction> fs(n);
+  ck(cuModuleEnumerateFunctions(fs.data(), n, mod), "cuModuleEnumerateFunctions");
+  std::string key = "_Z" + std::to_string(std::strlen(name)) + name;
+  for (CUfunction f : fs) {
+    const char* nm = nullptr;
+    ck(cuFuncGetName(&nm, f), "cuFuncGetName");
+    if (nm && std::strncmp(nm, key.c_str(), key.size()) == 0) return f;
+  }
+  die((std::string("kernel not found: ") + name).c_str());
+}
+
+template <class T> CUdeviceptr dalloc(size_t n, int fill_byte = 0) {
+  CUdeviceptr p = 0;
+  size_t bytes = (n ? n : 1) * sizeof(T);
+  ck(cuMemAlloc(&p, bytes), "cuMemAlloc");
+  ck(cuMemsetD8(p, (unsigned char)fill_byte, bytes), "cuMemsetD8");
+  return p;
+}
+
+template <class T> CUdeviceptr dupload(const std::vector<T>& v, size_t pad_to = 0) {
+  size_t n = v.size() > pad_to ? v.size() : pad_to;
+  CUdeviceptr p = dalloc<T>(n);
+  if (!v.empty()) ck(cuMemcpyHtoD(p, v.data(), v.size() * sizeof(T)), "cuMemcpyHtoD");
+  return p;
+}
+
+template <class T> std::vector<T> ddownload(CUdeviceptr p, size_t n) {
+  std::vector<T> v(n);
+  if (n) ck(cuMemcpyDtoH(v.data(), p, n * sizeof(T)), "cuMemcpyDtoH");
+  return v;
+}
+
+CUtexObject make_u32_tex(CUdeviceptr p, size_t count) {
+  CUDA_RESOURCE_DESC rd;
+  std::memset(&rd, 0, sizeof(rd));
+  rd.resType = CU_RESOURCE_TYPE_LINEAR;
+  rd.res.linear.devPtr = p;
+  rd.res.linear.format = CU_AD_FORMAT_UNSIGNED_INT32;
+  rd.res.linear.numChannels = 1;
+  rd.res.linear.sizeInBytes = count * sizeof(uint32_t);
+  CUDA_TEXTURE_DESC td;
+  std::memset(&td, 0, sizeof(td));
+  td.addressMode[0] = CU_TR_ADDRESS_MODE_CLAMP;
+  td.filterMode = CU_TR_FILTER_MODE_POINT;
+  td.flags = CU_TRSF_READ_AS_INTEGER;
+  CUtexObject t = 0;
+  ck(cuTexObjectCreate(&t, &rd, &td, nullptr), "cuTexObjectCreate");
+  return t;
+}
+
+void launch(CUfunction f, unsigned gx, unsigned gy, unsigned gz, unsigned bx, unsigned by,
+            unsigned bz, void** args) {
+  ck(cuLaunchKernel(f, gx, gy, gz, bx, by, bz, 0, nullptr, args, nullptr), "cuLaunchKernel");
+  ck(cuCtxSynchronize(), "cuCtxSynchronize");
+}
+
+unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
+
+std::vector<uint32_t> exclusive_scan(const std::vector<uint32_t>& in) {
+  std::vector<uint32_t> out(in.size());
+  uint32_t acc = 0;
+  for (size_t i = 0; i < in.size(); ++i) { out[i] = acc; acc += in[i]; }
+  return out;
+}
+
+struct Tables {
+  CUdeviceptr tri = 0, nverts = 0;
+  CUtexObject tri_tex = 0, nverts_tex = 0;
+};
+
+Tables load_tables(const std::string& path) {
+  auto b = slurp(path);
+  if (b.size() != 512 + 4096 + 256) die("tables file has the wrong size");
+  std::vector<uint32_t> tri(4096), nv(256);
+  for (int i = 0; i < 4096; ++i) tri[i] = b[512 + i];
+  for (int i = 0; i < 256; ++i) nv[i] = b[4608 + i];
+  Tables t;
+  t.tri = dupload(tri);
+  t.nverts = dupload(nv);
+  t.tri_tex = make_u32_tex(t.tri, 4096);
+  t.nverts_tex = make_u32_tex(t.nverts, 256);
+  return t;
+}
+
+// Classify + compact, shared by the plain and band cases.  The classify field
+// `vol` is the one whose `< iso` test makes the cube index (classifyVoxel_new,
+// src/MarchingCubes_kernel.cu:3207-3249).
+struct Classified {
+  uint32_t nvox = 0, active = 0, total = 0;
+  std::vector<uint32_t> verts, occ, occ_scan, verts_scan, compacted;
+  CUdeviceptr d_verts_scan = 0, d_compacted = 0;
+};
+
+Classified classify_and_compact(CUmodule mc, const Tables& T, CUdeviceptr vol, U3 gsize, float iso) {
+  Classified c;
+  U3 mask{gsize.x - 1, gsize.y - 1, gsize.z - 1};
+  U3 shift{1, gsize.x - 1, (gsize.x - 1) * (gsize.y - 1)};
+  c.nvox = mask.x * mask.y * mask.z;
+  CUdeviceptr d_verts = dalloc<uint32_t>(c.nvox), d_occ = dalloc<uint32_t>(c.nvox);
+  F3 vs{1.f, 1.f, 1.f};
+  CUfunction k_cls = find_kernel(mc, "classifyVoxel_new");
+  {
+    void* a[] = {&d_verts, &d_occ, &vol, &gsize, &shift, &mask, &c.nvox, &vs, &iso,
+                 const_cast<CUtexObject*>(&T.nverts_tex)};
+    launch(k_cls, blocks_for(c.nvox, 1024), 1, 1, 1024, 1, 1, a);
+  }
+  c.verts = ddownload<uint32_t>(d_verts, c.nvox);
+  c.occ = ddownload<uint32_t>(d_occ, c.nvox);
+  c.occ_scan = exclusive_scan(c.occ);
+  c.verts_scan = exclusive_scan(c.verts);
+  c.active = c.nvox ? c.occ_scan.back() + c.occ.back() : 0;
+  c.total = c.nvox ? c.verts_scan.back() + c.verts.back() : 0;
+  CUdeviceptr d_occ_scan = dupload(c.occ_scan);
+  c.d_compacted = dalloc<uint32_t>(c.active ? c.active : 1);
+  CUfunction k_cmp = find_kernel(mc, "compactVoxels");
+  {
+    void* a[] = {&c.d_compacted, &d_occ, &d_occ_scan, &c.nvox};
+    launch(k_cmp, blocks_for(c.nvox, 1024), 1, 1, 1024, 1, 1, a);
+  }
+  c.compacted = ddownload<uint32_t>(c.d_compacted, c.active);
+  c.d_verts_scan = dupload(c.verts_scan);
+  cuMemFree(d_verts);
+  cuMemFree(d_occ);
+  cuMemFree(d_occ_scan);
+  return c;
+}
+
+void write_classified(Writer& w, const Classified& c) {
+  w.put<uint32_t>(c.nvox);
+  w.put<uint32_t>(c.active);
+  w.put<uint32_t>(c.total);
+  w.arr(c.verts);
+  w.arr(c.occ);
+  w.arr(c.occ_scan);
+  w.arr(c.verts_scan);
+  w.arr(c.compacted);
+}
+
+// kind 1: plain marching cubes on a fed field.  generateTriangles_lattice_kernel_3
+// (src/MarchingCubes_kernel.cu:3041-3170) takes its cube index as
+// (f < iso) && (f > 0); jobs feed strictly positive fields so it equals the
+// classify index.
+void run_mc_plain(Reader& r, Writer& w, CUmodule mc, const Tables& T) {
+  U3 g{r.get<uint32_t>(), r.get<uint32_t>(), r.get<uint32_t>()};
+  float iso = r.get<float>();
+  F3 vs{r.get<float>(), r.get<float>(), r.get<float>()};
+  F3 gc{r.get<float>(), r.get<float>(), r.get<float>()};
+  auto field = r.arr<float>((size_t)g.x * g.y * g.z);
+  CUdeviceptr d_field = dupload(field);
+  Classified c = classify_and_compact(mc, T, d_field, g, iso);
+  uint32_t maxv = c.total + 16;
+  CUdeviceptr d_pos = dalloc<float>(4ull * maxv, 0xFF), d_norm = dalloc<float>(4ull * maxv, 0xFF);
+  U3 mask{g.x - 1, g.y - 1, g.z - 1};
+  U3 shift{1, g.x - 1, (g.x - 1) * (g.y - 1)};
+  if (c.active) {
+    CUfunction k = find_kernel(mc, "generateTriangles_lattice_kernel_3");
+    void* a[] = {&d_pos, &d_norm, &c.d_compacted, &c.d_verts_scan, &g, &shift, &mask, &vs, &gc,
+                 &iso, &c.active, &maxv, const_cast<CUtexObject*>(&T.tri_tex),
+                 const_cast<CUtexObject*>(&T.nverts_tex), &c.total, &d_field, &iso};
+    launch(k, blocks_for(c.active, 32), 1, 1, 32, 1, 1, a);
+  }
+  write_classified(w, c);
+  w.arr(ddownload<float>(d_pos, 4ull * c.total));
+  w.arr(ddownload<float>(d_norm, 4ull * c.total));
+  cuMemFree(d_field); cuMemFree(d_pos); cuMemFree(d_norm);
+  cuMemFree(c.d_compacted); cuMemFree(c.d_verts_scan);
+}
+
+// kind 2: band-mode marching cubes.  Cube index from a 0/1 label field, vertices
+// from the normalised field with the band edges (generateTriangles_lattice_kernel_newone,
+// src/MarchingCubes_kernel.cu:3678-3817).  Also runs the two-field variant
+// (generateTriangles_lattice_kernel_new, :3424-3570) with the arguments
+// spatial_lattice_run passes (src/main.cu:4006-4010: iso1 = iso2 = 0).
+void run_mc_band(Reader& r, Writer& w, CUmodule mc, const Tables& T) {
+  U3 g{r.get<uint32_t>(), r.get<uint32_t>(), r.get<uint32_t>()};
+  float iso = r.get<float>(), b1 = r.get<float>(), b2 = r.get<float>();
+  F3 vs{r.get<float>(), r.get<float>(), r.get<float>()};
+  F3 gc{r.get<float>(), r.get<float>(), r.get<float>()};
+  size_t P = (size_t)g.x * g.y * g.z;
+  auto label = r.arr<float>(P);
+  auto normf = r.arr<float>(P);
+  CUdeviceptr d_label = dupload(label), d_normf = dupload(normf), d_two = dupload(normf);
+  Classified c = classify_and_compact(mc, T, d_label, g, iso);
+  uint32_t maxv = c.total + 16;
+  U3 mask{g.x - 1, g.y - 1, g.z - 1};
+  U3 shift{1, g.x - 1, (g.x - 1) * (g.y - 1)};
+  write_classified(w, c);
+  for (int variant = 0; variant < 2; ++variant) {
+    CUdeviceptr d_pos = dalloc<float>(4ull * maxv, 0xFF), d_norm = dalloc<float>(4ull * maxv, 0xFF);
+    if (c.active) {
+      if (variant == 0) {
+        CUfunction k = find_kernel(mc, "generateTriangles_lattice_kernel_newone");
+        void* a[] = {&d_pos, &d_norm, &c.d_compacted, &c.d_verts_scan, &d_label, &g, &shift, &mask,
+                     &vs, &gc, &iso, &c.active, &maxv, const_cast<CUtexObject*>(&T.tri_tex),
+                     const_cast<CUtexObject*>(&T.nverts_tex), &c.total, &d_normf, &b1, &b2};
+        launch(k, blocks_for(c.active, 32), 1, 1, 32, 1, 1, a);
+      } else {
+        float z0 = 0.f, z1 = 0.f;
+        CUfunction k = find_kernel(mc, "generateTriangles_lattice_kernel_new");
+        void* a[] = {&d_pos, &d_norm, &c.d_compacted, &c.d_verts_scan, &d_label, &g, &shift, &mask,
+                     &vs, &gc, &iso, &c.active, &maxv, const_cast<CUtexObject*>(&T.tri_tex),
+                     const_cast<CUtexObject*>(&T.nverts_tex), &c.total, &d_normf, &d_two, &b1, &b2,
+                     &z0, &z1};
+        launch(k, blocks_for(c.active, 32), 1, 1, 32, 1, 1, a);
+      }
+    }
+    w.arr(ddownload<float>(d_pos, 4ull * c.total));
+    w.arr(ddownload<float>(d_norm, 4ull * c.total));
+    cuMemFree(d_pos); cuMemFree(d_norm);
+  }
+  cuMemFree(d_label); cuMemFree(d_normf); cuMemFree(d_two);
+  cuMemFree(c.d_compacted); cuMemFree(c.d_verts_scan);
+}
+
+// kind 3: TPMS unit cell (create_lattice_kernel, src/lattice_files/Fft_lattice.cu:11-93),
+// launched with the reference's 16x8x8 blocks (:95-98).
+void run_unit_cell(Reader& r, Writer& w, CUmodule fft) {
+  uint32_t nx = r.get<uint32_t>(), ny = r.get<uint32_t>(), nz = r.get<uint32_t>(), type = r.get<uint32_t>();
+  // The kernel calls __syncthreads() inside its bounds check; sizes that tile the
+  // 16x8x8 blocks exactly keep every thread of a block on the same path.
+  if (nx % 16 || ny % 8 || nz % 8) die("unit-cell jobs must tile the 16x8x8 blocks exactly");
+  uint32_t size = nx * ny * nz;
+  CUdeviceptr d = dalloc<float>(size);
+  CUfunction k = find_kernel(fft, "create_lattice_kernel");
+  void* a[] = {&d, &nx, &ny, &nz, &size, &type};
+  launch(k, (nx + 15) / 16, (ny + 7) / 8, (nz + 7) / 8, 16, 8, 8, a);
+  w.arr(ddownload<float>(d, size));
+  cuMemFree(d);
+}
+
+// kind 4: primitive fields (src/Modelling.cu:244-750), 1-D launches of 1024
+// threads.  Three of the kernels (cuboid, cuboid shell, pyramid frustum) have no
+// bounds check, so the output buffer is padded to the whole launch.
+void run_primitive(Reader& r, Writer& w, CUmodule mdl) {
+  uint32_t prim = r.get<uint32_t>();
+  int nx = r.get<int32_t>(), ny = r.get<int32_t>(), nz = r.get<int32_t>();
+  float dx = r.get<float>(), dy = r.get<float>(), dz = r.get<float>();
+  F3 center{r.get<float>(), r.get<float>(), r.get<float>()};
+  F3 v3{r.get<float>(), r.get<float>(), r.get<float>()};  // axis or Euler angles
+  float p[6];
+  for (float& x : p) x = r.get<float>();
+  uint32_t flag = r.get<uint32_t>();
+  size_t P = (size_t)nx * ny * nz;
+  unsigned blocks = blocks_for(P, 1024);
+  CUdeviceptr d = dalloc<float>((size_t)blocks * 1024);
+  bool sel = flag != 0;
+  CUfunction k;
+  switch (prim) {
+    case 0: {  // implicit_sphere_kernel(data, center, radius, thickness, Nx,Ny,Nz, dx,dy,dz, shell)
+      k = find_kernel(mdl, "implicit_sphere_kernel");
+      void* a[] = {&d, &center, &p[0], &p[1], &nx, &ny, &nz, &dx, &dy, &dz, &sel};
+      launch(k, blocks, 1, 1, 1024, 1, 1, a);
+      break;
+    }
+    case 1: {  // distance_from_line_kernel(data, center, axis, radius, t_radial, t_axial, Nx..dz, disc)
+      k = find_kernel(mdl, "distance_from_line_kernel");
+      void* a[] = {&d, &center, &v3, &p[0], &p[1], &p[2], &nx, &ny, &nz, &dx, &dy, &dz, &sel};
+      launch(k, blocks, 1, 1, 1024, 1, 1, a);
+      break;
+    }
+    case 2: {  // implicit_cuboid_kernel(data, center, angles, xw, yw, zw, Nx..dz)
+      k = find_kernel(mdl, "implicit_cuboid_kernel");
+      void* a[] = {&d, &center, &v3, &p[0], &p[1], &p[2], &nx, &ny, &nz, &dx, &dy, &dz};
+      launch(k, blocks, 1, 1, 1024, 1, 1, a);
+      break;
+    }
+    case 3: {  // implicit_cuboid_shell_kernel(data, center, angles, xw, yw, zw, thickness, Nx..dz)
+      k = find_kernel(mdl, "implicit_cuboid_shell_kernel");
+      void* a[] = {&d, &center, &v3, &p[0], &p[1], &p[2], &p[3], &nx, &ny, &nz, &dx, &dy, &dz};
+      launch(k, blocks, 1, 1, 1024, 1, 1, a);
+      break;
+    }
+    case 4: {  // implicit_torus_kernel(data, center, angles, R, r, Nx..dz)
+      k = find_kernel(mdl, "implicit_torus_kernel");
+      void* a[] = {&d, &center, &v3, &p[0], &p[1], &nx, &ny, &nz, &dx, &dy, &dz};
+      launch(k, blocks, 1, 1, 1024, 1, 1, a);
+      break;
+    }
+    case 5: {  // implicit_cone_kernel(data, center, angles, base_radius, height, Nx..dz)
+      k = find_kernel(mdl, "implicit_cone_kernel");
+      void* a[] = {&d, &center, &v3, &p[0], &p[1], &nx, &ny, &nz, &dx, &dy, &dz};
+      launch(k, blocks, 1, 1, 1024, 1, 1, a);
+      break;
+    }
+    case 6: {  // implicit_cone_frustum_kernel(data, center, angles, top_r, bottom_r, height, Nx..dz)
+      k = find_kernel(mdl, "implicit_cone_frustum_kernel");
+      void* a[] = {&d, &center, &v3, &p[0], &p[1], &p[2], &nx, &ny, &nz, &dx, &dy, &dz};
+      launch(k, blocks, 1, 1, 1024, 1, 1, a);
+      break;
+    }
+    case 7: {  // implicit_pyramid_frustum_kernel(data, center, angles, xb, xt, yh, zb, zt, Nx..dz)
+      k = find_kernel(mdl, "implicit_pyramid_frustum_kernel");
+      void* a[] = {&d, &center, &v3, &p[0], &p[1], &p[2], &p[3], &p[4], &nx, &ny, &nz, &dx, &dy, &dz};
+      launch(k, blocks, 1, 1, 1024, 1, 1, a);
+      break;
+    }
+    default:
+      die("unknown primitive");
+  }
+  w.arr(ddownload<float>(d, P));
+  cuMemFree(d);
+}
+
+// kind 5: band normalisation (GPU_buffer_normalise_four,
+// src/lattice_files/Gratings.cu:1579-1617).  Jobs use sizes that are multiples of
+// 1024: the first reduction kernel leaves the tail of a partial block unset.
+void run_normalise_four(Reader& r, Writer& w, CUmodule gr) {
+  int nx = r.get<int32_t>(), ny = r.get<int32_t>(), nz = r.get<int32_t>();
+  float i1 = r.get<float>(), i2 = r.get<float>();
+  size_t P = (size_t)nx * ny * nz;
+  auto data = r.arr<float>(P);
+  int n = (int)P;
+  int block_num = (int)blocks_for(P, 1024);
+  CUdeviceptr d_in = dupload(data), d_red = dalloc<float>(2 * (size_t)block_num);
+  CUdeviceptr d_label = dalloc<float>(P), d_norm = dalloc<float>(P);
+  {
+    CUfunction k = find_kernel(gr, "GPUScalar_normalise_kernel_lattice");
+    void* a[] = {&d_red, &d_in, &n};
+    launch(k, (unsigned)block_num, 1, 1, 1024, 1, 1, a);
+  }
+  {
+    CUfunction k = find_kernel(gr, "Min_reduction_lattice");
+    void* a[] = {&d_red, &block_num};
+    launch(k, 1, 1, 1, 1024, 1, 1, a);
+  }
+  float mm[2];
+  ck(cuMemcpyDtoH(mm, d_red, sizeof(mm)), "cuMemcpyDtoH");
+  {
+    CUfunction k = find_kernel(gr, "device_bufferfour");
+    void* a[] = {&d_in, &d_label, &d_norm, &mm[0], &mm[1], &nx, &ny, &nz, &i1, &i2};
+    launch(k, (unsigned)block_num, 1, 1, 1024, 1, 1, a);
+  }
+  w.put<float>(mm[0]);
+  w.put<float>(mm[1]);
+  w.arr(ddownload<float>(d_label, P));
+  w.arr(ddownload<float>(d_norm, P));
+  cuMemFree(d_in); cuMemFree(d_red); cuMemFree(d_label); cuMemFree(d_norm);
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc != 6) {
+    std::fprintf(stderr, "usage: ref_runner <fatbin-dir> <sm103a|ptx89> <tables.bin> <job.bin> <out.bin>\n");
+    return 2;
+  }
+  std::string dir = argv[1], var = argv[2];
+  ck(cuInit(0), "cuInit");
+  CUdevice dev;
+  ck(cuDeviceGet(&dev, 0), "cuDeviceGet");
+  CUcontext ctx;
+  CUctxCreateParams cp;
+  std::memset(&cp, 0, sizeof(cp));
+  ck(cuCtxCreate(&ctx, &cp, 0, dev), "cuCtxCreate");
+  auto load = [&](const char* unit) {
+    auto img = slurp(dir + "/ref_" + unit + "_" + var + ".fatbin");
+    CUmodule m;
+    ck(cuModuleLoadData(&m, img.data()), "cuModuleLoadData");
+    return m;
+  };
+  CUmodule mc = load("mc"), mdl = load("modelling"), fft = load("fft"), gr = load("gratings");
+  Tables T = load_tables(argv[3]);
+  auto job = slurp(argv[4]);
+  Reader r{job};
+  FILE* of = std::fopen(argv[5], "wb");
+  if (!of) die("cannot open output");
+  Writer w{of};
+  if (r.get<uint32_t>() != 0x4A4D4347u) die("bad job magic");
+  uint32_t ncases = r.get<uint32_t>();
+  for (uint32_t i = 0; i < ncases; ++i) {
+    uint32_t kind = r.get<uint32_t>();
+    w.put<uint32_t>(kind);
+    switch (kind) {
+      case 1: run_mc_plain(r, w, mc, T); break;
+      case 2: run_mc_band(r, w, mc, T); break;
+      case 3: run_unit_cell(r, w, fft); break;
+      case 4: run_primitive(r, w, mdl); break;
+      case 5: run_normalise_four(r, w, gr); break;
+      default: die("unknown job kind");
+    }
+  }
+  std::fclose(of);
+  cuCtxDestroy(ctx);
+  std::printf("ref_runner: %u cases done (%s)\n", ncases, var.c_str());
+  return 0;
+}
