@@ -1,0 +1,386 @@
+"""Benchmark of the field -> mesh hot path on GB300.
+
+Default workload (the headline configuration): a spatially varying TPMS lattice
+on a 512^3 FP32 grid.  Per control point of a 16^3 grid of seeded uniform values:
+type in {gyroid, Schwarz-P, diamond}, period U[16,64] voxels, Euler angles
+U[-pi/4, pi/4], thickness U[-0.6, 0.6]; parameters trilinear per voxel, type of
+the nearest control point (GCM_GRADE_PARAMS), isovalue 0, unshared float4
+position + normal triangles out.
+
+One step = field evaluation + fused marching cubes over the whole grid.
+`value` = voxels/s with the control grids resident in HBM; `e2e` = the same
+through the C ABI with host buffers (control grids copied in, the mesh copied
+out to pinned host memory, inside the timed region).  `--impl reference` times
+the CPU restatement of the reference's algorithm (oracle/) on the host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gcm|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+N_GRID = 512
+N_CTRL = 16
+SEED = 0xD4A + 2
+METRIC = "voxels/s & tris/s at 512^3 (%HBM roofline)"
+
+
+def c2_controls(n_ctrl=N_CTRL, seed=SEED):
+    rng = np.random.default_rng(seed)
+    n = n_ctrl ** 3
+    period = rng.uniform(16, 64, n).astype(np.float32)
+    euler = rng.uniform(-np.pi / 4, np.pi / 4, 3 * n).astype(np.float32)
+    thick = rng.uniform(-0.6, 0.6, n).astype(np.float32)
+    types = rng.choice(np.array([0, 1, 5], np.uint8), n)
+    return period, euler, thick, types
+
+
+def workload_config(n=N_GRID):
+    return {"workload": f"graded TPMS lattice {n}^3 FP32 (gyroid/Schwarz-P/diamond, period 16-64 vox, "
+                        f"Euler +-pi/4, thickness +-0.6, {N_CTRL}^3 control grid, trilinear parameters)",
+            "grid": [n, n, n], "control_grid": [N_CTRL] * 3, "grading": "params", "iso": 0.0,
+            "l2": "working set larger than L2 (512 MiB field + mesh); no flush",
+            "parallelism": "replicas"}
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel_key):
+    """DRAM bytes per launch of one kernel from a committed ncu summary (a small
+    JSON sidecar next to the text summary in profiles/), scaled to the workload
+    by the summary itself; None when no capture exists."""
+    p = os.path.join(HERE, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    v = d.get(kernel_key)
+    return None if v is None else float(v)
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if args.impl == "gcm" else "gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg, torch=None):
+    if torch is not None:
+        torch.cuda.synchronize()
+    if pg is not None:
+        pg.barrier()
+
+
+def allmax(pg, v, torch=None):
+    if pg is None:
+        return v
+    import torch as T
+
+    t = T.tensor([float(v)], dtype=T.float64, device="cuda" if torch is not None else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(pg, v, torch=None):
+    if pg is None:
+        return v
+    import torch as T
+
+    t = T.tensor([float(v)], dtype=T.float64, device="cuda" if torch is not None else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------- CPU
+
+
+def cpu_sample(threads, n=N_GRID, planes=256):
+    """Times the oracle's field evaluation + marching cubes (OpenMP) on a centred
+    z-slab of `planes` sample planes of the workload (same control grid, origin
+    and voxel numbering); returns voxels/s and the split."""
+    import oracle as O
+
+    period, euler, thick, types = c2_controls()
+    planes = min(planes or n, n)
+    z0 = (n - planes) // 2
+    origin = ((n - 1) / 2,) * 3
+    t0 = time.perf_counter()
+    f = O.lattice_slab((n, n, n), z0, planes, 0, (N_CTRL,) * 3, period, euler, thick, types, origin, threads=threads)
+    t1 = time.perf_counter()
+    vox = (n - 1) * (n - 1) * (planes - 1)
+    # the first pass sizes the output (it runs the whole pipeline, writing nothing)
+    total, _, _, _ = O.mesh_field_omp(f, (1, 1, 1), (0, 0, 0), 0.0, 0, threads)
+    t2 = time.perf_counter()
+    total, active, _, _ = O.mesh_field_omp(f, (1, 1, 1), (0, 0, 0), 0.0, total, threads)
+    t3 = time.perf_counter()
+    field_s, mesh_s = t1 - t0, t3 - t2
+    return {"voxels": vox, "verts": total, "active": active, "field_s": field_s, "mesh_s": mesh_s,
+            "voxels_per_s": vox / (field_s + mesh_s)}
+
+
+def run_reference(args):
+    world, rank, local, pg = dist_setup(args)
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    samples = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(threads, planes=args.cpu_planes)
+        if i >= args.warmup:
+            samples.append(r)
+    v = statistics.median(s["voxels_per_s"] for s in samples)
+    tris = statistics.median(s["verts"] / 3 / (s["field_s"] + s["mesh_s"]) for s in samples)
+    ms = statistics.median((s["field_s"] + s["mesh_s"]) * 1e3 for s in samples)
+    sample = (f"centred z-slab of {args.cpu_planes} of {N_GRID} sample planes of the same field per step "
+              f"(field evaluation + classify + scans + compaction + generation)")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "voxels/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": workload_config(), "tris_per_s": tris,
+            "cpu_baseline": {"value": v, "unit": "voxels/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ----------------------------------------------------------------------------- GPU
+
+
+def run_gcm(args):
+    import torch
+
+    world, rank, local, pg = dist_setup(args)
+    torch.cuda.set_device(local)
+    from gpucadforam_gb300 import _native as N
+    from gpucadforam_gb300.mesher import Context, Lattice, make_grid
+
+    n = args.grid
+    period, euler, thick, types = c2_controls()
+    origin = ((n - 1) / 2,) * 3
+    ctx = Context(local)
+    lat = Lattice.from_numpy(0, (N_CTRL,) * 3, period, euler, thick, types, origin, device=f"cuda:{local}")
+    s = ctx.lattice_struct(lat)
+    grid = make_grid((n, n, n))
+    stream = torch.cuda.current_stream()
+    cs = C.c_void_p(stream.cuda_stream)
+    field = torch.empty((n, n, n), dtype=torch.float32, device="cuda")
+    ctx.check(ctx.lib.gcm_field_lattice(ctx.h, C.byref(s), n, n, n, C.c_void_p(field.data_ptr()), cs))
+    cnt = ctx.count_field(field, 0.0)
+    cap = cnt.total_verts
+    pos = torch.empty((cap, 4), dtype=torch.float32, device="cuda")
+    norm = torch.empty((cap, 4), dtype=torch.float32, device="cuda")
+    d_counts = torch.zeros(4, dtype=torch.int64, device="cuda")
+    ctx.reserve(n ** 3)
+    vox = (n - 1) ** 3
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        ctx.check(ctx.lib.gcm_field_lattice(ctx.h, C.byref(s), n, n, n, C.c_void_p(field.data_ptr()), cs))
+        if ev:
+            ev[1].record(stream)
+        ctx.check(ctx.lib.gcm_mesh_field_async(ctx.h, C.c_void_p(field.data_ptr()), C.byref(grid), 0.0,
+                                               C.c_void_p(pos.data_ptr()), C.c_void_p(norm.data_ptr()), cap,
+                                               C.c_void_p(d_counts.data_ptr()), cs))
+        if ev:
+            ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    chk = d_counts.cpu().numpy().view(np.uint64)
+    assert int(chk[1]) == cap and int(chk[2] & 0xFFFFFFFF) == 0, chk
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    barrier(pg, torch)
+    launches0 = ctx.launches
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(args.steps):
+        step(evs[k])
+    t1.record(stream)
+    barrier(pg, torch)
+    launches = ctx.launches - launches0
+    clk = clocks.stop()
+    total_ms = t0.elapsed_time(t1)
+    field_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    mc_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    total_ms = allmax(pg, total_ms, torch)
+    ms_step = total_ms / args.steps
+    value = allsum(pg, vox * args.steps, torch) / (total_ms / 1e3)
+    tris = allsum(pg, cap / 3 * args.steps, torch) / (total_ms / 1e3)
+
+    peak, peak_kind = measured_peaks()
+    mc_bytes = 4 * n ** 3 + 32 * cap
+    mc_avg = statistics.mean(mc_ms) / 1e3
+    achieved = mc_bytes / mc_avg / 1e9
+    traffic = profile_traffic("mc_mesh_kernel_512")
+
+    # ---- e2e through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        h_period = torch.from_numpy(period).pin_memory()
+        h_euler = torch.from_numpy(euler).pin_memory()
+        h_thick = torch.from_numpy(thick).pin_memory()
+        h_types = torch.from_numpy(types).pin_memory()
+        h_pos = torch.empty((cap, 4), dtype=torch.float32).pin_memory()
+        h_norm = torch.empty((cap, 4), dtype=torch.float32).pin_memory()
+        gc = N.GcmCounts()
+
+        def e2e_step():
+            lat.period.copy_(h_period, non_blocking=True)
+            lat.euler.copy_(h_euler, non_blocking=True)
+            lat.thickness.copy_(h_thick, non_blocking=True)
+            lat.types.copy_(h_types, non_blocking=True)
+            ctx.check(ctx.lib.gcm_mesh_lattice(ctx.h, C.byref(s), C.byref(grid), 0.0, C.c_void_p(pos.data_ptr()),
+                                               C.c_void_p(norm.data_ptr()), cap, C.byref(gc), cs))
+            h_pos.copy_(pos, non_blocking=True)
+            h_norm.copy_(norm, non_blocking=True)
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(pg, torch)
+        a = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(pg, torch)
+        e2e_s = allmax(pg, time.perf_counter() - a, torch)
+        assert int(gc.total_verts) == cap
+        assert h_pos[:16].numpy().tobytes() == pos[:16].cpu().numpy().tobytes()
+        h2d = period.nbytes + euler.nbytes + thick.nbytes + types.nbytes
+        e2e = {"value": allsum(pg, vox * args.steps, torch) / e2e_s, "unit": "voxels/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(32 * cap + 32),
+               "ms_per_step": e2e_s / args.steps * 1e3}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        r = cpu_sample(os.cpu_count() or 1, planes=args.cpu_planes)
+        cpu = {"value": r["voxels_per_s"], "unit": "voxels/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"oracle OpenMP field + marching cubes on a centred z-slab of {args.cpu_planes} of {n} "
+                         f"sample planes"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "voxels/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded control grid)",
+                "config": workload_config(n), "tris_per_s": tris, "verts_per_step": cap,
+                "active_voxels": cnt.active_voxels,
+                "kernels_ms": {"lattice_params_kernel": statistics.mean(field_ms),
+                               "mc_mesh_kernel": statistics.mean(mc_ms)},
+                "roofline": {"bound": "hbm", "kernel": "mc_mesh_kernel", "achieved": achieved, "peak": peak,
+                             "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                             "algorithmic_bytes": mc_bytes, "traffic": traffic},
+                "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches)}
+        print(json.dumps(line))
+    ctx.close()
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gcm", "reference"], default="gcm")
+    ap.add_argument("--grid", type=int, default=N_GRID)
+    ap.add_argument("--cpu-planes", type=int, default=256)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gcm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

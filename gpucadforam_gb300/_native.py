@@ -1,0 +1,117 @@
+"""ctypes binding of libgcm.so (the C ABI in include/gcm.h).
+
+The library is the product: there is no Python or CPU fallback.  Importing this
+module loads ``gpucadforam_gb300/libgcm.so``; if it is missing the import fails
+with a message that says how to build it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgcm.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "gcm.h")
+
+GCM_OK = 0
+STATUS = {
+    0: "GCM_OK", 1: "GCM_ERR_INVALID_ARGUMENT", 2: "GCM_ERR_OUTPUT_OVERFLOW", 3: "GCM_ERR_DEVICE_TIMEOUT",
+    4: "GCM_ERR_CUDA", 5: "GCM_ERR_OUT_OF_MEMORY", 6: "GCM_ERR_NOT_SUPPORTED", 7: "GCM_ERR_IO",
+    8: "GCM_ERR_REJECTED", 9: "GCM_ERR_CANCELLED", 10: "GCM_ERR_BUSY",
+}
+GCM_ERR_OUTPUT_OVERFLOW = 2
+GCM_ERR_DEVICE_TIMEOUT = 3
+
+
+class GcmGrid(C.Structure):
+    _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("nz", C.c_uint32), ("voxel_size", C.c_float * 3),
+                ("grid_center", C.c_float * 3)]
+
+
+class GcmCounts(C.Structure):
+    _fields_ = [("active_voxels", C.c_uint64), ("total_verts", C.c_uint64), ("status", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class GcmLattice(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("cx", C.c_uint32), ("cy", C.c_uint32), ("cz", C.c_uint32),
+                ("d_period", C.c_void_p), ("d_euler", C.c_void_p), ("d_thickness", C.c_void_p),
+                ("d_type", C.c_void_p), ("origin", C.c_float * 3)]
+
+
+class GcmPrimitive(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("op", C.c_uint32), ("flag", C.c_uint32), ("reserved", C.c_uint32),
+                ("center", C.c_float * 3), ("v3", C.c_float * 3), ("p", C.c_float * 6)]
+
+
+class GcmFrame(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("spacing", C.c_float * 3)]
+
+
+P = C.c_void_p
+U32 = C.c_uint32
+U64 = C.c_uint64
+F32 = C.c_float
+I32 = C.c_int
+
+# name -> (restype, argtypes)
+PROTOTYPES = {
+    "gcm_abi_version": (C.c_int, []),
+    "gcm_status_string": (C.c_char_p, [I32]),
+    "gcm_ctx_create": (I32, [I32, C.POINTER(P)]),
+    "gcm_ctx_destroy": (I32, [P]),
+    "gcm_ctx_last_error": (C.c_char_p, [P]),
+    "gcm_ctx_reserve": (I32, [P, U64]),
+    "gcm_ctx_set_wait_limit": (I32, [P, U64]),
+    "gcm_ctx_launch_count": (U64, [P]),
+    "gcm_mesh_field": (I32, [P, P, C.POINTER(GcmGrid), F32, P, P, U64, C.POINTER(GcmCounts), P]),
+    "gcm_mesh_field_async": (I32, [P, P, C.POINTER(GcmGrid), F32, P, P, U64, P, P]),
+    "gcm_count_field": (I32, [P, P, C.POINTER(GcmGrid), F32, C.POINTER(GcmCounts), P]),
+    "gcm_mc_classify": (I32, [P, P, C.POINTER(GcmGrid), F32, P, P, P, P]),
+    "gcm_scan_exclusive_u32": (I32, [P, P, P, U64, C.POINTER(U64), P]),
+    "gcm_mc_compact": (I32, [P, P, P, U64, P, P]),
+    "gcm_mc_generate": (I32, [P, P, C.POINTER(GcmGrid), F32, P, U64, P, P, P, U64, P]),
+    "gcm_normalise_band": (I32, [P, P, U32, U32, U32, F32, F32, P, P, C.POINTER(F32), P]),
+    "gcm_mesh_band": (I32, [P, P, P, C.POINTER(GcmGrid), F32, F32, F32, P, P, U64, C.POINTER(GcmCounts), P]),
+    "gcm_field_unit_cell": (I32, [P, U32, U32, U32, U32, P, P]),
+    "gcm_field_lattice": (I32, [P, C.POINTER(GcmLattice), U32, U32, U32, P, P]),
+    "gcm_mesh_lattice": (I32, [P, C.POINTER(GcmLattice), C.POINTER(GcmGrid), F32, P, P, U64, C.POINTER(GcmCounts), P]),
+    "gcm_field_csg": (I32, [P, P, U32, C.POINTER(GcmFrame), U32, U32, U32, P, P]),
+    "gcm_test_lookback_stall": (I32, [P, U32, U32, U64, P, P]),
+    "gcm_mesh_csg": (I32, [P, P, U32, C.POINTER(GcmFrame), C.POINTER(GcmGrid), F32, P, P, U64,
+                           C.POINTER(GcmCounts), P]),
+}
+
+
+def header_symbols() -> list[str]:
+    """Every function declared in include/gcm.h."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gcm_[a-z0-9_]+)\s*\(", text)))
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(path)
+    for name, (res, args) in PROTOTYPES.items():
+        fn = getattr(L, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+class GcmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code

@@ -1,0 +1,655 @@
+// Host side of the C ABI declared in include/gcm.h.
+//
+// The reference runs every step of an extraction on the legacy default stream
+// with a cudaDeviceSynchronize and blocking count readbacks between them
+// (src/Isosurface.cu:44-134, :401-486).  Here each call is stream-ordered: the
+// counts come back in one copy at the end (or stay on the device for the
+// *_async forms), scratch lives in the context and is zeroed with one memset.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/gcm.h"
+#include "gcm_kernels.h"
+
+using gcm::MeshParams;
+
+namespace {
+
+constexpr uint64_t kDefaultWaitNs = 2000000000ull;
+constexpr uint32_t kMeshThreads = 256;
+constexpr uint32_t kTargetVoxelsPerTile = 2048;
+constexpr size_t kMeshSmemBudget = 96 * 1024;
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+struct gcm_ctx {
+  int device = 0;
+  int sm_count = 0;
+  size_t smem_optin = 0;
+  uint64_t wait_ns = kDefaultWaitNs;
+  std::atomic<uint64_t> launches{0};
+  std::string last_error;
+  // scratch (device): counts + counters + tile states
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  // derived field buffer for gcm_mesh_lattice / gcm_mesh_csg
+  float* field_buf = nullptr;
+  size_t field_bytes = 0;
+  float* blend_buf = nullptr;
+  size_t blend_bytes = 0;
+  // pinned host staging for count readback
+  gcm_counts* h_pinned = nullptr;
+};
+
+namespace gcm {
+
+gcm_status fail(gcm_ctx* ctx, gcm_status s, const char* fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    ctx->last_error = buf;
+  }
+  return s;
+}
+
+gcm_status cuda_fail(gcm_ctx* ctx, cudaError_t e, const char* what) {
+  if (e == cudaErrorMemoryAllocation) return fail(ctx, GCM_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+  return fail(ctx, GCM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define GCM_CUDA(ctx, call)                                 \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+gcm_status ensure_scratch(gcm_ctx* ctx, size_t bytes) {
+  // Growing allocates; under stream capture cudaMalloc fails and the error is
+  // returned, so callers that capture reserve first (gcm_ctx_reserve).
+  if (bytes <= ctx->scratch_bytes) return GCM_OK;
+  if (ctx->scratch) cudaFree(ctx->scratch);
+  ctx->scratch = nullptr;
+  ctx->scratch_bytes = 0;
+  const size_t sz = align_up(bytes + bytes / 4, 1 << 20);
+  GCM_CUDA(ctx, cudaMalloc(&ctx->scratch, sz));
+  ctx->scratch_bytes = sz;
+  return GCM_OK;
+}
+
+gcm_status ensure_buffer(gcm_ctx* ctx, float** buf, size_t* have, size_t bytes) {
+  if (bytes <= *have) return GCM_OK;
+  if (*buf) cudaFree(*buf);
+  *buf = nullptr;
+  *have = 0;
+  const size_t sz = align_up(bytes, 1 << 20);
+  GCM_CUDA(ctx, cudaMalloc(reinterpret_cast<void**>(buf), sz));
+  *have = sz;
+  return GCM_OK;
+}
+
+void count_launch(gcm_ctx* ctx, uint64_t n) { ctx->launches.fetch_add(n, std::memory_order_relaxed); }
+
+gcm_status check_grid(gcm_ctx* ctx, const gcm_grid* g) {
+  if (!g) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "grid is NULL");
+  if (g->nx < 2 || g->ny < 2 || g->nz < 2)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "grid needs at least 2 samples per axis (got %u x %u x %u)", g->nx,
+                g->ny, g->nz);
+  if (g->nx > 16384 || g->ny > 65536 || g->nz > 65536)
+    return fail(ctx, GCM_ERR_NOT_SUPPORTED, "grid %u x %u x %u exceeds the supported extent", g->nx, g->ny, g->nz);
+  return GCM_OK;
+}
+
+// Tile shape of the fused mesh kernel: R whole voxel rows, about 2048 voxels,
+// within the shared-memory budget.
+struct MeshPlan {
+  uint32_t rows, tiles_per_plane, blocks;
+  uint64_t ntiles;
+  size_t smem;
+};
+
+gcm_status plan_mesh(gcm_ctx* ctx, const gcm_grid* g, bool band, MeshPlan* out) {
+  const uint32_t vx = g->nx - 1, vy = g->ny - 1, vz = g->nz - 1;
+  uint32_t rows = std::max<uint32_t>(1, (kTargetVoxelsPerTile + vx / 2) / vx);
+  rows = std::min(rows, vy);
+  const size_t budget = std::min(kMeshSmemBudget, ctx->smem_optin);
+  while (rows > 1 && mesh_smem_bytes(g->nx, rows, band) > budget) --rows;
+  const size_t smem = mesh_smem_bytes(g->nx, rows, band);
+  if (smem > ctx->smem_optin)
+    return fail(ctx, GCM_ERR_NOT_SUPPORTED, "grid rows of %u samples do not fit in shared memory", g->nx);
+  out->rows = rows;
+  out->tiles_per_plane = (vy + rows - 1) / rows;
+  out->ntiles = (uint64_t)out->tiles_per_plane * vz;
+  out->smem = smem;
+  if (out->ntiles >= (1ull << 31)) return fail(ctx, GCM_ERR_NOT_SUPPORTED, "too many tiles");
+  out->blocks = 0;
+  return GCM_OK;
+}
+
+gcm_status launch_mesh_kernel(gcm_ctx* ctx, bool band, bool emit, MeshParams& p, MeshPlan& plan, cudaStream_t st) {
+  int per_sm = 0;
+  GCM_CUDA(ctx, gcm::mesh_prepare(band, emit, plan.smem, &per_sm));
+  per_sm = std::max(per_sm, 1);
+  const uint64_t want = (uint64_t)ctx->sm_count * (uint64_t)per_sm;
+  plan.blocks = (uint32_t)std::min<uint64_t>(want, plan.ntiles);
+  GCM_CUDA(ctx, gcm::launch_mesh(band, emit, p, plan.blocks, plan.smem, st));
+  count_launch(ctx, 1);
+  return GCM_OK;
+}
+
+// Scratch for one mesh call: [counts 64 B][counter 64 B][tile states].
+struct MeshScratch {
+  gcm_counts* counts;
+  uint32_t* counter;
+  uint64_t* status;
+  size_t bytes;
+};
+
+MeshScratch carve_mesh_scratch(void* base, uint64_t ntiles) {
+  MeshScratch s;
+  char* b = static_cast<char*>(base);
+  s.counts = reinterpret_cast<gcm_counts*>(b);
+  s.counter = reinterpret_cast<uint32_t*>(b + 64);
+  s.status = reinterpret_cast<uint64_t*>(b + 128);
+  s.bytes = 128 + ntiles * sizeof(uint64_t);
+  return s;
+}
+
+gcm_status status_of(gcm_ctx* ctx, const gcm_counts& c) {
+  switch (c.status) {
+    case 0: return GCM_OK;
+    case GCM_ERR_OUTPUT_OVERFLOW:
+      return fail(ctx, GCM_ERR_OUTPUT_OVERFLOW, "output capacity too small: %llu vertices needed",
+                  (unsigned long long)c.total_verts);
+    case GCM_ERR_DEVICE_TIMEOUT: return fail(ctx, GCM_ERR_DEVICE_TIMEOUT, "a device-side wait exceeded its limit");
+    default: return fail(ctx, GCM_ERR_CUDA, "device reported status %u", c.status);
+  }
+}
+
+// Core of every fused extraction.  counts_out: device pointer receiving the
+// counts (the context's scratch when null).  The caller zeroes nothing.
+gcm_status mesh_core(gcm_ctx* ctx, const float* f, const float* gfield, const gcm_grid* grid, float iso, float lo,
+                     float hi, bool band, bool emit, float* pos, float* norm, uint64_t capacity,
+                     gcm_counts* counts_out, cudaStream_t st, gcm_counts** counts_used) {
+  if (((reinterpret_cast<uintptr_t>(pos) | reinterpret_cast<uintptr_t>(norm)) & 15u) != 0)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "position and normal buffers must be 16-byte aligned");
+  MeshPlan plan;
+  gcm_status s = plan_mesh(ctx, grid, band, &plan);
+  if (s) return s;
+  const size_t need = 128 + plan.ntiles * sizeof(uint64_t);
+  s = ensure_scratch(ctx, need);
+  if (s) return s;
+  MeshScratch sc = carve_mesh_scratch(ctx->scratch, plan.ntiles);
+  gcm_counts* cnt = counts_out ? counts_out : sc.counts;
+  GCM_CUDA(ctx, cudaMemsetAsync(ctx->scratch, 0, emit ? sc.bytes : 128, st));
+  if (counts_out) GCM_CUDA(ctx, cudaMemsetAsync(counts_out, 0, sizeof(gcm_counts), st));
+  MeshParams p{};
+  p.f = f;
+  p.g = gfield ? gfield : f;
+  p.nx = grid->nx;
+  p.ny = grid->ny;
+  p.nz = grid->nz;
+  p.rows = plan.rows;
+  p.tiles_per_plane = plan.tiles_per_plane;
+  p.ntiles = plan.ntiles;
+  p.bulk = ((reinterpret_cast<uintptr_t>(f) | reinterpret_cast<uintptr_t>(p.g)) & 15u) == 0;
+  for (int a = 0; a < 3; ++a) {
+    p.vs[a] = grid->voxel_size[a];
+    p.gc[a] = grid->grid_center[a];
+  }
+  p.iso = iso;
+  p.lo = lo;
+  p.hi = hi;
+  p.pos = reinterpret_cast<float4*>(pos);
+  p.norm = reinterpret_cast<float4*>(norm);
+  p.capacity = capacity;
+  p.tile_status = sc.status;
+  p.counter = sc.counter;
+  p.counts_dev = cnt;
+  p.status = &cnt->status;
+  p.wait_ns = ctx->wait_ns;
+  s = launch_mesh_kernel(ctx, band, emit, p, plan, st);
+  if (counts_used) *counts_used = cnt;
+  return s;
+}
+
+gcm_status read_counts(gcm_ctx* ctx, const gcm_counts* d, gcm_counts* h, cudaStream_t st) {
+  GCM_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned, d, sizeof(gcm_counts), cudaMemcpyDeviceToHost, st));
+  GCM_CUDA(ctx, cudaStreamSynchronize(st));
+  *h = *ctx->h_pinned;
+  return status_of(ctx, *h);
+}
+
+uint32_t grid_blocks(gcm_ctx* ctx, uint64_t work, uint32_t threads, uint32_t per_sm = 8) {
+  const uint64_t want = (work + threads - 1) / threads;
+  const uint64_t cap = (uint64_t)ctx->sm_count * per_sm;
+  return (uint32_t)std::max<uint64_t>(1, std::min(want, cap));
+}
+
+}  // namespace gcm
+
+using namespace gcm;
+
+extern "C" {
+
+int gcm_abi_version(void) { return GCM_ABI_VERSION; }
+
+const char* gcm_status_string(gcm_status s) {
+  switch (s) {
+    case GCM_OK: return "ok";
+    case GCM_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case GCM_ERR_OUTPUT_OVERFLOW: return "output overflow";
+    case GCM_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+    case GCM_ERR_CUDA: return "CUDA error";
+    case GCM_ERR_OUT_OF_MEMORY: return "out of memory";
+    case GCM_ERR_NOT_SUPPORTED: return "not supported";
+    case GCM_ERR_IO: return "I/O error";
+    case GCM_ERR_REJECTED: return "rejected";
+    case GCM_ERR_CANCELLED: return "cancelled";
+    case GCM_ERR_BUSY: return "busy";
+  }
+  return "unknown status";
+}
+
+gcm_status gcm_ctx_create(int device, gcm_ctx** out) {
+  if (!out) return GCM_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return GCM_ERR_INVALID_ARGUMENT;
+  gcm_ctx* ctx = new gcm_ctx();
+  ctx->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+  int optin = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  ctx->smem_optin = (size_t)optin;
+  if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&ctx->h_pinned), sizeof(gcm_counts));
+  if (e != cudaSuccess) {
+    delete ctx;
+    return e == cudaErrorMemoryAllocation ? GCM_ERR_OUT_OF_MEMORY : GCM_ERR_CUDA;
+  }
+  *out = ctx;
+  return GCM_OK;
+}
+
+gcm_status gcm_ctx_destroy(gcm_ctx* ctx) {
+  if (!ctx) return GCM_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->scratch) cudaFree(ctx->scratch);
+  if (ctx->field_buf) cudaFree(ctx->field_buf);
+  if (ctx->blend_buf) cudaFree(ctx->blend_buf);
+  if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  delete ctx;
+  return GCM_OK;
+}
+
+const char* gcm_ctx_last_error(const gcm_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+gcm_status gcm_ctx_reserve(gcm_ctx* ctx, uint64_t max_points) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  // one tile holds at least one voxel row; bound tiles by the voxel count
+  const size_t need = 128 + (size_t)max_points * sizeof(uint64_t) / 64 + (1 << 16);
+  gcm_status s = ensure_scratch(ctx, need);
+  if (s) return s;
+  return ensure_buffer(ctx, &ctx->field_buf, &ctx->field_bytes, (size_t)max_points * sizeof(float));
+}
+
+gcm_status gcm_ctx_set_wait_limit(gcm_ctx* ctx, uint64_t ns) {
+  if (!ctx || ns == 0) return GCM_ERR_INVALID_ARGUMENT;
+  ctx->wait_ns = ns;
+  return GCM_OK;
+}
+
+uint64_t gcm_ctx_launch_count(const gcm_ctx* ctx) { return ctx ? ctx->launches.load() : 0; }
+
+// ------------------------------------------------------------------ mesh
+
+gcm_status gcm_mesh_field(gcm_ctx* ctx, const float* d_field, const gcm_grid* grid, float iso, float* d_pos,
+                          float* d_norm, uint64_t capacity, gcm_counts* h_counts, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_field || !h_counts || (capacity && (!d_pos || !d_norm)))
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_mesh_field: NULL field, counts or outputs");
+  gcm_status s = check_grid(ctx, grid);
+  if (s) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  gcm_counts* used = nullptr;
+  s = mesh_core(ctx, d_field, nullptr, grid, iso, 0, 0, false, true, d_pos, d_norm, capacity, nullptr, st, &used);
+  if (s) return s;
+  return read_counts(ctx, used, h_counts, st);
+}
+
+gcm_status gcm_mesh_field_async(gcm_ctx* ctx, const float* d_field, const gcm_grid* grid, float iso, float* d_pos,
+                                float* d_norm, uint64_t capacity, gcm_counts* d_counts, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_field || !d_counts || (capacity && (!d_pos || !d_norm)))
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_mesh_field_async: NULL field, counts or outputs");
+  gcm_status s = check_grid(ctx, grid);
+  if (s) return s;
+  return mesh_core(ctx, d_field, nullptr, grid, iso, 0, 0, false, true, d_pos, d_norm, capacity, d_counts,
+                   static_cast<cudaStream_t>(stream), nullptr);
+}
+
+gcm_status gcm_count_field(gcm_ctx* ctx, const float* d_field, const gcm_grid* grid, float iso, gcm_counts* h_counts,
+                           gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_field || !h_counts) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_count_field: NULL argument");
+  gcm_status s = check_grid(ctx, grid);
+  if (s) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  gcm_counts* used = nullptr;
+  s = mesh_core(ctx, d_field, nullptr, grid, iso, 0, 0, false, false, nullptr, nullptr, 0, nullptr, st, &used);
+  if (s) return s;
+  return read_counts(ctx, used, h_counts, st);
+}
+
+gcm_status gcm_mesh_band(gcm_ctx* ctx, const float* d_label, const float* d_norm_field, const gcm_grid* grid, float iso,
+                         float lo, float hi, float* d_pos, float* d_norm, uint64_t capacity, gcm_counts* h_counts,
+                         gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_label || !d_norm_field || !h_counts || (capacity && (!d_pos || !d_norm)))
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_mesh_band: NULL argument");
+  gcm_status s = check_grid(ctx, grid);
+  if (s) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  gcm_counts* used = nullptr;
+  s = mesh_core(ctx, d_label, d_norm_field, grid, iso, lo, hi, true, true, d_pos, d_norm, capacity, nullptr, st, &used);
+  if (s) return s;
+  return read_counts(ctx, used, h_counts, st);
+}
+
+// ------------------------------------------------------------ staged form
+
+gcm_status gcm_mc_classify(gcm_ctx* ctx, const float* d_field, const gcm_grid* grid, float iso, uint32_t* d_verts,
+                           uint32_t* d_occ, uint8_t* d_cube, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_field) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_mc_classify: NULL field");
+  gcm_status s = check_grid(ctx, grid);
+  if (s) return s;
+  const uint64_t nvox = (uint64_t)(grid->nx - 1) * (grid->ny - 1) * (grid->nz - 1);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  GCM_CUDA(ctx, gcm::launch_classify(d_field, grid->nx, grid->ny, nvox, iso, d_verts, d_occ, d_cube,
+                                      grid_blocks(ctx, nvox, 256), st));
+  count_launch(ctx, 1);
+  return GCM_OK;
+}
+
+gcm_status gcm_scan_exclusive_u32(gcm_ctx* ctx, const uint32_t* d_in, uint32_t* d_out, uint64_t n, uint64_t* h_total,
+                                  gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (n == 0) {
+    if (h_total) *h_total = 0;
+    return GCM_OK;
+  }
+  if (!d_in || !d_out) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_scan_exclusive_u32: NULL array");
+  const uint64_t tile = scan_tile_elems();
+  const uint64_t ntiles = (n + tile - 1) / tile;
+  if (ntiles >= (1ull << 31)) return fail(ctx, GCM_ERR_NOT_SUPPORTED, "scan too long");
+  gcm_status s = ensure_scratch(ctx, 128 + ntiles * 8);
+  if (s) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* b = static_cast<char*>(ctx->scratch);
+  gcm_counts* cnt = reinterpret_cast<gcm_counts*>(b);
+  GCM_CUDA(ctx, cudaMemsetAsync(b, 0, 128 + ntiles * 8, st));
+  ScanParams p{};
+  p.in = d_in;
+  p.out = d_out;
+  p.n = n;
+  p.ntiles = ntiles;
+  p.tile_status = reinterpret_cast<uint64_t*>(b + 128);
+  p.counter = reinterpret_cast<uint32_t*>(b + 64);
+  p.total = &cnt->total_verts;
+  p.status = &cnt->status;
+  p.wait_ns = ctx->wait_ns;
+  const uint32_t blocks = (uint32_t)std::min<uint64_t>(ntiles, (uint64_t)ctx->sm_count * 8);
+  GCM_CUDA(ctx, gcm::launch_scan(p, blocks, st));
+  count_launch(ctx, 1);
+  if (!h_total) return GCM_OK;
+  gcm_counts h{};
+  s = read_counts(ctx, cnt, &h, st);
+  *h_total = h.total_verts;
+  return s;
+}
+
+gcm_status gcm_mc_compact(gcm_ctx* ctx, const uint32_t* d_occ, const uint32_t* d_scan, uint64_t n, uint32_t* d_out,
+                          gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (n == 0) return GCM_OK;
+  if (!d_occ || !d_scan || !d_out) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_mc_compact: NULL array");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  GCM_CUDA(ctx, gcm::launch_compact(d_occ, d_scan, n, d_out, grid_blocks(ctx, n, 256), st));
+  count_launch(ctx, 1);
+  return GCM_OK;
+}
+
+gcm_status gcm_mc_generate(gcm_ctx* ctx, const float* d_field, const gcm_grid* grid, float iso,
+                           const uint32_t* d_compacted, uint64_t active, const uint32_t* d_verts_scan, float* d_pos,
+                           float* d_norm, uint64_t capacity, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  gcm_status s = check_grid(ctx, grid);
+  if (s) return s;
+  if (active == 0) return GCM_OK;
+  if (!d_field || !d_compacted || !d_verts_scan || !d_pos || !d_norm)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_mc_generate: NULL argument");
+  if (((reinterpret_cast<uintptr_t>(d_pos) | reinterpret_cast<uintptr_t>(d_norm)) & 15u) != 0)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "position and normal buffers must be 16-byte aligned");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  s = ensure_scratch(ctx, 128);
+  if (s) return s;
+  gcm_counts* cnt = static_cast<gcm_counts*>(ctx->scratch);
+  GCM_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(gcm_counts), st));
+  GenerateParams p{};
+  p.f = d_field;
+  p.g = d_field;
+  p.nx = grid->nx;
+  p.ny = grid->ny;
+  p.nz = grid->nz;
+  for (int a = 0; a < 3; ++a) {
+    p.vs[a] = grid->voxel_size[a];
+    p.gc[a] = grid->grid_center[a];
+  }
+  p.iso = iso;
+  p.compacted = d_compacted;
+  p.active = active;
+  p.verts_scan = d_verts_scan;
+  p.pos = reinterpret_cast<float4*>(d_pos);
+  p.norm = reinterpret_cast<float4*>(d_norm);
+  p.capacity = capacity;
+  p.status = &cnt->status;
+  GCM_CUDA(ctx, gcm::launch_generate(false, p, grid_blocks(ctx, active, 128, 16), st));
+  count_launch(ctx, 1);
+  gcm_counts h{};
+  return read_counts(ctx, cnt, &h, st);
+}
+
+// ------------------------------------------------------------------ fields
+
+gcm_status gcm_field_unit_cell(gcm_ctx* ctx, uint32_t type, uint32_t nx, uint32_t ny, uint32_t nz, float* d_out,
+                               gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_out || type > 5 || nx < 2 || ny < 2 || nz < 2)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_field_unit_cell: bad argument");
+  const uint64_t n = (uint64_t)nx * ny * nz;
+  GCM_CUDA(ctx, gcm::launch_unit_cell(type, nx, ny, nz, d_out, grid_blocks(ctx, n, 256),
+                                       static_cast<cudaStream_t>(stream)));
+  count_launch(ctx, 1);
+  return GCM_OK;
+}
+
+static gcm_status lattice_params(gcm_ctx* ctx, const gcm_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz,
+                                 LatticeParams* p) {
+  if (!L || !L->d_period || !L->d_type) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "lattice: NULL period or type");
+  if (L->cx == 0 || L->cy == 0 || L->cz == 0) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "lattice: empty control grid");
+  if (L->mode > 1) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "lattice: unknown grading mode %u", L->mode);
+  if ((uint64_t)L->cx * L->cy * L->cz > (1u << 24)) return fail(ctx, GCM_ERR_NOT_SUPPORTED, "control grid too large");
+  *p = LatticeParams{};
+  p->mode = L->mode;
+  p->cx = L->cx;
+  p->cy = L->cy;
+  p->cz = L->cz;
+  p->period = L->d_period;
+  p->euler = L->d_euler;
+  p->thickness = L->d_thickness;
+  p->type = L->d_type;
+  const uint32_t c[3] = {L->cx, L->cy, L->cz}, n[3] = {nx, ny, nz};
+  for (int a = 0; a < 3; ++a) {
+    p->origin[a] = L->origin[a];
+    p->scale[a] = (c[a] > 1 && n[a] > 1) ? (float)(c[a] - 1) / (float)(n[a] - 1) : 0.0f;
+    p->anchor[a] = (c[a] > 1) ? (float)(n[a] - 1) / (float)(c[a] - 1) : 0.0f;
+  }
+  p->nx = nx;
+  p->ny = ny;
+  p->nz = nz;
+  return GCM_OK;
+}
+
+static gcm_status run_lattice(gcm_ctx* ctx, LatticeParams& p, float* d_out, cudaStream_t st) {
+  p.out = d_out;
+  const uint64_t n = (uint64_t)p.nx * p.ny * p.nz;
+  if (p.mode == GCM_GRADE_BLEND) {
+    const uint64_t nc = (uint64_t)p.cx * p.cy * p.cz;
+    gcm_status s = ensure_buffer(ctx, &ctx->blend_buf, &ctx->blend_bytes, nc * 12 * sizeof(float));
+    if (s) return s;
+    GCM_CUDA(ctx, gcm::launch_lattice(p, ctx->blend_buf, grid_blocks(ctx, nc, 256), grid_blocks(ctx, n, 256), st));
+    count_launch(ctx, 2);
+  } else {
+    GCM_CUDA(ctx, gcm::launch_lattice(p, nullptr, 0, grid_blocks(ctx, n, 256), st));
+    count_launch(ctx, 1);
+  }
+  return GCM_OK;
+}
+
+gcm_status gcm_field_lattice(gcm_ctx* ctx, const gcm_lattice* lattice, uint32_t nx, uint32_t ny, uint32_t nz,
+                             float* d_out, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_out || nx == 0 || ny == 0 || nz == 0) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_field_lattice: bad output");
+  LatticeParams p;
+  gcm_status s = lattice_params(ctx, lattice, nx, ny, nz, &p);
+  if (s) return s;
+  return run_lattice(ctx, p, d_out, static_cast<cudaStream_t>(stream));
+}
+
+gcm_status gcm_mesh_lattice(gcm_ctx* ctx, const gcm_lattice* lattice, const gcm_grid* grid, float iso, float* d_pos,
+                            float* d_norm, uint64_t capacity, gcm_counts* h_counts, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!h_counts || (capacity && (!d_pos || !d_norm)))
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_mesh_lattice: NULL counts or outputs");
+  gcm_status s = check_grid(ctx, grid);
+  if (s) return s;
+  LatticeParams p;
+  s = lattice_params(ctx, lattice, grid->nx, grid->ny, grid->nz, &p);
+  if (s) return s;
+  const uint64_t n = (uint64_t)grid->nx * grid->ny * grid->nz;
+  s = ensure_buffer(ctx, &ctx->field_buf, &ctx->field_bytes, n * sizeof(float));
+  if (s) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  s = run_lattice(ctx, p, ctx->field_buf, st);
+  if (s) return s;
+  gcm_counts* used = nullptr;
+  s = mesh_core(ctx, ctx->field_buf, nullptr, grid, iso, 0, 0, false, true, d_pos, d_norm, capacity, nullptr, st, &used);
+  if (s) return s;
+  return read_counts(ctx, used, h_counts, st);
+}
+
+gcm_status gcm_field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
+                         uint32_t nx, uint32_t ny, uint32_t nz, float* d_out, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_prims || !frame || !d_out || n_prims == 0 || nx == 0 || ny == 0 || nz == 0)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_field_csg: bad argument");
+  if (n_prims > 256) return fail(ctx, GCM_ERR_NOT_SUPPORTED, "gcm_field_csg: at most 256 primitives");
+  CsgParams p{};
+  p.prims = d_prims;
+  p.n = n_prims;
+  for (int a = 0; a < 3; ++a) {
+    p.origin[a] = frame->origin[a];
+    p.spacing[a] = frame->spacing[a];
+  }
+  p.nx = nx;
+  p.ny = ny;
+  p.nz = nz;
+  p.out = d_out;
+  const uint64_t n = (uint64_t)nx * ny * nz;
+  GCM_CUDA(ctx, gcm::launch_csg(p, grid_blocks(ctx, n, 256, 4), static_cast<cudaStream_t>(stream)));
+  count_launch(ctx, 1);
+  return GCM_OK;
+}
+
+gcm_status gcm_mesh_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
+                        const gcm_grid* grid, float iso, float* d_pos, float* d_norm, uint64_t capacity,
+                        gcm_counts* h_counts, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!h_counts || (capacity && (!d_pos || !d_norm)))
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_mesh_csg: NULL counts or outputs");
+  gcm_status s = check_grid(ctx, grid);
+  if (s) return s;
+  const uint64_t n = (uint64_t)grid->nx * grid->ny * grid->nz;
+  s = ensure_buffer(ctx, &ctx->field_buf, &ctx->field_bytes, n * sizeof(float));
+  if (s) return s;
+  s = gcm_field_csg(ctx, d_prims, n_prims, frame, grid->nx, grid->ny, grid->nz, ctx->field_buf, stream);
+  if (s) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  gcm_counts* used = nullptr;
+  s = mesh_core(ctx, ctx->field_buf, nullptr, grid, iso, 0, 0, false, true, d_pos, d_norm, capacity, nullptr, st, &used);
+  if (s) return s;
+  return read_counts(ctx, used, h_counts, st);
+}
+
+gcm_status gcm_normalise_band(gcm_ctx* ctx, const float* d_field, uint32_t nx, uint32_t ny, uint32_t nz, float lo,
+                              float hi, float* d_label, float* d_norm_field, float* h_minmax, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_field || !d_label || !d_norm_field || nx == 0 || ny == 0 || nz == 0)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_normalise_band: bad argument");
+  gcm_status s = ensure_scratch(ctx, 128);
+  if (s) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned int* enc = reinterpret_cast<unsigned int*>(static_cast<char*>(ctx->scratch) + 64);
+  // key(0.0f) = 0x80000000 for both min and max
+  const unsigned int init[2] = {0x80000000u, 0x80000000u};
+  GCM_CUDA(ctx, cudaMemcpyAsync(enc, init, sizeof(init), cudaMemcpyHostToDevice, st));
+  const uint64_t n = (uint64_t)nx * ny * nz;
+  GCM_CUDA(ctx, gcm::launch_normalise(d_field, nx, ny, nz, enc, lo, hi, d_label, d_norm_field,
+                                       grid_blocks(ctx, n, 256, 4), st));
+  count_launch(ctx, 2);
+  if (h_minmax) {
+    unsigned int k[2];
+    GCM_CUDA(ctx, cudaMemcpyAsync(k, enc, sizeof(k), cudaMemcpyDeviceToHost, st));
+    GCM_CUDA(ctx, cudaStreamSynchronize(st));
+    for (int i = 0; i < 2; ++i) {
+      const unsigned int u = (k[i] & 0x80000000u) ? (k[i] & 0x7fffffffu) : ~k[i];
+      std::memcpy(&h_minmax[i], &u, 4);
+    }
+  }
+  return GCM_OK;
+}
+
+gcm_status gcm_test_lookback_stall(gcm_ctx* ctx, uint32_t ntiles, uint32_t stall_tile, uint64_t wait_ns,
+                                   uint64_t* d_prefix_out, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_prefix_out || ntiles == 0 || ntiles > (1u << 20) || wait_ns == 0 || wait_ns > 10000000000ull)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_test_lookback_stall: bad argument");
+  gcm_status s = ensure_scratch(ctx, 128 + (size_t)ntiles * 8);
+  if (s) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* b = static_cast<char*>(ctx->scratch);
+  GCM_CUDA(ctx, cudaMemsetAsync(b, 0, 128 + (size_t)ntiles * 8, st));
+  gcm_counts* cnt = reinterpret_cast<gcm_counts*>(b);
+  const uint32_t blocks = std::min<uint32_t>(ntiles, (uint32_t)ctx->sm_count * 4);
+  GCM_CUDA(ctx, gcm::launch_lookback_stall(ntiles, stall_tile, wait_ns, reinterpret_cast<uint64_t*>(b + 128),
+                                           reinterpret_cast<uint32_t*>(b + 64), d_prefix_out, &cnt->status, blocks,
+                                           st));
+  count_launch(ctx, 1);
+  gcm_counts h{};
+  return read_counts(ctx, cnt, &h, st);
+}
+
+}  // extern "C"

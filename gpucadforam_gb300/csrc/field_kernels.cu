@@ -1,0 +1,473 @@
+// Field evaluation kernels for sm_103a: TPMS unit cell, graded TPMS lattices,
+// primitive CSG scenes and the band normalisation.
+//
+// Operation order follows the reference's expressions and is written with
+// explicit IEEE intrinsics, so the only difference from a correctly rounded
+// evaluation is the accuracy of the CUDA trig functions.
+#include <cuda_runtime.h>
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "gcm_device.cuh"
+#include "gcm_kernels.h"
+
+namespace gcm {
+
+namespace {
+
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
+
+// TPMS from the sines and cosines of the phase (X, Y, Z).  Types: 0 gyroid,
+// 1 Schwarz-P, 2 FRD, 3 IWP, 5 Schwarz-D (diamond), after
+// src/lattice_files/Fft_lattice.cu:59-85.
+__device__ __forceinline__ float tpms_sc(uint32_t type, float sX, float cX, float sY, float cY, float sZ, float cZ) {
+  switch (type) {
+    case 0: return fa(fa(fm(sX, cY), fm(sY, cZ)), fm(sZ, cX));
+    case 1: return fa(fa(cX, cY), cZ);
+    case 2: {
+      const float c2X = fs(fm(fm(2.0f, cX), cX), 1.0f), c2Y = fs(fm(fm(2.0f, cY), cY), 1.0f),
+                  c2Z = fs(fm(fm(2.0f, cZ), cZ), 1.0f);
+      return fs(fm(4.0f, fm(fm(cX, cY), cZ)), fa(fa(fm(c2X, c2Y), fm(c2Y, c2Z)), fm(c2Z, c2X)));
+    }
+    case 3: {
+      const float c2X = fs(fm(fm(2.0f, cX), cX), 1.0f), c2Y = fs(fm(fm(2.0f, cY), cY), 1.0f),
+                  c2Z = fs(fm(fm(2.0f, cZ), cZ), 1.0f);
+      return fs(fm(2.0f, fa(fa(fm(cX, cY), fm(cY, cZ)), fm(cZ, cX))), fa(fa(c2X, c2Y), c2Z));
+    }
+    default: return fs(fm(fm(cX, cY), cZ), fm(fm(sX, sY), sZ));
+  }
+}
+
+// Euler basis rows, ZYX convention of src/Modelling.cu:401-407.
+__device__ __forceinline__ void euler_rows(float ax, float ay, float az, float R[9]) {
+  float sx, cx, sy, cy, sz, cz;
+  sincosf(ax, &sx, &cx);
+  sincosf(ay, &sy, &cy);
+  sincosf(az, &sz, &cz);
+  R[0] = fm(cz, cy);
+  R[1] = fs(fm(fm(cz, sy), sx), fm(sz, cx));
+  R[2] = fa(fm(fm(cz, sy), cx), fm(sz, sx));
+  R[3] = fm(sz, cy);
+  R[4] = fa(fm(fm(sz, sy), sx), fm(cz, cx));
+  R[5] = fs(fm(fm(sz, sy), cx), fm(cz, sx));
+  R[6] = -sy;
+  R[7] = fm(cy, sx);
+  R[8] = fm(cy, cx);
+}
+
+// One lattice: phase X = (R q) * h in half-turns (h = 2 / period).
+__device__ __forceinline__ float lattice_value(uint32_t type, const float R[9], float h, const float q[3],
+                                               float thick) {
+  float s[3], c[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const float X = fm(__fmaf_rn(R[3 * r + 2], q[2], __fmaf_rn(R[3 * r + 1], q[1], fm(R[3 * r], q[0]))), h);
+    sincospif(X, &s[r], &c[r]);
+  }
+  return fs(tpms_sc(type, s[0], c[0], s[1], c[1], s[2], c[2]), thick);
+}
+
+struct Cell {
+  int i0[3];
+  float f[3];
+  int nearest[3];
+};
+
+__device__ __forceinline__ Cell locate(const uint32_t pt[3], const uint32_t c[3], const float s[3]) {
+  Cell k;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float cu = fm((float)pt[a], s[a]);
+    int i0 = (int)cu;
+    if (c[a] == 1) i0 = 0;
+    else if (i0 > (int)c[a] - 2) i0 = (int)c[a] - 2;
+    k.i0[a] = i0;
+    k.f[a] = c[a] == 1 ? 0.0f : fs(cu, (float)i0);
+    int nn = (int)fa(cu, 0.5f);
+    if (nn > (int)c[a] - 1) nn = (int)c[a] - 1;
+    k.nearest[a] = nn;
+  }
+  return k;
+}
+
+__device__ __forceinline__ uint32_t cidx(int x, int y, int z, const uint32_t c[3]) {
+  return (uint32_t)x + c[0] * ((uint32_t)y + c[1] * (uint32_t)z);
+}
+
+__device__ __forceinline__ float lerpf(float u, float v, float t) { return __fmaf_rn(t, fs(v, u), u); }
+
+__device__ __forceinline__ float trilinear(const float* __restrict__ a, const Cell& k, const uint32_t c[3]) {
+  if (!a) return 0.0f;
+  const int x0 = k.i0[0], y0 = k.i0[1], z0 = k.i0[2];
+  const int x1 = c[0] > 1 ? x0 + 1 : 0, y1 = c[1] > 1 ? y0 + 1 : 0, z1 = c[2] > 1 ? z0 + 1 : 0;
+  const float c00 = lerpf(__ldg(a + cidx(x0, y0, z0, c)), __ldg(a + cidx(x1, y0, z0, c)), k.f[0]);
+  const float c10 = lerpf(__ldg(a + cidx(x0, y1, z0, c)), __ldg(a + cidx(x1, y1, z0, c)), k.f[0]);
+  const float c01 = lerpf(__ldg(a + cidx(x0, y0, z1, c)), __ldg(a + cidx(x1, y0, z1, c)), k.f[0]);
+  const float c11 = lerpf(__ldg(a + cidx(x0, y1, z1, c)), __ldg(a + cidx(x1, y1, z1, c)), k.f[0]);
+  return lerpf(lerpf(c00, c10, k.f[1]), lerpf(c01, c11, k.f[1]), k.f[2]);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// create_lattice_kernel (src/lattice_files/Fft_lattice.cu:11-93): the unit-cell
+// coordinate is formed in double and rounded to float, the products with the
+// literal 3.14 are double and rounded to float at the trig call, type 5 takes
+// its first factor through the double cos, type 4 sums double squares.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) unit_cell_kernel(uint32_t type, uint32_t nx, uint32_t ny, uint32_t nz,
+                                                        float* out) {
+  const uint64_t total = (uint64_t)nx * ny * nz;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t x = (uint32_t)(i % nx), y = (uint32_t)((i / nx) % ny), z = (uint32_t)(i / ((uint64_t)nx * ny));
+    const float xx = (float)(((x * 1.0) / (double)(nx - 1) - 0.5) / 0.5);
+    const float yy = (float)(((y * 1.0) / (double)(ny - 1) - 0.5) / 0.5);
+    const float zz = (float)(((z * 1.0) / (double)(nz - 1) - 0.5) / 0.5);
+    float aa = 0.0f;
+    switch (type) {
+      case 0:
+        aa = fa(fa(fm(cosf((float)(3.14 * xx)), sinf((float)(3.14 * yy))),
+                   fm(cosf((float)(3.14 * yy)), sinf((float)(3.14 * zz)))),
+                fm(cosf((float)(3.14 * zz)), sinf((float)(3.14 * xx))));
+        break;
+      case 1: aa = fa(fa(cosf((float)(3.14 * xx)), cosf((float)(3.14 * yy))), cosf((float)(3.14 * zz))); break;
+      case 2:
+        aa = fs(fm(4.0f, fm(fm(cosf(xx), cosf(yy)), cosf(zz))),
+                fa(fa(fm(cosf(fm(2.0f, xx)), cosf(fm(2.0f, yy))), fm(cosf(fm(2.0f, yy)), cosf(fm(2.0f, zz)))),
+                   fm(cosf(fm(2.0f, zz)), cosf(fm(2.0f, xx)))));
+        break;
+      case 3: {
+        const float cx = cosf((float)(3.14 * xx)), cy = cosf((float)(3.14 * yy)), cz = cosf((float)(3.14 * zz));
+        aa = fs(fm(2.0f, fa(fa(fm(cx, cy), fm(cy, cz)), fm(cz, cx))),
+                fa(fa(cosf((float)(2 * 3.14 * xx)), cosf((float)(2 * 3.14 * yy))), cosf((float)(2 * 3.14 * zz))));
+        break;
+      }
+      case 4: {
+        const double x2 = (double)fm(xx, xx), y2 = (double)yy * (double)yy, z2 = (double)zz * (double)zz;
+        const double xd2 = (double)xx * (double)xx;
+        aa = (float)fmin(fmin(x2 + y2, y2 + z2), z2 + xd2);
+        break;
+      }
+      case 5: {
+        // cos(3.14 x) is the double cos, so the product runs in double left to right
+        const double prod = cos(3.14 * xx) * (double)cosf((float)(3.14 * yy)) * (double)cosf((float)(3.14 * zz));
+        const float sss = fm(fm(sinf((float)(3.14 * xx)), sinf((float)(3.14 * yy))), sinf((float)(3.14 * zz)));
+        aa = (float)(prod - (double)sss);
+        break;
+      }
+      default: aa = 0.0f;
+    }
+    out[i] = aa;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Graded lattices.
+// ---------------------------------------------------------------------------
+
+// Blend mode setup: per control point the rotation rows, 2/period, thickness
+// and type, 12 words each.
+__global__ void __launch_bounds__(256) lattice_prep_kernel(LatticeParams p, float* blend_out) {
+  const uint32_t n = p.cx * p.cy * p.cz;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float R[9];
+    const float ax = p.euler ? p.euler[i] : 0.0f, ay = p.euler ? p.euler[n + i] : 0.0f,
+                az = p.euler ? p.euler[2 * n + i] : 0.0f;
+    euler_rows(ax, ay, az, R);
+    float* o = blend_out + 12 * (uint64_t)i;
+    for (int k = 0; k < 9; ++k) o[k] = R[k];
+    o[9] = __fdiv_rn(2.0f, p.period[i]);
+    o[10] = p.thickness ? p.thickness[i] : 0.0f;
+    o[11] = __uint_as_float((uint32_t)p.type[i]);
+  }
+}
+
+__global__ void __launch_bounds__(256) lattice_params_kernel(LatticeParams p) {
+  const uint64_t total = (uint64_t)p.nx * p.ny * p.nz;
+  const uint32_t c[3] = {p.cx, p.cy, p.cz};
+  const float s[3] = {p.scale[0], p.scale[1], p.scale[2]};
+  const uint32_t nc = p.cx * p.cy * p.cz;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t pt[3] = {(uint32_t)(i % p.nx), (uint32_t)((i / p.nx) % p.ny), (uint32_t)(i / ((uint64_t)p.nx * p.ny))};
+    const Cell k = locate(pt, c, s);
+    const uint32_t type = __ldg(p.type + cidx(k.nearest[0], k.nearest[1], k.nearest[2], c));
+    const float P = trilinear(p.period, k, c);
+    const float ax = trilinear(p.euler, k, c);
+    const float ay = trilinear(p.euler ? p.euler + nc : nullptr, k, c);
+    const float az = trilinear(p.euler ? p.euler + 2 * nc : nullptr, k, c);
+    const float th = trilinear(p.thickness, k, c);
+    float R[9];
+    euler_rows(ax, ay, az, R);
+    const float q[3] = {fs((float)pt[0], p.origin[0]), fs((float)pt[1], p.origin[1]), fs((float)pt[2], p.origin[2])};
+    p.out[i] = lattice_value(type, R, __fdiv_rn(2.0f, P), q, th);
+  }
+}
+
+__global__ void __launch_bounds__(256) lattice_blend_kernel(LatticeParams p) {
+  const uint64_t total = (uint64_t)p.nx * p.ny * p.nz;
+  const uint32_t c[3] = {p.cx, p.cy, p.cz};
+  const float s[3] = {p.scale[0], p.scale[1], p.scale[2]};
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t pt[3] = {(uint32_t)(i % p.nx), (uint32_t)((i / p.nx) % p.ny), (uint32_t)(i / ((uint64_t)p.nx * p.ny))};
+    const Cell k = locate(pt, c, s);
+    float acc = 0.0f;
+#pragma unroll 1
+    for (int corner = 0; corner < 8; ++corner) {
+      const int d[3] = {corner & 1, (corner >> 1) & 1, (corner >> 2) & 1};
+      int g[3];
+      float w = 1.0f, q[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        g[a] = c[a] > 1 ? k.i0[a] + d[a] : 0;
+        const float wa = d[a] ? k.f[a] : fs(1.0f, k.f[a]);
+        w = (c[a] > 1) ? fm(w, wa) : (d[a] ? 0.0f : w);
+        const float anchor = c[a] > 1 ? fm((float)g[a], p.anchor[a]) : 0.0f;
+        q[a] = fs((float)pt[a], anchor);
+      }
+      if (w == 0.0f) continue;
+      const float* rec = p.blend + 12 * (uint64_t)cidx(g[0], g[1], g[2], c);
+      float R[9];
+#pragma unroll
+      for (int r = 0; r < 9; ++r) R[r] = __ldg(rec + r);
+      const float v = lattice_value(__float_as_uint(__ldg(rec + 11)), R, __ldg(rec + 9), q, __ldg(rec + 10));
+      acc = __fmaf_rn(w, v, acc);
+    }
+    p.out[i] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Primitive CSG.  Per primitive, the point-independent parts of the reference
+// kernels (rotation rows, normalised cylinder axis, its end point and length)
+// are computed once per CTA; they are the same values every reference thread
+// computes for itself.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct PrimPre {
+  uint32_t kind, op, flag, pad;
+  float c[3];
+  float p[6];
+  float R[9];      // rotated kinds
+  float axis[3];   // cylinder: unit axis
+  float end[3];    // cylinder: center + axis
+  float w3[3];     // cylinder: end - center
+  float dis;       // cylinder: |w3|
+};
+
+__device__ __forceinline__ float sqf(float x) { return fm(x, x); }
+
+__device__ void prim_setup(const gcm_primitive& q, PrimPre& o) {
+  o.kind = q.kind;
+  o.op = q.op;
+  o.flag = q.flag;
+  for (int a = 0; a < 3; ++a) o.c[a] = q.center[a];
+  for (int a = 0; a < 6; ++a) o.p[a] = q.p[a];
+  if (q.kind == 1) {
+    const float am = __fsqrt_rn(fa(fa(sqf(q.v3[0]), sqf(q.v3[1])), sqf(q.v3[2])));
+    for (int a = 0; a < 3; ++a) {
+      o.axis[a] = __fdiv_rn(q.v3[a], am);
+      o.end[a] = fa(o.axis[a], q.center[a]);
+      o.w3[a] = fs(o.end[a], q.center[a]);
+    }
+    o.dis = __fsqrt_rn(fa(fa(sqf(o.w3[0]), sqf(o.w3[1])), sqf(o.w3[2])));
+  } else if (q.kind >= 2) {
+    euler_rows(q.v3[0], q.v3[1], q.v3[2], o.R);
+  }
+}
+
+// Field of one primitive at scene point (X, Y, Z); src/Modelling.cu kernels.
+__device__ float prim_eval(const PrimPre& P, float X, float Y, float Z) {
+  switch (P.kind) {
+    case 0: {  // implicit_sphere_kernel :314-361
+      const float x = fs(X, P.c[0]), y = fs(Y, P.c[1]), z = fs(Z, P.c[2]);
+      const float r = P.p[0], t = P.p[1] * 0.5f;
+      const float d2 = fa(fa(sqf(x), sqf(y)), sqf(z));
+      if (P.flag) return fmaxf(-fs(d2, sqf(fs(r, t))), fs(d2, sqf(fa(r, t))));
+      return fs(d2, sqf(r));
+    }
+    case 1: {  // distance_from_line_kernel :244-302
+      const float r = P.p[0], td = P.p[1] * 0.5f, tda = P.p[2] * 0.5f;
+      const float w1x = fs(X, P.c[0]), w1y = fs(Y, P.c[1]), w1z = fs(Z, P.c[2]);
+      const float w2x = fs(X, P.end[0]), w2y = fs(Y, P.end[1]), w2z = fs(Z, P.end[2]);
+      const float dx = fs(fm(w1y, w2z), fm(w1z, w2y)), dy = fs(fm(w1z, w2x), fm(w1x, w2z)),
+                  dz = fs(fm(w1x, w2y), fm(w1y, w2x));
+      const float e = __fsqrt_rn(fa(fa(sqf(dx), sqf(dy)), sqf(dz)));
+      const float f = __fdiv_rn(e, P.dis);
+      const float g = fa(fa(fm(fs(X, P.c[0]), P.axis[0]), fm(fs(Y, P.c[1]), P.axis[1])), fm(fs(Z, P.c[2]), P.axis[2]));
+      const float fld1 = fmaxf(fs(g, tda), -fa(g, tda));
+      const float fld2 = P.flag ? fmaxf(fs(f, fa(r, td)), -fs(f, fs(r, td))) : fs(f, r);
+      return fmaxf(fld1, fld2);
+    }
+    default: {
+      const float x = fs(X, P.c[0]), y = fs(Y, P.c[1]), z = fs(Z, P.c[2]);
+      const float a = fa(fa(fm(x, P.R[0]), fm(y, P.R[1])), fm(z, P.R[2]));
+      const float b = fa(fa(fm(x, P.R[3]), fm(y, P.R[4])), fm(z, P.R[5]));
+      const float cc = fa(fa(fm(x, P.R[6]), fm(y, P.R[7])), fm(z, P.R[8]));
+      switch (P.kind) {
+        case 2: {  // implicit_cuboid_kernel :375-421
+          return fmaxf(fmaxf(fs(fabsf(a), P.p[0] * 0.5f), fs(fabsf(b), P.p[1] * 0.5f)), fs(fabsf(cc), P.p[2] * 0.5f));
+        }
+        case 3: {  // implicit_cuboid_shell_kernel :435-487
+          const float wx = P.p[0] * 0.5f, wy = P.p[1] * 0.5f, wz = P.p[2] * 0.5f, th = P.p[3];
+          const float f11 = fs(fabsf(a), wx), f12 = fs(fabsf(a), fs(wx, th));
+          const float f21 = fs(fabsf(b), wy), f22 = fs(fabsf(b), fs(wy, th));
+          return fmaxf(fmaxf(fmaxf(f11, f21), -fmaxf(f12, f22)), fs(fabsf(cc), wz));
+        }
+        case 4: {  // implicit_torus_kernel :569-616
+          const float side = fs(P.p[0], __fsqrt_rn(fa(sqf(a), sqf(b))));
+          return fa(fs(sqf(cc), sqf(P.p[1])), sqf(side));
+        }
+        case 5: {  // implicit_cone_kernel :631-683
+          const float br = P.p[0], hgt = P.p[1];
+          const float k2 = sqf(__fdiv_rn(hgt, br));
+          const float g = (float)((double)b - (double)hgt / 2.0);
+          const float h = (float)fmax(((double)g - (double)hgt / 2.0) * 100.0, ((double)g + (double)hgt / 2.0) * 100.0 * -1.0);
+          const float f1 = fs(fm(fa(sqf(a), sqf(cc)), k2), sqf(fs(b, hgt)));
+          return fmaxf(f1, h);
+        }
+        case 6: {  // implicit_cone_frustum_kernel :698-750
+          const float tr = P.p[0], brr = P.p[1], hgt = P.p[2];
+          const float rd = fm(__fdiv_rn(fs(hgt, b), hgt), fs(brr, tr));
+          const float g = (float)((double)b - (double)hgt / 2.0);
+          const float h = (float)fmax(((double)g - (double)hgt / 2.0) * 100.0, ((double)g + (double)hgt / 2.0) * 100.0 * -1.0);
+          const double rr = (double)fa(rd, tr);
+          const float f1 = (float)((double)fa(sqf(a), sqf(cc)) - rr * rr);
+          return fmaxf(f1, h);
+        }
+        default: {  // 7: implicit_pyramid_frustum_kernel :501-557
+          const float xwb = P.p[0] * 0.5f, xwt = P.p[1] * 0.5f, yh = P.p[2];
+          const float zwb = P.p[3] * 0.5f, zwt = P.p[4] * 0.5f;
+          const float ratio = __fdiv_rn(fs(yh, b), yh);
+          const float xw = fa(fm(ratio, fs(xwb, xwt)), xwt);
+          const float f1 = fs(fabsf(a), xw);
+          const float f2 = fs(fabsf(fs(b, __fdiv_rn(yh, 2.0f))), __fdiv_rn(yh, 2.0f));
+          const float zw = fa(fm(ratio, fs(zwb, zwt)), zwt);
+          const float f3 = fs(fabsf(cc), zw);
+          return fmaxf(fmaxf(f1, f2), f3);
+        }
+      }
+    }
+  }
+}
+
+}  // namespace
+
+constexpr int kMaxPrimsSmem = 256;
+
+__global__ void __launch_bounds__(256) csg_kernel(CsgParams p) {
+  __shared__ PrimPre s_pre[kMaxPrimsSmem];
+  const uint32_t n = p.n < kMaxPrimsSmem ? p.n : kMaxPrimsSmem;
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) prim_setup(p.prims[i], s_pre[i]);
+  __syncthreads();
+  const uint64_t total = (uint64_t)p.nx * p.ny * p.nz;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t px = (uint32_t)(i % p.nx), py = (uint32_t)((i / p.nx) % p.ny), pz = (uint32_t)(i / ((uint64_t)p.nx * p.ny));
+    const float X = fm(fs((float)px, p.origin[0]), p.spacing[0]);
+    const float Y = fm(fs((float)py, p.origin[1]), p.spacing[1]);
+    const float Z = fm(fs((float)pz, p.origin[2]), p.spacing[2]);
+    float f = INFINITY;
+    for (uint32_t k = 0; k < n; ++k) {
+      const float g = prim_eval(s_pre[k], X, Y, Z);
+      const uint32_t op = s_pre[k].op;
+      f = op == 1 ? fmaxf(f, -g) : (op == 2 ? fmaxf(f, g) : fminf(f, g));
+    }
+    p.out[i] = f;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Band normalisation (GPU_buffer_normalise_four, src/lattice_files/Gratings.cu:
+// 1579-1617).  Floats are mapped to order-preserving unsigned keys for the
+// atomic min/max; both start from the key of 0.0 (the reference's reduction
+// starts from {0,0}, Min_reduction_lattice :1439-1495).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned int f2key(float f) {
+  const unsigned int u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key2f(unsigned int k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+__global__ void __launch_bounds__(256) minmax_kernel(const float* f, uint64_t n, unsigned int* enc_min,
+                                                     unsigned int* enc_max) {
+  unsigned int lo = f2key(0.0f), hi = f2key(0.0f);
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned int k = f2key(__ldg(f + i));
+    lo = min(lo, k);
+    hi = max(hi, k);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31u) == 0) {
+    atomicMin(enc_min, lo);
+    atomicMax(enc_max, hi);
+  }
+}
+
+__global__ void __launch_bounds__(256) band_map_kernel(const float* f, uint32_t nx, uint32_t ny, uint32_t nz,
+                                                       const unsigned int* enc, float lo, float hi, float* label,
+                                                       float* norm_field) {
+  const float a = key2f(enc[0]), b = key2f(enc[1]);
+  const uint64_t total = (uint64_t)nx * ny * nz;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t x = (uint32_t)(i % nx), y = (uint32_t)((i / nx) % ny), z = (uint32_t)(i / ((uint64_t)nx * ny));
+    float k = __fdiv_rn(fs(__ldg(f + i), a), fs(b, a));
+    float m;
+    if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 || z == nz - 1) {
+      m = 0.0f;
+      k = 0.0f;
+    } else {
+      m = (k >= lo && k <= hi) ? 1.0f : 0.0f;
+    }
+    label[i] = m;
+    norm_field[i] = k;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launch wrappers.
+// ---------------------------------------------------------------------------
+cudaError_t launch_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t nz, float* out, uint32_t blocks,
+                             cudaStream_t st) {
+  unit_cell_kernel<<<blocks, 256, 0, st>>>(type, nx, ny, nz, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t prep_blocks, uint32_t blocks,
+                           cudaStream_t st) {
+  if (p.mode == 1) {
+    lattice_prep_kernel<<<prep_blocks, 256, 0, st>>>(p, blend_buf);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    LatticeParams q = p;
+    q.blend = blend_buf;
+    lattice_blend_kernel<<<blocks, 256, 0, st>>>(q);
+  } else {
+    lattice_params_kernel<<<blocks, 256, 0, st>>>(p);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_csg(const CsgParams& p, uint32_t blocks, cudaStream_t st) {
+  csg_kernel<<<blocks, 256, 0, st>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_normalise(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, unsigned int* enc, float lo,
+                             float hi, float* label, float* norm_field, uint32_t blocks, cudaStream_t st) {
+  const uint64_t n = (uint64_t)nx * ny * nz;
+  minmax_kernel<<<blocks, 256, 0, st>>>(f, n, enc, enc + 1);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  band_map_kernel<<<blocks, 256, 0, st>>>(f, nx, ny, nz, enc, lo, hi, label, norm_field);
+  return cudaGetLastError();
+}
+
+}  // namespace gcm

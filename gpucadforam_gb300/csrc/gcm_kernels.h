@@ -1,0 +1,108 @@
+// Kernel parameter blocks and launch entry points shared by the host library
+// (api.cpp) and the CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/gcm.h"
+
+namespace gcm {
+
+struct MeshParams {
+  const float* f;  // classify field (band mode: the label field)
+  const float* g;  // band mode: normalised field used for vertex positions
+  uint32_t nx, ny, nz;
+  uint32_t rows;             // voxel rows per tile
+  uint32_t tiles_per_plane;  // ceil((ny-1) / rows)
+  uint32_t bulk;             // 1: stage rows with bulk copies (field bases 16-byte aligned)
+  uint64_t ntiles;
+  float vs[3], gc[3];
+  float iso, lo, hi;
+  float4* pos;
+  float4* norm;
+  uint64_t capacity;
+  uint64_t* tile_status;  // ntiles words, zeroed before the launch
+  uint32_t* counter;      // zeroed before the launch
+  gcm_counts* counts_dev; // zeroed before the launch
+  uint32_t* status;       // &counts_dev->status
+  uint64_t wait_ns;
+};
+
+struct GenerateParams {
+  const float* f;
+  const float* g;
+  uint32_t nx, ny, nz;
+  float vs[3], gc[3];
+  float iso, lo, hi;
+  const uint32_t* compacted;
+  uint64_t active;
+  const uint32_t* verts_scan;
+  float4* pos;
+  float4* norm;
+  uint64_t capacity;
+  uint32_t* status;
+};
+
+struct ScanParams {
+  const uint32_t* in;
+  uint32_t* out;
+  uint64_t n;
+  uint64_t ntiles;
+  uint64_t* tile_status;
+  uint32_t* counter;
+  uint64_t* total;
+  uint32_t* status;
+  uint64_t wait_ns;
+};
+
+// Graded lattice, device form of gcm_lattice.
+struct LatticeParams {
+  uint32_t mode;
+  uint32_t cx, cy, cz;
+  const float* period;
+  const float* euler;  // [3][n] or null
+  const float* thickness;
+  const uint8_t* type;
+  const float* blend;  // blend mode: per control point R[9], 2/period, thickness, type (12 words)
+  float origin[3];
+  float scale[3];   // control coordinate per voxel: (c-1)/(n-1)
+  float anchor[3];  // voxel spacing of control points: (n-1)/(c-1)
+  uint32_t nx, ny, nz;
+  float* out;
+};
+
+struct CsgParams {
+  const gcm_primitive* prims;
+  uint32_t n;
+  float origin[3], spacing[3];
+  uint32_t nx, ny, nz;
+  float* out;
+};
+
+// Launch wrappers (each kernel is launched from the file that defines it).
+cudaError_t mesh_prepare(bool band, bool emit, size_t smem, int* blocks_per_sm);
+cudaError_t launch_mesh(bool band, bool emit, const MeshParams& p, uint32_t blocks, size_t smem, cudaStream_t st);
+cudaError_t launch_classify(const float* f, uint32_t nx, uint32_t ny, uint64_t nvox, float iso, uint32_t* verts,
+                            uint32_t* occ, uint8_t* cube, uint32_t blocks, cudaStream_t st);
+cudaError_t launch_compact(const uint32_t* occ, const uint32_t* scan, uint64_t n, uint32_t* out, uint32_t blocks,
+                           cudaStream_t st);
+cudaError_t launch_generate(bool band, const GenerateParams& p, uint32_t blocks, cudaStream_t st);
+cudaError_t launch_scan(const ScanParams& p, uint32_t blocks, cudaStream_t st);
+cudaError_t launch_lookback_stall(uint32_t ntiles, uint32_t stall, uint64_t wait_ns, uint64_t* tile_status,
+                                  uint32_t* counter, uint64_t* prefix_out, uint32_t* status, uint32_t blocks,
+                                  cudaStream_t st);
+
+cudaError_t launch_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t nz, float* out, uint32_t blocks,
+                             cudaStream_t st);
+cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t prep_blocks, uint32_t blocks,
+                           cudaStream_t st);
+cudaError_t launch_csg(const CsgParams& p, uint32_t blocks, cudaStream_t st);
+cudaError_t launch_normalise(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, unsigned int* enc, float lo,
+                             float hi, float* label, float* norm_field, uint32_t blocks, cudaStream_t st);
+
+size_t mesh_smem_bytes(uint32_t nx, uint32_t rows, bool band);
+uint32_t scan_tile_elems();
+
+}  // namespace gcm

@@ -1,0 +1,246 @@
+"""Python front end over the C ABI, with torch tensors as device buffers.
+
+torch supplies device memory and streams only; every computation is a call into
+libgcm.so.  Names follow the reference's operations (classify, scan, compact,
+generate, normalise, mesh) so tests read like the reference's own pipeline
+(src/Isosurface.cu:401-572).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _native as N
+
+
+@dataclass
+class Counts:
+    active_voxels: int
+    total_verts: int
+    status: int
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+
+
+def _stream(stream):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def make_grid(shape_zyx, voxel_size=(1.0, 1.0, 1.0), grid_center=(0.0, 0.0, 0.0)):
+    nz, ny, nx = shape_zyx
+    return N.GcmGrid(nx, ny, nz, (C.c_float * 3)(*voxel_size), (C.c_float * 3)(*grid_center))
+
+
+class Context:
+    """One gcm_ctx: scratch owner for a stream of calls (not thread-safe)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = N.load()
+        self.device = device
+        h = C.c_void_p()
+        rc = self.lib.gcm_ctx_create(device, C.byref(h))
+        if rc != 0:
+            raise N.GcmError(rc, "gcm_ctx_create failed")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.gcm_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+    def check(self, rc, allow=()):
+        if rc != 0 and rc not in allow:
+            raise N.GcmError(rc, self.lib.gcm_ctx_last_error(self.h).decode())
+        return rc
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.gcm_ctx_launch_count(self.h))
+
+    def set_wait_limit(self, ns: int):
+        self.check(self.lib.gcm_ctx_set_wait_limit(self.h, int(ns)))
+
+    def reserve(self, max_points: int):
+        self.check(self.lib.gcm_ctx_reserve(self.h, int(max_points)))
+
+    # ------------------------------------------------------------ fused mesh
+    def count_field(self, field, iso, stream=None) -> Counts:
+        g = make_grid(field.shape)
+        c = N.GcmCounts()
+        self.check(self.lib.gcm_count_field(self.h, _ptr(field), C.byref(g), float(iso), C.byref(c), _stream(stream)))
+        return Counts(c.active_voxels, c.total_verts, c.status)
+
+    def mesh_field(self, field, iso, voxel_size=(1, 1, 1), grid_center=(0, 0, 0), capacity=None, pos=None, norm=None,
+                   stream=None, allow_overflow=False):
+        """Fused single-pass extraction.  Without buffers, counts first and
+        allocates the exact output."""
+        assert field.is_cuda and field.dtype == torch.float32 and field.dim() == 3
+        if pos is None:
+            if capacity is None:
+                capacity = self.count_field(field, iso, stream).total_verts
+            pos = torch.empty((max(capacity, 1), 4), dtype=torch.float32, device=field.device)
+            norm = torch.empty((max(capacity, 1), 4), dtype=torch.float32, device=field.device)
+        elif capacity is None:
+            capacity = pos.shape[0]
+        g = make_grid(field.shape, voxel_size, grid_center)
+        c = N.GcmCounts()
+        rc = self.lib.gcm_mesh_field(self.h, _ptr(field), C.byref(g), float(iso), _ptr(pos), _ptr(norm), int(capacity),
+                                     C.byref(c), _stream(stream))
+        self.check(rc, allow=(N.GCM_ERR_OUTPUT_OVERFLOW,) if allow_overflow else ())
+        n = int(c.total_verts)
+        return pos[: min(n, capacity)], norm[: min(n, capacity)], Counts(c.active_voxels, c.total_verts, c.status)
+
+    def mesh_field_async(self, field, iso, pos, norm, d_counts, voxel_size=(1, 1, 1), grid_center=(0, 0, 0),
+                         stream=None):
+        g = make_grid(field.shape, voxel_size, grid_center)
+        self.check(self.lib.gcm_mesh_field_async(self.h, _ptr(field), C.byref(g), float(iso), _ptr(pos), _ptr(norm),
+                                                 int(pos.shape[0]), _ptr(d_counts), _stream(stream)))
+
+    def mesh_band(self, label, norm_field, iso, lo, hi, voxel_size=(1, 1, 1), grid_center=(0, 0, 0), capacity=None,
+                  stream=None):
+        if capacity is None:
+            capacity = self.count_field(label, iso, stream).total_verts
+        pos = torch.empty((max(capacity, 1), 4), dtype=torch.float32, device=label.device)
+        norm = torch.empty((max(capacity, 1), 4), dtype=torch.float32, device=label.device)
+        g = make_grid(label.shape, voxel_size, grid_center)
+        c = N.GcmCounts()
+        self.check(self.lib.gcm_mesh_band(self.h, _ptr(label), _ptr(norm_field), C.byref(g), float(iso), float(lo),
+                                          float(hi), _ptr(pos), _ptr(norm), int(capacity), C.byref(c),
+                                          _stream(stream)))
+        n = int(c.total_verts)
+        return pos[:n], norm[:n], Counts(c.active_voxels, c.total_verts, c.status)
+
+    # ------------------------------------------------------------ staged form
+    def classify(self, field, iso, stream=None):
+        nz, ny, nx = field.shape
+        nv = (nx - 1) * (ny - 1) * (nz - 1)
+        verts = torch.empty(nv, dtype=torch.int32, device=field.device)
+        occ = torch.empty(nv, dtype=torch.int32, device=field.device)
+        cube = torch.empty(nv, dtype=torch.uint8, device=field.device)
+        g = make_grid(field.shape)
+        self.check(self.lib.gcm_mc_classify(self.h, _ptr(field), C.byref(g), float(iso), _ptr(verts), _ptr(occ),
+                                            _ptr(cube), _stream(stream)))
+        return verts, occ, cube
+
+    def scan(self, values, stream=None):
+        out = torch.empty_like(values)
+        tot = C.c_uint64(0)
+        self.check(self.lib.gcm_scan_exclusive_u32(self.h, _ptr(values), _ptr(out), values.numel(), C.byref(tot),
+                                                   _stream(stream)))
+        return out, int(tot.value)
+
+    def compact(self, occ, occ_scan, active, stream=None):
+        out = torch.zeros(max(active, 1), dtype=torch.int32, device=occ.device)
+        self.check(self.lib.gcm_mc_compact(self.h, _ptr(occ), _ptr(occ_scan), occ.numel(), _ptr(out), _stream(stream)))
+        return out[:active]
+
+    def generate(self, field, iso, compacted, verts_scan, total, voxel_size=(1, 1, 1), grid_center=(0, 0, 0),
+                 stream=None):
+        pos = torch.empty((max(total, 1), 4), dtype=torch.float32, device=field.device)
+        norm = torch.empty((max(total, 1), 4), dtype=torch.float32, device=field.device)
+        g = make_grid(field.shape, voxel_size, grid_center)
+        self.check(self.lib.gcm_mc_generate(self.h, _ptr(field), C.byref(g), float(iso), _ptr(compacted),
+                                            compacted.numel(), _ptr(verts_scan), _ptr(pos), _ptr(norm), int(total),
+                                            _stream(stream)))
+        return pos[:total], norm[:total]
+
+    # ------------------------------------------------------------ fields
+    def unit_cell(self, tpms_type, nx, ny, nz, stream=None):
+        out = torch.empty((nz, ny, nx), dtype=torch.float32, device=f"cuda:{self.device}")
+        self.check(self.lib.gcm_field_unit_cell(self.h, int(tpms_type), nx, ny, nz, _ptr(out), _stream(stream)))
+        return out
+
+    def normalise_band(self, field, lo, hi, stream=None):
+        nz, ny, nx = field.shape
+        label = torch.empty_like(field)
+        nf = torch.empty_like(field)
+        mm = (C.c_float * 2)()
+        self.check(self.lib.gcm_normalise_band(self.h, _ptr(field), nx, ny, nz, float(lo), float(hi), _ptr(label),
+                                               _ptr(nf), mm, _stream(stream)))
+        return label, nf, (mm[0], mm[1])
+
+    def lattice_struct(self, lat):
+        return N.GcmLattice(lat.mode, lat.ctrl[0], lat.ctrl[1], lat.ctrl[2], _ptr(lat.period), _ptr(lat.euler),
+                            _ptr(lat.thickness), _ptr(lat.types), (C.c_float * 3)(*lat.origin))
+
+    def lattice_field(self, lat, shape_zyx, stream=None):
+        nz, ny, nx = shape_zyx
+        out = torch.empty((nz, ny, nx), dtype=torch.float32, device=f"cuda:{self.device}")
+        s = self.lattice_struct(lat)
+        self.check(self.lib.gcm_field_lattice(self.h, C.byref(s), nx, ny, nz, _ptr(out), _stream(stream)))
+        return out
+
+    def mesh_lattice(self, lat, shape_zyx, iso, voxel_size=(1, 1, 1), grid_center=(0, 0, 0), pos=None, norm=None,
+                     stream=None, allow_overflow=False):
+        s = self.lattice_struct(lat)
+        g = make_grid(shape_zyx, voxel_size, grid_center)
+        c = N.GcmCounts()
+        rc = self.lib.gcm_mesh_lattice(self.h, C.byref(s), C.byref(g), float(iso), _ptr(pos), _ptr(norm),
+                                       int(pos.shape[0]) if pos is not None else 0, C.byref(c), _stream(stream))
+        self.check(rc, allow=(N.GCM_ERR_OUTPUT_OVERFLOW,) if allow_overflow or pos is None else ())
+        return Counts(c.active_voxels, c.total_verts, c.status)
+
+    def csg_field(self, prims_dev, n_prims, frame, shape_zyx, stream=None):
+        nz, ny, nx = shape_zyx
+        out = torch.empty((nz, ny, nx), dtype=torch.float32, device=f"cuda:{self.device}")
+        self.check(self.lib.gcm_field_csg(self.h, _ptr(prims_dev), n_prims, C.byref(frame), nx, ny, nz, _ptr(out),
+                                          _stream(stream)))
+        return out
+
+    def mesh_csg(self, prims_dev, n_prims, frame, shape_zyx, iso, voxel_size=(1, 1, 1), grid_center=(0, 0, 0),
+                 pos=None, norm=None, stream=None, allow_overflow=False):
+        g = make_grid(shape_zyx, voxel_size, grid_center)
+        c = N.GcmCounts()
+        rc = self.lib.gcm_mesh_csg(self.h, _ptr(prims_dev), n_prims, C.byref(frame), C.byref(g), float(iso), _ptr(pos),
+                                   _ptr(norm), int(pos.shape[0]) if pos is not None else 0, C.byref(c),
+                                   _stream(stream))
+        self.check(rc, allow=(N.GCM_ERR_OUTPUT_OVERFLOW,) if allow_overflow or pos is None else ())
+        return Counts(c.active_voxels, c.total_verts, c.status)
+
+
+@dataclass
+class Lattice:
+    """Graded lattice description with device control arrays."""
+    mode: int
+    ctrl: tuple
+    period: torch.Tensor
+    euler: torch.Tensor | None
+    thickness: torch.Tensor | None
+    types: torch.Tensor
+    origin: tuple = (0.0, 0.0, 0.0)
+
+    @staticmethod
+    def from_numpy(mode, ctrl, period, euler=None, thickness=None, types=None, origin=(0, 0, 0), device="cuda"):
+        n = int(np.prod(ctrl))
+        t = lambda a, dt: None if a is None else torch.from_numpy(np.ascontiguousarray(a, dt).reshape(-1)).to(device)
+        if types is None:
+            types = np.zeros(n, np.uint8)
+        return Lattice(mode, tuple(int(c) for c in ctrl), t(period, np.float32), t(euler, np.float32),
+                       t(thickness, np.float32), t(types, np.uint8), tuple(float(o) for o in origin))
+
+
+def primitives_to_device(prims, device="cuda"):
+    """prims: sequence of dicts (kind, op, flag, center, v3, p) -> device array."""
+    arr = (N.GcmPrimitive * max(len(prims), 1))()
+    for i, q in enumerate(prims):
+        pp = list(q.get("p", ())) + [0.0] * (6 - len(q.get("p", ())))
+        arr[i] = N.GcmPrimitive(q["kind"], q.get("op", 0), q.get("flag", 0), 0, (C.c_float * 3)(*q["center"]),
+                                (C.c_float * 3)(*q.get("v3", (0, 0, 0))), (C.c_float * 6)(*pp))
+    raw = np.frombuffer(bytes(arr), np.uint8).copy()
+    return torch.from_numpy(raw).to(device)
+
+
+def make_frame(origin, spacing):
+    return N.GcmFrame((C.c_float * 3)(*origin), (C.c_float * 3)(*spacing))

@@ -36,6 +36,12 @@
 extern "C" {
 #endif
 
+/* The library is built with hidden visibility; everything declared here is
+ * its exported interface. */
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
 #define GCM_ABI_VERSION 1
 
 typedef enum gcm_status {
@@ -232,6 +238,22 @@ gcm_status gcm_field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_
 gcm_status gcm_mesh_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
                         const gcm_grid* grid, float iso, float* d_pos, float* d_norm, uint64_t capacity_verts,
                         gcm_counts* h_counts, gcm_stream stream);
+
+/* ----------------------------------------------------------- test hooks */
+
+/* Exercises the bounded waits of the decoupled look-back: ntiles one-warp
+ * tiles of aggregate 1 each, except that tile `stall_tile` never publishes
+ * its state, so its successors' waits run out after wait_ns.  d_prefix_out
+ * (ntiles uint64, device) receives the prefix each tile used.  Returns
+ * GCM_ERR_DEVICE_TIMEOUT when the waits ran out as intended; the kernel
+ * always returns and the context stays usable.  No counterpart in the
+ * reference (which has no bounded waits). */
+gcm_status gcm_test_lookback_stall(gcm_ctx* ctx, uint32_t ntiles, uint32_t stall_tile, uint64_t wait_ns,
+                                   uint64_t* d_prefix_out, gcm_stream stream);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
 
 #ifdef __cplusplus
 }

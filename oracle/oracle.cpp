@@ -327,7 +327,8 @@ double lattice_value64(unsigned type, const double R[9], double h, const double 
 }
 
 template <bool F64, class Out>
-void lattice_field_impl(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, Out* out, int threads) {
+void lattice_field_impl(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, Out* out, int threads,
+                        uint32_t z0 = 0, uint32_t nplanes = 0) {
   const uint32_t c[3] = {L->cx, L->cy, L->cz};
   const uint32_t n[3] = {nx, ny, nz};
   const float s[3] = {ctrl_scale(c[0], nx), ctrl_scale(c[1], ny), ctrl_scale(c[2], nz)};
@@ -342,11 +343,13 @@ void lattice_field_impl(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t
     euler_rows<double>(ax, ay, az, &R64[9 * i]);
   }
   const int nt = set_threads(threads);
-  const uint64_t total = (uint64_t)nx * ny * nz;
+  if (nplanes == 0) nplanes = nz - z0;
+  const uint64_t plane = (uint64_t)nx * ny;
+  const uint64_t total = plane * nplanes;
 #pragma omp parallel for schedule(static) num_threads(nt)
   for (int64_t ii = 0; ii < (int64_t)total; ++ii) {
     const uint64_t i = (uint64_t)ii;
-    const uint32_t p[3] = {(uint32_t)(i % nx), (uint32_t)((i / nx) % ny), (uint32_t)(i / ((uint64_t)nx * ny))};
+    const uint32_t p[3] = {(uint32_t)(i % nx), (uint32_t)((i / nx) % ny), (uint32_t)(i / plane) + z0};
     const Cell k = locate(p, c, s);
     if (L->mode == 0) {
       const uint64_t ni = cidx(k.nearest[0], k.nearest[1], k.nearest[2], c);
@@ -745,6 +748,10 @@ void orc_lattice_field(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t 
 }
 void orc_lattice_field64(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, double* out, int threads) {
   lattice_field_impl<true>(L, nx, ny, nz, out, threads);
+}
+void orc_lattice_field_slab(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t z0,
+                            uint32_t nplanes, float* out, int threads) {
+  lattice_field_impl<false>(L, nx, ny, nz, out, threads, z0, nplanes);
 }
 
 void orc_csg_field(const orc_prim* prims, uint32_t n, const float* origin, const float* spacing, uint32_t nx,

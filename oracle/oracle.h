@@ -59,6 +59,9 @@ typedef struct orc_lattice {
 } orc_lattice;
 void orc_lattice_field(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, float* out, int threads);
 void orc_lattice_field64(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, double* out, int threads);
+// Planes z0 .. z0+nplanes-1 of the same nx*ny*nz field.
+void orc_lattice_field_slab(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t z0,
+                            uint32_t nplanes, float* out, int threads);
 
 // CSG scene of primitives: f = op_n(...op_1(op_0(+inf, g_0), g_1)..., g_n).
 typedef struct orc_prim {

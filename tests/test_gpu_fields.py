@@ -1,0 +1,183 @@
+"""GPU parity of the field kernels, through the C ABI.
+
+Unit cells and primitives against the reference's own kernels (fixtures);
+graded lattices and CSG scenes against the FP32 oracle (same operation order,
+so only the trig implementations differ) and the FP64 oracle.  Tolerances are
+written in each test.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from tests.helpers import assert_field_close, golden, n_cases
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = golden("golden_fields.npz")
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from gpucadforam_gb300.mesher import Context
+
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("i", range(n_cases(FIELDS, "unit")))
+def test_unit_cell_vs_reference(ctx, i):
+    nx, ny, nz, t = (int(v) for v in FIELDS[f"in/unit{i}"])
+    got = host(ctx.unit_cell(t, nx, ny, nz))
+    # same CUDA trig library as the reference; differences come only from
+    # expression contraction in the reference build
+    assert_field_close(got, FIELDS[f"sm103a/unit{i}"], k_rel=2, k_scale=4)
+
+
+@pytest.mark.parametrize("i", range(n_cases(FIELDS, "prim")))
+def test_primitive_vs_reference(ctx, i):
+    from gpucadforam_gb300.mesher import make_frame, primitives_to_device
+
+    q = FIELDS[f"in/prim{i}"]
+    nx, ny, nz = (int(v) for v in q[:3])
+    d = q[3:6]
+    prim = dict(kind=int(q[6]), flag=int(q[7]), center=q[8:11], v3=q[11:14], p=q[14:20], op=0)
+    origin = [np.float32((n - 1) / 2.0) for n in (nx, ny, nz)]  # the reference's centred frame
+    got = host(ctx.csg_field(primitives_to_device([prim]), 1, make_frame(origin, d), (nz, ny, nx)))
+    k_scale = 32 if prim["kind"] == 1 else 8
+    assert_field_close(got, FIELDS[f"sm103a/prim{i}"], k_scale=k_scale)
+
+
+@pytest.mark.parametrize("i", range(n_cases(FIELDS, "norm")))
+def test_normalise_band_vs_reference(ctx, i):
+    P = FIELDS[f"in/norm{i}/params"]
+    nx, ny, nz = (int(v) for v in P[:3])
+    f = FIELDS[f"in/norm{i}/field"].reshape(nz, ny, nx)
+    lab, nf, mm = ctx.normalise_band(dev(f), float(np.float32(P[3])), float(np.float32(P[4])))
+    assert np.array_equal(np.array(mm, np.float32), FIELDS[f"sm103a/norm{i}/minmax"])
+    assert np.array_equal(host(lab).reshape(-1), FIELDS[f"sm103a/norm{i}/label"])
+    assert np.array_equal(host(nf).reshape(-1), FIELDS[f"sm103a/norm{i}/normf"])
+
+
+def _graded(seed, C, mode):
+    rng = np.random.default_rng(seed)
+    n = C ** 3
+    return dict(mode=mode, ctrl=(C, C, C), period=rng.uniform(16, 64, n).astype(np.float32),
+                euler=rng.uniform(-np.pi / 4, np.pi / 4, 3 * n).astype(np.float32),
+                thickness=rng.uniform(-0.6, 0.6, n).astype(np.float32),
+                types=rng.choice(np.array([0, 1, 2, 3, 5], np.uint8), n))
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("shape", [(96, 96, 96), (40, 70, 33)])
+def test_graded_lattice_vs_oracle(ctx, mode, shape):
+    from gpucadforam_gb300.mesher import Lattice
+
+    nz, ny, nx = shape
+    L = _graded(7 + mode, 8, mode)
+    origin = ((nx - 1) / 2, (ny - 1) / 2, (nz - 1) / 2)
+    lat = Lattice.from_numpy(L["mode"], L["ctrl"], L["period"], L["euler"], L["thickness"], L["types"], origin)
+    got = host(ctx.lattice_field(lat, shape))
+    ref32 = O.lattice_field((nx, ny, nz), mode, L["ctrl"], L["period"], L["euler"], L["thickness"], L["types"], origin)
+    ref64 = O.lattice_field((nx, ny, nz), mode, L["ctrl"], L["period"], L["euler"], L["thickness"], L["types"], origin,
+                            fp64=True)
+    # FP32 oracle: identical operation order, different sin/cos implementations
+    # (CUDA sincosf/sincospif within 2 ulp).  An ulp of difference in a rotation
+    # entry moves the phase by |q| * 2/period * ulp, |q| <= 84 voxels here, so
+    # the bound is absolute: 2e-5.
+    err32 = np.abs(got.astype(np.float64) - ref32.astype(np.float64))
+    assert err32.max() < 2e-5, err32.max()
+    # FP64 oracle: the FP32 phase carries ~1 ulp of |X| (half-turns); with the
+    # phase magnitude below 2^6 here that bounds the field error by 4e-5 absolute
+    err = np.abs(got.astype(np.float64) - ref64)
+    assert err.max() < 4e-5, err.max()
+
+
+def test_c1_uniform_gyroid_fp64(ctx):
+    from gpucadforam_gb300.mesher import Lattice
+
+    lat = Lattice.from_numpy(0, (1, 1, 1), np.array([32.0], np.float32))
+    got = host(ctx.lattice_field(lat, (128, 128, 128)))
+    z, y, x = np.meshgrid(*(np.arange(128, dtype=np.float64),) * 3, indexing="ij")
+    k = 2 * np.pi / 32
+    ref = np.sin(k * x) * np.cos(k * y) + np.sin(k * y) * np.cos(k * z) + np.sin(k * z) * np.cos(k * x)
+    # phases i/16 are exact in FP32, so only sinpi/cospi rounding remains
+    assert np.abs(got - ref).max() < 1e-6
+
+
+def _csg_scene(seed, n_prims=64, n_sub=8):
+    rng = np.random.default_rng(seed)
+    prims = []
+    for i in range(n_prims):
+        kind = int(rng.integers(0, 3))
+        c = rng.uniform(0, 1, 3).astype(np.float32)
+        op = 1 if i >= n_prims - n_sub else 0
+        if kind == 0:
+            prims.append(dict(kind=0, op=op, center=c, p=[rng.uniform(0.02, 0.15), 0.0]))
+        elif kind == 1:
+            r, hh = rng.uniform(0.02, 0.12, 2)
+            prims.append(dict(kind=1, op=op, center=c, v3=(0.0, 0.0, 1.0), p=[r, 0.0, 2 * hh]))
+        else:
+            he = rng.uniform(0.02, 0.12, 3)
+            prims.append(dict(kind=2, op=op, center=c, v3=(0.0, 0.0, 0.0), p=list(2 * he)))
+    return prims
+
+
+def test_csg_scene_vs_oracle(ctx):
+    from gpucadforam_gb300.mesher import make_frame, primitives_to_device
+
+    n = 96
+    prims = _csg_scene(0xD4A + 3)
+    h = np.float32(1.0 / (n - 1))
+    got = host(ctx.csg_field(primitives_to_device(prims), len(prims), make_frame((0, 0, 0), (h, h, h)), (n, n, n)))
+    ref32 = O.csg_field(prims, (n, n, n), (0, 0, 0), (h, h, h))
+    # spheres, z-axis cylinders and unrotated boxes use no trig: same IEEE
+    # operations in the same order, so the FP32 oracle matches bit for bit
+    assert got.tobytes() == ref32.tobytes()
+    ref64 = O.csg_field(prims, (n, n, n), (0, 0, 0), (h, h, h), fp64=True)
+    assert np.abs(got - ref64).max() < 1e-5 * max(1.0, float(np.abs(ref64).max()))
+
+
+def test_lattice_mesh_equals_oracle_mc_of_device_field(ctx):
+    """End to end: the fused lattice mesher's output equals marching cubes (oracle)
+    of the field the device evaluated; cube indices of that field differ from the
+    FP64 field's only where |f - iso| < 4e-5 (the stated field tolerance)."""
+    from gpucadforam_gb300.mesher import Lattice
+
+    n = 80
+    L = _graded(11, 8, 0)
+    origin = ((n - 1) / 2,) * 3
+    lat = Lattice.from_numpy(0, L["ctrl"], L["period"], L["euler"], L["thickness"], L["types"], origin)
+    field = ctx.lattice_field(lat, (n, n, n))
+    cap = ctx.count_field(field, 0.0).total_verts
+    pos = torch.empty((cap, 4), device="cuda")
+    norm = torch.empty((cap, 4), device="cuda")
+    cnt = ctx.mesh_lattice(lat, (n, n, n), 0.0, pos=pos, norm=norm)
+    f = host(field)
+    opos, onorm, _ = O.mesh(f, (1, 1, 1), (0, 0, 0), 0.0)
+    assert cnt.total_verts == len(opos)
+    assert host(pos).tobytes() == opos.tobytes() and host(norm).tobytes() == onorm.tobytes()
+    f64 = O.lattice_field((n, n, n), 0, L["ctrl"], L["period"], L["euler"], L["thickness"], L["types"], origin,
+                          fp64=True)
+    _, _, c32 = O.mc_classify(f, 0.0)
+    _, _, c64 = O.mc_classify(f64.astype(np.float32), 0.0)
+    diff = c32 != c64
+    if diff.any():
+        # every differing voxel has a corner within tolerance of the isovalue
+        near = np.abs(f64) < 4e-5
+        nv = np.zeros(c32.shape, bool)
+        m = near
+        for dz in (0, 1):
+            for dy in (0, 1):
+                for dx in (0, 1):
+                    nv |= m[dz:dz + n - 1, dy:dy + n - 1, dx:dx + n - 1].reshape(-1)
+        assert nv[diff].all()
