@@ -239,6 +239,30 @@ gcm_status gcm_mesh_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_p
                         const gcm_grid* grid, float iso, float* d_pos, float* d_norm, uint64_t capacity_verts,
                         gcm_counts* h_counts, gcm_stream stream);
 
+/* ----------------------------------------------------- allocation-free form */
+
+/* Fused extraction of a fed field for callers that may not allocate device
+ * memory (an application that owns every allocation through its own arena, a
+ * stream being captured into a CUDA graph, a real-time loop that cannot take
+ * an allocation's synchronisation).  It needs no context: the look-back
+ * scratch is a fixed 1 MiB array in the library's device image, present on
+ * every GPU that loads the library until the process exits, and nothing is
+ * allocated or freed.  The caller passes the field, 16-byte aligned output
+ * buffers and a device gcm_counts; works on the current device and is
+ * stream-ordered (no host synchronisation).  Results equal gcm_mesh_field's.
+ *  - Grids whose tile states do not fit the array (about 131 thousand tiles;
+ *    512^3 and 1024^3 fit) return GCM_ERR_NOT_SUPPORTED before any launch.
+ *  - Every call shares the array and clears the part it uses first; calls
+ *    that overlap on the GPU (other streams, other host threads) race on it,
+ *    so serialise them.
+ *  - The first call on each device looks up the array's device address
+ *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *  - Device-side waits are bounded at 2 s (GCM_ERR_DEVICE_TIMEOUT in
+ *    d_counts->status).
+ * No counterpart in the reference (its scratch is always caller-allocated). */
+gcm_status gcm_mesh_field_noalloc(const float* d_field, const gcm_grid* grid, float iso, float* d_pos, float* d_norm,
+                                  uint64_t capacity_verts, gcm_counts* d_counts, gcm_stream stream);
+
 /* ----------------------------------------------------------- test hooks */
 
 /* Exercises the bounded waits of the decoupled look-back: ntiles one-warp
