@@ -95,10 +95,12 @@ def header_symbols() -> list[str]:
 _lib = None
 
 
-def load(path: str = LIB_PATH) -> C.CDLL:
+def load(path: str | None = None) -> C.CDLL:
+    """Loads libgcm.so (GCM_LIBRARY overrides the in-tree path)."""
     global _lib
     if _lib is not None:
         return _lib
+    path = path or os.environ.get("GCM_LIBRARY") or LIB_PATH
     if not os.path.exists(path):
         raise ImportError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
     L = C.CDLL(path)

@@ -237,6 +237,12 @@ uint32_t grid_blocks(gcm_ctx* ctx, uint64_t work, uint32_t threads, uint32_t per
   return (uint32_t)std::max<uint64_t>(1, std::min(want, cap));
 }
 
+// Row-structured field kernels: one CTA per sample row at a time.
+uint32_t row_blocks(gcm_ctx* ctx, uint32_t ny, uint32_t nz) {
+  const uint64_t rows = (uint64_t)ny * nz;
+  return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(rows, (uint64_t)ctx->sm_count * 8));
+}
+
 }  // namespace gcm
 
 using namespace gcm;
@@ -515,15 +521,14 @@ static gcm_status lattice_params(gcm_ctx* ctx, const gcm_lattice* L, uint32_t nx
 
 static gcm_status run_lattice(gcm_ctx* ctx, LatticeParams& p, float* d_out, cudaStream_t st) {
   p.out = d_out;
-  const uint64_t n = (uint64_t)p.nx * p.ny * p.nz;
   if (p.mode == GCM_GRADE_BLEND) {
     const uint64_t nc = (uint64_t)p.cx * p.cy * p.cz;
     gcm_status s = ensure_buffer(ctx, &ctx->blend_buf, &ctx->blend_bytes, nc * 12 * sizeof(float));
     if (s) return s;
-    GCM_CUDA(ctx, gcm::launch_lattice(p, ctx->blend_buf, grid_blocks(ctx, nc, 256), grid_blocks(ctx, n, 256), st));
+    GCM_CUDA(ctx, gcm::launch_lattice(p, ctx->blend_buf, grid_blocks(ctx, nc, 256), row_blocks(ctx, p.ny, p.nz), st));
     count_launch(ctx, 2);
   } else {
-    GCM_CUDA(ctx, gcm::launch_lattice(p, nullptr, 0, grid_blocks(ctx, n, 256), st));
+    GCM_CUDA(ctx, gcm::launch_lattice(p, nullptr, 0, row_blocks(ctx, p.ny, p.nz), st));
     count_launch(ctx, 1);
   }
   return GCM_OK;
@@ -578,8 +583,7 @@ gcm_status gcm_field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_
   p.ny = ny;
   p.nz = nz;
   p.out = d_out;
-  const uint64_t n = (uint64_t)nx * ny * nz;
-  GCM_CUDA(ctx, gcm::launch_csg(p, grid_blocks(ctx, n, 256, 4), static_cast<cudaStream_t>(stream)));
+  GCM_CUDA(ctx, gcm::launch_csg(p, row_blocks(ctx, ny, nz), static_cast<cudaStream_t>(stream)));
   count_launch(ctx, 1);
   return GCM_OK;
 }

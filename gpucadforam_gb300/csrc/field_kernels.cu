@@ -70,26 +70,26 @@ __device__ __forceinline__ float lattice_value(uint32_t type, const float R[9], 
   return fs(tpms_sc(type, s[0], c[0], s[1], c[1], s[2], c[2]), thick);
 }
 
-struct Cell {
-  int i0[3];
-  float f[3];
-  int nearest[3];
+// Control-grid cell of one sample coordinate along one axis: the cell index
+// i0 (clamped so that i0 + 1 exists), the FP32 fraction inside it, and the
+// nearest control point.  Made in FP32 by the kernels and the oracle alike.
+struct AxisCell {
+  int i0, i1, nearest;
+  float f;
 };
 
-__device__ __forceinline__ Cell locate(const uint32_t pt[3], const uint32_t c[3], const float s[3]) {
-  Cell k;
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    const float cu = fm((float)pt[a], s[a]);
-    int i0 = (int)cu;
-    if (c[a] == 1) i0 = 0;
-    else if (i0 > (int)c[a] - 2) i0 = (int)c[a] - 2;
-    k.i0[a] = i0;
-    k.f[a] = c[a] == 1 ? 0.0f : fs(cu, (float)i0);
-    int nn = (int)fa(cu, 0.5f);
-    if (nn > (int)c[a] - 1) nn = (int)c[a] - 1;
-    k.nearest[a] = nn;
-  }
+__device__ __forceinline__ AxisCell locate1(uint32_t pt, uint32_t c, float s) {
+  AxisCell k;
+  const float cu = fm((float)pt, s);
+  int i0 = (int)cu;
+  if (c == 1) i0 = 0;
+  else if (i0 > (int)c - 2) i0 = (int)c - 2;
+  k.i0 = i0;
+  k.i1 = c > 1 ? i0 + 1 : 0;
+  k.f = c == 1 ? 0.0f : fs(cu, (float)i0);
+  int nn = (int)fa(cu, 0.5f);
+  if (nn > (int)c - 1) nn = (int)c - 1;
+  k.nearest = nn;
   return k;
 }
 
@@ -99,15 +99,21 @@ __device__ __forceinline__ uint32_t cidx(int x, int y, int z, const uint32_t c[3
 
 __device__ __forceinline__ float lerpf(float u, float v, float t) { return __fmaf_rn(t, fs(v, u), u); }
 
-__device__ __forceinline__ float trilinear(const float* __restrict__ a, const Cell& k, const uint32_t c[3]) {
+// Trilinear interpolation is evaluated y first, then z, then x:
+//   a(xc) = lerp(lerp(v[xc,y0,z0], v[xc,y1,z0], fy), lerp(v[xc,y0,z1], v[xc,y1,z1], fy), fz)
+//   value = lerp(a(x0), a(x1), fx)
+// so that a(xc) is one number per control column for a whole sample row.
+__device__ __forceinline__ float column_yz(const float* __restrict__ a, int xc, const AxisCell& ky,
+                                           const AxisCell& kz, const uint32_t c[3]) {
   if (!a) return 0.0f;
-  const int x0 = k.i0[0], y0 = k.i0[1], z0 = k.i0[2];
-  const int x1 = c[0] > 1 ? x0 + 1 : 0, y1 = c[1] > 1 ? y0 + 1 : 0, z1 = c[2] > 1 ? z0 + 1 : 0;
-  const float c00 = lerpf(__ldg(a + cidx(x0, y0, z0, c)), __ldg(a + cidx(x1, y0, z0, c)), k.f[0]);
-  const float c10 = lerpf(__ldg(a + cidx(x0, y1, z0, c)), __ldg(a + cidx(x1, y1, z0, c)), k.f[0]);
-  const float c01 = lerpf(__ldg(a + cidx(x0, y0, z1, c)), __ldg(a + cidx(x1, y0, z1, c)), k.f[0]);
-  const float c11 = lerpf(__ldg(a + cidx(x0, y1, z1, c)), __ldg(a + cidx(x1, y1, z1, c)), k.f[0]);
-  return lerpf(lerpf(c00, c10, k.f[1]), lerpf(c01, c11, k.f[1]), k.f[2]);
+  return lerpf(lerpf(__ldg(a + cidx(xc, ky.i0, kz.i0, c)), __ldg(a + cidx(xc, ky.i1, kz.i0, c)), ky.f),
+               lerpf(__ldg(a + cidx(xc, ky.i0, kz.i1, c)), __ldg(a + cidx(xc, ky.i1, kz.i1, c)), ky.f), kz.f);
+}
+
+// Trilinear weight of corner offset d along one axis.
+__device__ __forceinline__ float axis_weight(const AxisCell& k, uint32_t c, int d) {
+  if (c == 1) return d ? 0.0f : 1.0f;
+  return d ? k.f : fs(1.0f, k.f);
 }
 
 }  // namespace
@@ -185,57 +191,104 @@ __global__ void __launch_bounds__(256) lattice_prep_kernel(LatticeParams p, floa
   }
 }
 
+// Rows of samples are the unit of work: a CTA takes sample row (y, z), stages
+// per control column the row's y/z-interpolated parameters in shared memory,
+// and its threads cover x.  No 64-bit index arithmetic per sample.
+constexpr uint32_t kRowCx = 1024;   // control columns staged per row (PARAMS)
+constexpr uint32_t kBlendCx = 128;  // control columns staged per row (BLEND)
+
 __global__ void __launch_bounds__(256) lattice_params_kernel(LatticeParams p) {
-  const uint64_t total = (uint64_t)p.nx * p.ny * p.nz;
+  __shared__ float s_a[5][kRowCx];
+  __shared__ uint8_t s_t[kRowCx];
   const uint32_t c[3] = {p.cx, p.cy, p.cz};
-  const float s[3] = {p.scale[0], p.scale[1], p.scale[2]};
   const uint32_t nc = p.cx * p.cy * p.cz;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t pt[3] = {(uint32_t)(i % p.nx), (uint32_t)((i / p.nx) % p.ny), (uint32_t)(i / ((uint64_t)p.nx * p.ny))};
-    const Cell k = locate(pt, c, s);
-    const uint32_t type = __ldg(p.type + cidx(k.nearest[0], k.nearest[1], k.nearest[2], c));
-    const float P = trilinear(p.period, k, c);
-    const float ax = trilinear(p.euler, k, c);
-    const float ay = trilinear(p.euler ? p.euler + nc : nullptr, k, c);
-    const float az = trilinear(p.euler ? p.euler + 2 * nc : nullptr, k, c);
-    const float th = trilinear(p.thickness, k, c);
-    float R[9];
-    euler_rows(ax, ay, az, R);
-    const float q[3] = {fs((float)pt[0], p.origin[0]), fs((float)pt[1], p.origin[1]), fs((float)pt[2], p.origin[2])};
-    p.out[i] = lattice_value(type, R, __fdiv_rn(2.0f, P), q, th);
+  const float* arr[5] = {p.period, p.euler, p.euler ? p.euler + nc : nullptr,
+                         p.euler ? p.euler + 2 * nc : nullptr, p.thickness};
+  const bool staged = p.cx <= kRowCx;
+  const uint32_t rows = p.ny * p.nz;
+  for (uint32_t row = blockIdx.x; row < rows; row += gridDim.x) {
+    const uint32_t y = row % p.ny, z = row / p.ny;
+    const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
+    if (staged) {
+      __syncthreads();  // the previous row's readers are done
+      for (uint32_t i = threadIdx.x; i < 5 * p.cx; i += blockDim.x) {
+        const uint32_t k = i / p.cx, xc = i % p.cx;
+        s_a[k][xc] = column_yz(arr[k], (int)xc, ky, kz, c);
+      }
+      for (uint32_t xc = threadIdx.x; xc < p.cx; xc += blockDim.x)
+        s_t[xc] = __ldg(p.type + cidx((int)xc, ky.nearest, kz.nearest, c));
+      __syncthreads();
+    }
+    float* out = p.out + (uint64_t)row * p.nx;
+    for (uint32_t x = threadIdx.x; x < p.nx; x += blockDim.x) {
+      const AxisCell kx = locate1(x, c[0], p.scale[0]);
+      float v[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        const float a0 = staged ? s_a[k][kx.i0] : column_yz(arr[k], kx.i0, ky, kz, c);
+        const float a1 = staged ? s_a[k][kx.i1] : column_yz(arr[k], kx.i1, ky, kz, c);
+        v[k] = lerpf(a0, a1, kx.f);
+      }
+      const uint32_t type = staged ? s_t[kx.nearest] : __ldg(p.type + cidx(kx.nearest, ky.nearest, kz.nearest, c));
+      float R[9];
+      euler_rows(v[1], v[2], v[3], R);
+      const float q[3] = {fs((float)x, p.origin[0]), fs((float)y, p.origin[1]), fs((float)z, p.origin[2])};
+      out[x] = lattice_value(type, R, __fdiv_rn(2.0f, v[0]), q, v[4]);
+    }
   }
 }
 
 __global__ void __launch_bounds__(256) lattice_blend_kernel(LatticeParams p) {
-  const uint64_t total = (uint64_t)p.nx * p.ny * p.nz;
+  // records of the 4 (y, z) corner rows of the current sample row, per control column
+  __shared__ float s_rec[4][kBlendCx][12];
   const uint32_t c[3] = {p.cx, p.cy, p.cz};
-  const float s[3] = {p.scale[0], p.scale[1], p.scale[2]};
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t pt[3] = {(uint32_t)(i % p.nx), (uint32_t)((i / p.nx) % p.ny), (uint32_t)(i / ((uint64_t)p.nx * p.ny))};
-    const Cell k = locate(pt, c, s);
-    float acc = 0.0f;
-#pragma unroll 1
-    for (int corner = 0; corner < 8; ++corner) {
-      const int d[3] = {corner & 1, (corner >> 1) & 1, (corner >> 2) & 1};
-      int g[3];
-      float w = 1.0f, q[3];
+  const bool staged = p.cx <= kBlendCx;
+  const uint32_t rows = p.ny * p.nz;
+  for (uint32_t row = blockIdx.x; row < rows; row += gridDim.x) {
+    const uint32_t y = row % p.ny, z = row / p.ny;
+    const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
+    const int gy[2] = {c[1] > 1 ? ky.i0 : 0, c[1] > 1 ? ky.i0 + 1 : 0};
+    const int gz[2] = {c[2] > 1 ? kz.i0 : 0, c[2] > 1 ? kz.i0 + 1 : 0};
+    float wyz[4], qy[2], qz[2];
 #pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        g[a] = c[a] > 1 ? k.i0[a] + d[a] : 0;
-        const float wa = d[a] ? k.f[a] : fs(1.0f, k.f[a]);
-        w = (c[a] > 1) ? fm(w, wa) : (d[a] ? 0.0f : w);
-        const float anchor = c[a] > 1 ? fm((float)g[a], p.anchor[a]) : 0.0f;
-        q[a] = fs((float)pt[a], anchor);
-      }
-      if (w == 0.0f) continue;
-      const float* rec = p.blend + 12 * (uint64_t)cidx(g[0], g[1], g[2], c);
-      float R[9];
-#pragma unroll
-      for (int r = 0; r < 9; ++r) R[r] = __ldg(rec + r);
-      const float v = lattice_value(__float_as_uint(__ldg(rec + 11)), R, __ldg(rec + 9), q, __ldg(rec + 10));
-      acc = __fmaf_rn(w, v, acc);
+    for (int d = 0; d < 2; ++d) {
+      qy[d] = fs((float)y, c[1] > 1 ? fm((float)gy[d], p.anchor[1]) : 0.0f);
+      qz[d] = fs((float)z, c[2] > 1 ? fm((float)gz[d], p.anchor[2]) : 0.0f);
     }
-    p.out[i] = acc;
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+      for (int dy = 0; dy < 2; ++dy) wyz[2 * dz + dy] = fm(axis_weight(ky, c[1], dy), axis_weight(kz, c[2], dz));
+    if (staged) {
+      __syncthreads();
+      for (uint32_t i = threadIdx.x; i < 4 * p.cx * 12; i += blockDim.x) {
+        const uint32_t corner = i / (p.cx * 12), rem = i % (p.cx * 12), xc = rem / 12, w = rem % 12;
+        const int dy = corner & 1, dz = corner >> 1;
+        s_rec[corner][xc][w] = __ldg(p.blend + 12 * (uint64_t)cidx((int)xc, gy[dy], gz[dz], c) + w);
+      }
+      __syncthreads();
+    }
+    float* out = p.out + (uint64_t)row * p.nx;
+    for (uint32_t x = threadIdx.x; x < p.nx; x += blockDim.x) {
+      const AxisCell kx = locate1(x, c[0], p.scale[0]);
+      const int gx[2] = {c[0] > 1 ? kx.i0 : 0, c[0] > 1 ? kx.i0 + 1 : 0};
+      float acc = 0.0f;
+#pragma unroll 1
+      for (int corner = 0; corner < 8; ++corner) {
+        const int dx = corner & 1, dy = (corner >> 1) & 1, dz = corner >> 2;
+        const float w = fm(axis_weight(kx, c[0], dx), wyz[2 * dz + dy]);
+        if (w == 0.0f) continue;
+        const float q[3] = {fs((float)x, c[0] > 1 ? fm((float)gx[dx], p.anchor[0]) : 0.0f), qy[dy], qz[dz]};
+        const float* rec = staged ? &s_rec[2 * dz + dy][gx[dx]][0]
+                                  : p.blend + 12 * (uint64_t)cidx(gx[dx], gy[dy], gz[dz], c);
+        float R[9];
+#pragma unroll
+        for (int r = 0; r < 9; ++r) R[r] = rec[r];
+        const float v = lattice_value(__float_as_uint(rec[11]), R, rec[9], q, rec[10]);
+        acc = __fmaf_rn(w, v, acc);
+      }
+      out[x] = acc;
+    }
   }
 }
 
@@ -363,19 +416,22 @@ __global__ void __launch_bounds__(256) csg_kernel(CsgParams p) {
   const uint32_t n = p.n < kMaxPrimsSmem ? p.n : kMaxPrimsSmem;
   for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) prim_setup(p.prims[i], s_pre[i]);
   __syncthreads();
-  const uint64_t total = (uint64_t)p.nx * p.ny * p.nz;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t px = (uint32_t)(i % p.nx), py = (uint32_t)((i / p.nx) % p.ny), pz = (uint32_t)(i / ((uint64_t)p.nx * p.ny));
-    const float X = fm(fs((float)px, p.origin[0]), p.spacing[0]);
+  const uint32_t rows = p.ny * p.nz;
+  for (uint32_t row = blockIdx.x; row < rows; row += gridDim.x) {
+    const uint32_t py = row % p.ny, pz = row / p.ny;
     const float Y = fm(fs((float)py, p.origin[1]), p.spacing[1]);
     const float Z = fm(fs((float)pz, p.origin[2]), p.spacing[2]);
-    float f = INFINITY;
-    for (uint32_t k = 0; k < n; ++k) {
-      const float g = prim_eval(s_pre[k], X, Y, Z);
-      const uint32_t op = s_pre[k].op;
-      f = op == 1 ? fmaxf(f, -g) : (op == 2 ? fmaxf(f, g) : fminf(f, g));
+    float* out = p.out + (uint64_t)row * p.nx;
+    for (uint32_t px = threadIdx.x; px < p.nx; px += blockDim.x) {
+      const float X = fm(fs((float)px, p.origin[0]), p.spacing[0]);
+      float f = INFINITY;
+      for (uint32_t k = 0; k < n; ++k) {
+        const float g = prim_eval(s_pre[k], X, Y, Z);
+        const uint32_t op = s_pre[k].op;
+        f = op == 1 ? fmaxf(f, -g) : (op == 2 ? fmaxf(f, g) : fminf(f, g));
+      }
+      out[px] = f;
     }
-    p.out[i] = f;
   }
 }
 

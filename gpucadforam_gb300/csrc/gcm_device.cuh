@@ -80,10 +80,14 @@ __device__ __forceinline__ float3 lerp3(float3 a, float3 b, float t) {
 }
 
 // Plain edge point (vertexInterp4, src/MarchingCubes_kernel.cu:1619-1629).
-__device__ __forceinline__ float3 edge_point_plain(const uint32_t g[3], const Frame& fr, uint32_t e, const float c[8],
+// `val(k)` returns the field at corner k; only the edge's two corners are read,
+// so no per-voxel corner array is indexed at run time.
+template <class Val>
+__device__ __forceinline__ float3 edge_point_plain(const uint32_t g[3], const Frame& fr, uint32_t e, Val&& val,
                                                    float iso) {
   const int ka = edge_a((int)e), kb = edge_b((int)e);
-  const float t = __fdiv_rn(__fsub_rn(iso, c[ka]), __fsub_rn(c[kb], c[ka]));
+  const float fa = val(ka), fb = val(kb);
+  const float t = __fdiv_rn(__fsub_rn(iso, fa), __fsub_rn(fb, fa));
   return lerp3(corner_pos(g, fr, ka), corner_pos(g, fr, kb), t);
 }
 
@@ -91,12 +95,14 @@ __device__ __forceinline__ float3 edge_point_plain(const uint32_t g[3], const Fr
 // endpoints with labels {0,1} are ordered so that f0 <= f1; the point snaps to
 // an endpoint within 0.0005 of a band edge (compared in double, as the
 // reference's double literal makes it) and otherwise lerps at the band edge
-// crossed.  Where the reference leaves t unset, t = 0.
-__device__ __forceinline__ float3 edge_point_band(const uint32_t g[3], const Frame& fr, uint32_t e, const float lab[8],
-                                                  const float fv[8], float lo, float hi) {
+// crossed.  Where the reference leaves t unset, t = 0.  `lab(k)` / `fv(k)`
+// return the label and the normalised field at corner k.
+template <class Lab, class Fv>
+__device__ __forceinline__ float3 edge_point_band(const uint32_t g[3], const Frame& fr, uint32_t e, Lab&& lab, Fv&& fv,
+                                                  float lo, float hi) {
   int ka = edge_a((int)e), kb = edge_b((int)e);
-  const float id0 = lab[ka], id1 = lab[kb];
-  float f0 = fv[ka], f1 = fv[kb];
+  const float id0 = lab(ka), id1 = lab(kb);
+  float f0 = fv(ka), f1 = fv(kb);
   const bool crossing = (id0 == 1.0f && id1 == 0.0f) || (id0 == 0.0f && id1 == 1.0f);
   if (crossing && f1 < f0) {
     const int tk = ka; ka = kb; kb = tk;

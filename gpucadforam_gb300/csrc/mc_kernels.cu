@@ -27,6 +27,11 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
+
+// Resident CTAs per SM the fused kernel is compiled for (register cap).
+#ifndef GCM_MESH_MIN_BLOCKS
+#define GCM_MESH_MIN_BLOCKS 5
+#endif
 constexpr int kMapPerWarp = 32 * 5;  // up to 5 triangles for each of 32 voxels
 
 struct SmemLayout {
@@ -110,7 +115,7 @@ __device__ __forceinline__ void gather_corners(const float* plane0, const float*
 size_t mesh_smem_bytes(uint32_t nx, uint32_t rows, bool band) { return smem_layout(nx, rows, band).total; }
 
 template <bool BAND, bool EMIT>
-__global__ void __launch_bounds__(kThreads) mc_mesh_kernel(MeshParams p) {
+__global__ void __launch_bounds__(kThreads, GCM_MESH_MIN_BLOCKS) mc_mesh_kernel(MeshParams p) {
   extern __shared__ __align__(16) unsigned char smem[];
   const SmemLayout L = smem_layout(p.nx, p.rows, BAND);
   uint64_t* s_tri = reinterpret_cast<uint64_t*>(smem + L.tri_off);
@@ -281,19 +286,23 @@ __global__ void __launch_bounds__(kThreads) mc_mesh_kernel(MeshParams p) {
           const uint32_t j = k - sexc;  // triangle within its voxel
           const uint32_t sx = xb + src;
           const uint32_t g[3] = {sx, y0 + r, z};
-          float c[8];
-          gather_corners<BAND>(s_f0, s_f1, nx, m0, m1, r, sx, c);
+          // corner k of voxel (sx, r) in the staged planes
+          const float* f0p = s_f0 + m0 + r * nx + sx;
+          const float* f1p = s_f1 + m1 + r * nx + sx;
+          auto fval = [&](int k) { return (corner_z(k) ? f1p : f0p)[corner_y(k) * nx + corner_x(k)]; };
           const uint64_t row = s_tri[sci];
           float3 v[3];
           if (BAND) {
-            float gv[8];
-            gather_corners<BAND>(s_g0, s_g1, nx, m0, m1, r, sx, gv);
+            const float* g0p = s_g0 + m0 + r * nx + sx;
+            const float* g1p = s_g1 + m1 + r * nx + sx;
+            auto gval = [&](int k) { return (corner_z(k) ? g1p : g0p)[corner_y(k) * nx + corner_x(k)]; };
 #pragma unroll
             for (int mI = 0; mI < 3; ++mI)
-              v[mI] = edge_point_band(g, fr, tri_edge_dev(row, 3u * j + mI), c, gv, p.lo, p.hi);
+              v[mI] = edge_point_band(g, fr, tri_edge_dev(row, 3u * j + mI), fval, gval, p.lo, p.hi);
           } else {
 #pragma unroll
-            for (int mI = 0; mI < 3; ++mI) v[mI] = edge_point_plain(g, fr, tri_edge_dev(row, 3u * j + mI), c, p.iso);
+            for (int mI = 0; mI < 3; ++mI)
+              v[mI] = edge_point_plain(g, fr, tri_edge_dev(row, 3u * j + mI), fval, p.iso);
           }
           const float3 n = normal_of(v[0], v[1], v[2]);
           const uint64_t idx = wbase + 3ull * k;
@@ -389,14 +398,17 @@ __global__ void __launch_bounds__(128) mc_generate_kernel(GenerateParams p) {
     const uint32_t ci = cube_index8(c, p.iso);
     const uint64_t row = s_tri[ci];
     const uint32_t nv = row_nverts(row);
-    float gv[8];
-    if (BAND) corners_global(p.g, g, p.nx, p.ny, gv);
+    const uint64_t b0 = (uint64_t)g[0] + (uint64_t)p.nx * ((uint64_t)g[1] + (uint64_t)p.ny * g[2]);
+    const uint64_t sy = p.nx, sz = (uint64_t)p.nx * p.ny;
+    auto off = [&](int k) { return b0 + corner_x(k) + corner_y(k) * sy + corner_z(k) * sz; };
+    auto fval = [&](int k) { return __ldg(p.f + off(k)); };
+    auto gval = [&](int k) { return __ldg(p.g + off(k)); };
     const uint64_t base = p.verts_scan[voxel];
     for (uint32_t j = 0; j < nv; j += 3) {
       float3 v[3];
       for (int m = 0; m < 3; ++m) {
         const uint32_t e = tri_edge_dev(row, j + m);
-        v[m] = BAND ? edge_point_band(g, fr, e, c, gv, p.lo, p.hi) : edge_point_plain(g, fr, e, c, p.iso);
+        v[m] = BAND ? edge_point_band(g, fr, e, fval, gval, p.lo, p.hi) : edge_point_plain(g, fr, e, fval, p.iso);
       }
       const float3 n = normal_of(v[0], v[1], v[2]);
       const uint64_t idx = base + j;
@@ -512,6 +524,11 @@ MeshFn mesh_fn(bool band, bool emit) {
 cudaError_t mesh_prepare(bool band, bool emit, size_t smem, int* blocks_per_sm) {
   const MeshFn f = mesh_fn(band, emit);
   cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  // all of the unified L1/shared storage as shared memory: occupancy is
+  // limited by shared memory, and the kernel reads global memory only
+  // through bulk copies and read-only loads
+  e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, kThreads, smem);
 }

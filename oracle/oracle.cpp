@@ -282,18 +282,20 @@ T ctrl_at(const float* a, int x, int y, int z, const uint32_t c[3]) {
   return a ? (T)a[cidx(x, y, z, c)] : (T)0;
 }
 
-// Trilinear interpolation of one control array, x then y then z, each step
-// lerp(a, b, t) = a + t*(b - a) (FP32: fma(t, b - a, a)).
+// Trilinear interpolation of one control array, y first, then z, then x, each
+// step lerp(a, b, t) = a + t*(b - a) (FP32: fma(t, b - a, a)):
+//   a(xc) = lerp(lerp(v[xc,y0,z0], v[xc,y1,z0], fy), lerp(v[xc,y0,z1], v[xc,y1,z1], fy), fz)
+//   value = lerp(a(x0), a(x1), fx)
 float trilinear32(const float* a, const Cell& k, const uint32_t c[3]) {
   if (!a) return 0.0f;
   const int x1 = c[0] > 1 ? k.i0[0] + 1 : 0, y1 = c[1] > 1 ? k.i0[1] + 1 : 0, z1 = c[2] > 1 ? k.i0[2] + 1 : 0;
   auto L = [](float u, float v, float t) { return std::fma(t, v - u, u); };
   const int x0 = k.i0[0], y0 = k.i0[1], z0 = k.i0[2];
-  const float c00 = L(a[cidx(x0, y0, z0, c)], a[cidx(x1, y0, z0, c)], k.f[0]);
-  const float c10 = L(a[cidx(x0, y1, z0, c)], a[cidx(x1, y1, z0, c)], k.f[0]);
-  const float c01 = L(a[cidx(x0, y0, z1, c)], a[cidx(x1, y0, z1, c)], k.f[0]);
-  const float c11 = L(a[cidx(x0, y1, z1, c)], a[cidx(x1, y1, z1, c)], k.f[0]);
-  return L(L(c00, c10, k.f[1]), L(c01, c11, k.f[1]), k.f[2]);
+  auto col = [&](int xc) {
+    return L(L(a[cidx(xc, y0, z0, c)], a[cidx(xc, y1, z0, c)], k.f[1]),
+             L(a[cidx(xc, y0, z1, c)], a[cidx(xc, y1, z1, c)], k.f[1]), k.f[2]);
+  };
+  return L(col(x0), col(x1), k.f[0]);
 }
 
 double trilinear64(const float* a, const Cell& k, const uint32_t c[3]) {
@@ -302,11 +304,11 @@ double trilinear64(const float* a, const Cell& k, const uint32_t c[3]) {
   auto L = [](double u, double v, double t) { return u + t * (v - u); };
   const int x0 = k.i0[0], y0 = k.i0[1], z0 = k.i0[2];
   const double f0 = k.f[0], f1 = k.f[1], f2 = k.f[2];
-  const double c00 = L(a[cidx(x0, y0, z0, c)], a[cidx(x1, y0, z0, c)], f0);
-  const double c10 = L(a[cidx(x0, y1, z0, c)], a[cidx(x1, y1, z0, c)], f0);
-  const double c01 = L(a[cidx(x0, y0, z1, c)], a[cidx(x1, y0, z1, c)], f0);
-  const double c11 = L(a[cidx(x0, y1, z1, c)], a[cidx(x1, y1, z1, c)], f0);
-  return L(L(c00, c10, f1), L(c01, c11, f1), f2);
+  auto col = [&](int xc) {
+    return L(L(a[cidx(xc, y0, z0, c)], a[cidx(xc, y1, z0, c)], f1), L(a[cidx(xc, y0, z1, c)], a[cidx(xc, y1, z1, c)], f1),
+             f2);
+  };
+  return L(col(x0), col(x1), f0);
 }
 
 // Phase of one lattice in half-turns: X = R q * (2 / period).
@@ -384,14 +386,14 @@ void lattice_field_impl(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t
         for (int corner = 0; corner < 8; ++corner) {
           const int d[3] = {corner & 1, (corner >> 1) & 1, (corner >> 2) & 1};
           int g[3];
-          float w = 1.0f, q[3];
+          float wa[3], q[3];
           for (int a = 0; a < 3; ++a) {
             g[a] = c[a] > 1 ? k.i0[a] + d[a] : 0;
-            const float wa = d[a] ? k.f[a] : 1.0f - k.f[a];
-            w = (c[a] > 1) ? w * wa : (d[a] ? 0.0f : w);
+            wa[a] = (c[a] > 1) ? (d[a] ? k.f[a] : 1.0f - k.f[a]) : (d[a] ? 0.0f : 1.0f);
             const float anchor = c[a] > 1 ? (float)g[a] * ((float)(n[a] - 1) / (float)(c[a] - 1)) : 0.0f;
             q[a] = (float)p[a] - anchor;
           }
+          const float w = wa[0] * (wa[1] * wa[2]);
           if (w == 0.0f) continue;
           const uint64_t ci = cidx(g[0], g[1], g[2], c);
           const float v = lattice_value32(L->type[ci], &R32[9 * ci], 2.0f / L->period[ci], q,
@@ -404,14 +406,14 @@ void lattice_field_impl(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t
         for (int corner = 0; corner < 8; ++corner) {
           const int d[3] = {corner & 1, (corner >> 1) & 1, (corner >> 2) & 1};
           int g[3];
-          double w = 1.0, q[3];
+          double wa[3], q[3];
           for (int a = 0; a < 3; ++a) {
             g[a] = c[a] > 1 ? k.i0[a] + d[a] : 0;
-            const double wa = d[a] ? (double)k.f[a] : 1.0 - (double)k.f[a];
-            w = (c[a] > 1) ? w * wa : (d[a] ? 0.0 : w);
+            wa[a] = (c[a] > 1) ? (d[a] ? (double)k.f[a] : 1.0 - (double)k.f[a]) : (d[a] ? 0.0 : 1.0);
             const double anchor = c[a] > 1 ? (double)g[a] * ((double)(n[a] - 1) / (double)(c[a] - 1)) : 0.0;
             q[a] = (double)p[a] - anchor;
           }
+          const double w = wa[0] * (wa[1] * wa[2]);
           if (w == 0.0) continue;
           const uint64_t ci = cidx(g[0], g[1], g[2], c);
           acc += w * lattice_value64(L->type[ci], &R64[9 * ci], 2.0 / (double)L->period[ci], q,
