@@ -79,6 +79,8 @@ PROTOTYPES = {
     "gcm_mesh_lattice": (I32, [P, C.POINTER(GcmLattice), C.POINTER(GcmGrid), F32, P, P, U64, C.POINTER(GcmCounts), P]),
     "gcm_field_csg": (I32, [P, P, U32, C.POINTER(GcmFrame), U32, U32, U32, P, P]),
     "gcm_test_lookback_stall": (I32, [P, U32, U32, U64, P, P]),
+    "gcm_weld_obj": (I32, [P, P, U64, P, U64, P, U64, C.POINTER(U64), C.POINTER(U64), P]),
+    "gcm_write_obj": (I32, [P, P, U64, C.c_char_p, C.POINTER(U64), C.POINTER(U64), P]),
     "gcm_mesh_field_noalloc": (I32, [P, C.POINTER(GcmGrid), F32, P, P, U64, P, P]),
     "gcm_mesh_csg": (I32, [P, P, U32, C.POINTER(GcmFrame), C.POINTER(GcmGrid), F32, P, P, U64,
                            C.POINTER(GcmCounts), P]),

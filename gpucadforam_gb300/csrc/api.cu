@@ -16,39 +16,19 @@
 #include <string>
 
 #include "../../include/gcm.h"
+#include "gcm_ctx.h"
 #include "gcm_kernels.h"
 
 using gcm::MeshParams;
 
 namespace {
 
-constexpr uint64_t kDefaultWaitNs = 2000000000ull;
-constexpr uint32_t kMeshThreads = 256;
-constexpr uint32_t kTargetVoxelsPerTile = 2048;
+constexpr uint32_t kTargetVoxelsPerTile = GCM_MESH_TILE_VOXELS;
 constexpr size_t kMeshSmemBudget = 96 * 1024;
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 }  // namespace
-
-struct gcm_ctx {
-  int device = 0;
-  int sm_count = 0;
-  size_t smem_optin = 0;
-  uint64_t wait_ns = kDefaultWaitNs;
-  std::atomic<uint64_t> launches{0};
-  std::string last_error;
-  // scratch (device): counts + counters + tile states
-  void* scratch = nullptr;
-  size_t scratch_bytes = 0;
-  // derived field buffer for gcm_mesh_lattice / gcm_mesh_csg
-  float* field_buf = nullptr;
-  size_t field_bytes = 0;
-  float* blend_buf = nullptr;
-  size_t blend_bytes = 0;
-  // pinned host staging for count readback
-  gcm_counts* h_pinned = nullptr;
-};
 
 namespace gcm {
 
@@ -69,11 +49,6 @@ gcm_status cuda_fail(gcm_ctx* ctx, cudaError_t e, const char* what) {
   return fail(ctx, GCM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
-#define GCM_CUDA(ctx, call)                                 \
-  do {                                                      \
-    cudaError_t e_ = (call);                                \
-    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
-  } while (0)
 
 gcm_status ensure_scratch(gcm_ctx* ctx, size_t bytes) {
   // Growing allocates; under stream capture cudaMalloc fails and the error is
@@ -231,7 +206,7 @@ gcm_status read_counts(gcm_ctx* ctx, const gcm_counts* d, gcm_counts* h, cudaStr
   return status_of(ctx, *h);
 }
 
-uint32_t grid_blocks(gcm_ctx* ctx, uint64_t work, uint32_t threads, uint32_t per_sm = 8) {
+uint32_t grid_blocks(gcm_ctx* ctx, uint64_t work, uint32_t threads, uint32_t per_sm) {
   const uint64_t want = (work + threads - 1) / threads;
   const uint64_t cap = (uint64_t)ctx->sm_count * per_sm;
   return (uint32_t)std::max<uint64_t>(1, std::min(want, cap));
@@ -296,6 +271,7 @@ gcm_status gcm_ctx_destroy(gcm_ctx* ctx) {
   if (ctx->field_buf) cudaFree(ctx->field_buf);
   if (ctx->blend_buf) cudaFree(ctx->blend_buf);
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  if (ctx->weld_buf) cudaFree(ctx->weld_buf);
   delete ctx;
   return GCM_OK;
 }

@@ -8,6 +8,11 @@
 
 #include "../../include/gcm.h"
 
+// Voxels per tile the fused kernel aims for (whole voxel rows of one z-plane).
+#ifndef GCM_MESH_TILE_VOXELS
+#define GCM_MESH_TILE_VOXELS 2048
+#endif
+
 namespace gcm {
 
 struct MeshParams {

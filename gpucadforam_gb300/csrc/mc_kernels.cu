@@ -25,7 +25,10 @@ namespace gcm {
 
 namespace {
 
-constexpr int kThreads = 256;
+#ifndef GCM_MESH_THREADS
+#define GCM_MESH_THREADS 256
+#endif
+constexpr int kThreads = GCM_MESH_THREADS;
 constexpr int kWarps = kThreads / 32;
 
 // Resident CTAs per SM the fused kernel is compiled for (register cap).

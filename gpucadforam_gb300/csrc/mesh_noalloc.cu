@@ -41,7 +41,7 @@ namespace {
 
 constexpr size_t kHeaderBytes = 128;  // [64, 128): tile counter
 constexpr uint64_t kNoAllocMaxTiles = (kNoAllocScratchBytes - kHeaderBytes) / sizeof(uint64_t);
-constexpr uint32_t kTargetVoxelsPerTile = 2048;
+constexpr uint32_t kTargetVoxelsPerTile = GCM_MESH_TILE_VOXELS;
 constexpr size_t kSmemBudget = 96 * 1024;
 constexpr int kMaxDevices = 64;
 

@@ -239,6 +239,25 @@ gcm_status gcm_mesh_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_p
                         const gcm_grid* grid, float iso, float* d_pos, float* d_norm, uint64_t capacity_verts,
                         gcm_counts* h_counts, gcm_stream stream);
 
+/* --------------------------------------------------------------- .obj out */
+
+/* Welds an unshared triangle mesh the way File_output::file_write_obj
+ * (src/File_output.cu:5-81) does, on the device: positions quantised to
+ * float(int(x*1000)*0.001), one .obj vertex per distinct quantised position
+ * numbered (1-based) in order of first occurrence, faces with a repeated
+ * vertex dropped, repeated identical faces kept once, faces stored in the
+ * reference's written order (a, c, b).  d_vertices gets 3 floats per vertex,
+ * d_faces 3 uint32 per face (either may be NULL to count only).  Coordinates
+ * must stay within |x| < 1048.576 (GCM_ERR_NOT_SUPPORTED otherwise).  Syncs. */
+gcm_status gcm_weld_obj(gcm_ctx* ctx, const float* d_pos, uint64_t nverts, float* d_vertices, uint64_t cap_vertices,
+                        uint32_t* d_faces, uint64_t cap_faces, uint64_t* h_nvertices, uint64_t* h_nfaces,
+                        gcm_stream stream);
+/* Welds on the device and writes the .obj text file byte for byte as
+ * file_write_obj writes it (header, "v x y z" lines with %g numbers, two blank
+ * lines, " f  a c b" lines).  h_nvertices / h_nfaces are optional. */
+gcm_status gcm_write_obj(gcm_ctx* ctx, const float* d_pos, uint64_t nverts, const char* path, uint64_t* h_nvertices,
+                         uint64_t* h_nfaces, gcm_stream stream);
+
 /* ----------------------------------------------------- allocation-free form */
 
 /* Fused extraction of a fed field for callers that may not allocate device

@@ -10,7 +10,11 @@ working tree).  Outputs:
   Makefile ships it (``-gencode arch=compute_89,code=compute_89``, PTX only, JIT
   compiled by the driver at load time), Makefile:46-48;
 * ``tests/golden/ref_tables.bin`` - the reference's tables.h data, dumped by a tiny
-  host program (``oracle/ref/dump_tables.cpp``).
+  host program (``oracle/ref/dump_tables.cpp``);
+* ``oracle/_ref/obj_ref_writer`` - the reference's own ``.obj`` writer
+  (``File_output.cu``, host C++) linked with ``oracle/ref/obj_ref_driver.cpp``,
+  which supplies a host-memory ``cudaMemcpy`` so it runs without a GPU; used
+  here to make ``tests/golden/golden_obj.json``.
 
 The reference files are compiled with nvcc's defaults (no fast-math; FMA
 contraction on), as the reference Makefile does, but with ``--std=c++17`` instead of
@@ -83,6 +87,16 @@ def dump_tables() -> str:
     return out
 
 
+def build_obj_writer() -> str:
+    exe = os.path.join(OUT, "obj_ref_writer")
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    cmd = ["g++", "-O1", "-std=c++17", "-include", "cuda_runtime_api.h", "-I", cuda_inc, "-I", REF_SRC,
+           "-x", "c++", os.path.join(REF_SRC, "File_output.cu"), "-x", "c++", os.path.join(HERE, "obj_ref_driver.cpp"),
+           "-o", exe]
+    subprocess.run(cmd, check=True, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    return exe
+
+
 def build() -> list[str]:
     if not available():
         return []
@@ -91,6 +105,7 @@ def build() -> list[str]:
     with ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
         outs = list(ex.map(lambda j: _compile(*j), jobs))
     outs.append(dump_tables())
+    outs.append(build_obj_writer())
     return outs
 
 
