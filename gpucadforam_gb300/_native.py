@@ -40,6 +40,29 @@ class GcmLattice(C.Structure):
                 ("d_type", C.c_void_p), ("origin", C.c_float * 3)]
 
 
+class GcmBatchInstance(C.Structure):
+    _fields_ = [("lattice", GcmLattice), ("grid", GcmGrid), ("iso", C.c_float), ("reserved", C.c_uint32)]
+
+
+class GcmServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("lanes", C.c_uint32), ("queue_capacity", C.c_uint32),
+                ("fault_flags", C.c_uint32), ("device_pool_bytes", C.c_uint64), ("host_pool_bytes", C.c_uint64),
+                ("fault_param", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class GcmResult(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("user_tag", C.c_uint64), ("status", C.c_int32), ("lane", C.c_uint32),
+                ("total_verts", C.c_uint64), ("active_voxels", C.c_uint64), ("pos", C.c_void_p),
+                ("norm", C.c_void_p), ("on_host", C.c_uint32), ("reserved", C.c_uint32), ("t_submit", C.c_double),
+                ("t_start", C.c_double), ("t_done", C.c_double)]
+
+
+class GcmServerStats(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "rejected", "cancelled", "failed", "requeued",
+                                          "pool_faults", "device_pool_peak", "device_pool_used",
+                                          "host_pool_peak")] + [("lanes_alive", C.c_uint32), ("pending", C.c_uint32)]
+
+
 class GcmPrimitive(C.Structure):
     _fields_ = [("kind", C.c_uint32), ("op", C.c_uint32), ("flag", C.c_uint32), ("reserved", C.c_uint32),
                 ("center", C.c_float * 3), ("v3", C.c_float * 3), ("p", C.c_float * 6)]
@@ -47,6 +70,12 @@ class GcmPrimitive(C.Structure):
 
 class GcmFrame(C.Structure):
     _fields_ = [("origin", C.c_float * 3), ("spacing", C.c_float * 3)]
+
+
+class GcmRequest(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("n_prims", C.c_uint32), ("lattice", GcmLattice), ("d_prims", C.c_void_p),
+                ("frame", GcmFrame), ("d_field", C.c_void_p), ("grid", GcmGrid), ("iso", C.c_float),
+                ("reserved", C.c_uint32), ("user_tag", C.c_uint64)]
 
 
 P = C.c_void_p
@@ -79,6 +108,22 @@ PROTOTYPES = {
     "gcm_mesh_lattice": (I32, [P, C.POINTER(GcmLattice), C.POINTER(GcmGrid), F32, P, P, U64, C.POINTER(GcmCounts), P]),
     "gcm_field_csg": (I32, [P, P, U32, C.POINTER(GcmFrame), U32, U32, U32, P, P]),
     "gcm_test_lookback_stall": (I32, [P, U32, U32, U64, P, P]),
+    "gcm_batch_create": (I32, [P, P, U32, C.POINTER(P)]),
+    "gcm_batch_destroy": (I32, [P]),
+    "gcm_batch_count": (I32, [P, P, P, C.POINTER(GcmCounts), P]),
+    "gcm_batch_mesh_async": (I32, [P, P, P, U64, P, P, P]),
+    "gcm_batch_mesh_graph": (I32, [P, P, P, U64, P, P, P]),
+    "gcm_batch_tune": (I32, [P, P, P, U64, C.c_char_p, C.POINTER(I32), C.POINTER(U32), P]),
+    "gcm_ctx_set_launch_shape": (I32, [P, I32, U32]),
+    "gcm_server_create": (I32, [C.POINTER(GcmServerConfig), C.POINTER(P)]),
+    "gcm_server_destroy": (I32, [P]),
+    "gcm_server_submit": (I32, [P, C.POINTER(GcmRequest), C.POINTER(U64)]),
+    "gcm_server_poll": (I32, [P, P, U32, C.POINTER(U32), U64]),
+    "gcm_server_release": (I32, [P, U64]),
+    "gcm_server_cancel": (I32, [P, U64]),
+    "gcm_server_get_stats": (I32, [P, C.POINTER(GcmServerStats)]),
+    "gcm_server_now": (C.c_double, [P]),
+    "gcm_test_pool_script": (C.c_int64, [U64, P, P, U32]),
     "gcm_weld_obj": (I32, [P, P, U64, P, U64, P, U64, C.POINTER(U64), C.POINTER(U64), P]),
     "gcm_write_obj": (I32, [P, P, U64, C.c_char_p, C.POINTER(U64), C.POINTER(U64), P]),
     "gcm_mesh_field_noalloc": (I32, [P, C.POINTER(GcmGrid), F32, P, P, U64, P, P]),

@@ -23,7 +23,6 @@ using gcm::MeshParams;
 
 namespace {
 
-constexpr uint32_t kTargetVoxelsPerTile = GCM_MESH_TILE_VOXELS;
 constexpr size_t kMeshSmemBudget = 96 * 1024;
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -86,27 +85,34 @@ gcm_status check_grid(gcm_ctx* ctx, const gcm_grid* g) {
   return GCM_OK;
 }
 
-// Tile shape of the fused mesh kernel: R whole voxel rows, about 2048 voxels,
-// within the shared-memory budget.
+// Tile shape of the fused mesh kernel: R whole voxel rows of about
+// ctx->tile_voxels voxels, within the shared-memory budget.
 struct MeshPlan {
   uint32_t rows, tiles_per_plane, blocks;
+  int threads;
   uint64_t ntiles;
-  size_t smem;
+  MeshLayout layout;
 };
 
+uint32_t rows_for(uint32_t nx, uint32_t ny, uint32_t tile_voxels) {
+  const uint32_t vx = nx - 1;
+  return std::min(std::max<uint32_t>(1, (tile_voxels + vx / 2) / vx), ny - 1);
+}
+
 gcm_status plan_mesh(gcm_ctx* ctx, const gcm_grid* g, bool band, MeshPlan* out) {
-  const uint32_t vx = g->nx - 1, vy = g->ny - 1, vz = g->nz - 1;
-  uint32_t rows = std::max<uint32_t>(1, (kTargetVoxelsPerTile + vx / 2) / vx);
-  rows = std::min(rows, vy);
+  const uint32_t vy = g->ny - 1, vz = g->nz - 1;
+  const int threads = ctx->mesh_threads;
+  uint32_t rows = rows_for(g->nx, g->ny, ctx->tile_voxels);
   const size_t budget = std::min(kMeshSmemBudget, ctx->smem_optin);
-  while (rows > 1 && mesh_smem_bytes(g->nx, rows, band) > budget) --rows;
-  const size_t smem = mesh_smem_bytes(g->nx, rows, band);
-  if (smem > ctx->smem_optin)
+  while (rows > 1 && mesh_layout_for(g->nx, rows, band, threads).total > budget) --rows;
+  const MeshLayout L = mesh_layout_for(g->nx, rows, band, threads);
+  if (L.total > ctx->smem_optin)
     return fail(ctx, GCM_ERR_NOT_SUPPORTED, "grid rows of %u samples do not fit in shared memory", g->nx);
   out->rows = rows;
+  out->threads = threads;
   out->tiles_per_plane = (vy + rows - 1) / rows;
   out->ntiles = (uint64_t)out->tiles_per_plane * vz;
-  out->smem = smem;
+  out->layout = L;
   if (out->ntiles >= (1ull << 31)) return fail(ctx, GCM_ERR_NOT_SUPPORTED, "too many tiles");
   out->blocks = 0;
   return GCM_OK;
@@ -114,11 +120,11 @@ gcm_status plan_mesh(gcm_ctx* ctx, const gcm_grid* g, bool band, MeshPlan* out) 
 
 gcm_status launch_mesh_kernel(gcm_ctx* ctx, bool band, bool emit, MeshParams& p, MeshPlan& plan, cudaStream_t st) {
   int per_sm = 0;
-  GCM_CUDA(ctx, gcm::mesh_prepare(band, emit, plan.smem, &per_sm));
+  GCM_CUDA(ctx, gcm::mesh_prepare(band, emit, plan.threads, plan.layout.total, &per_sm));
   per_sm = std::max(per_sm, 1);
   const uint64_t want = (uint64_t)ctx->sm_count * (uint64_t)per_sm;
   plan.blocks = (uint32_t)std::min<uint64_t>(want, plan.ntiles);
-  GCM_CUDA(ctx, gcm::launch_mesh(band, emit, p, plan.blocks, plan.smem, st));
+  GCM_CUDA(ctx, gcm::launch_mesh(band, emit, plan.threads, p, plan.layout, plan.blocks, st));
   count_launch(ctx, 1);
   return GCM_OK;
 }

@@ -9,6 +9,7 @@
 #include <string>
 
 #include "../../include/gcm.h"
+#include "gcm_kernels.h"
 
 constexpr uint64_t kDefaultWaitNs = 2000000000ull;
 
@@ -17,6 +18,9 @@ struct gcm_ctx {
   int sm_count = 0;
   size_t smem_optin = 0;
   uint64_t wait_ns = kDefaultWaitNs;
+  // fused-kernel launch shape (the autotuner may change both)
+  int mesh_threads = 256;
+  uint32_t tile_voxels = GCM_MESH_TILE_VOXELS;
   std::atomic<uint64_t> launches{0};
   std::string last_error;
   // scratch (device): counts + counters + tile states

@@ -35,6 +35,41 @@ struct MeshParams {
   uint64_t wait_ns;
 };
 
+// Shared-memory layout of the fused kernel (computed on the host for the
+// largest tile the launch will see).
+struct MeshLayout {
+  uint32_t plane_stride;  // floats between the two staged planes of one field
+  uint32_t f_off, g_off, cube_off, win_off, map_off, bar_off, total;
+};
+
+// One grid of a batched extraction.
+struct BatchInstance {
+  const float* f;  // field (16-byte aligned when bulk)
+  uint32_t nx, ny, nz;
+  uint32_t rows, tiles_per_plane, bulk;
+  uint64_t tile_begin;  // first tile in the batch's tile sequence
+  float vs[3], gc[3];
+  float iso;
+  uint32_t pad;
+};
+
+struct BatchMeshParams {
+  const BatchInstance* inst;
+  uint32_t n_inst;
+  uint64_t ntiles;
+  float4* pos;
+  float4* norm;
+  uint64_t capacity;
+  uint64_t* tile_status;
+  uint32_t* counter;
+  uint32_t* status;
+  uint64_t wait_ns;
+  uint64_t* offsets;      // n_inst + 1 vertex offsets (emit pass)
+  uint64_t* inst_active;  // n_inst active-voxel counts
+  uint64_t* inst_verts;   // n_inst vertex counts (count pass)
+  gcm_counts* counts_dev; // whole-batch totals and status
+};
+
 struct GenerateParams {
   const float* f;
   const float* g;
@@ -78,6 +113,13 @@ struct LatticeParams {
   float* out;
 };
 
+// One graded lattice of a batch (GCM_GRADE_PARAMS), its sample rows starting
+// at row_begin of the batch's row sequence.
+struct BatchLattice {
+  LatticeParams p;
+  uint64_t row_begin;
+};
+
 struct CsgParams {
   const gcm_primitive* prims;
   uint32_t n;
@@ -87,8 +129,15 @@ struct CsgParams {
 };
 
 // Launch wrappers (each kernel is launched from the file that defines it).
-cudaError_t mesh_prepare(bool band, bool emit, size_t smem, int* blocks_per_sm);
-cudaError_t launch_mesh(bool band, bool emit, const MeshParams& p, uint32_t blocks, size_t smem, cudaStream_t st);
+bool mesh_threads_supported(int threads);
+MeshLayout mesh_layout(uint32_t plane_floats, uint32_t tile_voxels, uint32_t windows, bool band, int threads);
+MeshLayout mesh_layout_for(uint32_t nx, uint32_t rows, bool band, int threads);
+cudaError_t mesh_prepare(bool band, bool emit, int threads, size_t smem, int* blocks_per_sm);
+cudaError_t launch_mesh(bool band, bool emit, int threads, const MeshParams& p, const MeshLayout& L, uint32_t blocks,
+                        cudaStream_t st);
+cudaError_t batch_prepare(bool emit, int threads, size_t smem, int* blocks_per_sm);
+cudaError_t launch_batch_mesh(bool emit, int threads, const BatchMeshParams& p, const MeshLayout& L, uint32_t blocks,
+                              cudaStream_t st);
 cudaError_t launch_classify(const float* f, uint32_t nx, uint32_t ny, uint64_t nvox, float iso, uint32_t* verts,
                             uint32_t* occ, uint8_t* cube, uint32_t blocks, cudaStream_t st);
 cudaError_t launch_compact(const uint32_t* occ, const uint32_t* scan, uint64_t n, uint32_t* out, uint32_t blocks,
@@ -103,6 +152,8 @@ cudaError_t launch_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t n
                              cudaStream_t st);
 cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t prep_blocks, uint32_t blocks,
                            cudaStream_t st);
+cudaError_t launch_lattice_batch(const BatchLattice* inst, uint32_t n_inst, uint64_t total_rows, uint32_t blocks,
+                                 cudaStream_t st);
 cudaError_t launch_csg(const CsgParams& p, uint32_t blocks, cudaStream_t st);
 cudaError_t launch_normalise(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, unsigned int* enc, float lo,
                              float hi, float* label, float* norm_field, uint32_t blocks, cudaStream_t st);

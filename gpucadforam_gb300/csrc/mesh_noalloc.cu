@@ -44,6 +44,7 @@ constexpr uint64_t kNoAllocMaxTiles = (kNoAllocScratchBytes - kHeaderBytes) / si
 constexpr uint32_t kTargetVoxelsPerTile = GCM_MESH_TILE_VOXELS;
 constexpr size_t kSmemBudget = 96 * 1024;
 constexpr int kMaxDevices = 64;
+constexpr int kThreads = 256;
 
 std::mutex g_setup_mutex;
 void* g_scratch_addr[kMaxDevices] = {};
@@ -85,10 +86,12 @@ extern "C" gcm_status gcm_mesh_field_noalloc(const float* d_field, const gcm_gri
   const size_t budget = std::min(kSmemBudget, (size_t)optin);
   uint32_t rows = std::min<uint32_t>(std::max<uint32_t>(1, (kTargetVoxelsPerTile + vx / 2) / vx), vy);
   auto tiles_for = [&](uint32_t r) { return (uint64_t)((vy + r - 1) / r) * vz; };
-  while (tiles_for(rows) > kNoAllocMaxTiles && rows < vy && gcm::mesh_smem_bytes(grid->nx, rows + 1, false) <= budget)
+  while (tiles_for(rows) > kNoAllocMaxTiles && rows < vy &&
+         gcm::mesh_layout_for(grid->nx, rows + 1, false, kThreads).total <= budget)
     ++rows;
-  while (rows > 1 && gcm::mesh_smem_bytes(grid->nx, rows, false) > budget) --rows;
-  const size_t smem = gcm::mesh_smem_bytes(grid->nx, rows, false);
+  while (rows > 1 && gcm::mesh_layout_for(grid->nx, rows, false, kThreads).total > budget) --rows;
+  const gcm::MeshLayout layout = gcm::mesh_layout_for(grid->nx, rows, false, kThreads);
+  const size_t smem = layout.total;
   const uint64_t ntiles = tiles_for(rows);
   if (ntiles > kNoAllocMaxTiles || smem > (size_t)optin) return GCM_ERR_NOT_SUPPORTED;
 
@@ -125,8 +128,8 @@ extern "C" gcm_status gcm_mesh_field_noalloc(const float* d_field, const gcm_gri
   p.wait_ns = 2000000000ull;
 
   int per_sm = 0;
-  if (gcm::mesh_prepare(false, true, smem, &per_sm) != cudaSuccess) return GCM_ERR_CUDA;
+  if (gcm::mesh_prepare(false, true, kThreads, smem, &per_sm) != cudaSuccess) return GCM_ERR_CUDA;
   const uint32_t blocks = (uint32_t)std::min<uint64_t>((uint64_t)sms * (uint64_t)std::max(per_sm, 1), ntiles);
-  if (gcm::launch_mesh(false, true, p, blocks, smem, st) != cudaSuccess) return GCM_ERR_CUDA;
+  if (gcm::launch_mesh(false, true, kThreads, p, layout, blocks, st) != cudaSuccess) return GCM_ERR_CUDA;
   return GCM_OK;
 }

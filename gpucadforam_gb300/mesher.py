@@ -8,6 +8,7 @@ generate, normalise, mesh) so tests read like the reference's own pipeline
 from __future__ import annotations
 
 import ctypes as C
+import time
 from dataclasses import dataclass
 
 import numpy as np
@@ -171,7 +172,7 @@ class Context:
                                                _ptr(nf), mm, _stream(stream)))
         return label, nf, (mm[0], mm[1])
 
-    def lattice_struct(self, lat):
+    def lattice_struct(self, lat):  # noqa: D401 - also used unbound by Server
         return N.GcmLattice(lat.mode, lat.ctrl[0], lat.ctrl[1], lat.ctrl[2], _ptr(lat.period), _ptr(lat.euler),
                             _ptr(lat.thickness), _ptr(lat.types), (C.c_float * 3)(*lat.origin))
 
@@ -244,3 +245,192 @@ def primitives_to_device(prims, device="cuda"):
 
 def make_frame(origin, spacing):
     return N.GcmFrame((C.c_float * 3)(*origin), (C.c_float * 3)(*spacing))
+
+
+class Batch:
+    """Many graded lattices meshed in one field launch + one fused launch."""
+
+    def __init__(self, ctx: Context, lattices, shapes_zyx, isos=None, voxel_sizes=None, grid_centers=None):
+        self.ctx = ctx
+        self.lattices = list(lattices)  # keeps the device control arrays alive
+        n = len(self.lattices)
+        arr = (N.GcmBatchInstance * n)()
+        for i, lat in enumerate(self.lattices):
+            vs = voxel_sizes[i] if voxel_sizes is not None else (1.0, 1.0, 1.0)
+            gc = grid_centers[i] if grid_centers is not None else (0.0, 0.0, 0.0)
+            arr[i] = N.GcmBatchInstance(ctx.lattice_struct(lat), make_grid(shapes_zyx[i], vs, gc),
+                                        float(isos[i]) if isos is not None else 0.0, 0)
+        self.n = n
+        self.shapes = [tuple(s) for s in shapes_zyx]
+        h = C.c_void_p()
+        ctx.check(ctx.lib.gcm_batch_create(ctx.h, arr, n, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.gcm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+    def count(self, stream=None):
+        verts = (C.c_uint64 * self.n)()
+        active = (C.c_uint64 * self.n)()
+        c = N.GcmCounts()
+        self.ctx.check(self.ctx.lib.gcm_batch_count(self.h, verts, active, C.byref(c), _stream(stream)))
+        return list(verts), list(active), Counts(c.active_voxels, c.total_verts, c.status)
+
+    def buffers(self, capacity, device="cuda"):
+        pos = torch.empty((max(capacity, 1), 4), dtype=torch.float32, device=device)
+        norm = torch.empty((max(capacity, 1), 4), dtype=torch.float32, device=device)
+        offsets = torch.zeros(self.n + 1, dtype=torch.int64, device=device)
+        counts = torch.zeros(4, dtype=torch.int64, device=device)
+        return pos, norm, offsets, counts
+
+    def mesh_async(self, pos, norm, offsets, counts, capacity=None, stream=None, graph=False):
+        cap = pos.shape[0] if capacity is None else capacity
+        fn = self.ctx.lib.gcm_batch_mesh_graph if graph else self.ctx.lib.gcm_batch_mesh_async
+        self.ctx.check(fn(self.h, _ptr(pos), _ptr(norm), int(cap), _ptr(offsets), _ptr(counts), _stream(stream)))
+
+    def tune(self, pos, norm, cache_path=None, stream=None):
+        t = C.c_int(0)
+        v = C.c_uint32(0)
+        self.ctx.check(self.ctx.lib.gcm_batch_tune(self.h, _ptr(pos), _ptr(norm), int(pos.shape[0]),
+                                                   cache_path.encode() if cache_path else None, C.byref(t),
+                                                   C.byref(v), _stream(stream)))
+        return int(t.value), int(v.value)
+
+
+def random_batch_lattices(n, seed, dims=(32, 256), period=(8.0, 48.0), ctrl=8, blend_every=0, device="cuda"):
+    """Config-C4-style instances: dims U{32..256} per axis, one lattice type and
+    one period per instance, thickness and rotation graded on a ctrl^3 grid.
+    Returns (lattices, shapes_zyx)."""
+    rng = np.random.default_rng(seed)
+    lats, shapes = [], []
+    nc = ctrl ** 3
+    for i in range(n):
+        nx, ny, nz = (int(v) for v in rng.integers(dims[0], dims[1] + 1, 3))
+        typ = int(rng.choice([0, 1, 5]))
+        per = float(rng.uniform(*period))
+        mode = 1 if (blend_every and i % blend_every == blend_every - 1) else 0
+        lats.append(Lattice.from_numpy(
+            mode, (ctrl, ctrl, ctrl), np.full(nc, per, np.float32),
+            rng.uniform(-np.pi / 4, np.pi / 4, 3 * nc).astype(np.float32),
+            rng.uniform(-0.6, 0.6, nc).astype(np.float32), np.full(nc, typ, np.uint8),
+            origin=((nx - 1) / 2, (ny - 1) / 2, (nz - 1) / 2), device=device))
+        shapes.append((nz, ny, nx))
+    return lats, shapes
+
+
+class Server:
+    """Continuous-batching mesh server (gcm_server)."""
+
+    def __init__(self, lanes=4, device_pool_bytes=8 << 30, host_pool_bytes=4 << 30, queue_capacity=4096,
+                 fault_flags=0, fault_param=0, device=0):
+        self.lib = N.load()
+        cfg = N.GcmServerConfig(device, lanes, queue_capacity, fault_flags, device_pool_bytes, host_pool_bytes,
+                                fault_param, 0)
+        h = C.c_void_p()
+        rc = self.lib.gcm_server_create(C.byref(cfg), C.byref(h))
+        if rc != 0:
+            raise N.GcmError(rc, "gcm_server_create failed")
+        self.h = h
+        self._keep = {}
+
+    def close(self):
+        if self.h:
+            self.lib.gcm_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+    def now(self):
+        return float(self.lib.gcm_server_now(self.h))
+
+    def submit_lattice(self, lat, shape_zyx, iso=0.0, tag=0, ctx=None):
+        r = N.GcmRequest()
+        r.kind = 0
+        r.lattice = Context.lattice_struct(None, lat)
+        r.grid = make_grid(shape_zyx)
+        r.iso = float(iso)
+        r.user_tag = tag
+        return self._submit(r, lat)
+
+    def submit_csg(self, prims_dev, n_prims, frame, shape_zyx, iso=0.0, tag=0):
+        r = N.GcmRequest()
+        r.kind = 1
+        r.n_prims = n_prims
+        r.d_prims = prims_dev.data_ptr()
+        r.frame = frame
+        r.grid = make_grid(shape_zyx)
+        r.iso = float(iso)
+        r.user_tag = tag
+        return self._submit(r, prims_dev)
+
+    def submit_field(self, field, iso=0.0, tag=0):
+        r = N.GcmRequest()
+        r.kind = 2
+        r.d_field = field.data_ptr()
+        r.grid = make_grid(field.shape)
+        r.iso = float(iso)
+        r.user_tag = tag
+        return self._submit(r, field)
+
+    def _submit(self, r, keep):
+        t = C.c_uint64(0)
+        rc = self.lib.gcm_server_submit(self.h, C.byref(r), C.byref(t))
+        if rc != 0:
+            return rc, None
+        self._keep[int(t.value)] = keep
+        return 0, int(t.value)
+
+    def poll(self, max_results=256, timeout_us=100000):
+        arr = (N.GcmResult * max_results)()
+        n = C.c_uint32(0)
+        rc = self.lib.gcm_server_poll(self.h, arr, max_results, C.byref(n), int(timeout_us))
+        if rc != 0:
+            raise N.GcmError(rc, "gcm_server_poll failed")
+        return [arr[i] for i in range(n.value)]
+
+    def result_arrays(self, res):
+        """(pos, norm) numpy copies of a completed host result."""
+        n = int(res.total_verts)
+        if not res.on_host or n == 0:
+            return np.zeros((0, 4), np.float32), np.zeros((0, 4), np.float32)
+        pos = np.ctypeslib.as_array(C.cast(res.pos, C.POINTER(C.c_float)), shape=(n, 4)).copy()
+        norm = np.ctypeslib.as_array(C.cast(res.norm, C.POINTER(C.c_float)), shape=(n, 4)).copy()
+        return pos, norm
+
+    def release(self, ticket):
+        self._keep.pop(ticket, None)
+        return self.lib.gcm_server_release(self.h, int(ticket))
+
+    def cancel(self, ticket):
+        return self.lib.gcm_server_cancel(self.h, int(ticket))
+
+    def stats(self):
+        s = N.GcmServerStats()
+        self.lib.gcm_server_get_stats(self.h, C.byref(s))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def drain(self, tickets, timeout_s=120.0):
+        """Waits for the given tickets; returns {ticket: (result, pos, norm)}."""
+        want = set(tickets)
+        out = {}
+        t0 = time.time()
+        while want and time.time() - t0 < timeout_s:
+            for r in self.poll():
+                if r.ticket in want:
+                    pos, norm = self.result_arrays(r)
+                    out[r.ticket] = (r, pos, norm)
+                    want.discard(r.ticket)
+                    self.release(r.ticket)
+        return out

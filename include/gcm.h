@@ -239,6 +239,141 @@ gcm_status gcm_mesh_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_p
                         const gcm_grid* grid, float iso, float* d_pos, float* d_norm, uint64_t capacity_verts,
                         gcm_counts* h_counts, gcm_stream stream);
 
+/* ---------------------------------------------------------------- batches */
+
+/* Many graded lattices meshed together: one launch evaluates every
+ * instance's field, one persistent launch meshes every instance's tiles
+ * (a single work list and look-back chain), so the outputs are concatenated
+ * in instance order and instance i's mesh is exactly what gcm_mesh_lattice
+ * produces for it alone.  No counterpart in the reference, which meshes one
+ * grid per call (src/Isosurface.cu:401-486).  Control arrays stay owned by the
+ * caller and must outlive the batch. */
+typedef struct gcm_batch gcm_batch;
+typedef struct gcm_batch_instance {
+  gcm_lattice lattice;
+  gcm_grid grid;
+  float iso;
+  uint32_t reserved;
+} gcm_batch_instance;
+
+/* Allocates everything the batch needs (fields, tile states, instance tables). */
+gcm_status gcm_batch_create(gcm_ctx* ctx, const gcm_batch_instance* h_instances, uint32_t n, gcm_batch** out);
+gcm_status gcm_batch_destroy(gcm_batch* batch);
+/* Counting pass: per-instance vertex and active-voxel counts (host arrays of
+ * n, optional) and totals.  Syncs. */
+gcm_status gcm_batch_count(gcm_batch* batch, uint64_t* h_verts, uint64_t* h_active, gcm_counts* h_counts,
+                           gcm_stream stream);
+/* Fields + fused marching cubes of every instance into one output.
+ * d_offsets (n+1 uint64, device): instance i's vertices are
+ * [d_offsets[i], d_offsets[i+1]).  d_counts: totals and status.  Allocates
+ * nothing and never synchronises (capturable). */
+gcm_status gcm_batch_mesh_async(gcm_batch* batch, float* d_pos, float* d_norm, uint64_t capacity_verts,
+                                uint64_t* d_offsets, gcm_counts* d_counts, gcm_stream stream);
+/* The same launches recorded once into a CUDA graph (per set of buffers and
+ * stream) and replayed. */
+gcm_status gcm_batch_mesh_graph(gcm_batch* batch, float* d_pos, float* d_norm, uint64_t capacity_verts,
+                                uint64_t* d_offsets, gcm_counts* d_counts, gcm_stream stream);
+/* Times the fused launch over CTA sizes {128, 256} x tile sizes {1024 ..
+ * 8192 voxels} on this batch and keeps the fastest; with cache_path, reuses a
+ * recorded choice for the same batch shape and appends new ones.  Writes into
+ * the given output buffers while timing. */
+gcm_status gcm_batch_tune(gcm_batch* batch, float* d_pos, float* d_norm, uint64_t capacity_verts,
+                          const char* cache_path, int* h_threads, uint32_t* h_tile_voxels, gcm_stream stream);
+/* Launch shape of the fused kernel for this context's single-grid calls:
+ * CTA size (128 or 256) and voxels per tile. */
+gcm_status gcm_ctx_set_launch_shape(gcm_ctx* ctx, int threads, uint32_t tile_voxels);
+
+/* ----------------------------------------------------------------- server */
+
+/* Mesh request server with continuous batching.  `lanes` worker threads, each
+ * with its own context and stream, take requests from a bounded FIFO as soon
+ * as one is free and the request's memory can be reserved from a device pool
+ * of device_pool_bytes; requests that arrive while others run are admitted as
+ * lanes and memory free up, and their work overlaps on the GPU.  Memory is
+ * admitted exactly in two passes (field, count, then mesh buffers).  With
+ * host_pool_bytes > 0 each mesh is copied into pinned host memory before its
+ * result completes (latency = submit -> mesh on the host) and its device
+ * memory is returned at once.  No counterpart in the reference (an
+ * interactive single-request application). */
+typedef struct gcm_server gcm_server;
+
+typedef enum gcm_request_kind {
+  GCM_REQUEST_LATTICE = 0, /* graded lattice: lattice + grid */
+  GCM_REQUEST_CSG = 1,     /* primitive scene: d_prims, n_prims, frame + grid */
+  GCM_REQUEST_FIELD = 2    /* caller-owned device field d_field + grid */
+} gcm_request_kind;
+
+/* Host-side fault injection for tests (0 in production). */
+enum {
+  GCM_FAULT_POOL_ALLOC = 1, /* every fault_param-th device reservation fails (retried 3 times) */
+  GCM_FAULT_SLOW_LANE = 2,  /* lane 0 sleeps fault_param ms before each request */
+  GCM_FAULT_LANE_DIES = 4   /* lane 0 exits after taking its first request, which is re-queued */
+};
+
+typedef struct gcm_server_config {
+  int device;
+  uint32_t lanes;          /* concurrent requests on the GPU (1..64) */
+  uint32_t queue_capacity; /* pending requests before submit returns GCM_ERR_BUSY */
+  uint32_t fault_flags;
+  uint64_t device_pool_bytes; /* budget for fields and meshes in flight */
+  uint64_t host_pool_bytes;   /* pinned host memory for results, 0 = results stay on the device */
+  uint32_t fault_param;
+  uint32_t reserved;
+} gcm_server_config;
+
+typedef struct gcm_request {
+  uint32_t kind; /* gcm_request_kind */
+  uint32_t n_prims;
+  gcm_lattice lattice;          /* GCM_REQUEST_LATTICE: device control arrays (resident) */
+  const gcm_primitive* d_prims; /* GCM_REQUEST_CSG */
+  gcm_frame frame;              /* GCM_REQUEST_CSG */
+  const float* d_field;         /* GCM_REQUEST_FIELD */
+  gcm_grid grid;
+  float iso;
+  uint32_t reserved;
+  uint64_t user_tag;
+} gcm_request;
+
+typedef struct gcm_result {
+  uint64_t ticket;
+  uint64_t user_tag;
+  int32_t status; /* gcm_status of the request */
+  uint32_t lane;
+  uint64_t total_verts;
+  uint64_t active_voxels;
+  const float* pos;  /* mesh (host memory when on_host, else device); valid until gcm_server_release */
+  const float* norm;
+  uint32_t on_host;
+  uint32_t reserved;
+  double t_submit, t_start, t_done; /* seconds on the server clock (gcm_server_now) */
+} gcm_result;
+
+typedef struct gcm_server_stats {
+  uint64_t submitted, completed, rejected, cancelled, failed, requeued, pool_faults;
+  uint64_t device_pool_peak, device_pool_used, host_pool_peak;
+  uint32_t lanes_alive, pending;
+} gcm_server_stats;
+
+gcm_status gcm_server_create(const gcm_server_config* cfg, gcm_server** out);
+/* Stops the lanes (running requests finish their current step) and frees the pools. */
+gcm_status gcm_server_destroy(gcm_server* server);
+/* Non-blocking.  GCM_ERR_BUSY when the queue is full; GCM_ERR_REJECTED when the
+ * request's field alone exceeds the device pool (a mesh found too large after
+ * counting completes with GCM_ERR_REJECTED). */
+gcm_status gcm_server_submit(gcm_server* server, const gcm_request* req, uint64_t* h_ticket);
+/* Up to `max` completed results, waiting up to timeout_us for the first. */
+gcm_status gcm_server_poll(gcm_server* server, gcm_result* out, uint32_t max, uint32_t* n_out, uint64_t timeout_us);
+/* Returns a completed request's memory to the pools. */
+gcm_status gcm_server_release(gcm_server* server, uint64_t ticket);
+/* Cancels a pending request at once, a running one at its next step. */
+gcm_status gcm_server_cancel(gcm_server* server, uint64_t ticket);
+gcm_status gcm_server_get_stats(gcm_server* server, gcm_server_stats* out);
+double gcm_server_now(const gcm_server* server);
+/* Host-only check of the server's range allocator (no GPU needed): op[i] > 0
+ * reserves op[i] bytes, op[i] < 0 releases the reservation of operation
+ * -op[i]-1; result[i] = offset or -1.  Returns the number of free ranges left. */
+int64_t gcm_test_pool_script(uint64_t size, const int64_t* op, int64_t* result, uint32_t n);
+
 /* --------------------------------------------------------------- .obj out */
 
 /* Welds an unshared triangle mesh the way File_output::file_write_obj

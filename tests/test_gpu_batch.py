@@ -1,0 +1,106 @@
+"""Batched extraction (config-C4 style) against one-at-a-time extraction.
+
+Every instance's mesh in the batched output must be bit for bit the mesh
+gcm_mesh_lattice makes for that instance alone; graph replay and autotuned
+launch shapes must not change a bit either."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from gpucadforam_gb300.mesher import Context
+
+    c = Context(0)
+    yield c
+    c.close()
+
+
+def _plain(ctx, lat, shape):
+    cnt = ctx.mesh_lattice(lat, shape, 0.0)  # count through the public call (no outputs)
+    pos = torch.empty((max(cnt.total_verts, 1), 4), device="cuda")
+    norm = torch.empty((max(cnt.total_verts, 1), 4), device="cuda")
+    c2 = ctx.mesh_lattice(lat, shape, 0.0, pos=pos, norm=norm)
+    assert c2.total_verts == cnt.total_verts
+    return pos[: c2.total_verts], norm[: c2.total_verts], c2
+
+
+@pytest.fixture(scope="module")
+def batch(ctx):
+    from gpucadforam_gb300.mesher import Batch, random_batch_lattices
+
+    lats, shapes = random_batch_lattices(14, seed=0xD4A + 4, dims=(17, 72), blend_every=5)
+    b = Batch(ctx, lats, shapes)
+    yield b, lats, shapes
+    b.close()
+
+
+def test_batch_equals_one_at_a_time(ctx, batch):
+    b, lats, shapes = batch
+    verts, active, tot = b.count()
+    pos, norm, offsets, counts = b.buffers(tot.total_verts)
+    b.mesh_async(pos, norm, offsets, counts)
+    torch.cuda.synchronize()
+    off = offsets.cpu().numpy().view(np.uint64)
+    c = counts.cpu().numpy().view(np.uint64)
+    assert int(c[1]) == tot.total_verts and int(c[2]) & 0xFFFFFFFF == 0
+    assert int(off[-1]) == tot.total_verts
+    for i, (lat, shape) in enumerate(zip(lats, shapes)):
+        ppos, pnorm, pc = _plain(ctx, lat, shape)
+        a, e = int(off[i]), int(off[i + 1])
+        assert e - a == pc.total_verts == verts[i], i
+        assert active[i] == pc.active_voxels, i
+        assert pos[a:e].cpu().numpy().tobytes() == ppos.cpu().numpy().tobytes(), f"instance {i} positions"
+        assert norm[a:e].cpu().numpy().tobytes() == pnorm.cpu().numpy().tobytes(), f"instance {i} normals"
+
+
+def test_graph_replay_is_identical(ctx, batch):
+    b, _, _ = batch
+    _, _, tot = b.count()
+    pos, norm, offsets, counts = b.buffers(tot.total_verts)
+    b.mesh_async(pos, norm, offsets, counts)
+    torch.cuda.synchronize()
+    ref = pos.clone(), norm.clone(), offsets.clone()
+    for _ in range(3):
+        pos.fill_(0)
+        offsets.fill_(0)
+        b.mesh_async(pos, norm, offsets, counts, graph=True)
+        torch.cuda.synchronize()
+        assert torch.equal(pos, ref[0]) and torch.equal(norm, ref[1]) and torch.equal(offsets, ref[2])
+
+
+def test_tuner_keeps_results_and_reuses_its_cache(ctx, batch, tmp_path):
+    b, _, _ = batch
+    _, _, tot = b.count()
+    pos, norm, offsets, counts = b.buffers(tot.total_verts)
+    b.mesh_async(pos, norm, offsets, counts)
+    torch.cuda.synchronize()
+    ref = pos.clone()
+    cache = str(tmp_path / "tune.txt")
+    t, v = b.tune(pos, norm, cache)
+    assert t in (128, 256) and v in (1024, 2048, 4096, 8192)
+    lines = open(cache).read().splitlines()
+    assert len(lines) == 1 and lines[0].startswith("gcm-tune-v1 ")
+    assert b.tune(pos, norm, cache) == (t, v)
+    assert len(open(cache).read().splitlines()) == 1  # second call read the cache
+    b.mesh_async(pos, norm, offsets, counts)
+    torch.cuda.synchronize()
+    assert torch.equal(pos, ref)
+
+
+@pytest.mark.parametrize("shape_", [(128, 1024), (256, 4096), (128, 8192)])
+def test_single_grid_launch_shapes_are_identical(shape_):
+    import oracle as O
+    from gpucadforam_gb300.mesher import Context
+
+    c = Context(0)
+    f = torch.from_numpy(O.lattice_field((90, 70, 50), 0, (1, 1, 1), np.array([14.0], np.float32),
+                                         types=np.array([1], np.uint8))).cuda()
+    ref_pos, ref_norm, _ = c.mesh_field(f, 0.2)
+    c.check(c.lib.gcm_ctx_set_launch_shape(c.h, shape_[0], shape_[1]))
+    pos, norm, _ = c.mesh_field(f, 0.2)
+    assert torch.equal(pos, ref_pos) and torch.equal(norm, ref_norm)
+    c.close()
