@@ -280,6 +280,120 @@ def run_batched(ctx, steps, warmup, n_inst=256, seed=SEED + 2):
             "graph": True, "identical_to_plain": same}
 
 
+def served_requests(seed, duration_s, rate, device="cuda"):
+    """Config C5 request stream: Poisson arrivals, cubic grids with edges
+    log-uniform in [64, 512], 70% graded TPMS lattices (blend grading against
+    one of 8 resident 8^3 grading fields), 30% CSG scenes of U{8..64}
+    primitives.  Returns (arrival_s, requests, resident lattices)."""
+    from gpucadforam_gb300.mesher import Lattice, make_frame, primitives_to_device
+
+    rng = np.random.default_rng(seed)
+    nc = 8 ** 3
+    resident = [Lattice.from_numpy(1, (8, 8, 8), rng.uniform(16, 64, nc).astype(np.float32),
+                                   rng.uniform(-np.pi / 4, np.pi / 4, 3 * nc).astype(np.float32),
+                                   rng.uniform(-0.6, 0.6, nc).astype(np.float32),
+                                   rng.choice(np.array([0, 1, 5], np.uint8), nc), device=device) for _ in range(8)]
+    t, arrivals, reqs = 0.0, [], []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration_s:
+            break
+        edge = int(round(np.exp(rng.uniform(np.log(64), np.log(512)))))
+        shape = (edge, edge, edge)
+        if rng.random() < 0.7:
+            reqs.append(("lattice", resident[int(rng.integers(0, 8))], shape))
+        else:
+            k = int(rng.integers(8, 65))
+            prims = []
+            for j in range(k):
+                kind = int(rng.integers(0, 3))
+                c = rng.uniform(0, 1, 3)
+                op = 1 if j >= k - max(1, k // 8) else 0
+                if kind == 0:
+                    prims.append(dict(kind=0, op=op, center=c, p=[rng.uniform(0.02, 0.15), 0.0]))
+                elif kind == 1:
+                    r, hh = rng.uniform(0.02, 0.12, 2)
+                    prims.append(dict(kind=1, op=op, center=c, v3=(0, 0, 1), p=[r, 0.0, 2 * hh]))
+                else:
+                    prims.append(dict(kind=2, op=op, center=c, p=list(2 * rng.uniform(0.02, 0.12, 3))))
+            h = np.float32(1.0 / (edge - 1))
+            reqs.append(("csg", (primitives_to_device(prims, device), k, make_frame((0, 0, 0), (h, h, h))), shape))
+        arrivals.append(t)
+    return arrivals, reqs, resident
+
+
+def serve_stream(arrivals, reqs, lanes, pool_bytes=64 << 30, host_bytes=16 << 30, saturate=False):
+    """Runs the stream through a gcm_server; returns latency and throughput."""
+    from gpucadforam_gb300.mesher import Server
+
+    srv = Server(lanes=lanes, device_pool_bytes=pool_bytes, host_pool_bytes=host_bytes,
+                 queue_capacity=max(64, len(reqs) + 1))
+    done = {}
+    t_sub = {}
+    lock = threading.Lock()
+
+    def submitter():
+        t0 = time.perf_counter()
+        for i, (arr, r) in enumerate(zip(arrivals, reqs)):
+            if not saturate:
+                dt = arr - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+            kind, payload, shape = r
+            if kind == "lattice":
+                rc, tk = srv.submit_lattice(payload, shape, 0.0, i)
+            else:
+                rc, tk = srv.submit_csg(payload[0], payload[1], payload[2], shape, 0.0, i)
+            with lock:
+                t_sub[i] = (rc, tk)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    n_ok = n_bad = 0
+    lat, tdone, tsub, verts = [], [], [], 0
+    deadline = time.time() + 600
+    while (th.is_alive() or n_ok + n_bad < len(reqs)) and time.time() < deadline:
+        for res in srv.poll(timeout_us=20000):
+            if res.status == 0:
+                n_ok += 1
+                lat.append(res.t_done - res.t_submit)
+                tdone.append(res.t_done)
+                tsub.append(res.t_submit)
+                verts += res.total_verts
+            else:
+                n_bad += 1
+            srv.release(res.ticket)
+        with lock:
+            n_bad += sum(1 for v in t_sub.values() if v[0] != 0)
+            t_sub = {k: v for k, v in t_sub.items() if v[0] == 0}
+    th.join()
+    st = srv.stats()
+    srv.close()
+    span = (max(tdone) - min(tsub)) if tdone else float("nan")
+    lat_ms = np.array(lat) * 1e3
+    return {"lanes": lanes, "requests": len(reqs), "completed": n_ok, "failed_or_rejected": n_bad,
+            "p50_ms": float(np.percentile(lat_ms, 50)) if n_ok else None,
+            "p99_ms": float(np.percentile(lat_ms, 99)) if n_ok else None,
+            "meshes_per_s": n_ok / span if n_ok else 0.0, "span_s": span, "verts": int(verts),
+            "device_pool_peak_gb": st["device_pool_peak"] / 1e9}
+
+
+def run_served(duration_s=4.0, rate=200.0, lanes=6, seed=SEED + 3):
+    arrivals, reqs, resident = served_requests(seed, duration_s, rate)
+    served = serve_stream(arrivals, reqs, lanes)
+    plain = serve_stream(arrivals, reqs, 1)
+    sat_served = serve_stream(arrivals, reqs, lanes, saturate=True)
+    sat_plain = serve_stream(arrivals, reqs, 1, saturate=True)
+    return {"workload": f"Poisson {rate:g} req/s for {duration_s:g} s, edges log-U[64,512], 70% graded TPMS "
+                        f"(blend grading, 8 resident 8^3 grading fields) / 30% CSG (8-64 primitives), 64 GB pool, "
+                        f"meshes copied to pinned host memory",
+            "offered_rate": rate, "served": served, "plain_one_lane": plain,
+            "saturation_meshes_per_s": sat_served["meshes_per_s"],
+            "saturation_plain_meshes_per_s": sat_plain["meshes_per_s"],
+            "saturation_speedup": (sat_served["meshes_per_s"] / sat_plain["meshes_per_s"]
+                                   if sat_plain["meshes_per_s"] else None)}
+
+
 def run_gcm(args):
     import torch
 
@@ -395,6 +509,9 @@ def run_gcm(args):
     batched = None
     if not args.no_batched:
         batched = run_batched(ctx, args.steps, args.warmup)
+    served = None
+    if not args.no_served and rank == 0:
+        served = run_served()
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -415,7 +532,7 @@ def run_gcm(args):
                              "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                              "algorithmic_bytes": mc_bytes, "traffic": traffic},
                 "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
-                "batched": batched}
+                "batched": batched, "served": served}
         print(json.dumps(line))
     ctx.close()
     if pg is not None:
@@ -434,6 +551,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -96,7 +96,7 @@ struct MeshPlan {
 
 uint32_t rows_for(uint32_t nx, uint32_t ny, uint32_t tile_voxels) {
   const uint32_t vx = nx - 1;
-  return std::min(std::max<uint32_t>(1, (tile_voxels + vx / 2) / vx), ny - 1);
+  return std::min(std::min(std::max<uint32_t>(1, (tile_voxels + vx / 2) / vx), ny - 1), max_tile_rows(vx));
 }
 
 gcm_status plan_mesh(gcm_ctx* ctx, const gcm_grid* g, bool band, MeshPlan* out) {
@@ -104,8 +104,8 @@ gcm_status plan_mesh(gcm_ctx* ctx, const gcm_grid* g, bool band, MeshPlan* out) 
   const int threads = ctx->mesh_threads;
   uint32_t rows = rows_for(g->nx, g->ny, ctx->tile_voxels);
   const size_t budget = std::min(kMeshSmemBudget, ctx->smem_optin);
-  while (rows > 1 && mesh_layout_for(g->nx, rows, band, threads).total > budget) --rows;
-  const MeshLayout L = mesh_layout_for(g->nx, rows, band, threads);
+  while (rows > 1 && mesh_layout_for(g->nx, rows, band).total > budget) --rows;
+  const MeshLayout L = mesh_layout_for(g->nx, rows, band);
   if (L.total > ctx->smem_optin)
     return fail(ctx, GCM_ERR_NOT_SUPPORTED, "grid rows of %u samples do not fit in shared memory", g->nx);
   out->rows = rows;

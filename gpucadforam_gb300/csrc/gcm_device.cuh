@@ -28,6 +28,23 @@ __device__ __forceinline__ uint32_t row_nverts(uint64_t row) {
 }
 __device__ __forceinline__ uint32_t row_ntris(uint64_t row) { return row_nverts(row) / 3u; }
 
+// The fused kernel's copy of the table: the lowest nibble of every row (the
+// 0xF terminator in every configuration, which has at most 15 edge entries)
+// holds the configuration's triangle count instead, so `row & 0xF` is the
+// count and the edge nibbles of triangles 0..4 are unchanged.
+__device__ __forceinline__ void load_tri_table_counted(uint64_t* s_tri) {
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    const uint64_t r = g_tri_rows[i];
+    s_tri[i] = (r & ~0xFull) | row_ntris(r);
+  }
+}
+
+// Edges 3j, 3j+1, 3j+2 of triangle j (j < 5) as a 12-bit group, first edge in
+// the top nibble.
+__device__ __forceinline__ uint32_t tri_edges3(uint64_t row, uint32_t j) {
+  return (uint32_t)(row >> (52u - 12u * j)) & 0xFFFu;
+}
+
 __device__ __forceinline__ uint32_t tri_edge_dev(uint64_t row, uint32_t j) {
   return (uint32_t)((row >> (4u * (15u - j))) & 0xFu);
 }
@@ -79,6 +96,29 @@ __device__ __forceinline__ float3 lerp3(float3 a, float3 b, float t) {
   return make_float3(lerp_coord(a.x, b.x, t), lerp_coord(a.y, b.y, t), lerp_coord(a.z, b.z, t));
 }
 
+// The two candidate coordinates of a voxel's corners on each axis:
+// corner_coord(g, gc, vs, 0) and corner_coord(g, gc, vs, 1).
+struct VoxelCorners {
+  float x0, x1, y0, y1, z0, z1;
+};
+
+__device__ __forceinline__ void axis_corners(uint32_t g, float gc, float vs, float& c0, float& c1) {
+  c0 = corner_coord(g, gc, vs, 0);
+  c1 = corner_coord(g, gc, vs, 1);
+}
+
+// Corner with bits (x | y << 1 | z << 2): equal to corner_pos for that corner.
+__device__ __forceinline__ float3 corner_sel(const VoxelCorners& V, uint32_t bits) {
+  return make_float3((bits & 1u) ? V.x1 : V.x0, (bits & 2u) ? V.y1 : V.y0, (bits & 4u) ? V.z1 : V.z0);
+}
+
+// Plain edge point from the two corner values and positions (the same
+// arithmetic as edge_point_plain).
+__device__ __forceinline__ float3 edge_point_plain_v(float fa, float fb, float3 pa, float3 pb, float iso) {
+  const float t = __fdiv_rn(__fsub_rn(iso, fa), __fsub_rn(fb, fa));
+  return lerp3(pa, pb, t);
+}
+
 // Plain edge point (vertexInterp4, src/MarchingCubes_kernel.cu:1619-1629).
 // `val(k)` returns the field at corner k; only the edge's two corners are read,
 // so no per-voxel corner array is indexed at run time.
@@ -109,6 +149,38 @@ __device__ __forceinline__ float3 edge_point_band(const uint32_t g[3], const Fra
     const float tf = f0; f0 = f1; f1 = tf;
   }
   const float3 pa = corner_pos(g, fr, ka), pb = corner_pos(g, fr, kb);
+  float t = 0.0f;
+  if (crossing) {
+    bool done = false;
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      const float lev = side ? hi : lo;
+      if (!done && (f1 >= lev) && (f0 <= lev)) {
+        if ((double)fabsf(__fsub_rn(lev, f0)) < 0.0005) return pa;
+        if ((double)fabsf(__fsub_rn(lev, f1)) < 0.0005) return pb;
+        if ((double)fabsf(__fsub_rn(f1, f0)) < 0.0005) return pa;
+        t = __fdiv_rn(__fsub_rn(lev, f0), __fsub_rn(f1, f0));
+        done = true;
+      }
+    }
+    if (!done) {
+      if ((f1 == f0) && ((double)pa.z == 0.0)) t = 1.0f;
+      else if (f1 == f0) t = 0.0f;
+    }
+  }
+  return lerp3(pa, pb, t);
+}
+
+// Band edge point from the corner labels, normalised values and corner bits
+// (the same arithmetic and branch order as edge_point_band).
+__device__ __forceinline__ float3 edge_point_band_v(float id0, float id1, float f0, float f1, uint32_t ba, uint32_t bb,
+                                                    const VoxelCorners& V, float lo, float hi) {
+  const bool crossing = (id0 == 1.0f && id1 == 0.0f) || (id0 == 0.0f && id1 == 1.0f);
+  if (crossing && f1 < f0) {
+    const uint32_t tb = ba; ba = bb; bb = tb;
+    const float tf = f0; f0 = f1; f1 = tf;
+  }
+  const float3 pa = corner_sel(V, ba), pb = corner_sel(V, bb);
   float t = 0.0f;
   if (crossing) {
     bool done = false;

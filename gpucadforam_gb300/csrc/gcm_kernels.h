@@ -12,8 +12,18 @@
 #ifndef GCM_MESH_TILE_VOXELS
 #define GCM_MESH_TILE_VOXELS 2048
 #endif
+// Triangle-list entries per two voxels of a tile: a tile with more triangles
+// emits in several rounds.
+#ifndef GCM_MESH_LIST_PER_2VOX
+#define GCM_MESH_LIST_PER_2VOX 3
+#endif
 
 namespace gcm {
+
+// Most voxels in one tile (the triangle list keeps a voxel's index within its
+// tile in 16 bits), as a row limit for rows of vx voxels.
+constexpr uint32_t kMaxTileVoxels = 65535;
+inline uint32_t max_tile_rows(uint32_t vx) { return vx >= kMaxTileVoxels ? 1u : kMaxTileVoxels / vx; }
 
 struct MeshParams {
   const float* f;  // classify field (band mode: the label field)
@@ -38,8 +48,9 @@ struct MeshParams {
 // Shared-memory layout of the fused kernel (computed on the host for the
 // largest tile the launch will see).
 struct MeshLayout {
-  uint32_t plane_stride;  // floats between the two staged planes of one field
-  uint32_t f_off, g_off, cube_off, win_off, map_off, bar_off, total;
+  uint32_t plane_stride;  // floats between consecutive staged planes
+  uint32_t list_cap;      // triangle-list entries per emission round
+  uint32_t f_off, cube_off, win_off, edge_off, list_off, bar_off, total;
 };
 
 // One grid of a batched extraction.
@@ -130,8 +141,8 @@ struct CsgParams {
 
 // Launch wrappers (each kernel is launched from the file that defines it).
 bool mesh_threads_supported(int threads);
-MeshLayout mesh_layout(uint32_t plane_floats, uint32_t tile_voxels, uint32_t windows, bool band, int threads);
-MeshLayout mesh_layout_for(uint32_t nx, uint32_t rows, bool band, int threads);
+MeshLayout mesh_layout(uint32_t plane_floats, uint32_t tile_voxels, uint32_t windows, bool band);
+MeshLayout mesh_layout_for(uint32_t nx, uint32_t rows, bool band);
 cudaError_t mesh_prepare(bool band, bool emit, int threads, size_t smem, int* blocks_per_sm);
 cudaError_t launch_mesh(bool band, bool emit, int threads, const MeshParams& p, const MeshLayout& L, uint32_t blocks,
                         cudaStream_t st);

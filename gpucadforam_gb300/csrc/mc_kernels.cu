@@ -18,6 +18,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "gcm_device.cuh"
 #include "gcm_kernels.h"
 
@@ -25,7 +27,6 @@ namespace gcm {
 
 namespace {
 
-constexpr int kMapPerWarp = 32 * 5;  // up to 5 triangles for each of 32 voxels
 
 // Register cap per CTA size: resident CTAs per SM the kernel is compiled for.
 #ifndef GCM_MESH_MIN_BLOCKS
@@ -79,6 +80,7 @@ struct TileGeom {
   uint32_t nx, ny, z, y0, rows, bulk;
   Frame fr;
   float iso, lo, hi;
+  uint32_t inst, local;  // batch bookkeeping: instance and tile within it
 };
 
 // What a tile leaves for the kernel around it (shared memory).
@@ -87,6 +89,7 @@ struct TileOut {
   uint32_t tris;    // triangles in the tile
   uint32_t active;  // active voxels in the tile
   uint32_t ok;
+  uint32_t next_window;  // emission work counter
 };
 
 struct EmitTarget {
@@ -98,81 +101,131 @@ struct EmitTarget {
   uint64_t wait_ns;
 };
 
-// Steps 1-5 of one tile (see the file comment).  Every thread of the CTA calls
-// it; it ends with a barrier.  Returns false when the CTA has to stop taking
-// tiles (a bulk copy did not land within the wait limit).
-template <bool BAND, bool EMIT, int THREADS>
-__device__ __forceinline__ bool mesh_tile(const TileGeom& tg, uint64_t t, const MeshLayout& L, unsigned char* smem,
-                                          uint32_t& parity, const EmitTarget& out, TileOut& res) {
-  constexpr uint32_t kWarps = THREADS / 32;
-  const uint64_t* s_tri = reinterpret_cast<const uint64_t*>(smem);
-  float* s_f0 = reinterpret_cast<float*>(smem + L.f_off);
-  float* s_f1 = s_f0 + L.plane_stride;
-  float* s_g0 = reinterpret_cast<float*>(smem + L.g_off);
-  float* s_g1 = s_g0 + L.plane_stride;
-  uint8_t* s_cube = smem + L.cube_off;
-  uint32_t* s_win = reinterpret_cast<uint32_t*>(smem + L.win_off);
-  uint8_t* s_map = smem + L.map_off;
-  uint64_t* s_bar = reinterpret_cast<uint64_t*>(smem + L.bar_off);
+// The staging buffer: planes z and z+1 of the classify field, then (band
+// mode) of the interpolation field.
+struct Planes {
+  float *f0, *f1, *g0, *g1;
+};
 
-  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const uint32_t nx = tg.nx, vx = nx - 1;
-  const uint32_t nwx = (vx + 31u) / 32u;
-  const uint32_t rows = tg.rows, z = tg.z, y0 = tg.y0;
+__device__ __forceinline__ Planes planes_of(unsigned char* smem, const MeshLayout& L) {
+  unsigned char* base = smem + L.f_off;
+  Planes P;
+  P.f0 = reinterpret_cast<float*>(base);
+  P.f1 = P.f0 + L.plane_stride;
+  P.g0 = P.f1 + L.plane_stride;
+  P.g1 = P.g0 + L.plane_stride;
+  return P;
+}
 
-  // 1. stage sample rows y0..y0+rows of planes z and z+1
-  const uint64_t st0 = ((uint64_t)z * tg.ny + y0) * nx;
-  const uint64_t st1 = st0 + (uint64_t)tg.ny * nx;
-  const uint32_t cnt = (rows + 1) * nx;
+__device__ __forceinline__ uint64_t* bar_of(unsigned char* smem, const MeshLayout& L) {
+  return reinterpret_cast<uint64_t*>(smem + L.bar_off);
+}
+
+// Phase 1: issue the staging of tile tg (every thread calls it; thread 0
+// issues the bulk copies, every thread loads the ragged ends).  The caller
+// guarantees that no thread still reads the buffer.
+template <bool BAND>
+__device__ __forceinline__ void tile_stage(const TileGeom& tg, const MeshLayout& L, unsigned char* smem) {
+  const Planes P = planes_of(smem, L);
+  uint64_t* bar = bar_of(smem, L);
+  const uint64_t st0 = ((uint64_t)tg.z * tg.ny + tg.y0) * tg.nx;
+  const uint64_t st1 = st0 + (uint64_t)tg.ny * tg.nx;
+  const uint32_t cnt = (tg.rows + 1) * tg.nx;
   const bool bulk = tg.bulk != 0;
   const Run r0 = plan_run(st0, cnt, bulk), r1 = plan_run(st1, cnt, bulk);
-  if (bulk && tid == 0) {
-    // The barrier before this tile ordered every thread's reads of the previous
-    // one; the proxy fence orders them before the async-proxy writes.  Expect
-    // the bytes first, then issue the copies.
+  if (bulk && threadIdx.x == 0) {
+    // Every thread's reads of this buffer were ordered by a barrier before
+    // this call; the proxy fence orders them before the async-proxy writes.
+    // Expect the bytes first, then issue the copies.
     fence_proxy_async();
     const uint32_t bytes = (r0.body + r1.body) * 4u * (BAND ? 2u : 1u);
-    mbar_arrive_expect_tx(s_bar, bytes);
-    stage_bulk(s_f0, tg.f, st0, r0, s_bar);
-    stage_bulk(s_f1, tg.f, st1, r1, s_bar);
+    mbar_arrive_expect_tx(bar, bytes);
+    stage_bulk(P.f0, tg.f, st0, r0, bar);
+    stage_bulk(P.f1, tg.f, st1, r1, bar);
     if (BAND) {
-      stage_bulk(s_g0, tg.g, st0, r0, s_bar);
-      stage_bulk(s_g1, tg.g, st1, r1, s_bar);
+      stage_bulk(P.g0, tg.g, st0, r0, bar);
+      stage_bulk(P.g1, tg.g, st1, r1, bar);
     }
   }
-  stage_scalar(s_f0, tg.f, st0, cnt, r0);
-  stage_scalar(s_f1, tg.f, st1, cnt, r1);
+  stage_scalar(P.f0, tg.f, st0, cnt, r0);
+  stage_scalar(P.f1, tg.f, st1, cnt, r1);
   if (BAND) {
-    stage_scalar(s_g0, tg.g, st0, cnt, r0);
-    stage_scalar(s_g1, tg.g, st1, cnt, r1);
+    stage_scalar(P.g0, tg.g, st0, cnt, r0);
+    stage_scalar(P.g1, tg.g, st1, cnt, r1);
   }
+}
+
+// Phase 2: wait for the staging (bounded).  Returns false when the CTA has to
+// stop taking tiles (a copy did not land within twice the limit).
+__device__ __forceinline__ bool tile_wait(const TileGeom& tg, const MeshLayout& L, unsigned char* smem,
+                                          uint32_t& parity, const EmitTarget& out, TileOut& res) {
   bool lost = false;
-  if (bulk) {
-    if (!mbar_wait_bounded(s_bar, parity, out.wait_ns)) {
+  if (tg.bulk) {
+    uint64_t* bar = bar_of(smem, L);
+    if (!mbar_wait_bounded(bar, parity, out.wait_ns)) {
       set_status(out.status, kStatusTimeout);
       res.ok = 0;
       // The copy is still owed to this barrier: wait for it once more before
       // the buffer is reused; if it still has not landed, stop taking tiles.
-      lost = !mbar_wait_bounded(s_bar, parity, out.wait_ns);
+      lost = !mbar_wait_bounded(bar, parity, out.wait_ns);
     }
     parity ^= 1u;
   }
-  if (__syncthreads_or(lost)) return false;
-  const uint32_t m0 = (uint32_t)(st0 & 3u), m1 = (uint32_t)(st1 & 3u);
+  return !__syncthreads_or(lost);
+}
 
-  // 2. classify in warp windows of 32 consecutive voxels of a row
-  const uint32_t nwin = rows * nwx;
+// Window w of a tile as (row, window within the row), stepped without a
+// division: windows are taken with a fixed stride per warp.
+struct WindowCursor {
+  uint32_t r, xw;
+  __device__ __forceinline__ WindowCursor(uint32_t w, uint32_t nwx) : r(0), xw(w) { advance(0, nwx); }
+  __device__ __forceinline__ void advance(uint32_t by, uint32_t nwx) {
+    xw += by;
+    while (xw >= nwx) {
+      xw -= nwx;
+      ++r;
+    }
+  }
+};
+
+// Phase 3: classify in warp windows of 32 consecutive voxels of a row, scan the
+// window triangle counts and write the tile's edge table.  Ends with a barrier.
+template <int THREADS>
+__device__ __forceinline__ void tile_classify(const TileGeom& tg, const MeshLayout& L, unsigned char* smem,
+                                              TileOut& res) {
+  constexpr uint32_t kWarps = THREADS / 32;
+  const uint64_t* s_tri = reinterpret_cast<const uint64_t*>(smem);
+  const Planes P = planes_of(smem, L);
+  uint8_t* s_cube = smem + L.cube_off;
+  uint32_t* s_win = reinterpret_cast<uint32_t*>(smem + L.win_off);
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t nx = tg.nx, vx = nx - 1, nwx = (vx + 31u) / 32u, nwin = tg.rows * nwx;
+  const uint64_t st0 = ((uint64_t)tg.z * tg.ny + tg.y0) * nx;
+  const uint32_t m0 = (uint32_t)(st0 & 3u), m1 = (uint32_t)((st0 + (uint64_t)tg.ny * nx) & 3u);
+  if (threadIdx.x >= THREADS - 12) {
+    // edge table: shared-memory offsets of the edge's corners from the
+    // voxel's first sample (plane z + 1 lies `dplane` floats after plane z),
+    // and the corners' bits
+    const uint32_t e = threadIdx.x - (THREADS - 12);
+    const uint32_t dplane = L.plane_stride + m1 - m0;
+    auto off = [&](uint32_t k) { return (uint32_t)corner_z((int)k) * dplane + (uint32_t)corner_y((int)k) * nx + (uint32_t)corner_x((int)k); };
+    auto bits = [&](uint32_t k) { return (uint32_t)(corner_x((int)k) | (corner_y((int)k) << 1) | (corner_z((int)k) << 2)); };
+    const uint32_t ka = (uint32_t)edge_a((int)e), kb = (uint32_t)edge_b((int)e);
+    reinterpret_cast<uint64_t*>(smem + L.edge_off)[e] =
+        (uint64_t)off(ka) | ((uint64_t)off(kb) << 16) | ((uint64_t)bits(ka) << 32) | ((uint64_t)bits(kb) << 35);
+  }
   uint32_t my_active = 0;
-  for (uint32_t w = warp; w < nwin; w += kWarps) {
-    const uint32_t r = w / nwx, x = (w % nwx) * 32u + lane;
+  WindowCursor cur(warp, nwx);
+  for (uint32_t w = warp; w < nwin; w += kWarps, cur.advance(kWarps, nwx)) {
+    const uint32_t r = cur.r, x = cur.xw * 32u + lane;
     uint32_t nt = 0;
     if (x < vx) {
-      const float* a = s_f0 + m0 + r * nx + x;
-      const float* b = s_f1 + m1 + r * nx + x;
-      const float c[8] = {a[0], a[1], a[nx + 1], a[nx], b[0], b[1], b[nx + 1], b[nx]};
+      const float* a = P.f0 + m0 + r * nx + x;
+      const float* c1 = P.f1 + m1 + r * nx + x;
+      const float c[8] = {a[0], a[1], a[nx + 1], a[nx], c1[0], c1[1], c1[nx + 1], c1[nx]};
       const uint32_t ci = cube_index8(c, tg.iso);
       s_cube[r * vx + x] = (uint8_t)ci;
-      nt = row_ntris(s_tri[ci]);
+      nt = (uint32_t)(s_tri[ci] & 0xFu);
     }
     my_active += __popc(__ballot_sync(0xffffffffu, nt > 0));
     const uint32_t wsum = warp_sum_u32(nt);
@@ -180,150 +233,221 @@ __device__ __forceinline__ bool mesh_tile(const TileGeom& tg, uint64_t t, const 
   }
   if (lane == 0 && my_active) atomicAdd(&res.active, my_active);
   __syncthreads();
-
-  // 3. exclusive scan of the window triangle counts (warp 0)
   if (warp == 0) {
     uint32_t carry = 0;
-    for (uint32_t b = 0; b < nwin; b += 32u) {
-      const uint32_t v = (b + lane < nwin) ? s_win[b + lane] : 0u;
+    for (uint32_t bb = 0; bb < nwin; bb += 32u) {
+      const uint32_t v = (bb + lane < nwin) ? s_win[bb + lane] : 0u;
       const uint32_t inc = warp_incl_scan(v);
-      if (b + lane < nwin) s_win[b + lane] = carry + inc - v;
+      if (bb + lane < nwin) s_win[bb + lane] = carry + inc - v;
       carry += __shfl_sync(0xffffffffu, inc, 31);
     }
     if (lane == 0) res.tris = carry;
   }
   __syncthreads();
-  if (!EMIT) return true;
-  const uint64_t tile_verts = 3ull * res.tris;
+}
 
-  // 4. decoupled look-back for the tile's first vertex
-  if (warp == 0) {
-    const uint64_t excl = lookback_exclusive(out.tile_status, t, tile_verts, out.wait_ns, out.status);
-    if (lane == 0) res.prefix = excl;
-  }
-  __syncthreads();
-  if (!res.ok) {
-    __syncthreads();
-    return true;
-  }
-  const uint64_t prefix = res.prefix;
+// floor(v / d) for v, d < 2^16 as a multiply-high by m = ceil(2^32 / d)
+// (exact there: the error term v * (m - 2^32 / d) / 2^32 stays below 1/d);
+// d == 1 has no 32-bit multiplier and is passed through.
+struct SmallDiv {
+  uint32_t d, m;
+  __device__ __forceinline__ explicit SmallDiv(uint32_t d_) : d(d_), m(d_ > 1 ? 0xFFFFFFFFu / d_ + 1u : 0u) {}
+  __device__ __forceinline__ uint32_t operator()(uint32_t v) const { return d > 1 ? __umulhi(v, m) : v; }
+};
 
-  // 5. emit, one lane per triangle
-  uint8_t* map = s_map + warp * kMapPerWarp;
-  bool dropped = false;
-  for (uint32_t w = warp; w < nwin; w += kWarps) {
-    const uint32_t r = w / nwx, xb = (w % nwx) * 32u, x = xb + lane;
-    uint32_t ci = 0, nt = 0;
-    if (x < vx) {
-      ci = s_cube[r * vx + x];
-      nt = row_ntris(s_tri[ci]);
-    }
-    const uint32_t inc = warp_incl_scan(nt);
-    const uint32_t exc = inc - nt;
-    const uint32_t wtot = __shfl_sync(0xffffffffu, inc, 31);
-    if (wtot == 0) continue;
-    for (uint32_t k = 0; k < nt; ++k) map[exc + k] = (uint8_t)lane;
-    __syncwarp();
-    const uint64_t wbase = prefix + 3ull * s_win[w];
-    for (uint32_t k0 = 0; k0 < wtot; k0 += 32u) {
-      const uint32_t k = k0 + lane;
-      const uint32_t src = (k < wtot) ? map[k] : 0u;
-      const uint32_t sci = __shfl_sync(0xffffffffu, ci, src);
-      const uint32_t sexc = __shfl_sync(0xffffffffu, exc, src);
-      if (k < wtot) {
-        const uint32_t j = k - sexc;  // triangle within its voxel
-        const uint32_t sx = xb + src;
-        const uint32_t g[3] = {sx, y0 + r, z};
-        // corner k of voxel (sx, r) in the staged planes
-        const float* f0p = s_f0 + m0 + r * nx + sx;
-        const float* f1p = s_f1 + m1 + r * nx + sx;
-        auto fval = [&](int kk) { return (corner_z(kk) ? f1p : f0p)[corner_y(kk) * nx + corner_x(kk)]; };
-        const uint64_t row = s_tri[sci];
-        float3 v[3];
-        if (BAND) {
-          const float* g0p = s_g0 + m0 + r * nx + sx;
-          const float* g1p = s_g1 + m1 + r * nx + sx;
-          auto gval = [&](int kk) { return (corner_z(kk) ? g1p : g0p)[corner_y(kk) * nx + corner_x(kk)]; };
-#pragma unroll
-          for (int mI = 0; mI < 3; ++mI)
-            v[mI] = edge_point_band(g, tg.fr, tri_edge_dev(row, 3u * j + mI), fval, gval, tg.lo, tg.hi);
-        } else {
-#pragma unroll
-          for (int mI = 0; mI < 3; ++mI) v[mI] = edge_point_plain(g, tg.fr, tri_edge_dev(row, 3u * j + mI), fval, tg.iso);
-        }
-        const float3 n = normal_of(v[0], v[1], v[2]);
-        const uint64_t idx = wbase + 3ull * k;
-        if (idx + 3 <= out.capacity) {
-          float4* P = out.pos + idx;
-          float4* N = out.norm + idx;
-          __stcs(P + 0, make_float4(v[0].x, v[0].y, v[0].z, 1.0f));
-          __stcs(P + 1, make_float4(v[1].x, v[1].y, v[1].z, 1.0f));
-          __stcs(P + 2, make_float4(v[2].x, v[2].y, v[2].z, 1.0f));
-          const float4 nn = make_float4(n.x, n.y, n.z, 0.0f);
-          __stcs(N + 0, nn);
-          __stcs(N + 1, nn);
-          __stcs(N + 2, nn);
-        } else {
-          dropped = true;
-        }
+// Triangle list entry: the voxel's index within the tile (row * vx + x,
+// 16 bits) and the triangle's three edges (12 bits).
+__device__ __forceinline__ uint32_t list_entry(uint32_t v, uint32_t e3) { return v | (e3 << 16); }
+
+// Phase 4: decoupled look-back for the tile's first vertex, then emission.
+// The tile's triangles are listed in output order (as many as the list holds
+// per round) and emitted one lane per triangle in full warps.  Warp 0 walks
+// back while the other warps list the first round's triangles, taking windows
+// from a shared counter; warp 0 joins when its look-back ends.  Ends with a
+// barrier.
+template <bool BAND, int THREADS>
+__device__ __forceinline__ void tile_emit(const TileGeom& tg, uint64_t t, const MeshLayout& L, unsigned char* smem,
+                                          const EmitTarget& out, TileOut& res) {
+  constexpr uint32_t kWarps = THREADS / 32;
+  const uint64_t* s_tri = reinterpret_cast<const uint64_t*>(smem);
+  const Planes P = planes_of(smem, L);
+  const uint8_t* s_cube = smem + L.cube_off;
+  const uint32_t* s_win = reinterpret_cast<const uint32_t*>(smem + L.win_off);
+  const uint64_t* s_edge = reinterpret_cast<const uint64_t*>(smem + L.edge_off);
+  uint32_t* s_list = reinterpret_cast<uint32_t*>(smem + L.list_off);
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t nx = tg.nx, vx = nx - 1, nwx = (vx + 31u) / 32u, nwin = tg.rows * nwx;
+  const SmallDiv by_vx(vx), by_nwx(nwx);
+  const uint64_t st0 = ((uint64_t)tg.z * tg.ny + tg.y0) * nx;
+  const uint32_t m0 = (uint32_t)(st0 & 3u);
+  const uint32_t tris = res.tris;
+  // list the triangles [base, base + n) of the tile: entry u = triangle base + u
+  auto build = [&](uint32_t base, uint32_t n, auto&& next_window) {
+    for (uint32_t w = next_window(); w < nwin; w = next_window()) {
+      const uint32_t r = by_nwx(w), x = (w - r * nwx) * 32u + lane;
+      const uint32_t v = r * vx + x;
+      uint64_t row = 0;
+      uint32_t nt = 0;
+      if (x < vx) {
+        row = s_tri[s_cube[v]];
+        nt = (uint32_t)(row & 0xFu);
+      }
+      if (__ballot_sync(0xffffffffu, nt) == 0) continue;
+      const uint32_t first = s_win[w] + warp_incl_scan(nt) - nt;
+      for (uint32_t j = 0; j < nt; ++j) {
+        const uint32_t u = first + j - base;
+        if (u < n) s_list[u] = list_entry(v, tri_edges3(row, j));
       }
     }
-    __syncwarp();
+  };
+  auto shared_windows = [&] {
+    uint32_t w = 0;
+    if (lane == 0) w = atomicAdd(&res.next_window, 1u);
+    return __shfl_sync(0xffffffffu, w, 0);
+  };
+  if (warp == 0) {
+    const uint64_t excl = lookback_exclusive(out.tile_status, t, 3ull * tris, out.wait_ns, out.status);
+    if (lane == 0) res.prefix = excl;
+  }
+  const uint32_t n0 = min(L.list_cap, tris);
+  if (n0) build(0, n0, shared_windows);
+  __syncthreads();
+  const bool ok = res.ok != 0;
+  const uint64_t prefix = res.prefix;
+  if (!ok || tris == 0) {
+    __syncthreads();  // every thread has read the record
+    return;
+  }
+  VoxelCorners V;
+  axis_corners(tg.z, tg.fr.gc[2], tg.fr.vs[2], V.z0, V.z1);
+  const float* F = P.f0 + m0;  // sample (x, r) of plane z at F[r * nx + x]
+  bool dropped = false;
+  for (uint32_t base = 0; base < tris; base += L.list_cap) {
+    const uint32_t n = min(L.list_cap, tris - base);
+    if (base) {
+      uint32_t next = warp;
+      build(base, n, [&] {
+        const uint32_t w = next;
+        next += kWarps;
+        return w;
+      });
+      __syncthreads();
+    }
+    for (uint32_t u0 = warp * 32u; u0 < n; u0 += THREADS) {
+      const uint32_t u = u0 + lane;
+      if (u >= n) continue;
+      const uint32_t ent = s_list[u];
+      const uint32_t v = ent & 0xFFFFu, e3 = ent >> 16;
+      const uint32_t r = by_vx(v), x = v - r * vx;
+      axis_corners(x, tg.fr.gc[0], tg.fr.vs[0], V.x0, V.x1);
+      axis_corners(tg.y0 + r, tg.fr.gc[1], tg.fr.vs[1], V.y0, V.y1);
+      const uint32_t vb = v + r;  // r * nx + x
+      float3 vtx[3];
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const uint64_t ed = s_edge[(e3 >> (8 - 4 * m)) & 0xFu];
+        const uint32_t oa = (uint32_t)ed & 0xFFFFu, ob = ((uint32_t)ed >> 16) & 0xFFFFu;
+        const uint32_t ba = (uint32_t)(ed >> 32) & 7u, bb = (uint32_t)(ed >> 35) & 7u;
+        if (BAND) {
+          const float* G = F + 2 * L.plane_stride;
+          vtx[m] = edge_point_band_v(F[vb + oa], F[vb + ob], G[vb + oa], G[vb + ob], ba, bb, V, tg.lo, tg.hi);
+        } else {
+          vtx[m] = edge_point_plain_v(F[vb + oa], F[vb + ob], corner_sel(V, ba), corner_sel(V, bb), tg.iso);
+        }
+      }
+      const float3 nrm = normal_of(vtx[0], vtx[1], vtx[2]);
+      const uint64_t idx = prefix + 3ull * (base + u);
+      if (idx + 3 <= out.capacity) {
+        float4* Pp = out.pos + idx;
+        float4* N = out.norm + idx;
+        __stcs(Pp + 0, make_float4(vtx[0].x, vtx[0].y, vtx[0].z, 1.0f));
+        __stcs(Pp + 1, make_float4(vtx[1].x, vtx[1].y, vtx[1].z, 1.0f));
+        __stcs(Pp + 2, make_float4(vtx[2].x, vtx[2].y, vtx[2].z, 1.0f));
+        const float4 nn = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+        __stcs(N + 0, nn);
+        __stcs(N + 1, nn);
+        __stcs(N + 2, nn);
+      } else {
+        dropped = true;
+      }
+    }
+    __syncthreads();
   }
   if (dropped) set_status(out.status, kStatusOverflow);
-  __syncthreads();
-  return true;
 }
 
 __device__ __forceinline__ void mesh_cta_init(unsigned char* smem, const MeshLayout& L) {
-  load_tri_table(reinterpret_cast<uint64_t*>(smem));
+  load_tri_table_counted(reinterpret_cast<uint64_t*>(smem));
   if (threadIdx.x == 0) {
-    mbar_init(reinterpret_cast<uint64_t*>(smem + L.bar_off), 1);
+    mbar_init(bar_of(smem, L), 1);
     fence_mbar_init();
   }
   __syncthreads();
 }
 
+// The tile loop shared by the single-grid and the batch kernel: take a tile,
+// stage, classify, look back and emit, repeat.  `geom(t)` resolves tile t,
+// `book(tg, t, res)` (thread 0) records a finished tile.  Thread 0 writes the
+// tile number and resets the tile record after the barrier that ends the
+// previous tile, when no thread reads either any more; every thread reads the
+// tile number only after the barrier that follows.
+template <bool BAND, bool EMIT, int THREADS, class Geom, class Book>
+__device__ __forceinline__ void tile_loop(unsigned char* smem, const MeshLayout& L, uint32_t* counter, uint64_t ntiles,
+                                          const EmitTarget& out, Geom&& geom, Book&& book) {
+  __shared__ uint32_t sh_tile;
+  __shared__ TileOut res;
+  mesh_cta_init(smem, L);
+  uint32_t parity = 0;
+  while (true) {
+    if (threadIdx.x == 0) {
+      sh_tile = atomicAdd(counter, 1u);
+      res.tris = 0;
+      res.active = 0;
+      res.ok = 1;
+      res.next_window = 0;
+    }
+    __syncthreads();
+    const uint32_t t = sh_tile;
+    if ((uint64_t)t >= ntiles) return;
+    const TileGeom tg = geom(t);
+    tile_stage<BAND>(tg, L, smem);
+    if (!tile_wait(tg, L, smem, parity, out, res)) return;
+    tile_classify<THREADS>(tg, L, smem, res);
+    if (EMIT) tile_emit<BAND, THREADS>(tg, t, L, smem, out, res);
+    // classify and emit end with a barrier after their last use of the
+    // staged planes and of the record: thread 0 may book and reset at once
+    if (threadIdx.x == 0) book(tg, t, res);
+  }
+}
+
 }  // namespace
 
-MeshLayout mesh_layout(uint32_t plane_floats, uint32_t tile_voxels, uint32_t windows, bool band, int threads) {
+MeshLayout mesh_layout(uint32_t plane_floats, uint32_t tile_voxels, uint32_t windows, bool band) {
   MeshLayout L;
   const uint32_t plane_bytes = align16(plane_floats * 4);
   L.plane_stride = plane_bytes / 4;
+  L.list_cap = std::max<uint32_t>(64, (GCM_MESH_LIST_PER_2VOX * tile_voxels / 2 + 31) / 32 * 32);
   L.f_off = 2048;  // after the 256-entry triangle table
-  L.g_off = L.f_off + 2 * plane_bytes;
-  L.cube_off = L.g_off + (band ? 2 * plane_bytes : 0);
+  L.cube_off = L.f_off + (band ? 4 : 2) * plane_bytes;
   L.win_off = L.cube_off + align16(tile_voxels);
-  L.map_off = L.win_off + align16(windows * 4);
-  L.bar_off = L.map_off + align16((uint32_t)(threads / 32) * kMapPerWarp);
+  L.edge_off = L.win_off + align16(windows * 4);
+  L.list_off = L.edge_off + 128;
+  L.bar_off = L.list_off + align16(L.list_cap * 4);
   L.total = L.bar_off + 16;
   return L;
 }
 
-MeshLayout mesh_layout_for(uint32_t nx, uint32_t rows, bool band, int threads) {
-  return mesh_layout((rows + 1) * nx + 4, rows * (nx - 1), rows * ((nx - 1 + 31) / 32), band, threads);
+MeshLayout mesh_layout_for(uint32_t nx, uint32_t rows, bool band) {
+  return mesh_layout((rows + 1) * nx + 4, rows * (nx - 1), rows * ((nx - 1 + 31) / 32), band);
 }
 
-size_t mesh_smem_bytes(uint32_t nx, uint32_t rows, bool band) { return mesh_layout_for(nx, rows, band, 256).total; }
+size_t mesh_smem_bytes(uint32_t nx, uint32_t rows, bool band) { return mesh_layout_for(nx, rows, band).total; }
 
 template <bool BAND, bool EMIT, int THREADS>
 __global__ void __launch_bounds__(THREADS, mesh_min_blocks(THREADS)) mc_mesh_kernel(MeshParams p, MeshLayout L) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ uint32_t sh_tile;
-  __shared__ TileOut res;
-  mesh_cta_init(smem, L);
   const EmitTarget out{p.pos, p.norm, p.capacity, p.tile_status, p.status, p.wait_ns};
-  uint32_t parity = 0;
-  while (true) {
-    if (threadIdx.x == 0) {
-      sh_tile = atomicAdd(p.counter, 1u);
-      res.tris = 0;
-      res.active = 0;
-      res.ok = 1;
-    }
-    __syncthreads();
-    const uint32_t t = sh_tile;
-    if ((uint64_t)t >= p.ntiles) break;
+  auto geom = [&](uint32_t t) {
     TileGeom tg;
     tg.f = p.f;
     tg.g = p.g;
@@ -337,14 +461,17 @@ __global__ void __launch_bounds__(THREADS, mesh_min_blocks(THREADS)) mc_mesh_ker
     tg.iso = p.iso;
     tg.lo = p.lo;
     tg.hi = p.hi;
-    if (!mesh_tile<BAND, EMIT, THREADS>(tg, t, L, smem, parity, out, res)) break;
-    if (threadIdx.x == 0) {
-      auto* cnt = p.counts_dev;
-      atomicAdd(reinterpret_cast<unsigned long long*>(&cnt->active_voxels), (unsigned long long)res.active);
-      if (!EMIT) atomicAdd(reinterpret_cast<unsigned long long*>(&cnt->total_verts), 3ull * res.tris);
-      else if ((uint64_t)t == p.ntiles - 1) cnt->total_verts = res.prefix + 3ull * res.tris;
-    }
-  }
+    tg.inst = 0;
+    tg.local = t;
+    return tg;
+  };
+  auto book = [&](const TileGeom&, uint32_t t, const TileOut& res) {
+    auto* cnt = p.counts_dev;
+    atomicAdd(reinterpret_cast<unsigned long long*>(&cnt->active_voxels), (unsigned long long)res.active);
+    if (!EMIT) atomicAdd(reinterpret_cast<unsigned long long*>(&cnt->total_verts), 3ull * res.tris);
+    else if ((uint64_t)t == p.ntiles - 1) cnt->total_verts = res.prefix + 3ull * res.tris;
+  };
+  tile_loop<BAND, EMIT, THREADS>(smem, L, p.counter, p.ntiles, out, geom, book);
 }
 
 // Batch of grids in one launch: the tiles of all instances form one sequence
@@ -353,21 +480,8 @@ __global__ void __launch_bounds__(THREADS, mesh_min_blocks(THREADS)) mc_mesh_ker
 template <bool EMIT, int THREADS>
 __global__ void __launch_bounds__(THREADS, mesh_min_blocks(THREADS)) mc_batch_kernel(BatchMeshParams p, MeshLayout L) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ uint32_t sh_tile;
-  __shared__ TileOut res;
-  mesh_cta_init(smem, L);
   const EmitTarget out{p.pos, p.norm, p.capacity, p.tile_status, p.status, p.wait_ns};
-  uint32_t parity = 0;
-  while (true) {
-    if (threadIdx.x == 0) {
-      sh_tile = atomicAdd(p.counter, 1u);
-      res.tris = 0;
-      res.active = 0;
-      res.ok = 1;
-    }
-    __syncthreads();
-    const uint32_t t = sh_tile;
-    if ((uint64_t)t >= p.ntiles) break;
+  auto geom = [&](uint32_t t) {
     // instance owning tile t: last i with tile_begin[i] <= t
     uint32_t lo = 0, hi = p.n_inst - 1;
     while (lo < hi) {
@@ -390,23 +504,26 @@ __global__ void __launch_bounds__(THREADS, mesh_min_blocks(THREADS)) mc_batch_ke
     tg.iso = I.iso;
     tg.lo = 0.0f;
     tg.hi = 0.0f;
-    if (!mesh_tile<false, EMIT, THREADS>(tg, t, L, smem, parity, out, res)) break;
-    if (threadIdx.x == 0) {
-      auto* cnt = p.counts_dev;
-      atomicAdd(reinterpret_cast<unsigned long long*>(&p.inst_active[lo]), (unsigned long long)res.active);
-      atomicAdd(reinterpret_cast<unsigned long long*>(&cnt->active_voxels), (unsigned long long)res.active);
-      if (!EMIT) {
-        atomicAdd(reinterpret_cast<unsigned long long*>(&p.inst_verts[lo]), 3ull * res.tris);
-        atomicAdd(reinterpret_cast<unsigned long long*>(&cnt->total_verts), 3ull * res.tris);
-      } else {
-        if (local == 0) p.offsets[lo] = res.prefix;
-        if ((uint64_t)t == p.ntiles - 1) {
-          p.offsets[p.n_inst] = res.prefix + 3ull * res.tris;
-          cnt->total_verts = res.prefix + 3ull * res.tris;
-        }
+    tg.inst = lo;
+    tg.local = local;
+    return tg;
+  };
+  auto book = [&](const TileGeom& tg, uint32_t t, const TileOut& res) {
+    auto* cnt = p.counts_dev;
+    atomicAdd(reinterpret_cast<unsigned long long*>(&p.inst_active[tg.inst]), (unsigned long long)res.active);
+    atomicAdd(reinterpret_cast<unsigned long long*>(&cnt->active_voxels), (unsigned long long)res.active);
+    if (!EMIT) {
+      atomicAdd(reinterpret_cast<unsigned long long*>(&p.inst_verts[tg.inst]), 3ull * res.tris);
+      atomicAdd(reinterpret_cast<unsigned long long*>(&cnt->total_verts), 3ull * res.tris);
+    } else {
+      if (tg.local == 0) p.offsets[tg.inst] = res.prefix;
+      if ((uint64_t)t == p.ntiles - 1) {
+        p.offsets[p.n_inst] = res.prefix + 3ull * res.tris;
+        cnt->total_verts = res.prefix + 3ull * res.tris;
       }
     }
-  }
+  };
+  tile_loop<false, EMIT, THREADS>(smem, L, p.counter, p.ntiles, out, geom, book);
 }
 
 // ----------------------------------------------------------------------------
@@ -610,8 +727,22 @@ BatchFn batch_fn(bool emit, int threads) {
 }
 template <class F>
 cudaError_t prepare(F f, size_t smem, int threads, int* blocks_per_sm) {
-  cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // The dynamic shared memory limit is a per-kernel, process-wide attribute:
+  // it is always raised to the kernel's full opt-in limit (the same value from
+  // every thread), so that concurrent callers with different tile sizes never
+  // lower it under one another's launch.  Occupancy follows `smem`, not it.
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa{};
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, f);
   if (e != cudaSuccess) return e;
+  const int limit = optin - (int)fa.sharedSizeBytes;
+  if ((int)smem > limit) return cudaErrorInvalidValue;
+  if (fa.maxDynamicSharedSizeBytes != limit) {
+    e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
+    if (e != cudaSuccess) return e;
+  }
   // all of the unified L1/shared storage as shared memory: occupancy is
   // limited by shared memory, and the kernel reads global memory only
   // through bulk copies and read-only loads

@@ -84,13 +84,15 @@ extern "C" gcm_status gcm_mesh_field_noalloc(const float* d_field, const gcm_gri
   // states fit the fixed array, within the shared-memory budget.
   const uint32_t vx = grid->nx - 1, vy = grid->ny - 1, vz = grid->nz - 1;
   const size_t budget = std::min(kSmemBudget, (size_t)optin);
-  uint32_t rows = std::min<uint32_t>(std::max<uint32_t>(1, (kTargetVoxelsPerTile + vx / 2) / vx), vy);
+  uint32_t rows =
+      std::min<uint32_t>(std::min<uint32_t>(std::max<uint32_t>(1, (kTargetVoxelsPerTile + vx / 2) / vx), vy),
+                         gcm::max_tile_rows(vx));
   auto tiles_for = [&](uint32_t r) { return (uint64_t)((vy + r - 1) / r) * vz; };
-  while (tiles_for(rows) > kNoAllocMaxTiles && rows < vy &&
-         gcm::mesh_layout_for(grid->nx, rows + 1, false, kThreads).total <= budget)
+  while (tiles_for(rows) > kNoAllocMaxTiles && rows < vy && rows < gcm::max_tile_rows(vx) &&
+         gcm::mesh_layout_for(grid->nx, rows + 1, false).total <= budget)
     ++rows;
-  while (rows > 1 && gcm::mesh_layout_for(grid->nx, rows, false, kThreads).total > budget) --rows;
-  const gcm::MeshLayout layout = gcm::mesh_layout_for(grid->nx, rows, false, kThreads);
+  while (rows > 1 && gcm::mesh_layout_for(grid->nx, rows, false).total > budget) --rows;
+  const gcm::MeshLayout layout = gcm::mesh_layout_for(grid->nx, rows, false);
   const size_t smem = layout.total;
   const uint64_t ntiles = tiles_for(rows);
   if (ntiles > kNoAllocMaxTiles || smem > (size_t)optin) return GCM_ERR_NOT_SUPPORTED;

@@ -76,6 +76,9 @@ class Context:
     def reserve(self, max_points: int):
         self.check(self.lib.gcm_ctx_reserve(self.h, int(max_points)))
 
+    def set_launch_shape(self, threads: int, tile_voxels: int):
+        self.check(self.lib.gcm_ctx_set_launch_shape(self.h, int(threads), int(tile_voxels)))
+
     # ------------------------------------------------------------ fused mesh
     def count_field(self, field, iso, stream=None) -> Counts:
         g = make_grid(field.shape)

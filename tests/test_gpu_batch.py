@@ -91,7 +91,7 @@ def test_tuner_keeps_results_and_reuses_its_cache(ctx, batch, tmp_path):
     assert torch.equal(pos, ref)
 
 
-@pytest.mark.parametrize("shape_", [(128, 1024), (256, 4096), (128, 8192)])
+@pytest.mark.parametrize("shape_", [(128, 1024), (256, 4096), (128, 8192), (256, 64)])
 def test_single_grid_launch_shapes_are_identical(shape_):
     import oracle as O
     from gpucadforam_gb300.mesher import Context
@@ -100,7 +100,7 @@ def test_single_grid_launch_shapes_are_identical(shape_):
     f = torch.from_numpy(O.lattice_field((90, 70, 50), 0, (1, 1, 1), np.array([14.0], np.float32),
                                          types=np.array([1], np.uint8))).cuda()
     ref_pos, ref_norm, _ = c.mesh_field(f, 0.2)
-    c.check(c.lib.gcm_ctx_set_launch_shape(c.h, shape_[0], shape_[1]))
+    c.set_launch_shape(*shape_)
     pos, norm, _ = c.mesh_field(f, 0.2)
     assert torch.equal(pos, ref_pos) and torch.equal(norm, ref_norm)
     c.close()

@@ -17,11 +17,13 @@ pytestmark = pytest.mark.gpu
 MC = golden("golden_mc.npz")
 
 
-@pytest.fixture(scope="module")
-def ctx():
+@pytest.fixture(scope="module", params=[(256, 2048), (128, 1024)], ids=["256x2048", "128x1024"])
+def ctx(request):
+    """Every case runs through two launch shapes of the fused kernel."""
     from gpucadforam_gb300.mesher import Context
 
     c = Context(0)
+    c.set_launch_shape(*request.param)
     yield c
     c.close()
 
