@@ -104,8 +104,8 @@ gcm_status plan_mesh(gcm_ctx* ctx, const gcm_grid* g, bool band, MeshPlan* out) 
   const int threads = ctx->mesh_threads;
   uint32_t rows = rows_for(g->nx, g->ny, ctx->tile_voxels);
   const size_t budget = std::min(kMeshSmemBudget, ctx->smem_optin);
-  while (rows > 1 && mesh_layout_for(g->nx, rows, band).total > budget) --rows;
-  const MeshLayout L = mesh_layout_for(g->nx, rows, band);
+  while (rows > 1 && mesh_layout_for(g->nx, rows, band, threads).total > budget) --rows;
+  const MeshLayout L = mesh_layout_for(g->nx, rows, band, threads);
   if (L.total > ctx->smem_optin)
     return fail(ctx, GCM_ERR_NOT_SUPPORTED, "grid rows of %u samples do not fit in shared memory", g->nx);
   out->rows = rows;

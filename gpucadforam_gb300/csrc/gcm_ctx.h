@@ -19,7 +19,7 @@ struct gcm_ctx {
   size_t smem_optin = 0;
   uint64_t wait_ns = kDefaultWaitNs;
   // fused-kernel launch shape (the autotuner may change both)
-  int mesh_threads = 256;
+  int mesh_threads = GCM_MESH_THREADS;
   uint32_t tile_voxels = GCM_MESH_TILE_VOXELS;
   std::atomic<uint64_t> launches{0};
   std::string last_error;

@@ -8,9 +8,13 @@
 
 #include "../../include/gcm.h"
 
-// Voxels per tile the fused kernel aims for (whole voxel rows of one z-plane).
+// Default launch shape of the fused kernel: CTA size (128 or 256) and the
+// voxels per tile it aims for (whole voxel rows of one z-plane).
+#ifndef GCM_MESH_THREADS
+#define GCM_MESH_THREADS 128
+#endif
 #ifndef GCM_MESH_TILE_VOXELS
-#define GCM_MESH_TILE_VOXELS 2048
+#define GCM_MESH_TILE_VOXELS 1024
 #endif
 // Triangle-list entries per two voxels of a tile: a tile with more triangles
 // emits in several rounds.
@@ -50,7 +54,7 @@ struct MeshParams {
 struct MeshLayout {
   uint32_t plane_stride;  // floats between consecutive staged planes
   uint32_t list_cap;      // triangle-list entries per emission round
-  uint32_t f_off, cube_off, win_off, edge_off, list_off, bar_off, total;
+  uint32_t f_off, cube_off, win_off, edge_off, list_off, xpose_off, bar_off, total;
 };
 
 // One grid of a batched extraction.
@@ -141,8 +145,8 @@ struct CsgParams {
 
 // Launch wrappers (each kernel is launched from the file that defines it).
 bool mesh_threads_supported(int threads);
-MeshLayout mesh_layout(uint32_t plane_floats, uint32_t tile_voxels, uint32_t windows, bool band);
-MeshLayout mesh_layout_for(uint32_t nx, uint32_t rows, bool band);
+MeshLayout mesh_layout(uint32_t plane_floats, uint32_t tile_voxels, uint32_t windows, bool band, int threads);
+MeshLayout mesh_layout_for(uint32_t nx, uint32_t rows, bool band, int threads);
 cudaError_t mesh_prepare(bool band, bool emit, int threads, size_t smem, int* blocks_per_sm);
 cudaError_t launch_mesh(bool band, bool emit, int threads, const MeshParams& p, const MeshLayout& L, uint32_t blocks,
                         cudaStream_t st);

@@ -203,16 +203,20 @@ __device__ __forceinline__ void tile_classify(const TileGeom& tg, const MeshLayo
   const uint64_t st0 = ((uint64_t)tg.z * tg.ny + tg.y0) * nx;
   const uint32_t m0 = (uint32_t)(st0 & 3u), m1 = (uint32_t)((st0 + (uint64_t)tg.ny * nx) & 3u);
   if (threadIdx.x >= THREADS - 12) {
-    // edge table: shared-memory offsets of the edge's corners from the
+    // edge table: shared-memory byte offsets of the edge's corners from the
     // voxel's first sample (plane z + 1 lies `dplane` floats after plane z),
     // and the corners' bits
     const uint32_t e = threadIdx.x - (THREADS - 12);
     const uint32_t dplane = L.plane_stride + m1 - m0;
-    auto off = [&](uint32_t k) { return (uint32_t)corner_z((int)k) * dplane + (uint32_t)corner_y((int)k) * nx + (uint32_t)corner_x((int)k); };
+    auto off = [&](uint32_t k) {
+      return 4u * ((uint32_t)corner_z((int)k) * dplane + (uint32_t)corner_y((int)k) * nx + (uint32_t)corner_x((int)k));
+    };
     auto bits = [&](uint32_t k) { return (uint32_t)(corner_x((int)k) | (corner_y((int)k) << 1) | (corner_z((int)k) << 2)); };
     const uint32_t ka = (uint32_t)edge_a((int)e), kb = (uint32_t)edge_b((int)e);
+    // [a offset : 24][b offset : 24][a bits : 3][b bits : 3] (shared memory
+    // offsets stay below 2^18 bytes)
     reinterpret_cast<uint64_t*>(smem + L.edge_off)[e] =
-        (uint64_t)off(ka) | ((uint64_t)off(kb) << 16) | ((uint64_t)bits(ka) << 32) | ((uint64_t)bits(kb) << 35);
+        (uint64_t)off(ka) | ((uint64_t)off(kb) << 24) | ((uint64_t)bits(ka) << 48) | ((uint64_t)bits(kb) << 51);
   }
   uint32_t my_active = 0;
   WindowCursor cur(warp, nwx);
@@ -276,6 +280,9 @@ __device__ __forceinline__ void tile_emit(const TileGeom& tg, uint64_t t, const 
   const uint64_t* s_edge = reinterpret_cast<const uint64_t*>(smem + L.edge_off);
   uint32_t* s_list = reinterpret_cast<uint32_t*>(smem + L.list_off);
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  float4* xp = reinterpret_cast<float4*>(smem + L.xpose_off) + warp * 96u;  // this warp's 96 vertices
+  // triangle of the chunk's vertex lane + 32k
+  const uint32_t q3[3] = {lane / 3u, (lane + 32u) / 3u, (lane + 64u) / 3u};
   const uint32_t nx = tg.nx, vx = nx - 1, nwx = (vx + 31u) / 32u, nwin = tg.rows * nwx;
   const SmallDiv by_vx(vx), by_nwx(nwx);
   const uint64_t st0 = ((uint64_t)tg.z * tg.ny + tg.y0) * nx;
@@ -334,42 +341,72 @@ __device__ __forceinline__ void tile_emit(const TileGeom& tg, uint64_t t, const 
       __syncthreads();
     }
     for (uint32_t u0 = warp * 32u; u0 < n; u0 += THREADS) {
+      // lane = triangle u0 + lane; the chunk's vertices are written in order
+      // through shared memory so that every store covers 512 contiguous bytes
       const uint32_t u = u0 + lane;
-      if (u >= n) continue;
-      const uint32_t ent = s_list[u];
-      const uint32_t v = ent & 0xFFFFu, e3 = ent >> 16;
-      const uint32_t r = by_vx(v), x = v - r * vx;
-      axis_corners(x, tg.fr.gc[0], tg.fr.vs[0], V.x0, V.x1);
-      axis_corners(tg.y0 + r, tg.fr.gc[1], tg.fr.vs[1], V.y0, V.y1);
-      const uint32_t vb = v + r;  // r * nx + x
-      float3 vtx[3];
+      const bool live = u < n;
+      float3 nrm = make_float3(0.0f, 0.0f, 0.0f);
+      if (live) {
+        const uint32_t ent = s_list[u];
+        const uint32_t v = ent & 0xFFFFu, e3 = ent >> 16;
+        const uint32_t r = by_vx(v), x = v - r * vx;
+        axis_corners(x, tg.fr.gc[0], tg.fr.vs[0], V.x0, V.x1);
+        axis_corners(tg.y0 + r, tg.fr.gc[1], tg.fr.vs[1], V.y0, V.y1);
+        const char* Fv = reinterpret_cast<const char*>(F + v + r);  // sample (x, r): r * nx + x
+        auto at = [](const char* base, uint32_t off) { return *reinterpret_cast<const float*>(base + off); };
+        float3 vtx[3];
 #pragma unroll
-      for (int m = 0; m < 3; ++m) {
-        const uint64_t ed = s_edge[(e3 >> (8 - 4 * m)) & 0xFu];
-        const uint32_t oa = (uint32_t)ed & 0xFFFFu, ob = ((uint32_t)ed >> 16) & 0xFFFFu;
-        const uint32_t ba = (uint32_t)(ed >> 32) & 7u, bb = (uint32_t)(ed >> 35) & 7u;
-        if (BAND) {
-          const float* G = F + 2 * L.plane_stride;
-          vtx[m] = edge_point_band_v(F[vb + oa], F[vb + ob], G[vb + oa], G[vb + ob], ba, bb, V, tg.lo, tg.hi);
-        } else {
-          vtx[m] = edge_point_plain_v(F[vb + oa], F[vb + ob], corner_sel(V, ba), corner_sel(V, bb), tg.iso);
+        for (int m = 0; m < 3; ++m) {
+          const uint64_t ed = s_edge[(e3 >> (8 - 4 * m)) & 0xFu];
+          const uint32_t oa = (uint32_t)ed & 0xFFFFFFu, ob = (uint32_t)(ed >> 24) & 0xFFFFFFu;
+          const uint32_t bits = (uint32_t)(ed >> 48), ba = bits & 7u, bb = bits >> 3;
+          if (BAND) {
+            const char* Gv = Fv + 8u * L.plane_stride;
+            vtx[m] = edge_point_band_v(at(Fv, oa), at(Fv, ob), at(Gv, oa), at(Gv, ob), ba, bb, V, tg.lo, tg.hi);
+          } else {
+            vtx[m] = edge_point_plain_v(at(Fv, oa), at(Fv, ob), corner_sel(V, ba), corner_sel(V, bb), tg.iso);
+          }
+        }
+        nrm = normal_of(vtx[0], vtx[1], vtx[2]);
+        xp[3 * lane + 0] = make_float4(vtx[0].x, vtx[0].y, vtx[0].z, 1.0f);
+        xp[3 * lane + 1] = make_float4(vtx[1].x, vtx[1].y, vtx[1].z, 1.0f);
+        xp[3 * lane + 2] = make_float4(vtx[2].x, vtx[2].y, vtx[2].z, 1.0f);
+      }
+      const uint32_t nv = 3u * min(32u, n - u0);      // vertices of the chunk
+      const uint64_t cb = prefix + 3ull * (base + u0);  // its first output vertex
+      float4* gp = out.pos + cb;
+      float4* gn = out.norm + cb;
+      __syncwarp();
+      if (nv == 96u && cb + 96u <= out.capacity) {
+        // whole chunk, inside the output
+        __stcs(gp + lane, xp[lane]);
+        __stcs(gp + lane + 32u, xp[lane + 32u]);
+        __stcs(gp + lane + 64u, xp[lane + 64u]);
+        __syncwarp();
+        xp[lane] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+        __syncwarp();
+        __stcs(gn + lane, xp[q3[0]]);
+        __stcs(gn + lane + 32u, xp[q3[1]]);
+        __stcs(gn + lane + 64u, xp[q3[2]]);
+      } else {
+        // ragged or overflowing chunk: a triangle is written only when all of
+        // its vertices fit
+        if (live && cb + 3ull * lane + 3 > out.capacity) dropped = true;
+#pragma unroll
+        for (uint32_t k = 0; k < 3; ++k) {
+          const uint32_t q = lane + 32u * k;
+          if (q < nv && cb + 3ull * q3[k] + 3 <= out.capacity) __stcs(gp + q, xp[q]);
+        }
+        __syncwarp();
+        if (live) xp[lane] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+        __syncwarp();
+#pragma unroll
+        for (uint32_t k = 0; k < 3; ++k) {
+          const uint32_t q = lane + 32u * k;
+          if (q < nv && cb + 3ull * q3[k] + 3 <= out.capacity) __stcs(gn + q, xp[q3[k]]);
         }
       }
-      const float3 nrm = normal_of(vtx[0], vtx[1], vtx[2]);
-      const uint64_t idx = prefix + 3ull * (base + u);
-      if (idx + 3 <= out.capacity) {
-        float4* Pp = out.pos + idx;
-        float4* N = out.norm + idx;
-        __stcs(Pp + 0, make_float4(vtx[0].x, vtx[0].y, vtx[0].z, 1.0f));
-        __stcs(Pp + 1, make_float4(vtx[1].x, vtx[1].y, vtx[1].z, 1.0f));
-        __stcs(Pp + 2, make_float4(vtx[2].x, vtx[2].y, vtx[2].z, 1.0f));
-        const float4 nn = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
-        __stcs(N + 0, nn);
-        __stcs(N + 1, nn);
-        __stcs(N + 2, nn);
-      } else {
-        dropped = true;
-      }
+      __syncwarp();
     }
     __syncthreads();
   }
@@ -422,26 +459,28 @@ __device__ __forceinline__ void tile_loop(unsigned char* smem, const MeshLayout&
 
 }  // namespace
 
-MeshLayout mesh_layout(uint32_t plane_floats, uint32_t tile_voxels, uint32_t windows, bool band) {
+MeshLayout mesh_layout(uint32_t plane_floats, uint32_t tile_voxels, uint32_t windows, bool band, int threads) {
   MeshLayout L;
   const uint32_t plane_bytes = align16(plane_floats * 4);
   L.plane_stride = plane_bytes / 4;
-  L.list_cap = std::max<uint32_t>(64, (GCM_MESH_LIST_PER_2VOX * tile_voxels / 2 + 31) / 32 * 32);
+  // at most 6144 entries: tiles of very wide rows take more rounds instead
+  L.list_cap = std::min<uint32_t>(6144, std::max<uint32_t>(64, (GCM_MESH_LIST_PER_2VOX * tile_voxels / 2 + 31) / 32 * 32));
   L.f_off = 2048;  // after the 256-entry triangle table
   L.cube_off = L.f_off + (band ? 4 : 2) * plane_bytes;
   L.win_off = L.cube_off + align16(tile_voxels);
   L.edge_off = L.win_off + align16(windows * 4);
   L.list_off = L.edge_off + 128;
-  L.bar_off = L.list_off + align16(L.list_cap * 4);
+  L.xpose_off = L.list_off + align16(L.list_cap * 4);
+  L.bar_off = L.xpose_off + (uint32_t)(threads / 32) * 96u * 16u;
   L.total = L.bar_off + 16;
   return L;
 }
 
-MeshLayout mesh_layout_for(uint32_t nx, uint32_t rows, bool band) {
-  return mesh_layout((rows + 1) * nx + 4, rows * (nx - 1), rows * ((nx - 1 + 31) / 32), band);
+MeshLayout mesh_layout_for(uint32_t nx, uint32_t rows, bool band, int threads) {
+  return mesh_layout((rows + 1) * nx + 4, rows * (nx - 1), rows * ((nx - 1 + 31) / 32), band, threads);
 }
 
-size_t mesh_smem_bytes(uint32_t nx, uint32_t rows, bool band) { return mesh_layout_for(nx, rows, band).total; }
+size_t mesh_smem_bytes(uint32_t nx, uint32_t rows, bool band) { return mesh_layout_for(nx, rows, band, 256).total; }
 
 template <bool BAND, bool EMIT, int THREADS>
 __global__ void __launch_bounds__(THREADS, mesh_min_blocks(THREADS)) mc_mesh_kernel(MeshParams p, MeshLayout L) {

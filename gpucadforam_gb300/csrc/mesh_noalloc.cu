@@ -44,7 +44,7 @@ constexpr uint64_t kNoAllocMaxTiles = (kNoAllocScratchBytes - kHeaderBytes) / si
 constexpr uint32_t kTargetVoxelsPerTile = GCM_MESH_TILE_VOXELS;
 constexpr size_t kSmemBudget = 96 * 1024;
 constexpr int kMaxDevices = 64;
-constexpr int kThreads = 256;
+constexpr int kThreads = GCM_MESH_THREADS;
 
 std::mutex g_setup_mutex;
 void* g_scratch_addr[kMaxDevices] = {};
@@ -89,10 +89,10 @@ extern "C" gcm_status gcm_mesh_field_noalloc(const float* d_field, const gcm_gri
                          gcm::max_tile_rows(vx));
   auto tiles_for = [&](uint32_t r) { return (uint64_t)((vy + r - 1) / r) * vz; };
   while (tiles_for(rows) > kNoAllocMaxTiles && rows < vy && rows < gcm::max_tile_rows(vx) &&
-         gcm::mesh_layout_for(grid->nx, rows + 1, false).total <= budget)
+         gcm::mesh_layout_for(grid->nx, rows + 1, false, kThreads).total <= budget)
     ++rows;
-  while (rows > 1 && gcm::mesh_layout_for(grid->nx, rows, false).total > budget) --rows;
-  const gcm::MeshLayout layout = gcm::mesh_layout_for(grid->nx, rows, false);
+  while (rows > 1 && gcm::mesh_layout_for(grid->nx, rows, false, kThreads).total > budget) --rows;
+  const gcm::MeshLayout layout = gcm::mesh_layout_for(grid->nx, rows, false, kThreads);
   const size_t smem = layout.total;
   const uint64_t ntiles = tiles_for(rows);
   if (ntiles > kNoAllocMaxTiles || smem > (size_t)optin) return GCM_ERR_NOT_SUPPORTED;

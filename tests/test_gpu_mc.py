@@ -88,7 +88,8 @@ def test_c1_gyroid_128_bit_exact_vs_oracle(ctx):
     assert host(norm).tobytes() == onorm.tobytes()
 
 
-@pytest.mark.parametrize("shape", [(2, 2, 2), (3, 2, 5), (2, 17, 3), (9, 33, 70), (5, 300, 7), (40, 3, 600)])
+@pytest.mark.parametrize("shape", [(2, 2, 2), (3, 2, 5), (2, 17, 3), (9, 33, 70), (5, 300, 7), (40, 3, 600),
+                                   (3, 2, 9000)])
 def test_ragged_shapes_vs_oracle(ctx, shape):
     rng = np.random.default_rng(sum(shape))
     f = rng.standard_normal(shape).astype(np.float32)
