@@ -433,6 +433,89 @@ void run_normalise_four(Reader& r, Writer& w, CUmodule gr) {
 
 }  // namespace
 
+// kind 6: timing of the reference's plain marching-cubes kernels on one field.
+// Per repetition classifyVoxel_new, compactVoxels and
+// generateTriangles_lattice_kernel_3 are timed with events on a GB300, launched
+// as the reference launches them (1024-thread classify and compaction, 32-thread
+// generate, src/Isosurface.cu:44-150); the two scans run on the host between them
+// and are not timed.  Writes nvox, active, total, reps, then per repetition the
+// three kernel times (ms) and a checksum of the position words.
+void run_mc_timing(Reader& r, Writer& w, CUmodule mc, const Tables& T) {
+  U3 g{r.get<uint32_t>(), r.get<uint32_t>(), r.get<uint32_t>()};
+  float iso = r.get<float>();
+  F3 vs{r.get<float>(), r.get<float>(), r.get<float>()};
+  F3 gc{r.get<float>(), r.get<float>(), r.get<float>()};
+  uint32_t reps = r.get<uint32_t>();
+  auto field = r.arr<float>((size_t)g.x * g.y * g.z);
+  CUdeviceptr d_field = dupload(field);
+  U3 mask{g.x - 1, g.y - 1, g.z - 1};
+  U3 shift{1, g.x - 1, (g.x - 1) * (g.y - 1)};
+  uint32_t nvox = mask.x * mask.y * mask.z;
+  CUdeviceptr d_verts = dalloc<uint32_t>(nvox), d_occ = dalloc<uint32_t>(nvox);
+  CUdeviceptr d_occ_scan = dalloc<uint32_t>(nvox), d_verts_scan = dalloc<uint32_t>(nvox);
+  CUdeviceptr d_comp = dalloc<uint32_t>(nvox);
+  CUfunction k_cls = find_kernel(mc, "classifyVoxel_new");
+  CUfunction k_cmp = find_kernel(mc, "compactVoxels");
+  CUfunction k_gen = find_kernel(mc, "generateTriangles_lattice_kernel_3");
+  CUevent e0, e1;
+  ck(cuEventCreate(&e0, CU_EVENT_DEFAULT), "cuEventCreate");
+  ck(cuEventCreate(&e1, CU_EVENT_DEFAULT), "cuEventCreate");
+  auto timed = [&](CUfunction f, unsigned gx, unsigned bx, void** a) {
+    ck(cuEventRecord(e0, nullptr), "cuEventRecord");
+    ck(cuLaunchKernel(f, gx, 1, 1, bx, 1, 1, 0, nullptr, a, nullptr), "cuLaunchKernel");
+    ck(cuEventRecord(e1, nullptr), "cuEventRecord");
+    ck(cuEventSynchronize(e1), "cuEventSynchronize");
+    float ms = 0;
+    ck(cuEventElapsedTime(&ms, e0, e1), "cuEventElapsedTime");
+    return ms;
+  };
+  uint32_t active = 0, total = 0;
+  CUdeviceptr d_pos = 0, d_norm = 0;
+  uint32_t maxv = 0;
+  std::vector<float> times;
+  std::vector<uint64_t> sums;
+  for (uint32_t rep = 0; rep < reps; ++rep) {
+    void* ac[] = {&d_verts, &d_occ, &d_field, &g, &shift, &mask, &nvox, &vs, &iso,
+                  const_cast<CUtexObject*>(&T.nverts_tex)};
+    const float t_cls = timed(k_cls, blocks_for(nvox, 1024), 1024, ac);
+    auto verts = ddownload<uint32_t>(d_verts, nvox);
+    auto occ = ddownload<uint32_t>(d_occ, nvox);
+    auto occ_scan = exclusive_scan(occ), verts_scan = exclusive_scan(verts);
+    active = occ_scan.back() + occ.back();
+    total = verts_scan.back() + verts.back();
+    ck(cuMemcpyHtoD(d_occ_scan, occ_scan.data(), 4ull * nvox), "cuMemcpyHtoD");
+    ck(cuMemcpyHtoD(d_verts_scan, verts_scan.data(), 4ull * nvox), "cuMemcpyHtoD");
+    if (!d_pos) {
+      maxv = total + 16;
+      d_pos = dalloc<float>(4ull * maxv);
+      d_norm = dalloc<float>(4ull * maxv);
+    }
+    void* am[] = {&d_comp, &d_occ, &d_occ_scan, &nvox};
+    const float t_cmp = timed(k_cmp, blocks_for(nvox, 1024), 1024, am);
+    void* ag[] = {&d_pos, &d_norm, &d_comp, &d_verts_scan, &g, &shift, &mask, &vs, &gc,
+                  &iso, &active, &maxv, const_cast<CUtexObject*>(&T.tri_tex),
+                  const_cast<CUtexObject*>(&T.nverts_tex), &total, &d_field, &iso};
+    const float t_gen = active ? timed(k_gen, blocks_for(active, 32), 32, ag) : 0.0f;
+    times.push_back(t_cls);
+    times.push_back(t_cmp);
+    times.push_back(t_gen);
+    auto head = ddownload<uint32_t>(d_pos, 4ull * (total < 4096 ? total : 4096));
+    uint64_t cs = 0;
+    for (uint32_t v : head) cs = cs * 1000003ull + v;
+    sums.push_back(cs);
+  }
+  w.put<uint32_t>(nvox);
+  w.put<uint32_t>(active);
+  w.put<uint32_t>(total);
+  w.put<uint32_t>(reps);
+  w.arr(times);
+  w.arr(sums);
+  cuEventDestroy(e0); cuEventDestroy(e1);
+  cuMemFree(d_field); cuMemFree(d_verts); cuMemFree(d_occ); cuMemFree(d_occ_scan);
+  cuMemFree(d_verts_scan); cuMemFree(d_comp);
+  if (d_pos) { cuMemFree(d_pos); cuMemFree(d_norm); }
+}
+
 int main(int argc, char** argv) {
   if (argc != 6) {
     std::fprintf(stderr, "usage: ref_runner <fatbin-dir> <sm103a|ptx89> <tables.bin> <job.bin> <out.bin>\n");
@@ -470,6 +553,7 @@ int main(int argc, char** argv) {
       case 3: run_unit_cell(r, w, fft); break;
       case 4: run_primitive(r, w, mdl); break;
       case 5: run_normalise_four(r, w, gr); break;
+      case 6: run_mc_timing(r, w, mc, T); break;
       default: die("unknown job kind");
     }
   }
