@@ -20,8 +20,16 @@ STATUS = {
     4: "GCM_ERR_CUDA", 5: "GCM_ERR_OUT_OF_MEMORY", 6: "GCM_ERR_NOT_SUPPORTED", 7: "GCM_ERR_IO",
     8: "GCM_ERR_REJECTED", 9: "GCM_ERR_CANCELLED", 10: "GCM_ERR_BUSY",
 }
+GCM_ERR_INVALID_ARGUMENT = 1
 GCM_ERR_OUTPUT_OVERFLOW = 2
 GCM_ERR_DEVICE_TIMEOUT = 3
+GCM_ERR_CUDA = 4
+GCM_ERR_OUT_OF_MEMORY = 5
+GCM_ERR_NOT_SUPPORTED = 6
+GCM_ERR_IO = 7
+GCM_ERR_REJECTED = 8
+GCM_ERR_CANCELLED = 9
+GCM_ERR_BUSY = 10
 
 
 class GcmGrid(C.Structure):
@@ -107,6 +115,9 @@ PROTOTYPES = {
     "gcm_field_lattice": (I32, [P, C.POINTER(GcmLattice), U32, U32, U32, P, P]),
     "gcm_mesh_lattice": (I32, [P, C.POINTER(GcmLattice), C.POINTER(GcmGrid), F32, P, P, U64, C.POINTER(GcmCounts), P]),
     "gcm_field_csg": (I32, [P, P, U32, C.POINTER(GcmFrame), U32, U32, U32, P, P]),
+    "gcm_csg_retain": (I32, [P, P, P, U32, U32, U32, F32, U32, P]),
+    "gcm_mesh_retained": (I32, [P, P, P, U32, C.POINTER(GcmGrid), F32, P, P, U64, C.POINTER(GcmCounts), P]),
+    "gcm_count_retained": (I32, [P, P, P, U32, C.POINTER(GcmGrid), F32, C.POINTER(GcmCounts), P]),
     "gcm_test_lookback_stall": (I32, [P, U32, U32, U64, P, P]),
     "gcm_batch_create": (I32, [P, P, U32, C.POINTER(P)]),
     "gcm_batch_destroy": (I32, [P]),

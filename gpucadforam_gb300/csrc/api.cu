@@ -99,13 +99,13 @@ uint32_t rows_for(uint32_t nx, uint32_t ny, uint32_t tile_voxels) {
   return std::min(std::min(std::max<uint32_t>(1, (tile_voxels + vx / 2) / vx), ny - 1), max_tile_rows(vx));
 }
 
-gcm_status plan_mesh(gcm_ctx* ctx, const gcm_grid* g, bool band, MeshPlan* out) {
+gcm_status plan_mesh(gcm_ctx* ctx, const gcm_grid* g, int mode, MeshPlan* out) {
   const uint32_t vy = g->ny - 1, vz = g->nz - 1;
   const int threads = ctx->mesh_threads;
   uint32_t rows = rows_for(g->nx, g->ny, ctx->tile_voxels);
   const size_t budget = std::min(kMeshSmemBudget, ctx->smem_optin);
-  while (rows > 1 && mesh_layout_for(g->nx, rows, band, threads).total > budget) --rows;
-  const MeshLayout L = mesh_layout_for(g->nx, rows, band, threads);
+  while (rows > 1 && mesh_layout_for(g->nx, rows, mode, threads).total > budget) --rows;
+  const MeshLayout L = mesh_layout_for(g->nx, rows, mode, threads);
   if (L.total > ctx->smem_optin)
     return fail(ctx, GCM_ERR_NOT_SUPPORTED, "grid rows of %u samples do not fit in shared memory", g->nx);
   out->rows = rows;
@@ -118,13 +118,13 @@ gcm_status plan_mesh(gcm_ctx* ctx, const gcm_grid* g, bool band, MeshPlan* out) 
   return GCM_OK;
 }
 
-gcm_status launch_mesh_kernel(gcm_ctx* ctx, bool band, bool emit, MeshParams& p, MeshPlan& plan, cudaStream_t st) {
+gcm_status launch_mesh_kernel(gcm_ctx* ctx, int mode, bool emit, MeshParams& p, MeshPlan& plan, cudaStream_t st) {
   int per_sm = 0;
-  GCM_CUDA(ctx, gcm::mesh_prepare(band, emit, plan.threads, plan.layout.total, &per_sm));
+  GCM_CUDA(ctx, gcm::mesh_prepare(mode, emit, plan.threads, plan.layout.total, &per_sm));
   per_sm = std::max(per_sm, 1);
   const uint64_t want = (uint64_t)ctx->sm_count * (uint64_t)per_sm;
   plan.blocks = (uint32_t)std::min<uint64_t>(want, plan.ntiles);
-  GCM_CUDA(ctx, gcm::launch_mesh(band, emit, plan.threads, p, plan.layout, plan.blocks, st));
+  GCM_CUDA(ctx, gcm::launch_mesh(mode, emit, plan.threads, p, plan.layout, plan.blocks, st));
   count_launch(ctx, 1);
   return GCM_OK;
 }
@@ -161,12 +161,12 @@ gcm_status status_of(gcm_ctx* ctx, const gcm_counts& c) {
 // Core of every fused extraction.  counts_out: device pointer receiving the
 // counts (the context's scratch when null).  The caller zeroes nothing.
 gcm_status mesh_core(gcm_ctx* ctx, const float* f, const float* gfield, const gcm_grid* grid, float iso, float lo,
-                     float hi, bool band, bool emit, float* pos, float* norm, uint64_t capacity,
+                     float hi, int mode, uint32_t op, bool emit, float* pos, float* norm, uint64_t capacity,
                      gcm_counts* counts_out, cudaStream_t st, gcm_counts** counts_used) {
   if (((reinterpret_cast<uintptr_t>(pos) | reinterpret_cast<uintptr_t>(norm)) & 15u) != 0)
     return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "position and normal buffers must be 16-byte aligned");
   MeshPlan plan;
-  gcm_status s = plan_mesh(ctx, grid, band, &plan);
+  gcm_status s = plan_mesh(ctx, grid, mode, &plan);
   if (s) return s;
   const size_t need = 128 + plan.ntiles * sizeof(uint64_t);
   s = ensure_scratch(ctx, need);
@@ -192,6 +192,7 @@ gcm_status mesh_core(gcm_ctx* ctx, const float* f, const float* gfield, const gc
   p.iso = iso;
   p.lo = lo;
   p.hi = hi;
+  p.op = op;
   p.pos = reinterpret_cast<float4*>(pos);
   p.norm = reinterpret_cast<float4*>(norm);
   p.capacity = capacity;
@@ -200,7 +201,7 @@ gcm_status mesh_core(gcm_ctx* ctx, const float* f, const float* gfield, const gc
   p.counts_dev = cnt;
   p.status = &cnt->status;
   p.wait_ns = ctx->wait_ns;
-  s = launch_mesh_kernel(ctx, band, emit, p, plan, st);
+  s = launch_mesh_kernel(ctx, mode, emit, p, plan, st);
   if (counts_used) *counts_used = cnt;
   return s;
 }
@@ -312,7 +313,7 @@ gcm_status gcm_mesh_field(gcm_ctx* ctx, const float* d_field, const gcm_grid* gr
   if (s) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   gcm_counts* used = nullptr;
-  s = mesh_core(ctx, d_field, nullptr, grid, iso, 0, 0, false, true, d_pos, d_norm, capacity, nullptr, st, &used);
+  s = mesh_core(ctx, d_field, nullptr, grid, iso, 0, 0, kMeshPlain, 0, true, d_pos, d_norm, capacity, nullptr, st, &used);
   if (s) return s;
   return read_counts(ctx, used, h_counts, st);
 }
@@ -324,7 +325,7 @@ gcm_status gcm_mesh_field_async(gcm_ctx* ctx, const float* d_field, const gcm_gr
     return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_mesh_field_async: NULL field, counts or outputs");
   gcm_status s = check_grid(ctx, grid);
   if (s) return s;
-  return mesh_core(ctx, d_field, nullptr, grid, iso, 0, 0, false, true, d_pos, d_norm, capacity, d_counts,
+  return mesh_core(ctx, d_field, nullptr, grid, iso, 0, 0, kMeshPlain, 0, true, d_pos, d_norm, capacity, d_counts,
                    static_cast<cudaStream_t>(stream), nullptr);
 }
 
@@ -336,7 +337,7 @@ gcm_status gcm_count_field(gcm_ctx* ctx, const float* d_field, const gcm_grid* g
   if (s) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   gcm_counts* used = nullptr;
-  s = mesh_core(ctx, d_field, nullptr, grid, iso, 0, 0, false, false, nullptr, nullptr, 0, nullptr, st, &used);
+  s = mesh_core(ctx, d_field, nullptr, grid, iso, 0, 0, kMeshPlain, 0, false, nullptr, nullptr, 0, nullptr, st, &used);
   if (s) return s;
   return read_counts(ctx, used, h_counts, st);
 }
@@ -351,9 +352,57 @@ gcm_status gcm_mesh_band(gcm_ctx* ctx, const float* d_label, const float* d_norm
   if (s) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   gcm_counts* used = nullptr;
-  s = mesh_core(ctx, d_label, d_norm_field, grid, iso, lo, hi, true, true, d_pos, d_norm, capacity, nullptr, st, &used);
+  s = mesh_core(ctx, d_label, d_norm_field, grid, iso, lo, hi, kMeshBand, 0, true, d_pos, d_norm, capacity, nullptr, st, &used);
   if (s) return s;
   return read_counts(ctx, used, h_counts, st);
+}
+
+// ------------------------------------------------------- retained CSG form
+
+gcm_status gcm_csg_retain(gcm_ctx* ctx, gcm_csg_point* d_acc, const float* d_field, uint32_t nx, uint32_t ny,
+                          uint32_t nz, float iso, gcm_csg_op op, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_acc || !d_field) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_csg_retain: NULL argument");
+  if (op > GCM_CSG_INTERSECT) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_csg_retain: unknown op %u", (unsigned)op);
+  if (nx == 0 || ny == 0 || nz == 0) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_csg_retain: empty grid");
+  const uint64_t n = (uint64_t)nx * ny * nz;
+  GCM_CUDA(ctx, launch_csg_retain(d_acc, d_field, nx, ny, nz, iso, (uint32_t)op, grid_blocks(ctx, n, 256),
+                                  static_cast<cudaStream_t>(stream)));
+  count_launch(ctx, 1);
+  return GCM_OK;
+}
+
+static gcm_status retained_core(gcm_ctx* ctx, const char* who, const gcm_csg_point* d_acc, const float* d_field,
+                                gcm_csg_op op, const gcm_grid* grid, float iso, bool emit, float* d_pos,
+                                float* d_norm, uint64_t capacity, gcm_counts* h_counts, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_acc || !h_counts || (emit && capacity && (!d_pos || !d_norm)))
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "%s: NULL accumulator, counts or outputs", who);
+  if ((reinterpret_cast<uintptr_t>(d_acc) & 15u) != 0)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "%s: the accumulator must be 16-byte aligned", who);
+  if (op > GCM_CSG_INTERSECT) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "%s: unknown op %u", who, (unsigned)op);
+  gcm_status s = check_grid(ctx, grid);
+  if (s) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  gcm_counts* used = nullptr;
+  const int mode = d_field ? kMeshPreview : kMeshRegion;
+  s = mesh_core(ctx, reinterpret_cast<const float*>(d_acc), d_field, grid, iso, 0, 0, mode, (uint32_t)op, emit,
+                emit ? d_pos : nullptr, emit ? d_norm : nullptr, emit ? capacity : 0, nullptr, st, &used);
+  if (s) return s;
+  return read_counts(ctx, used, h_counts, st);
+}
+
+gcm_status gcm_mesh_retained(gcm_ctx* ctx, const gcm_csg_point* d_acc, const float* d_field, gcm_csg_op op,
+                             const gcm_grid* grid, float iso, float* d_pos, float* d_norm, uint64_t capacity,
+                             gcm_counts* h_counts, gcm_stream stream) {
+  return retained_core(ctx, "gcm_mesh_retained", d_acc, d_field, op, grid, iso, true, d_pos, d_norm, capacity,
+                       h_counts, stream);
+}
+
+gcm_status gcm_count_retained(gcm_ctx* ctx, const gcm_csg_point* d_acc, const float* d_field, gcm_csg_op op,
+                              const gcm_grid* grid, float iso, gcm_counts* h_counts, gcm_stream stream) {
+  return retained_core(ctx, "gcm_count_retained", d_acc, d_field, op, grid, iso, false, nullptr, nullptr, 0,
+                       h_counts, stream);
 }
 
 // ------------------------------------------------------------ staged form
@@ -543,7 +592,7 @@ gcm_status gcm_mesh_lattice(gcm_ctx* ctx, const gcm_lattice* lattice, const gcm_
   s = run_lattice(ctx, p, ctx->field_buf, st);
   if (s) return s;
   gcm_counts* used = nullptr;
-  s = mesh_core(ctx, ctx->field_buf, nullptr, grid, iso, 0, 0, false, true, d_pos, d_norm, capacity, nullptr, st, &used);
+  s = mesh_core(ctx, ctx->field_buf, nullptr, grid, iso, 0, 0, kMeshPlain, 0, true, d_pos, d_norm, capacity, nullptr, st, &used);
   if (s) return s;
   return read_counts(ctx, used, h_counts, st);
 }
@@ -585,7 +634,7 @@ gcm_status gcm_mesh_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_p
   if (s) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   gcm_counts* used = nullptr;
-  s = mesh_core(ctx, ctx->field_buf, nullptr, grid, iso, 0, 0, false, true, d_pos, d_norm, capacity, nullptr, st, &used);
+  s = mesh_core(ctx, ctx->field_buf, nullptr, grid, iso, 0, 0, kMeshPlain, 0, true, d_pos, d_norm, capacity, nullptr, st, &used);
   if (s) return s;
   return read_counts(ctx, used, h_counts, st);
 }

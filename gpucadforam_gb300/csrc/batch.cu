@@ -94,7 +94,7 @@ gcm_status make_plan(gcm_batch* b, int threads, uint32_t tile_voxels) {
     const gcm_grid& g = b->inst[i].grid;
     const uint32_t vx = g.nx - 1, vy = g.ny - 1, vz = g.nz - 1;
     uint32_t rows = std::min(std::min(std::max<uint32_t>(1, (tile_voxels + vx / 2) / vx), vy), max_tile_rows(vx));
-    while (rows > 1 && mesh_layout_for(g.nx, rows, false, threads).total > budget) --rows;
+    while (rows > 1 && mesh_layout_for(g.nx, rows, kMeshPlain, threads).total > budget) --rows;
     BatchInstance& I = bi[i];
     I.f = b->field + b->field_off[i];
     I.nx = g.nx;
@@ -116,7 +116,7 @@ gcm_status make_plan(gcm_batch* b, int threads, uint32_t tile_voxels) {
     max_win = std::max(max_win, rows * ((vx + 31) / 32));
   }
   if (tiles >= (1ull << 31)) return fail(ctx, GCM_ERR_NOT_SUPPORTED, "batch has too many tiles");
-  const MeshLayout L = mesh_layout(max_plane, max_vox, max_win, false, threads);
+  const MeshLayout L = mesh_layout(max_plane, max_vox, max_win, kMeshPlain, threads);
   if (L.total > ctx->smem_optin) return fail(ctx, GCM_ERR_NOT_SUPPORTED, "batch rows do not fit in shared memory");
   drop_graph(b);
   free_plan_buffers(b);

@@ -203,6 +203,22 @@ __device__ __forceinline__ float3 edge_point_band_v(float id0, float id1, float 
   return lerp3(pa, pb, t);
 }
 
+// Retained edge point (vertexInterp_primitive, src/MarchingCubes_kernel.cu:
+// 1640-1672): the crossing fraction t2 of the fed field on the edge (inclusive
+// tests on both sides), averaged with the accumulated fraction t1 when both
+// are positive, else whichever is positive alone, else 0; p0 is the edge's
+// lower corner.  (t1 + t2) * 0.5 runs in double in the reference, which rounds
+// to the same float as the float product.
+__device__ __forceinline__ float3 edge_point_retained(float iso, float3 p0, float3 p1, float f0, float f1, float t1) {
+  float t2 = 0.0f;
+  if (((f1 >= iso) && (f0 <= iso)) || ((f0 >= iso) && (f1 <= iso))) t2 = __fdiv_rn(__fsub_rn(iso, f0), __fsub_rn(f1, f0));
+  float t = 0.0f;
+  if ((t1 > 0.0f) && (t2 > 0.0f)) t = __fmul_rn(__fadd_rn(t1, t2), 0.5f);
+  else if ((t1 > 0.0f) && (t2 == 0.0f)) t = t1;
+  else if ((t2 > 0.0f) && (t1 == 0.0f)) t = t2;
+  return lerp3(p0, p1, t);
+}
+
 __device__ __forceinline__ uint32_t cube_index8(const float c[8], float iso) {
   uint32_t ci = 0;
 #pragma unroll

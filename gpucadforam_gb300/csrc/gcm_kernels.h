@@ -24,6 +24,15 @@
 
 namespace gcm {
 
+// Extraction modes of the fused kernel: plain (field < iso), band (label
+// field + normalised field), and the two meshes of a retained primitive
+// accumulator (gcm_csg_point): its region alone, or its preview combined
+// with a fed primitive field.
+enum MeshMode : int { kMeshPlain = 0, kMeshBand = 1, kMeshRegion = 2, kMeshPreview = 3 };
+__host__ __device__ constexpr bool mode_has_g(int mode) { return mode == kMeshBand || mode == kMeshPreview; }
+// floats per sample of the classify input (accumulator records are 4 words)
+__host__ __device__ constexpr uint32_t mode_fw(int mode) { return mode >= kMeshRegion ? 4u : 1u; }
+
 // Most voxels in one tile (the triangle list keeps a voxel's index within its
 // tile in 16 bits), as a row limit for rows of vx voxels.
 constexpr uint32_t kMaxTileVoxels = 65535;
@@ -39,6 +48,7 @@ struct MeshParams {
   uint64_t ntiles;
   float vs[3], gc[3];
   float iso, lo, hi;
+  uint32_t op;            // preview mode: gcm_csg_op combining accumulator and field
   float4* pos;
   float4* norm;
   uint64_t capacity;
@@ -145,10 +155,10 @@ struct CsgParams {
 
 // Launch wrappers (each kernel is launched from the file that defines it).
 bool mesh_threads_supported(int threads);
-MeshLayout mesh_layout(uint32_t plane_floats, uint32_t tile_voxels, uint32_t windows, bool band, int threads);
-MeshLayout mesh_layout_for(uint32_t nx, uint32_t rows, bool band, int threads);
-cudaError_t mesh_prepare(bool band, bool emit, int threads, size_t smem, int* blocks_per_sm);
-cudaError_t launch_mesh(bool band, bool emit, int threads, const MeshParams& p, const MeshLayout& L, uint32_t blocks,
+MeshLayout mesh_layout(uint32_t plane_floats, uint32_t tile_voxels, uint32_t windows, int mode, int threads);
+MeshLayout mesh_layout_for(uint32_t nx, uint32_t rows, int mode, int threads);
+cudaError_t mesh_prepare(int mode, bool emit, int threads, size_t smem, int* blocks_per_sm);
+cudaError_t launch_mesh(int mode, bool emit, int threads, const MeshParams& p, const MeshLayout& L, uint32_t blocks,
                         cudaStream_t st);
 cudaError_t batch_prepare(bool emit, int threads, size_t smem, int* blocks_per_sm);
 cudaError_t launch_batch_mesh(bool emit, int threads, const BatchMeshParams& p, const MeshLayout& L, uint32_t blocks,
@@ -173,7 +183,10 @@ cudaError_t launch_csg(const CsgParams& p, uint32_t blocks, cudaStream_t st);
 cudaError_t launch_normalise(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, unsigned int* enc, float lo,
                              float hi, float* label, float* norm_field, uint32_t blocks, cudaStream_t st);
 
-size_t mesh_smem_bytes(uint32_t nx, uint32_t rows, bool band);
+size_t mesh_smem_bytes(uint32_t nx, uint32_t rows, int mode);
+// Folds one primitive field into a retained accumulator (gcm_csg_point per sample).
+cudaError_t launch_csg_retain(gcm_csg_point* acc, const float* f, uint32_t nx, uint32_t ny, uint32_t nz, float iso,
+                              uint32_t op, uint32_t blocks, cudaStream_t st);
 uint32_t scan_tile_elems();
 
 }  // namespace gcm

@@ -73,13 +73,17 @@ __device__ __forceinline__ void stage_bulk(float* dst, const float* __restrict__
   if (r.body) bulk_copy_g2s(dst + r.m + r.head, src + start + r.head, r.body * 4u, bar);
 }
 
-// One tile, resolved: rows y0..y0+rows-1 of voxel plane z of a grid.
+// One tile, resolved: rows y0..y0+rows-1 of voxel plane z of a grid.  f is
+// the classify input (floats, or 4-word accumulator records in the retained
+// modes), g the second field (band: normalised field; preview: the fed
+// primitive field).
 struct TileGeom {
   const float* f;
   const float* g;
   uint32_t nx, ny, z, y0, rows, bulk;
   Frame fr;
   float iso, lo, hi;
+  uint32_t op;
   uint32_t inst, local;  // batch bookkeeping: instance and tile within it
 };
 
@@ -101,8 +105,8 @@ struct EmitTarget {
   uint64_t wait_ns;
 };
 
-// The staging buffer: planes z and z+1 of the classify field, then (band
-// mode) of the interpolation field.
+// The staging buffer: planes z and z+1 of the classify input, then (band and
+// preview modes) of the second field.
 struct Planes {
   float *f0, *f1, *g0, *g1;
 };
@@ -124,34 +128,37 @@ __device__ __forceinline__ uint64_t* bar_of(unsigned char* smem, const MeshLayou
 // Phase 1: issue the staging of tile tg (every thread calls it; thread 0
 // issues the bulk copies, every thread loads the ragged ends).  The caller
 // guarantees that no thread still reads the buffer.
-template <bool BAND>
+template <int MODE>
 __device__ __forceinline__ void tile_stage(const TileGeom& tg, const MeshLayout& L, unsigned char* smem) {
+  constexpr uint32_t W = mode_fw(MODE);
   const Planes P = planes_of(smem, L);
   uint64_t* bar = bar_of(smem, L);
   const uint64_t st0 = ((uint64_t)tg.z * tg.ny + tg.y0) * tg.nx;
   const uint64_t st1 = st0 + (uint64_t)tg.ny * tg.nx;
   const uint32_t cnt = (tg.rows + 1) * tg.nx;
   const bool bulk = tg.bulk != 0;
-  const Run r0 = plan_run(st0, cnt, bulk), r1 = plan_run(st1, cnt, bulk);
+  // classify input in units of floats (W per sample), second field per sample
+  const Run r0 = plan_run(W * st0, W * cnt, bulk), r1 = plan_run(W * st1, W * cnt, bulk);
+  const Run q0 = plan_run(st0, cnt, bulk), q1 = plan_run(st1, cnt, bulk);
   if (bulk && threadIdx.x == 0) {
     // Every thread's reads of this buffer were ordered by a barrier before
     // this call; the proxy fence orders them before the async-proxy writes.
     // Expect the bytes first, then issue the copies.
     fence_proxy_async();
-    const uint32_t bytes = (r0.body + r1.body) * 4u * (BAND ? 2u : 1u);
+    const uint32_t bytes = (r0.body + r1.body + (mode_has_g(MODE) ? q0.body + q1.body : 0u)) * 4u;
     mbar_arrive_expect_tx(bar, bytes);
-    stage_bulk(P.f0, tg.f, st0, r0, bar);
-    stage_bulk(P.f1, tg.f, st1, r1, bar);
-    if (BAND) {
-      stage_bulk(P.g0, tg.g, st0, r0, bar);
-      stage_bulk(P.g1, tg.g, st1, r1, bar);
+    stage_bulk(P.f0, tg.f, W * st0, r0, bar);
+    stage_bulk(P.f1, tg.f, W * st1, r1, bar);
+    if (mode_has_g(MODE)) {
+      stage_bulk(P.g0, tg.g, st0, q0, bar);
+      stage_bulk(P.g1, tg.g, st1, q1, bar);
     }
   }
-  stage_scalar(P.f0, tg.f, st0, cnt, r0);
-  stage_scalar(P.f1, tg.f, st1, cnt, r1);
-  if (BAND) {
-    stage_scalar(P.g0, tg.g, st0, cnt, r0);
-    stage_scalar(P.g1, tg.g, st1, cnt, r1);
+  stage_scalar(P.f0, tg.f, W * st0, W * cnt, r0);
+  stage_scalar(P.f1, tg.f, W * st1, W * cnt, r1);
+  if (mode_has_g(MODE)) {
+    stage_scalar(P.g0, tg.g, st0, cnt, q0);
+    stage_scalar(P.g1, tg.g, st1, cnt, q1);
   }
 }
 
@@ -188,12 +195,29 @@ struct WindowCursor {
   }
 };
 
+// Corner k of a voxel inside the solid: the cube-index bit of each mode.
+// Plain and band: f < iso (classifyVoxel_new, src/MarchingCubes_kernel.cu:
+// 3207-3249).  Region: the accumulated sign, (float)val < iso.  Preview: the
+// accumulated sign combined with the fed field (classifyVoxel,
+// src/MarchingCubes_kernel.cu:869-1052): union (val < iso) | (f < iso),
+// difference (f >= iso) & (val < iso), intersection (val < iso) & (f < iso).
+template <int MODE>
+__device__ __forceinline__ bool corner_inside(float fval, float gval, uint32_t op, float iso) {
+  if (MODE == kMeshPlain || MODE == kMeshBand) return fval < iso;
+  const bool a = (float)__float_as_int(fval) < iso;
+  if (MODE == kMeshRegion) return a;
+  if (op == GCM_CSG_SUBTRACT) return (gval >= iso) && a;
+  if (op == GCM_CSG_INTERSECT) return a && (gval < iso);
+  return a || (gval < iso);
+}
+
 // Phase 3: classify in warp windows of 32 consecutive voxels of a row, scan the
 // window triangle counts and write the tile's edge table.  Ends with a barrier.
-template <int THREADS>
+template <int MODE, int THREADS>
 __device__ __forceinline__ void tile_classify(const TileGeom& tg, const MeshLayout& L, unsigned char* smem,
                                               TileOut& res) {
   constexpr uint32_t kWarps = THREADS / 32;
+  constexpr uint32_t W = mode_fw(MODE);
   const uint64_t* s_tri = reinterpret_cast<const uint64_t*>(smem);
   const Planes P = planes_of(smem, L);
   uint8_t* s_cube = smem + L.cube_off;
@@ -201,22 +225,44 @@ __device__ __forceinline__ void tile_classify(const TileGeom& tg, const MeshLayo
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t nx = tg.nx, vx = nx - 1, nwx = (vx + 31u) / 32u, nwin = tg.rows * nwx;
   const uint64_t st0 = ((uint64_t)tg.z * tg.ny + tg.y0) * nx;
-  const uint32_t m0 = (uint32_t)(st0 & 3u), m1 = (uint32_t)((st0 + (uint64_t)tg.ny * nx) & 3u);
+  // shifts of the staged planes: classify input (W floats per sample), second field
+  const uint32_t m0 = (uint32_t)((W * st0) & 3u), m1 = (uint32_t)((W * (st0 + (uint64_t)tg.ny * nx)) & 3u);
+  const uint32_t n0 = (uint32_t)(st0 & 3u), n1 = (uint32_t)((st0 + (uint64_t)tg.ny * nx) & 3u);
   if (threadIdx.x >= THREADS - 12) {
-    // edge table: shared-memory byte offsets of the edge's corners from the
-    // voxel's first sample (plane z + 1 lies `dplane` floats after plane z),
-    // and the corners' bits
+    // edge table, two words per edge: [first corner's offset : 24][second
+    // corner's offset : 24][first bits : 3][second bits : 3], and (retained
+    // modes) the byte offset of the first corner's accumulated fraction for
+    // the edge's axis.  Offsets are shared-memory bytes from the voxel's
+    // first sample (plane z + 1 lies `dplane` floats after plane z) of the
+    // field the vertex is interpolated in; they stay below 2^18.  Plain and
+    // band edges run edge_a -> edge_b; retained edges run from the corner with
+    // the lower coordinate (generateTriangles_lattice_kernel,
+    // src/MarchingCubes_kernel.cu:2087-2098).
     const uint32_t e = threadIdx.x - (THREADS - 12);
-    const uint32_t dplane = L.plane_stride + m1 - m0;
+    const bool retained = MODE == kMeshRegion || MODE == kMeshPreview;
+    const uint32_t dplane = L.plane_stride + (retained ? n1 - n0 : m1 - m0);
     auto off = [&](uint32_t k) {
       return 4u * ((uint32_t)corner_z((int)k) * dplane + (uint32_t)corner_y((int)k) * nx + (uint32_t)corner_x((int)k));
     };
     auto bits = [&](uint32_t k) { return (uint32_t)(corner_x((int)k) | (corner_y((int)k) << 1) | (corner_z((int)k) << 2)); };
-    const uint32_t ka = (uint32_t)edge_a((int)e), kb = (uint32_t)edge_b((int)e);
-    // [a offset : 24][b offset : 24][a bits : 3][b bits : 3] (shared memory
-    // offsets stay below 2^18 bytes)
-    reinterpret_cast<uint64_t*>(smem + L.edge_off)[e] =
-        (uint64_t)off(ka) | ((uint64_t)off(kb) << 24) | ((uint64_t)bits(ka) << 48) | ((uint64_t)bits(kb) << 51);
+    uint32_t ka = (uint32_t)edge_a((int)e), kb = (uint32_t)edge_b((int)e);
+    uint64_t word1 = 0;
+    if (retained) {
+      const uint32_t axis_bit = bits(ka) ^ bits(kb);
+      if (bits(ka) & axis_bit) {
+        const uint32_t tk = ka;
+        ka = kb;
+        kb = tk;
+      }
+      const uint32_t axis = axis_bit == 1u ? 0u : (axis_bit == 2u ? 1u : 2u);
+      // record of corner ka in the staged accumulator planes (m0 = m1 = 0),
+      // word 1 + axis of it (t_x, t_y, t_z)
+      word1 = 4u * ((uint32_t)corner_z((int)ka) * L.plane_stride +
+                    4u * ((uint32_t)corner_y((int)ka) * nx + (uint32_t)corner_x((int)ka)) + 1u + axis);
+    }
+    uint64_t* te = reinterpret_cast<uint64_t*>(smem + L.edge_off) + 2u * e;
+    te[0] = (uint64_t)off(ka) | ((uint64_t)off(kb) << 24) | ((uint64_t)bits(ka) << 48) | ((uint64_t)bits(kb) << 51);
+    te[1] = word1;
   }
   uint32_t my_active = 0;
   WindowCursor cur(warp, nwx);
@@ -224,10 +270,19 @@ __device__ __forceinline__ void tile_classify(const TileGeom& tg, const MeshLayo
     const uint32_t r = cur.r, x = cur.xw * 32u + lane;
     uint32_t nt = 0;
     if (x < vx) {
-      const float* a = P.f0 + m0 + r * nx + x;
-      const float* c1 = P.f1 + m1 + r * nx + x;
-      const float c[8] = {a[0], a[1], a[nx + 1], a[nx], c1[0], c1[1], c1[nx + 1], c1[nx]};
-      const uint32_t ci = cube_index8(c, tg.iso);
+      const float* a = P.f0 + m0 + W * (r * nx + x);
+      const float* c1 = P.f1 + m1 + W * (r * nx + x);
+      const float c[8] = {a[0], a[W], a[W * (nx + 1)], a[W * nx], c1[0], c1[W], c1[W * (nx + 1)], c1[W * nx]};
+      float gv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      if (MODE == kMeshPreview) {
+        const float* ga = P.g0 + n0 + r * nx + x;
+        const float* gb = P.g1 + n1 + r * nx + x;
+        gv[0] = ga[0]; gv[1] = ga[1]; gv[2] = ga[nx + 1]; gv[3] = ga[nx];
+        gv[4] = gb[0]; gv[5] = gb[1]; gv[6] = gb[nx + 1]; gv[7] = gb[nx];
+      }
+      uint32_t ci = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) ci |= (uint32_t)corner_inside<MODE>(c[k], gv[k], tg.op, tg.iso) << k;
       s_cube[r * vx + x] = (uint8_t)ci;
       nt = (uint32_t)(s_tri[ci] & 0xFu);
     }
@@ -269,10 +324,11 @@ __device__ __forceinline__ uint32_t list_entry(uint32_t v, uint32_t e3) { return
 // back while the other warps list the first round's triangles, taking windows
 // from a shared counter; warp 0 joins when its look-back ends.  Ends with a
 // barrier.
-template <bool BAND, int THREADS>
+template <int MODE, int THREADS>
 __device__ __forceinline__ void tile_emit(const TileGeom& tg, uint64_t t, const MeshLayout& L, unsigned char* smem,
                                           const EmitTarget& out, TileOut& res) {
   constexpr uint32_t kWarps = THREADS / 32;
+  constexpr bool kRetained = MODE == kMeshRegion || MODE == kMeshPreview;
   const uint64_t* s_tri = reinterpret_cast<const uint64_t*>(smem);
   const Planes P = planes_of(smem, L);
   const uint8_t* s_cube = smem + L.cube_off;
@@ -286,7 +342,7 @@ __device__ __forceinline__ void tile_emit(const TileGeom& tg, uint64_t t, const 
   const uint32_t nx = tg.nx, vx = nx - 1, nwx = (vx + 31u) / 32u, nwin = tg.rows * nwx;
   const SmallDiv by_vx(vx), by_nwx(nwx);
   const uint64_t st0 = ((uint64_t)tg.z * tg.ny + tg.y0) * nx;
-  const uint32_t m0 = (uint32_t)(st0 & 3u);
+  const uint32_t m0 = (uint32_t)(st0 & 3u);  // shift of single-float planes
   const uint32_t tris = res.tris;
   // list the triangles [base, base + n) of the tile: entry u = triangle base + u
   auto build = [&](uint32_t base, uint32_t n, auto&& next_window) {
@@ -327,7 +383,13 @@ __device__ __forceinline__ void tile_emit(const TileGeom& tg, uint64_t t, const 
   }
   VoxelCorners V;
   axis_corners(tg.z, tg.fr.gc[2], tg.fr.vs[2], V.z0, V.z1);
-  const float* F = P.f0 + m0;  // sample (x, r) of plane z at F[r * nx + x]
+  // sample (x, r) of plane z: F[r * nx + x] (plain, band; the band's second
+  // field 2 planes further), G[r * nx + x] (preview field), accumulator
+  // record at A[4 * (r * nx + x)]
+  const float* F = P.f0 + m0;
+  const float* G = P.g0 + m0;
+  const float* A = P.f0;
+  const float w_norm = kRetained ? 0.5f : 0.0f;
   bool dropped = false;
   for (uint32_t base = 0; base < tris; base += L.list_cap) {
     const uint32_t n = min(L.list_cap, tris - base);
@@ -352,22 +414,33 @@ __device__ __forceinline__ void tile_emit(const TileGeom& tg, uint64_t t, const 
         const uint32_t r = by_vx(v), x = v - r * vx;
         axis_corners(x, tg.fr.gc[0], tg.fr.vs[0], V.x0, V.x1);
         axis_corners(tg.y0 + r, tg.fr.gc[1], tg.fr.vs[1], V.y0, V.y1);
-        const char* Fv = reinterpret_cast<const char*>(F + v + r);  // sample (x, r): r * nx + x
+        const uint32_t s = v + r;  // sample (x, r): r * nx + x
+        const char* Fv = reinterpret_cast<const char*>(F + s);
+        const char* Gv = reinterpret_cast<const char*>(G + s);
+        const char* Av = reinterpret_cast<const char*>(A + 4u * s);
         auto at = [](const char* base, uint32_t off) { return *reinterpret_cast<const float*>(base + off); };
         float3 vtx[3];
 #pragma unroll
         for (int m = 0; m < 3; ++m) {
-          const uint64_t ed = s_edge[(e3 >> (8 - 4 * m)) & 0xFu];
+          const uint64_t* te = s_edge + 2u * ((e3 >> (8 - 4 * m)) & 0xFu);
+          const uint64_t ed = te[0];
           const uint32_t oa = (uint32_t)ed & 0xFFFFFFu, ob = (uint32_t)(ed >> 24) & 0xFFFFFFu;
           const uint32_t bits = (uint32_t)(ed >> 48), ba = bits & 7u, bb = bits >> 3;
-          if (BAND) {
-            const char* Gv = Fv + 8u * L.plane_stride;
-            vtx[m] = edge_point_band_v(at(Fv, oa), at(Fv, ob), at(Gv, oa), at(Gv, ob), ba, bb, V, tg.lo, tg.hi);
+          if (MODE == kMeshBand) {
+            const char* Nv = Fv + 8u * L.plane_stride;
+            vtx[m] = edge_point_band_v(at(Fv, oa), at(Fv, ob), at(Nv, oa), at(Nv, ob), ba, bb, V, tg.lo, tg.hi);
+          } else if (MODE == kMeshRegion) {
+            vtx[m] = lerp3(corner_sel(V, ba), corner_sel(V, bb), at(Av, (uint32_t)te[1]));
+          } else if (MODE == kMeshPreview) {
+            vtx[m] = edge_point_retained(tg.iso, corner_sel(V, ba), corner_sel(V, bb), at(Gv, oa), at(Gv, ob),
+                                         at(Av, (uint32_t)te[1]));
           } else {
             vtx[m] = edge_point_plain_v(at(Fv, oa), at(Fv, ob), corner_sel(V, ba), corner_sel(V, bb), tg.iso);
           }
         }
-        nrm = normal_of(vtx[0], vtx[1], vtx[2]);
+        // the retained modes' generate kernel takes calcNormal(v0, v2, v1) with
+        // w = 0.5 (src/MarchingCubes_kernel.cu:2178-2189)
+        nrm = kRetained ? normal_of(vtx[0], vtx[2], vtx[1]) : normal_of(vtx[0], vtx[1], vtx[2]);
         xp[3 * lane + 0] = make_float4(vtx[0].x, vtx[0].y, vtx[0].z, 1.0f);
         xp[3 * lane + 1] = make_float4(vtx[1].x, vtx[1].y, vtx[1].z, 1.0f);
         xp[3 * lane + 2] = make_float4(vtx[2].x, vtx[2].y, vtx[2].z, 1.0f);
@@ -383,7 +456,7 @@ __device__ __forceinline__ void tile_emit(const TileGeom& tg, uint64_t t, const 
         __stcs(gp + lane + 32u, xp[lane + 32u]);
         __stcs(gp + lane + 64u, xp[lane + 64u]);
         __syncwarp();
-        xp[lane] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+        xp[lane] = make_float4(nrm.x, nrm.y, nrm.z, w_norm);
         __syncwarp();
         __stcs(gn + lane, xp[q3[0]]);
         __stcs(gn + lane + 32u, xp[q3[1]]);
@@ -398,7 +471,7 @@ __device__ __forceinline__ void tile_emit(const TileGeom& tg, uint64_t t, const 
           if (q < nv && cb + 3ull * q3[k] + 3 <= out.capacity) __stcs(gp + q, xp[q]);
         }
         __syncwarp();
-        if (live) xp[lane] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+        if (live) xp[lane] = make_float4(nrm.x, nrm.y, nrm.z, w_norm);
         __syncwarp();
 #pragma unroll
         for (uint32_t k = 0; k < 3; ++k) {
@@ -428,7 +501,7 @@ __device__ __forceinline__ void mesh_cta_init(unsigned char* smem, const MeshLay
 // tile number and resets the tile record after the barrier that ends the
 // previous tile, when no thread reads either any more; every thread reads the
 // tile number only after the barrier that follows.
-template <bool BAND, bool EMIT, int THREADS, class Geom, class Book>
+template <int MODE, bool EMIT, int THREADS, class Geom, class Book>
 __device__ __forceinline__ void tile_loop(unsigned char* smem, const MeshLayout& L, uint32_t* counter, uint64_t ntiles,
                                           const EmitTarget& out, Geom&& geom, Book&& book) {
   __shared__ uint32_t sh_tile;
@@ -447,10 +520,10 @@ __device__ __forceinline__ void tile_loop(unsigned char* smem, const MeshLayout&
     const uint32_t t = sh_tile;
     if ((uint64_t)t >= ntiles) return;
     const TileGeom tg = geom(t);
-    tile_stage<BAND>(tg, L, smem);
+    tile_stage<MODE>(tg, L, smem);
     if (!tile_wait(tg, L, smem, parity, out, res)) return;
-    tile_classify<THREADS>(tg, L, smem, res);
-    if (EMIT) tile_emit<BAND, THREADS>(tg, t, L, smem, out, res);
+    tile_classify<MODE, THREADS>(tg, L, smem, res);
+    if (EMIT) tile_emit<MODE, THREADS>(tg, t, L, smem, out, res);
     // classify and emit end with a barrier after their last use of the
     // staged planes and of the record: thread 0 may book and reset at once
     if (threadIdx.x == 0) book(tg, t, res);
@@ -459,30 +532,31 @@ __device__ __forceinline__ void tile_loop(unsigned char* smem, const MeshLayout&
 
 }  // namespace
 
-MeshLayout mesh_layout(uint32_t plane_floats, uint32_t tile_voxels, uint32_t windows, bool band, int threads) {
+MeshLayout mesh_layout(uint32_t plane_floats, uint32_t tile_voxels, uint32_t windows, int mode, int threads) {
   MeshLayout L;
   const uint32_t plane_bytes = align16(plane_floats * 4);
   L.plane_stride = plane_bytes / 4;
   // at most 6144 entries: tiles of very wide rows take more rounds instead
   L.list_cap = std::min<uint32_t>(6144, std::max<uint32_t>(64, (GCM_MESH_LIST_PER_2VOX * tile_voxels / 2 + 31) / 32 * 32));
   L.f_off = 2048;  // after the 256-entry triangle table
-  L.cube_off = L.f_off + (band ? 4 : 2) * plane_bytes;
+  L.cube_off = L.f_off + (mode_has_g(mode) ? 4 : 2) * plane_bytes;
   L.win_off = L.cube_off + align16(tile_voxels);
   L.edge_off = L.win_off + align16(windows * 4);
-  L.list_off = L.edge_off + 128;
+  L.list_off = L.edge_off + 256;  // 12 edges x 2 words
   L.xpose_off = L.list_off + align16(L.list_cap * 4);
   L.bar_off = L.xpose_off + (uint32_t)(threads / 32) * 96u * 16u;
   L.total = L.bar_off + 16;
   return L;
 }
 
-MeshLayout mesh_layout_for(uint32_t nx, uint32_t rows, bool band, int threads) {
-  return mesh_layout((rows + 1) * nx + 4, rows * (nx - 1), rows * ((nx - 1 + 31) / 32), band, threads);
+MeshLayout mesh_layout_for(uint32_t nx, uint32_t rows, int mode, int threads) {
+  return mesh_layout(mode_fw(mode) * (rows + 1) * nx + 4, rows * (nx - 1), rows * ((nx - 1 + 31) / 32), mode,
+                     threads);
 }
 
-size_t mesh_smem_bytes(uint32_t nx, uint32_t rows, bool band) { return mesh_layout_for(nx, rows, band, 256).total; }
+size_t mesh_smem_bytes(uint32_t nx, uint32_t rows, int mode) { return mesh_layout_for(nx, rows, mode, 256).total; }
 
-template <bool BAND, bool EMIT, int THREADS>
+template <int MODE, bool EMIT, int THREADS>
 __global__ void __launch_bounds__(THREADS, mesh_min_blocks(THREADS)) mc_mesh_kernel(MeshParams p, MeshLayout L) {
   extern __shared__ __align__(16) unsigned char smem[];
   const EmitTarget out{p.pos, p.norm, p.capacity, p.tile_status, p.status, p.wait_ns};
@@ -500,6 +574,7 @@ __global__ void __launch_bounds__(THREADS, mesh_min_blocks(THREADS)) mc_mesh_ker
     tg.iso = p.iso;
     tg.lo = p.lo;
     tg.hi = p.hi;
+    tg.op = p.op;
     tg.inst = 0;
     tg.local = t;
     return tg;
@@ -510,7 +585,7 @@ __global__ void __launch_bounds__(THREADS, mesh_min_blocks(THREADS)) mc_mesh_ker
     if (!EMIT) atomicAdd(reinterpret_cast<unsigned long long*>(&cnt->total_verts), 3ull * res.tris);
     else if ((uint64_t)t == p.ntiles - 1) cnt->total_verts = res.prefix + 3ull * res.tris;
   };
-  tile_loop<BAND, EMIT, THREADS>(smem, L, p.counter, p.ntiles, out, geom, book);
+  tile_loop<MODE, EMIT, THREADS>(smem, L, p.counter, p.ntiles, out, geom, book);
 }
 
 // Batch of grids in one launch: the tiles of all instances form one sequence
@@ -543,6 +618,7 @@ __global__ void __launch_bounds__(THREADS, mesh_min_blocks(THREADS)) mc_batch_ke
     tg.iso = I.iso;
     tg.lo = 0.0f;
     tg.hi = 0.0f;
+    tg.op = 0;
     tg.inst = lo;
     tg.local = local;
     return tg;
@@ -562,7 +638,7 @@ __global__ void __launch_bounds__(THREADS, mesh_min_blocks(THREADS)) mc_batch_ke
       }
     }
   };
-  tile_loop<false, EMIT, THREADS>(smem, L, p.counter, p.ntiles, out, geom, book);
+  tile_loop<kMeshPlain, EMIT, THREADS>(smem, L, p.counter, p.ntiles, out, geom, book);
 }
 
 // ----------------------------------------------------------------------------
@@ -750,14 +826,57 @@ __global__ void __launch_bounds__(32) lookback_stall_kernel(uint32_t ntiles, uin
 // Launch wrappers.
 // ----------------------------------------------------------------------------
 namespace {
-using MeshFn = void (*)(MeshParams, MeshLayout);
-template <int T>
-MeshFn mesh_fn_t(bool band, bool emit) {
-  if (band) return emit ? mc_mesh_kernel<true, true, T> : mc_mesh_kernel<true, false, T>;
-  return emit ? mc_mesh_kernel<false, true, T> : mc_mesh_kernel<false, false, T>;
+// Retained primitive accumulation (classify_copy_Voxel, static mode,
+// src/MarchingCubes_kernel.cu:158-447): per sample the sign becomes -1 or 1
+// by the boolean of the new field f and the old sign (union: f < iso or
+// val < iso; difference: f >= iso and val < iso; intersection: f < iso and
+// val < iso), and on each of the sample's +x, +y, +z edges that f crosses the
+// crossing fraction t = (iso - f) / (f' - f) replaces a non-positive stored
+// fraction or is averaged with a positive one.  Like the reference, the last
+// sample of the grid is left as it is.
+__global__ void __launch_bounds__(256) csg_retain_kernel(gcm_csg_point* __restrict__ acc, const float* __restrict__ f,
+                                                         uint32_t nx, uint32_t ny, uint32_t nz, float iso, uint32_t op) {
+  const uint64_t plane = (uint64_t)nx * ny, total = plane * nz;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i + 1 < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t x = (uint32_t)(i % nx), y = (uint32_t)((i / nx) % ny), z = (uint32_t)(i / plane);
+    gcm_csg_point pt = acc[i];
+    const float v = __ldg(f + i);
+    const bool in_v = v < iso, in_a = (float)pt.val < iso;
+    bool inside;
+    if (op == GCM_CSG_SUBTRACT) inside = (v >= iso) && in_a;
+    else if (op == GCM_CSG_INTERSECT) inside = in_v && in_a;
+    else inside = in_v || in_a;
+    pt.val = inside ? -1 : 1;
+    auto fold = [&](float& ts, float w) {
+      if ((w < iso && v >= iso) || (w >= iso && v < iso)) {
+        const float t = __fdiv_rn(__fsub_rn(iso, v), __fsub_rn(w, v));
+        ts = ts > 0.0f ? __fmul_rn(__fadd_rn(ts, t), 0.5f) : t;
+      }
+    };
+    if (x + 1 < nx) fold(pt.t_x, __ldg(f + i + 1));
+    if (y + 1 < ny) fold(pt.t_y, __ldg(f + i + nx));
+    if (z + 1 < nz) fold(pt.t_z, __ldg(f + i + plane));
+    acc[i] = pt;
+  }
 }
-MeshFn mesh_fn(bool band, bool emit, int threads) {
-  return threads == 128 ? mesh_fn_t<128>(band, emit) : mesh_fn_t<256>(band, emit);
+
+using MeshFn = void (*)(MeshParams, MeshLayout);
+template <int M, int T>
+MeshFn mesh_fn_e(bool emit) {
+  return emit ? mc_mesh_kernel<M, true, T> : mc_mesh_kernel<M, false, T>;
+}
+template <int T>
+MeshFn mesh_fn_t(int mode, bool emit) {
+  switch (mode) {
+    case kMeshBand: return mesh_fn_e<kMeshBand, T>(emit);
+    case kMeshRegion: return mesh_fn_e<kMeshRegion, T>(emit);
+    case kMeshPreview: return mesh_fn_e<kMeshPreview, T>(emit);
+    default: return mesh_fn_e<kMeshPlain, T>(emit);
+  }
+}
+MeshFn mesh_fn(int mode, bool emit, int threads) {
+  return threads == 128 ? mesh_fn_t<128>(mode, emit) : mesh_fn_t<256>(mode, emit);
 }
 using BatchFn = void (*)(BatchMeshParams, MeshLayout);
 BatchFn batch_fn(bool emit, int threads) {
@@ -793,13 +912,13 @@ cudaError_t prepare(F f, size_t smem, int threads, int* blocks_per_sm) {
 
 bool mesh_threads_supported(int threads) { return threads == 128 || threads == 256; }
 
-cudaError_t mesh_prepare(bool band, bool emit, int threads, size_t smem, int* blocks_per_sm) {
-  return prepare(mesh_fn(band, emit, threads), smem, threads, blocks_per_sm);
+cudaError_t mesh_prepare(int mode, bool emit, int threads, size_t smem, int* blocks_per_sm) {
+  return prepare(mesh_fn(mode, emit, threads), smem, threads, blocks_per_sm);
 }
 
-cudaError_t launch_mesh(bool band, bool emit, int threads, const MeshParams& p, const MeshLayout& L, uint32_t blocks,
+cudaError_t launch_mesh(int mode, bool emit, int threads, const MeshParams& p, const MeshLayout& L, uint32_t blocks,
                         cudaStream_t st) {
-  mesh_fn(band, emit, threads)<<<blocks, threads, L.total, st>>>(p, L);
+  mesh_fn(mode, emit, threads)<<<blocks, threads, L.total, st>>>(p, L);
   return cudaGetLastError();
 }
 
@@ -810,6 +929,12 @@ cudaError_t batch_prepare(bool emit, int threads, size_t smem, int* blocks_per_s
 cudaError_t launch_batch_mesh(bool emit, int threads, const BatchMeshParams& p, const MeshLayout& L, uint32_t blocks,
                               cudaStream_t st) {
   batch_fn(emit, threads)<<<blocks, threads, L.total, st>>>(p, L);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_csg_retain(gcm_csg_point* acc, const float* f, uint32_t nx, uint32_t ny, uint32_t nz, float iso,
+                              uint32_t op, uint32_t blocks, cudaStream_t st) {
+  csg_retain_kernel<<<blocks, 256, 0, st>>>(acc, f, nx, ny, nz, iso, op);
   return cudaGetLastError();
 }
 

@@ -89,10 +89,10 @@ extern "C" gcm_status gcm_mesh_field_noalloc(const float* d_field, const gcm_gri
                          gcm::max_tile_rows(vx));
   auto tiles_for = [&](uint32_t r) { return (uint64_t)((vy + r - 1) / r) * vz; };
   while (tiles_for(rows) > kNoAllocMaxTiles && rows < vy && rows < gcm::max_tile_rows(vx) &&
-         gcm::mesh_layout_for(grid->nx, rows + 1, false, kThreads).total <= budget)
+         gcm::mesh_layout_for(grid->nx, rows + 1, gcm::kMeshPlain, kThreads).total <= budget)
     ++rows;
-  while (rows > 1 && gcm::mesh_layout_for(grid->nx, rows, false, kThreads).total > budget) --rows;
-  const gcm::MeshLayout layout = gcm::mesh_layout_for(grid->nx, rows, false, kThreads);
+  while (rows > 1 && gcm::mesh_layout_for(grid->nx, rows, gcm::kMeshPlain, kThreads).total > budget) --rows;
+  const gcm::MeshLayout layout = gcm::mesh_layout_for(grid->nx, rows, gcm::kMeshPlain, kThreads);
   const size_t smem = layout.total;
   const uint64_t ntiles = tiles_for(rows);
   if (ntiles > kNoAllocMaxTiles || smem > (size_t)optin) return GCM_ERR_NOT_SUPPORTED;
@@ -130,8 +130,8 @@ extern "C" gcm_status gcm_mesh_field_noalloc(const float* d_field, const gcm_gri
   p.wait_ns = 2000000000ull;
 
   int per_sm = 0;
-  if (gcm::mesh_prepare(false, true, kThreads, smem, &per_sm) != cudaSuccess) return GCM_ERR_CUDA;
+  if (gcm::mesh_prepare(gcm::kMeshPlain, true, kThreads, smem, &per_sm) != cudaSuccess) return GCM_ERR_CUDA;
   const uint32_t blocks = (uint32_t)std::min<uint64_t>((uint64_t)sms * (uint64_t)std::max(per_sm, 1), ntiles);
-  if (gcm::launch_mesh(false, true, kThreads, p, layout, blocks, st) != cudaSuccess) return GCM_ERR_CUDA;
+  if (gcm::launch_mesh(gcm::kMeshPlain, true, kThreads, p, layout, blocks, st) != cudaSuccess) return GCM_ERR_CUDA;
   return GCM_OK;
 }

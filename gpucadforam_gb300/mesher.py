@@ -203,6 +203,44 @@ class Context:
                                           _stream(stream)))
         return out
 
+    # ------------------------------------------------- retained CSG editing
+    CSG_OPS = {"union": 0, "subtract": 1, "intersect": 2}
+
+    def csg_accumulator(self, shape_zyx):
+        """An empty retained model: int32 sign + 3 float32 fractions per sample,
+        as an (nz, ny, nx, 4) int32 tensor (the fractions are float bits)."""
+        return torch.zeros((*shape_zyx, 4), dtype=torch.int32, device=f"cuda:{self.device}")
+
+    def csg_retain(self, acc, field, op="union", iso=0.0, stream=None):
+        nz, ny, nx = field.shape
+        assert tuple(acc.shape[:3]) == (nz, ny, nx) and acc.shape[3] == 4
+        self.check(self.lib.gcm_csg_retain(self.h, _ptr(acc), _ptr(field), nx, ny, nz, float(iso),
+                                           self.CSG_OPS.get(op, op), _stream(stream)))
+
+    def count_retained(self, acc, field=None, op="union", iso=0.0, stream=None) -> Counts:
+        g = make_grid(acc.shape[:3])
+        c = N.GcmCounts()
+        self.check(self.lib.gcm_count_retained(self.h, _ptr(acc), _ptr(field), self.CSG_OPS.get(op, op), C.byref(g),
+                                               float(iso), C.byref(c), _stream(stream)))
+        return Counts(c.active_voxels, c.total_verts, c.status)
+
+    def mesh_retained(self, acc, field=None, op="union", iso=0.0, voxel_size=(1, 1, 1), grid_center=(0, 0, 0),
+                      capacity=None, stream=None):
+        """Region mesh of the accumulator (field None) or the live model with
+        one more primitive field combined by op."""
+        if capacity is None:
+            capacity = self.count_retained(acc, field, op, iso, stream).total_verts
+        dev = acc.device
+        pos = torch.empty((max(capacity, 1), 4), dtype=torch.float32, device=dev)
+        norm = torch.empty((max(capacity, 1), 4), dtype=torch.float32, device=dev)
+        g = make_grid(acc.shape[:3], voxel_size, grid_center)
+        c = N.GcmCounts()
+        self.check(self.lib.gcm_mesh_retained(self.h, _ptr(acc), _ptr(field), self.CSG_OPS.get(op, op), C.byref(g),
+                                              float(iso), _ptr(pos), _ptr(norm), int(capacity), C.byref(c),
+                                              _stream(stream)))
+        n = int(c.total_verts)
+        return pos[:n], norm[:n], Counts(c.active_voxels, c.total_verts, c.status)
+
     def mesh_csg(self, prims_dev, n_prims, frame, shape_zyx, iso, voxel_size=(1, 1, 1), grid_center=(0, 0, 0),
                  pos=None, norm=None, stream=None, allow_overflow=False):
         g = make_grid(shape_zyx, voxel_size, grid_center)

@@ -239,6 +239,41 @@ gcm_status gcm_mesh_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_p
                         const gcm_grid* grid, float iso, float* d_pos, float* d_norm, uint64_t capacity_verts,
                         gcm_counts* h_counts, gcm_stream stream);
 
+/* ------------------------------------------------- retained CSG accumulation */
+
+/* The reference's interactive primitive editing keeps the model as a grid of
+ * these (grid_points, src/MarchingCubes_kernel.h:12-18): per sample an inside
+ * sign (-1 inside, 1 outside, 0 never touched) and the crossing fraction on
+ * its +x, +y and +z edges, averaged over the primitives that crossed it.
+ * A zeroed array is the empty model.  16 bytes per sample, x fastest. */
+typedef struct gcm_csg_point {
+  int32_t val;
+  float t_x, t_y, t_z;
+} gcm_csg_point;
+
+/* Folds one primitive field into the accumulator with op
+ * (Isosurface::copy_parameter -> classify_copy_Voxel static mode,
+ * src/Isosurface.cu:16-27, src/MarchingCubes_kernel.cu:158-447).  The field
+ * has the accumulator's nx*ny*nz samples; the reference folds at iso 0. */
+gcm_status gcm_csg_retain(gcm_ctx* ctx, gcm_csg_point* d_acc, const float* d_field, uint32_t nx, uint32_t ny,
+                          uint32_t nz, float iso, gcm_csg_op op, gcm_stream stream);
+/* Mesh of the accumulator, one fused pass (Isosurface::computeIsosurface,
+ * src/Isosurface.cu:44-135, with classifyVoxel and
+ * generateTriangles_lattice_kernel, src/MarchingCubes_kernel.cu:869-1052,
+ * 1865-2200).  d_field NULL: the region mode (make_region: cube index from
+ * the sign alone, vertices at the accumulated fractions).  d_field set: the
+ * live model, the accumulator combined with that primitive field by op, and
+ * vertices from vertexInterp_primitive (src/MarchingCubes_kernel.cu:1640-1672).
+ * Normals are cross(v2 - v0, v1 - v0) with w = 0.5, as that kernel writes them.
+ * Vertex order, capacity and status rules as gcm_mesh_field; d_acc must be
+ * 16-byte aligned. */
+gcm_status gcm_mesh_retained(gcm_ctx* ctx, const gcm_csg_point* d_acc, const float* d_field, gcm_csg_op op,
+                             const gcm_grid* grid, float iso, float* d_pos, float* d_norm, uint64_t capacity_verts,
+                             gcm_counts* h_counts, gcm_stream stream);
+/* Counting pass of gcm_mesh_retained. */
+gcm_status gcm_count_retained(gcm_ctx* ctx, const gcm_csg_point* d_acc, const float* d_field, gcm_csg_op op,
+                              const gcm_grid* grid, float iso, gcm_counts* h_counts, gcm_stream stream);
+
 /* ---------------------------------------------------------------- batches */
 
 /* Many graded lattices meshed together: one launch evaluates every

@@ -65,6 +65,11 @@ def lib():
         L.orc_normalise_band.argtypes = [F32P, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, F32P, F32P, F32P]
         L.orc_write_obj.argtypes = [F32P, C.c_uint64, C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.orc_write_obj.restype = C.c_int
+        L.orc_csg_retain.argtypes = [C.c_void_p, F32P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32]
+        L.orc_mesh_retained.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                        F32P, F32P, C.c_float, C.c_void_p, C.c_void_p, C.c_uint64,
+                                        C.POINTER(C.c_uint64)]
+        L.orc_mesh_retained.restype = C.c_uint64
         _lib = L
     return _lib
 
@@ -272,3 +277,39 @@ def write_obj(pos, path):
     if rc:
         raise OSError(f"orc_write_obj failed ({rc})")
     return int(nv.value), int(nf.value)
+
+
+CSG_OPS = {"union": 0, "subtract": 1, "intersect": 2}
+
+
+def csg_accumulator(shape_zyx):
+    """Empty retained model: (nz, ny, nx, 4) int32 = sign + 3 fractions (float bits)."""
+    return np.zeros((*shape_zyx, 4), np.int32)
+
+
+def csg_retain(acc, field, op="union", iso=0.0):
+    """classify_copy_Voxel static mode (src/MarchingCubes_kernel.cu:158-447), in place."""
+    assert acc.dtype == np.int32 and acc.flags.c_contiguous and acc.shape[3] == 4
+    field = np.ascontiguousarray(field, np.float32)
+    nz, ny, nx = field.shape
+    assert acc.shape[:3] == field.shape
+    lib().orc_csg_retain(acc.ctypes.data, field, nx, ny, nz, iso, CSG_OPS.get(op, op))
+    return acc
+
+
+def mesh_retained(acc, field, op, vs, gc, iso=0.0):
+    """Region mesh (field None) or live-model mesh of the accumulator; returns
+    (pos, norm, active_voxels)."""
+    nz, ny, nx = acc.shape[:3]
+    g = None if field is None else np.ascontiguousarray(field, np.float32)
+    L = lib()
+    act = C.c_uint64(0)
+    gp = None if g is None else g.ctypes.data
+    total = L.orc_mesh_retained(acc.ctypes.data, gp, CSG_OPS.get(op, op), nx, ny, nz, _f3(vs), _f3(gc), iso,
+                                None, None, 0, C.byref(act))
+    pos = np.zeros((max(total, 1), 4), np.float32)
+    norm = np.zeros((max(total, 1), 4), np.float32)
+    L.orc_mesh_retained(acc.ctypes.data, gp, CSG_OPS.get(op, op), nx, ny, nz, _f3(vs), _f3(gc), iso,
+                        pos.ctypes.data, norm.ctypes.data, total, C.byref(act))
+    return pos[:total], norm[:total], int(act.value)
+

@@ -692,6 +692,128 @@ uint64_t orc_mesh_field(const float* field, uint32_t nx, uint32_t ny, uint32_t n
   return total;
 }
 
+// ---- retained CSG accumulation ---------------------------------------------------
+
+// classify_copy_Voxel, static mode (src/MarchingCubes_kernel.cu:158-447), as
+// Isosurface::copy_parameter launches it (src/Isosurface.cu:16-27): samples
+// 0 .. P-2 (the launch bound excludes the last one); the new sign from the
+// boolean of f and the old sign; on each +x, +y, +z edge that f crosses the
+// fraction (iso - v) / (w - v) replaces a non-positive stored fraction or is
+// averaged with a positive one, (t_old + t) * 0.5 in double.
+void orc_csg_retain(orc_csg_point* acc, const float* f, uint32_t nx, uint32_t ny, uint32_t nz, float iso,
+                    uint32_t op) {
+  const uint64_t plane = (uint64_t)nx * ny, total = plane * nz;
+  for (uint64_t i = 0; i + 1 < total; ++i) {
+    const uint32_t x = (uint32_t)(i % nx), y = (uint32_t)((i / nx) % ny), z = (uint32_t)(i / plane);
+    orc_csg_point pt = acc[i];
+    const float v = f[i];
+    bool inside;
+    if (op == 1) inside = (v >= iso) && ((float)pt.val < iso);
+    else if (op == 2) inside = (v < iso) && ((float)pt.val < iso);
+    else inside = (v < iso) || ((float)pt.val < iso);
+    pt.val = inside ? -1 : 1;
+    const uint64_t stride[3] = {1, nx, plane};
+    const bool has[3] = {x + 1 < nx, y + 1 < ny, z + 1 < nz};
+    for (int a = 0; a < 3; ++a) {
+      if (!has[a]) continue;
+      const float w = f[i + stride[a]];
+      if ((w < iso && v >= iso) || (w >= iso && v < iso)) {
+        const float t = (iso - v) / (w - v);
+        pt.t[a] = pt.t[a] > 0 ? (float)((double)(pt.t[a] + t) * 0.5) : t;
+      }
+    }
+    acc[i] = pt;
+  }
+}
+
+// Meshes of the accumulator: classifyVoxel and generateTriangles_lattice_kernel
+// (src/MarchingCubes_kernel.cu:869-1052, 1865-2200) in their make_region mode
+// (field == NULL) and their plain primitive mode (fixed = dynamic = false): the
+// corner test, the edge running from its lower corner, the vertex at the stored
+// fraction or at vertexInterp_primitive's average (:1640-1672), the normal
+// calcNormal(v0, v2, v1) with w = 0.5.
+uint64_t orc_mesh_retained(const orc_csg_point* acc, const float* g, uint32_t op, uint32_t nx, uint32_t ny,
+                           uint32_t nz, const float* vs, const float* gc, float iso, float* pos, float* norm,
+                           uint64_t capacity, uint64_t* active_out) {
+  const uint64_t nvox = (uint64_t)(nx - 1) * (ny - 1) * (nz - 1);
+  auto inside = [&](uint64_t i) {
+    const bool a = (float)acc[i].val < iso;
+    if (!g) return a;
+    if (op == 1) return (g[i] >= iso) && a;
+    if (op == 2) return a && (g[i] < iso);
+    return a || (g[i] < iso);
+  };
+  auto cube = [&](uint32_t x, uint32_t y, uint32_t z) {
+    unsigned ci = 0;
+    for (int k = 0; k < 8; ++k)
+      ci |= (unsigned)inside(pidx(x + gcm::kCornerX[k], y + gcm::kCornerY[k], z + gcm::kCornerZ[k], nx, ny)) << k;
+    return ci;
+  };
+  std::vector<uint64_t> scan(nvox);
+  uint64_t total = 0, active = 0;
+  for (uint64_t v = 0; v < nvox; ++v) {
+    uint32_t x, y, z;
+    voxel_pos(v, nx, ny, x, y, z);
+    const unsigned n = kNumVerts(cube(x, y, z));
+    scan[v] = total;
+    total += n;
+    active += n > 0;
+  }
+  if (active_out) *active_out = active;
+  const Arith A = decode(orc_default_arith());
+  for (uint64_t v = 0; v < nvox; ++v) {
+    uint32_t gp[3];
+    voxel_pos(v, nx, ny, gp[0], gp[1], gp[2]);
+    const unsigned ci = cube(gp[0], gp[1], gp[2]);
+    const uint64_t row = gcm::kTriRows[ci];
+    const unsigned nv = kNumVerts(ci);
+    for (unsigned j = 0; j < nv; j += 3) {
+      float vv[3][3];
+      for (int m = 0; m < 3; ++m) {
+        const int e = (int)gcm::tri_edge(row, j + m);
+        int lo = gcm::kEdgeA[e], up = gcm::kEdgeB[e];
+        const int olo[3] = {gcm::kCornerX[lo], gcm::kCornerY[lo], gcm::kCornerZ[lo]};
+        const int oup[3] = {gcm::kCornerX[up], gcm::kCornerY[up], gcm::kCornerZ[up]};
+        int axis = 0;
+        for (int a = 0; a < 3; ++a)
+          if (olo[a] != oup[a]) axis = a;
+        if (olo[axis] > oup[axis]) std::swap(lo, up);
+        const int o0[3] = {gcm::kCornerX[lo], gcm::kCornerY[lo], gcm::kCornerZ[lo]};
+        const int o1[3] = {gcm::kCornerX[up], gcm::kCornerY[up], gcm::kCornerZ[up]};
+        const uint64_t plo = pidx(gp[0] + o0[0], gp[1] + o0[1], gp[2] + o0[2], nx, ny);
+        const uint64_t pup = pidx(gp[0] + o1[0], gp[1] + o1[1], gp[2] + o1[2], nx, ny);
+        const float t1 = acc[plo].t[axis];
+        float t = t1;
+        if (g) {
+          const float f0 = g[plo], f1 = g[pup];
+          float t2 = 0.0f;
+          if (((f1 >= iso) && (f0 <= iso)) || ((f0 >= iso) && (f1 <= iso))) t2 = (iso - f0) / (f1 - f0);
+          t = 0.0f;
+          if ((t1 > 0) && (t2 > 0)) t = (float)((double)(t1 + t2) * 0.5);
+          else if ((t1 > 0) && (t2 == 0)) t = t1;
+          else if ((t2 > 0) && (t1 == 0)) t = t2;
+        }
+        for (int a = 0; a < 3; ++a) {
+          const float d = (float)gp[a] - gc[a];
+          vv[m][a] = lerp_axis(d, vs[a], o0[a], o1[a], t, A);
+        }
+      }
+      float n[3];
+      normal_of(vv[0], vv[2], vv[1], A.cross, n);
+      const uint64_t idx = scan[v] + j;
+      if (idx + 3 > capacity) continue;
+      for (int m = 0; m < 3; ++m) {
+        float* P = pos + 4 * (idx + m);
+        float* N = norm + 4 * (idx + m);
+        P[0] = vv[m][0]; P[1] = vv[m][1]; P[2] = vv[m][2]; P[3] = 1.0f;
+        N[0] = n[0]; N[1] = n[1]; N[2] = n[2]; N[3] = 0.5f;
+      }
+    }
+  }
+  (void)nz;
+  return total;
+}
+
 // create_lattice_kernel (src/lattice_files/Fft_lattice.cu:11-93): unit cell on
 // [-1, 1]^3 with the literal 3.14; the coordinate is formed in double and
 // rounded to float, and the products with 3.14 are double, rounded to float at

@@ -85,6 +85,20 @@ void orc_normalise_band(const float* field, int nx, int ny, int nz, float band_l
 // ---- .obj -----------------------------------------------------------------------------
 int orc_write_obj(const float* pos, uint64_t nverts, const char* path, uint64_t* nv_out, uint64_t* nf_out);
 
+/* Retained primitive accumulation (grid_points, src/MarchingCubes_kernel.h:12-18)
+ * and its meshes.  op: 0 union, 1 subtract, 2 intersect. */
+typedef struct orc_csg_point {
+  int32_t val;
+  float t[3];
+} orc_csg_point;
+void orc_csg_retain(orc_csg_point* acc, const float* field, uint32_t nx, uint32_t ny, uint32_t nz, float iso,
+                    uint32_t op);
+/* field NULL: region mesh; else the accumulator combined with field by op.
+ * Returns the vertex total; writes the triangles whose vertices fit. */
+uint64_t orc_mesh_retained(const orc_csg_point* acc, const float* field, uint32_t op, uint32_t nx, uint32_t ny,
+                           uint32_t nz, const float* voxel_size, const float* grid_center, float iso, float* pos,
+                           float* norm, uint64_t capacity, uint64_t* active_out);
+
 #ifdef __cplusplus
 }
 #endif

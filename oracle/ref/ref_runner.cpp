@@ -433,6 +433,87 @@ void run_normalise_four(Reader& r, Writer& w, CUmodule gr) {
 
 }  // namespace
 
+// kind 7: retained primitive editing.  A zeroed grid_points accumulator
+// (src/MarchingCubes_kernel.h:12-18) folds a sequence of primitive fields with
+// classify_copy_Voxel as Isosurface::copy_parameter launches it
+// (src/Isosurface.cu:16-27, static mode); then the accumulator is meshed as
+// Isosurface::computeIsosurface does (src/Isosurface.cu:44-135): classifyVoxel,
+// scans, compactVoxels, generateTriangles_lattice_kernel, in the make_region
+// mode (mode 0) or the plain primitive mode with one more primitive field
+// (mode 1).  Unused field arguments get zeroed buffers (the kernels read them).
+void run_retain(Reader& r, Writer& w, CUmodule mc, const Tables& T) {
+  U3 g{r.get<uint32_t>(), r.get<uint32_t>(), r.get<uint32_t>()};
+  float iso = r.get<float>();
+  F3 vs{r.get<float>(), r.get<float>(), r.get<float>()};
+  F3 gc{r.get<float>(), r.get<float>(), r.get<float>()};
+  const size_t P = (size_t)g.x * g.y * g.z;
+  U3 mask{g.x - 1, g.y - 1, g.z - 1};
+  U3 shift{1, g.x - 1, (g.x - 1) * (g.y - 1)};
+  uint32_t nvox = mask.x * mask.y * mask.z;
+  CUdeviceptr d_acc = dalloc<uint8_t>(16 * P), d_zero = dalloc<float>(P), d_verts = dalloc<uint32_t>(nvox);
+  uint32_t n_folds = r.get<uint32_t>();
+  CUfunction k_fold = find_kernel(mc, "classify_copy_Voxel");
+  for (uint32_t i = 0; i < n_folds; ++i) {
+    uint32_t op = r.get<uint32_t>();
+    auto f = r.arr<float>(P);
+    CUdeviceptr d_f = dupload(f);
+    bool fixed = false, dynamic = false, ou = op == 0, od = op == 1, oi = op == 2;
+    float iso1 = 0.0f, iso2 = 0.0f;
+    void* a[] = {&d_verts, &d_acc, &d_f, &d_zero, &fixed, &dynamic, &iso1, &iso2, &g, &shift, &mask, &nvox,
+                 &vs, &iso, const_cast<CUtexObject*>(&T.nverts_tex), &ou, &od, &oi};
+    launch(k_fold, blocks_for(P, 1024), 1, 1, 1024, 1, 1, a);
+    cuMemFree(d_f);
+  }
+  uint32_t mode = r.get<uint32_t>(), pop = r.get<uint32_t>();
+  CUdeviceptr d_dyn = d_zero;
+  if (mode == 1) d_dyn = dupload(r.arr<float>(P));
+  bool ou = pop == 0, od = pop == 1, oi = pop == 2, prim = true, topo = false, lat = false, fixed = false,
+       dynamic = false, region = mode == 0;
+  float iso1 = 0.0f, iso2 = 0.0f;
+  CUdeviceptr d_occ = dalloc<uint32_t>(nvox);
+  CUfunction k_cls = find_kernel(mc, "classifyVoxel");
+  {
+    void* a[] = {&d_zero, &g, &d_verts, &d_occ, &d_acc, &d_dyn, &d_zero, &d_zero, &g, &shift, &mask, &nvox,
+                 &iso1, &iso2, &vs, &iso, const_cast<CUtexObject*>(&T.nverts_tex), &ou, &od, &oi, &prim, &topo,
+                 &lat, &fixed, &dynamic, &region};
+    launch(k_cls, blocks_for(nvox, 1024), 1, 1, 1024, 1, 1, a);
+  }
+  Classified c;
+  c.nvox = nvox;
+  c.verts = ddownload<uint32_t>(d_verts, nvox);
+  c.occ = ddownload<uint32_t>(d_occ, nvox);
+  c.occ_scan = exclusive_scan(c.occ);
+  c.verts_scan = exclusive_scan(c.verts);
+  c.active = nvox ? c.occ_scan.back() + c.occ.back() : 0;
+  c.total = nvox ? c.verts_scan.back() + c.verts.back() : 0;
+  CUdeviceptr d_occ_scan = dupload(c.occ_scan);
+  c.d_compacted = dalloc<uint32_t>(c.active ? c.active : 1);
+  CUfunction k_cmp = find_kernel(mc, "compactVoxels");
+  {
+    void* a[] = {&c.d_compacted, &d_occ, &d_occ_scan, &nvox};
+    launch(k_cmp, blocks_for(nvox, 1024), 1, 1, 1024, 1, 1, a);
+  }
+  c.compacted = ddownload<uint32_t>(c.d_compacted, c.active);
+  c.d_verts_scan = dupload(c.verts_scan);
+  uint32_t maxv = c.total + 16;
+  CUdeviceptr d_pos = dalloc<float>(4ull * maxv, 0xFF), d_norm = dalloc<float>(4ull * maxv, 0xFF);
+  if (c.active) {
+    CUfunction k = find_kernel(mc, "generateTriangles_lattice_kernel");
+    void* a[] = {&d_pos, &d_norm, &c.d_compacted, &c.d_verts_scan, &g, &shift, &mask, &vs, &gc, &iso,
+                 &c.active, &maxv, const_cast<CUtexObject*>(&T.tri_tex), const_cast<CUtexObject*>(&T.nverts_tex),
+                 &c.total, &d_acc, &d_dyn, &d_zero, &d_zero, &iso1, &iso2, &d_verts, &ou, &od, &oi, &prim, &topo,
+                 &lat, &fixed, &dynamic, &region};
+    launch(k, blocks_for(c.active, 32), 1, 1, 32, 1, 1, a);
+  }
+  w.arr(ddownload<uint8_t>(d_acc, 16 * P));
+  write_classified(w, c);
+  w.arr(ddownload<float>(d_pos, 4ull * c.total));
+  w.arr(ddownload<float>(d_norm, 4ull * c.total));
+  if (d_dyn != d_zero) cuMemFree(d_dyn);
+  cuMemFree(d_acc); cuMemFree(d_zero); cuMemFree(d_verts); cuMemFree(d_occ); cuMemFree(d_occ_scan);
+  cuMemFree(d_pos); cuMemFree(d_norm); cuMemFree(c.d_compacted); cuMemFree(c.d_verts_scan);
+}
+
 // kind 6: timing of the reference's plain marching-cubes kernels on one field.
 // Per repetition classifyVoxel_new, compactVoxels and
 // generateTriangles_lattice_kernel_3 are timed with events on a GB300, launched
@@ -554,6 +635,7 @@ int main(int argc, char** argv) {
       case 4: run_primitive(r, w, mdl); break;
       case 5: run_normalise_four(r, w, gr); break;
       case 6: run_mc_timing(r, w, mc, T); break;
+      case 7: run_retain(r, w, mc, T); break;
       default: die("unknown job kind");
     }
   }

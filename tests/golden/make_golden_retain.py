@@ -1,0 +1,158 @@
+"""Fixtures of the reference's retained primitive editing, from its own kernels.
+
+Run on a machine with a GPU after ``oracle/ref/build_ref.py`` has produced the
+reference fatbins in ``oracle/_ref/``:
+
+    python tests/golden/make_golden_retain.py --out <dir>
+
+Each case folds a seeded sequence of primitive fields into a zeroed
+grid_points accumulator with the reference's classify_copy_Voxel
+(src/MarchingCubes_kernel.cu:158-447) and meshes it with its classifyVoxel,
+compactVoxels and generateTriangles_lattice_kernel (:869-1052, :1594-1608,
+:1865-2200), in the region mode or with one more primitive field (job kind 7
+of oracle/ref/ref_runner.cpp).  Both reference build variants (sm103a SASS and
+the Makefile's compute_89 PTX) must agree bit for bit; the sm103a outputs are
+written to ``golden_retain.npz`` with the inputs.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import make_golden as MG  # noqa: E402
+
+OPS = {"union": 0, "subtract": 1, "intersect": 2}
+
+
+def _grid(n):
+    nx, ny, nz = n
+    z, y, x = np.meshgrid(np.arange(nz, dtype=np.float32), np.arange(ny, dtype=np.float32),
+                          np.arange(nx, dtype=np.float32), indexing="ij")
+    return x, y, z
+
+
+def sphere(n, c, r):
+    x, y, z = _grid(n)
+    return ((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2 - np.float32(r * r)).astype(np.float32)
+
+
+def box(n, c, h):
+    x, y, z = _grid(n)
+    return np.maximum(np.maximum(np.abs(x - c[0]) - h[0], np.abs(y - c[1]) - h[1]),
+                      np.abs(z - c[2]) - h[2]).astype(np.float32)
+
+
+def cases():
+    """(name, n, iso, vs, gc, folds [(op, field)], mode, preview op, preview field)."""
+    rng = np.random.default_rng(0xD4A7)
+    out = []
+    n = (20, 18, 16)
+    a = sphere(n, (7.3, 8.1, 7.6), 4.7)
+    b = box(n, (11.2, 9.4, 8.3), (3.6, 2.9, 4.1))
+    c = sphere(n, (9.5, 6.2, 9.1), 3.1)
+    d = sphere(n, (9.0, 9.0, 8.0), 7.9)
+    e = sphere(n, (12.6, 11.3, 6.4), 3.3)
+    folds = [("union", a), ("union", b), ("subtract", c)]
+    out.append(("region", n, 0.0, (0.5, 0.5, 0.5), (0.0, 0.0, 0.0), folds + [("intersect", d)], 0, "union", None))
+    for op in ("union", "subtract", "intersect"):
+        out.append((f"preview_{op}", n, 0.0, (0.5, 0.5, 0.5), (0.0, 0.0, 0.0), folds, 1, op, e))
+    # integer-valued fields: samples exactly at the isovalue, fractions of 0
+    n = (14, 13, 12)
+    s1 = sphere(n, (6, 6, 5), 4)
+    s2 = sphere(n, (8, 7, 6), 3)
+    s3 = box(n, (5, 5, 5), (3, 2, 4))
+    out.append(("exact_region", n, 0.0, (1.0, 1.0, 1.0), (2.0, -1.5, 0.25),
+                [("union", s1), ("union", s2), ("subtract", s3)], 0, "union", None))
+    out.append(("exact_preview", n, 0.0, (0.37, 1.3, 0.011), (2.0, -1.5, 0.25), [("union", s1), ("union", s3)], 1,
+                "subtract", s2))
+    # random fields (every cube configuration), random ops
+    n = (17, 15, 13)
+    folds = [(["union", "subtract", "intersect"][int(rng.integers(0, 3))], rng.uniform(-1, 1, n[::-1]).astype(np.float32))
+             for _ in range(5)]
+    out.append(("random_region", n, 0.0, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), folds, 0, "union", None))
+    out.append(("random_preview", n, 0.0, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), folds[:3], 1, "intersect",
+                rng.uniform(-1, 1, n[::-1]).astype(np.float32)))
+    return out
+
+
+def build_job():
+    parts, meta = [], []
+    for name, n, iso, vs, gc, folds, mode, pop, pf in cases():
+        b = MG._p("I", 7) + MG._p("3I", *n) + MG._p("f", iso) + MG._p("3f", *vs) + MG._p("3f", *gc)
+        b += MG._p("I", len(folds))
+        for op, f in folds:
+            b += MG._p("I", OPS[op]) + f.astype("<f4").tobytes()
+        b += MG._p("2I", mode, OPS[pop])
+        if mode == 1:
+            b += pf.astype("<f4").tobytes()
+        parts.append(b)
+        meta.append(dict(name=name, n=n, iso=iso, vs=vs, gc=gc, folds=folds, mode=mode, pop=pop, pf=pf))
+    return MG._p("I", MG.MAGIC) + MG._p("I", len(parts)) + b"".join(parts), meta
+
+
+def parse(blob, meta):
+    B = MG.Buf(blob)
+    res = []
+    for c in meta:
+        assert int(B.u32()) == 7
+        P = c["n"][0] * c["n"][1] * c["n"][2]
+        r = dict(meta=c, acc=B.arr(np.int32, 4 * P).reshape(*c["n"][::-1], 4))
+        nvox, act, tot = int(B.u32()), int(B.u32()), int(B.u32())
+        r.update(verts=B.u32(nvox), occ=B.u32(nvox), occ_scan=B.u32(nvox), verts_scan=B.u32(nvox),
+                 compacted=B.u32(act))
+        r["pos"] = B.f32(4 * tot).reshape(-1, 4)
+        r["norm"] = B.f32(4 * tot).reshape(-1, 4)
+        res.append(r)
+    assert B.o == len(blob)
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=HERE)
+    args = ap.parse_args()
+    os.makedirs(args.out, exist_ok=True)
+    exe = MG.build_runner()
+    blob, meta = build_job()
+    job = os.path.join(args.out, "job_retain.bin")
+    with open(job, "wb") as f:
+        f.write(blob)
+    results = {}
+    for var in ("sm103a", "ptx89"):
+        out = os.path.join(args.out, f"out_retain_{var}.bin")
+        subprocess.run([exe, MG.REF_DIR, var, MG.TABLES, job, out], check=True)
+        with open(out, "rb") as f:
+            results[var] = parse(f.read(), meta)
+    bad = []
+    for a, b in zip(results["sm103a"], results["ptx89"]):
+        for k in ("acc", "verts", "occ", "compacted", "pos", "norm"):
+            if a[k].tobytes() != b[k].tobytes():
+                bad.append(f"{a['meta']['name']}: {k}")
+    print("variant differences:", bad or "none")
+    if bad:
+        return 1
+    d = {}
+    for i, r in enumerate(results["sm103a"]):
+        c = r["meta"]
+        pre = f"case{i}/"
+        d[pre + "params"] = np.array([*c["n"], c["iso"], *c["vs"], *c["gc"], c["mode"], OPS[c["pop"]]], np.float64)
+        d[pre + "name"] = np.array(c["name"])
+        d[pre + "fold_ops"] = np.array([OPS[op] for op, _ in c["folds"]], np.int32)
+        d[pre + "fold_fields"] = np.stack([f for _, f in c["folds"]])
+        if c["pf"] is not None:
+            d[pre + "preview_field"] = c["pf"]
+        for k in ("acc", "verts", "occ", "compacted", "pos", "norm"):
+            d[pre + k] = r[k]
+    np.savez_compressed(os.path.join(args.out, "golden_retain.npz"), **d)
+    print("wrote", os.path.join(args.out, "golden_retain.npz"), len(results["sm103a"]), "cases")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -28,3 +28,12 @@ def test_null_arguments_are_rejected_without_a_device():
     assert lib.gcm_ctx_create(0, None) == 1
     assert lib.gcm_ctx_destroy(None) == 0
     assert lib.gcm_mesh_field(None, None, None, 0.0, None, None, 0, None, None) == 1
+
+
+def test_status_constants_match_the_header():
+    import re
+
+    text = open(N.HEADER).read()
+    enum = dict((m.group(1), int(m.group(2))) for m in re.finditer(r"\b(GCM_(?:OK|ERR_[A-Z_]+)) = (\d+)", text))
+    assert enum and all(getattr(N, k) == v for k, v in enum.items())
+    assert {v: k for k, v in enum.items()} == N.STATUS
