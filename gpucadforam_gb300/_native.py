@@ -32,6 +32,14 @@ GCM_ERR_CANCELLED = 9
 GCM_ERR_BUSY = 10
 
 
+class GcmSvlParams(C.Structure):
+    _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("nz", C.c_uint32), ("dx", C.c_float), ("dy", C.c_float),
+                ("dz", C.c_float), ("kind", C.c_uint32), ("period_type", C.c_uint32), ("period", C.c_float),
+                ("period_x", C.c_float), ("period_y", C.c_float), ("period_z", C.c_float), ("lcon", C.c_float),
+                ("lcon_1", C.c_float), ("sinewave_z", C.c_uint32), ("range", C.c_uint32), ("n_coeff", C.c_uint32),
+                ("max_iter", C.c_uint32), ("end_res", C.c_float)]
+
+
 class GcmGrid(C.Structure):
     _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("nz", C.c_uint32), ("voxel_size", C.c_float * 3),
                 ("grid_center", C.c_float * 3)]
@@ -116,6 +124,8 @@ PROTOTYPES = {
     "gcm_mesh_lattice": (I32, [P, C.POINTER(GcmLattice), C.POINTER(GcmGrid), F32, P, P, U64, C.POINTER(GcmCounts), P]),
     "gcm_field_csg": (I32, [P, P, U32, C.POINTER(GcmFrame), U32, U32, U32, P, P]),
     "gcm_csg_retain": (I32, [P, P, P, U32, U32, U32, F32, U32, P]),
+    "gcm_svl_coefficients": (I32, [P, U32, U32, U32, P, P]),
+    "gcm_svl_lattice": (I32, [P, C.POINTER(GcmSvlParams), P, P, P, P, P, P]),
     "gcm_mesh_retained": (I32, [P, P, P, U32, C.POINTER(GcmGrid), F32, P, P, U64, C.POINTER(GcmCounts), P]),
     "gcm_count_retained": (I32, [P, P, P, U32, C.POINTER(GcmGrid), F32, C.POINTER(GcmCounts), P]),
     "gcm_test_lookback_stall": (I32, [P, U32, U32, U64, P, P]),

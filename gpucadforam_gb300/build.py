@@ -18,7 +18,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgcm.so")
 REPO = os.path.dirname(HERE)
 
-SOURCES = ["mc_kernels.cu", "field_kernels.cu", "api.cu", "mesh_noalloc.cu", "obj_writer.cu", "batch.cu", "server.cu"]
+SOURCES = ["mc_kernels.cu", "field_kernels.cu", "api.cu", "mesh_noalloc.cu", "obj_writer.cu", "batch.cu", "server.cu",
+           "svl.cu"]
 HEADERS = ["gcm_device.cuh", "gcm_kernels.h", "mc_tables.h", "gcm_ctx.h", "pool.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",

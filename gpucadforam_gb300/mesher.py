@@ -203,6 +203,34 @@ class Context:
                                           _stream(stream)))
         return out
 
+    # ------------------------------------------------- spatially variant lattices
+    def svl_coefficients(self, unit_type, unit_n=61, rng=2, stream=None):
+        """(2 rng + 1)^3 complex Fourier coefficients of a unit cell, as a
+        complex64 tensor in the reference's order (i fastest)."""
+        w = 2 * rng + 1
+        out = torch.empty((w ** 3, 2), dtype=torch.float32, device=f"cuda:{self.device}")
+        self.check(self.lib.gcm_svl_coefficients(self.h, int(unit_type), int(unit_n), int(rng), _ptr(out),
+                                                 _stream(stream)))
+        return out
+
+    def svl_lattice(self, shape_xyz, coeff, kind="n", period_type=0, period=8.0, periods=(8.0, 8.0, 8.0),
+                    d_period=None, spacing=(1.0, 1.0, 1.0), lcon=0.0, lcon_1=0.0, sinewave_z=False, rng=2,
+                    n_coeff=62, max_iter=500, end_res=0.01, svl=None, want_phase=False, stream=None):
+        """Adds the lattice of the first n_coeff coefficients to svl (created
+        zeroed when None) on the 2x grid; returns (svl[2nz, 2ny, 2nx],
+        iterations per solve, phases or None)."""
+        nx, ny, nz = shape_xyz
+        dev = f"cuda:{self.device}"
+        if svl is None:
+            svl = torch.zeros((2 * nz, 2 * ny, 2 * nx), dtype=torch.float32, device=dev)
+        phase = torch.empty((n_coeff, nz, ny, nx), dtype=torch.float32, device=dev) if want_phase else None
+        p = N.GcmSvlParams(nx, ny, nz, *spacing, ord(kind), period_type, period, *periods, lcon, lcon_1,
+                           1 if sinewave_z else 0, rng, n_coeff, max_iter, end_res)
+        iters = (C.c_uint32 * n_coeff)()
+        self.check(self.lib.gcm_svl_lattice(self.h, C.byref(p), _ptr(d_period), _ptr(coeff), _ptr(svl), _ptr(phase),
+                                            iters, _stream(stream)))
+        return svl, list(iters), phase
+
     # ------------------------------------------------- retained CSG editing
     CSG_OPS = {"union": 0, "subtract": 1, "intersect": 2}
 

@@ -274,6 +274,44 @@ gcm_status gcm_mesh_retained(gcm_ctx* ctx, const gcm_csg_point* d_acc, const flo
 gcm_status gcm_count_retained(gcm_ctx* ctx, const gcm_csg_point* d_acc, const float* d_field, gcm_csg_op op,
                               const gcm_grid* grid, float iso, gcm_counts* h_counts, gcm_stream stream);
 
+/* ------------------------------------------------- spatially variant lattices */
+
+/* The reference's Fourier-grating lattice (SVL, src/main.cu:3578-3711 and
+ * 3904-4030, src/lattice_files/Gratings.cu:100-1050).  Coefficient m of the
+ * (2 range + 1)^3 unit-cell Fourier coefficients has frequencies (i, j, k),
+ * i fastest then j then k, each in [-range, range]. */
+typedef struct gcm_svl_params {
+  uint32_t nx, ny, nz;      /* solve (control) grid, at least 4 per axis; the lattice is 2nx x 2ny x 2nz */
+  float dx, dy, dz;         /* solve grid spacing (the reference uses 1) */
+  uint32_t kind;            /* grating rotation: 'n' none, 'r' round, 'b' bend, 's' sine wave */
+  uint32_t period_type;     /* 0 constant, 1 per axis, 2 per sample from d_period (nx*ny*nz floats) */
+  float period, period_x, period_y, period_z;
+  float lcon, lcon_1;       /* 's': amplitude and frequency of the wave */
+  uint32_t sinewave_z;      /* 's': also the z-axis wave term */
+  uint32_t range;           /* coefficient range (the reference: 2, i.e. 5^3 coefficients) */
+  uint32_t n_coeff;         /* coefficients used, from m = 0 (the reference: 62) */
+  uint32_t max_iter;        /* CG step cap, the reference's iter (500) */
+  float end_res;            /* CG stop when r.d falls to end_res^2 (the reference: 0.01) */
+} gcm_svl_params;
+
+/* Unit cell of TPMS unit_type (gcm_field_unit_cell) on unit_n^3 samples and its
+ * Fourier coefficients c_m = (1/N) sum f e^{-2 pi i (i x/n + j y/n + k z/n)}
+ * (what the reference takes from an R2C cuFFT scaled by 1/N,
+ * src/main.cu:3578-3700), as (re, im) pairs into d_coeff
+ * (2 (2 range + 1)^3 floats). */
+gcm_status gcm_svl_coefficients(gcm_ctx* ctx, uint32_t unit_type, uint32_t unit_n, uint32_t range, float* d_coeff,
+                                gcm_stream stream);
+/* Solves the phase field of each of the first n_coeff coefficients on the
+ * solve grid (finding_phi_kernel right-hand side, GPUCG_lattice conjugate
+ * gradients with the reference's stopping rule) and adds
+ * Re(c_m exp(i phi_m)) sampled on the 2x grid (grating_kernel + svl_kernel)
+ * to d_svl (8 nx ny nz floats, x fastest), m = 0 .. n_coeff - 1 in order.
+ * All solves run together on the device.  d_phase (optional): the solved
+ * phases, n_coeff x nx ny nz floats.  h_iters (optional): each solve's
+ * final step count (the reference's FinalIter).  Syncs. */
+gcm_status gcm_svl_lattice(gcm_ctx* ctx, const gcm_svl_params* params, const float* d_period, const float* d_coeff,
+                           float* d_svl, float* d_phase, uint32_t* h_iters, gcm_stream stream);
+
 /* ---------------------------------------------------------------- batches */
 
 /* Many graded lattices meshed together: one launch evaluates every

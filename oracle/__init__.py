@@ -33,6 +33,14 @@ class OrcPrim(C.Structure):
                 ("center", C.c_float * 3), ("v3", C.c_float * 3), ("p", C.c_float * 6)]
 
 
+class OrcSvl(C.Structure):
+    _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("nz", C.c_uint32), ("dx", C.c_float), ("dy", C.c_float),
+                ("dz", C.c_float), ("kind", C.c_uint32), ("period_type", C.c_uint32), ("period", C.c_float),
+                ("period_x", C.c_float), ("period_y", C.c_float), ("period_z", C.c_float), ("lcon", C.c_float),
+                ("lcon_1", C.c_float), ("sinewave_z", C.c_uint32), ("range", C.c_uint32), ("n_coeff", C.c_uint32),
+                ("max_iter", C.c_uint32), ("end_res", C.c_float)]
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -70,6 +78,11 @@ def lib():
                                         F32P, F32P, C.c_float, C.c_void_p, C.c_void_p, C.c_uint64,
                                         C.POINTER(C.c_uint64)]
         L.orc_mesh_retained.restype = C.c_uint64
+        L.orc_svl_dft.argtypes = [F32P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, F32P]
+        L.orc_svl_rhs.argtypes = [C.POINTER(OrcSvl), C.c_void_p, C.c_uint32, F32P]
+        L.orc_svl_cg.argtypes = [C.POINTER(OrcSvl), F32P, F32P]
+        L.orc_svl_cg.restype = C.c_uint32
+        L.orc_svl_accumulate.argtypes = [C.POINTER(OrcSvl), F32P, F32P, F32P]
         _lib = L
     return _lib
 
@@ -312,4 +325,53 @@ def mesh_retained(acc, field, op, vs, gc, iso=0.0):
     L.orc_mesh_retained(acc.ctypes.data, gp, CSG_OPS.get(op, op), nx, ny, nz, _f3(vs), _f3(gc), iso,
                         pos.ctypes.data, norm.ctypes.data, total, C.byref(act))
     return pos[:total], norm[:total], int(act.value)
+
+
+def svl_params(shape_xyz, kind="n", period_type=0, period=8.0, periods=(8.0, 8.0, 8.0), spacing=(1.0, 1.0, 1.0),
+               lcon=0.0, lcon_1=0.0, sinewave_z=False, rng=2, n_coeff=62, max_iter=500, end_res=0.01):
+    return OrcSvl(*shape_xyz, *spacing, ord(kind), period_type, period, *periods, lcon, lcon_1,
+                  1 if sinewave_z else 0, rng, n_coeff, max_iter, end_res)
+
+
+def svl_dft(field, rng=2):
+    """Unit-cell Fourier coefficients (w^3, 2) float32 in the reference's order."""
+    f = np.ascontiguousarray(field, np.float32)
+    nz, ny, nx = f.shape
+    out = np.zeros(2 * (2 * rng + 1) ** 3, np.float32)
+    lib().orc_svl_dft(f, nx, ny, nz, rng, out)
+    return out.reshape(-1, 2)
+
+
+def svl_rhs(p, m, period=None):
+    out = np.zeros(p.nx * p.ny * p.nz, np.float32)
+    per = None if period is None else np.ascontiguousarray(period, np.float32)
+    lib().orc_svl_rhs(C.byref(p), None if per is None else per.ctypes.data, m, out)
+    return out
+
+
+def svl_cg(p, rhs):
+    x = np.zeros(p.nx * p.ny * p.nz, np.float32)
+    it = lib().orc_svl_cg(C.byref(p), np.ascontiguousarray(rhs, np.float32), x)
+    return x, int(it)
+
+
+def svl_accumulate(p, phases, coef, svl=None):
+    if svl is None:
+        svl = np.zeros(8 * p.nx * p.ny * p.nz, np.float32)
+    svl = np.ascontiguousarray(svl, np.float32).copy()
+    lib().orc_svl_accumulate(C.byref(p), np.ascontiguousarray(phases, np.float32),
+                             np.ascontiguousarray(coef, np.float32).reshape(-1), svl)
+    return svl
+
+
+def svl_lattice(p, coef, period=None):
+    """Whole SVL synthesis: (svl on the 2x grid, phases (n, P), iterations)."""
+    P = p.nx * p.ny * p.nz
+    phases = np.zeros((p.n_coeff, P), np.float32)
+    iters = []
+    for m in range(p.n_coeff):
+        x, it = svl_cg(p, svl_rhs(p, m, period))
+        phases[m] = x
+        iters.append(it)
+    return svl_accumulate(p, phases, coef), phases, iters
 

@@ -814,6 +814,227 @@ uint64_t orc_mesh_retained(const orc_csg_point* acc, const float* g, uint32_t op
   return total;
 }
 
+// ---- spatially variant lattices ---------------------------------------------------
+
+// Coefficient m's frequencies: k outer, j, i inner over [-range, range]
+// (src/main.cu:3615-3690).
+static void svl_freq(uint32_t m, int range, int& i, int& j, int& k) {
+  const int w = 2 * range + 1;
+  i = (int)(m % w) - range;
+  j = (int)((m / w) % w) - range;
+  k = (int)(m / (w * w)) - range;
+}
+
+// Fourier coefficients of the sampled unit cell in double
+// (c = (1/N) sum f e^{-2 pi i (ix/Nx + jy/Ny + kz/Nz)}, the R2C cuFFT scaled by
+// 1/N and completed by symmetry in the reference, src/main.cu:3581-3690).
+void orc_svl_dft(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t range, float* out) {
+  const uint32_t w = 2 * range + 1, nc = w * w * w;
+  const double two_pi = 6.283185307179586476925286766559;
+  for (uint32_t m = 0; m < nc; ++m) {
+    int i, j, k;
+    svl_freq(m, (int)range, i, j, k);
+    double ar = 0, ai = 0;
+    for (uint32_t z = 0; z < nz; ++z)
+      for (uint32_t y = 0; y < ny; ++y)
+        for (uint32_t x = 0; x < nx; ++x) {
+          const double turns = (double)(((int64_t)i * x) % (int64_t)nx) / nx +
+                               (double)(((int64_t)j * y) % (int64_t)ny) / ny +
+                               (double)(((int64_t)k * z) % (int64_t)nz) / nz;
+          const double v = f[x + (uint64_t)nx * (y + (uint64_t)ny * z)];
+          ar += v * std::cos(-two_pi * turns);
+          ai += v * std::sin(-two_pi * turns);
+        }
+    const double N = (double)nx * ny * nz;
+    out[2 * m] = (float)(ar / N);
+    out[2 * m + 1] = (float)(ai / N);
+  }
+}
+
+namespace {
+struct SvlSt {
+  float a1, a2;
+  int n1, n2;
+};
+SvlSt svl_stencil(int x, int n) {
+  if (x == 0) return {-1.0f, -0.5f, x, x + 1};
+  if (x == 1) return {1.0f, -0.5f, x - 1, x + 1};
+  if (x == n - 2) return {0.5f, -1.0f, x - 1, x + 1};
+  if (x == n - 1) return {0.5f, 1.0f, x - 1, x};
+  return {0.5f, -0.5f, x - 1, x + 1};
+}
+inline float svl_k(float per, float v) { return (float)((2.0 * 3.14159265358979323846 / (double)per) * (double)v); }
+}  // namespace
+
+// finding_phi_kernel (src/lattice_files/Gratings.cu:100-417) for coefficient m:
+// the stencil weights by boundary, the grating rotation by kind, the periods by
+// period type; (2 pi / per) * (...) in double; i c - j s and i s + j c with the
+// first product fused (nvcc's contraction in the reference build).
+void orc_svl_rhs(const orc_svl* p, const float* period, uint32_t m, float* out) {
+  const int X = (int)p->nx, Y = (int)p->ny, Z = (int)p->nz;
+  int qi, qj, qk;
+  svl_freq(m, (int)p->range, qi, qj, qk);
+  const float fi = (float)qi, fj = (float)qj;
+  for (int tx = 0; tx < X * Y * Z; ++tx) {
+    const int x = tx % X, y = (tx % (X * Y)) / X, z = tx / (X * Y);
+    const SvlSt sx = svl_stencil(x, X), sy = svl_stencil(y, Y), sz = svl_stencil(z, Z);
+    float t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0, t6 = 0, t7 = 0, t8 = 0;
+    if (p->kind == 'r' || p->kind == 'b') {
+      const float mx = p->kind == 'r' ? (float)(X + 1) / 2.0f : 0.0f, my = p->kind == 'r' ? (float)(Y + 1) / 2.0f : 0.0f;
+      const float yy = ((float)(y + 1) - my) * p->dx;
+      t1 = std::atan2(yy, ((float)(sx.n1 + 1) - mx) * p->dx);
+      t2 = std::atan2(yy, ((float)(sx.n2 + 1) - mx) * p->dx);
+      const float xx = ((float)(x + 1) - mx) * p->dx;
+      t3 = std::atan2(((float)(sy.n1 + 1) - my) * p->dx, xx);
+      t4 = std::atan2(((float)(sy.n2 + 1) - my) * p->dx, xx);
+    } else if (p->kind == 's') {
+      auto wave = [&](float u) { return p->lcon * std::sin((float)(6.28 * (double)p->lcon_1 * (double)u)); };
+      t1 = wave((float)(sx.n1 + 1) * p->dx);
+      t5 = wave((float)(sz.n1 + 1) * p->dz);
+      t2 = wave((float)(sx.n2 + 1) * p->dx);
+      t6 = wave((float)(sz.n2 + 1) * p->dz);
+      t3 = wave((float)(x + 1) * p->dx);
+      t7 = wave((float)(z + 1) * p->dz);
+      t4 = t3;
+      t8 = t7;
+    }
+    float p1, p2, p3, p4, p5, p6;
+    if (p->period_type == 1) {
+      p1 = p2 = p->period_x; p3 = p4 = p->period_y; p5 = p6 = p->period_z;
+    } else if (p->period_type == 2) {
+      p1 = period[sx.n1 + y * X + z * X * Y]; p2 = period[sx.n2 + y * X + z * X * Y];
+      p3 = period[x + sy.n1 * X + z * X * Y]; p4 = period[x + sy.n2 * X + z * X * Y];
+      p5 = period[x + y * X + sz.n1 * X * Y]; p6 = period[x + y * X + sz.n2 * X * Y];
+    } else {
+      p1 = p2 = p3 = p4 = p5 = p6 = p->period;
+    }
+    auto ra = [&](float th) { return std::fma(fi, std::cos(th), -(fj * std::sin(th))); };
+    auto rb = [&](float th) { return std::fma(fi, std::sin(th), fj * std::cos(th)); };
+    const float kx1 = svl_k(p1, ra(t1)), kx2 = svl_k(p2, ra(t2));
+    const float ky1 = svl_k(p3, rb(t3)), ky2 = svl_k(p4, rb(t4));
+    const float kz1 = (float)((2.0 * 3.14159265358979323846 / (double)p5) * (double)qk);
+    const float kz2 = (float)((2.0 * 3.14159265358979323846 / (double)p6) * (double)qk);
+    float phii = ((sx.a1 * kx1 + sx.a2 * kx2) + (sy.a1 * ky1 + sy.a2 * ky2)) + (sz.a1 * kz1 + sz.a2 * kz2);
+    if (p->kind == 's' && p->sinewave_z) {
+      const float fk = (float)qk;
+      const float kz1b = svl_k(p5, std::fma(fj, std::sin(t5), fk * std::cos(t5)));
+      const float kz2b = svl_k(p6, std::fma(fj, std::sin(t6), fk * std::cos(t6)));
+      const float ky1b = svl_k(p3, std::fma(fj, std::cos(t7), -(fk * std::sin(t7))));
+      const float ky2b = svl_k(p4, std::fma(fj, std::cos(t8), -(fk * std::sin(t8))));
+      const float kx1b = (float)((2.0 * 3.14159265358979323846 / (double)p1) * (double)qi);
+      const float kx2b = (float)((2.0 * 3.14159265358979323846 / (double)p2) * (double)qi);
+      phii += ((sx.a1 * kx1b + sx.a2 * kx2b) + (sy.a1 * ky1b + sy.a2 * ky2b)) + (sz.a1 * kz1b + sz.a2 * kz2b);
+    }
+    out[tx] = phii;
+  }
+}
+
+namespace {
+// GPUMatvec_lattice_kernel (Gratings.cu:420-597)
+void svl_axis(const float* dv, int c, int n, long st, float& w, float& t2, float& t3) {
+  if (c == 0) { w = 1.25f; t2 = -dv[st]; t3 = -0.25f * dv[2 * st]; }
+  else if (c == 1) { w = 1.25f; t2 = -dv[-st]; t3 = -0.25f * dv[2 * st]; }
+  else if (c == n - 2) { w = 1.25f; t2 = -0.25f * dv[-2 * st]; t3 = -dv[st]; }
+  else if (c == n - 1) { w = 1.25f; t2 = -0.25f * dv[-2 * st]; t3 = -dv[-st]; }
+  else { w = 0.5f; t2 = -0.25f * dv[-2 * st]; t3 = -0.25f * dv[2 * st]; }
+}
+void svl_matvec(const float* d, float* q, int X, int Y, int Z) {
+  for (int tx = 0; tx < X * Y * Z; ++tx) {
+    const int x = tx % X, y = (tx % (X * Y)) / X, z = tx / (X * Y);
+    float wx, x2, x3, wy, y2, y3, wz, z2, z3;
+    svl_axis(d + tx, x, X, 1, wx, x2, x3);
+    svl_axis(d + tx, y, Y, X, wy, y2, y3);
+    svl_axis(d + tx, z, Z, (long)X * Y, wz, z2, z3);
+    float a = std::fma((wx + wy) + wz, d[tx], x2);
+    a = ((((a + x3) + y2) + y3) + z2) + z3;
+    q[tx] = a;
+  }
+}
+// GPUScalar_lattice_kernel + Reduction_lattice (Gratings.cu:22-75, 600-651):
+// 1024-element blocks summed as a tree, then thread t of one 1024-thread block
+// adds partials t, t + 1024, ... in sequence and the block sums as a tree.
+float svl_tree(float* cc) {
+  for (int s = 512; s > 0; s /= 2)
+    for (int t = 0; t < s; ++t) cc[t] = cc[t] + cc[t + s];
+  return cc[0];
+}
+float svl_dot(const float* a, const float* b, long n) {
+  const long nb = (n + 1023) / 1024;
+  std::vector<float> part(nb);
+  float cc[1024];
+  for (long blk = 0; blk < nb; ++blk) {
+    for (int t = 0; t < 1024; ++t) {
+      const long i = blk * 1024 + t;
+      cc[t] = i < n ? a[i] * b[i] : 0.0f;
+    }
+    part[blk] = svl_tree(cc);
+  }
+  for (int t = 0; t < 1024; ++t) {
+    float c = 0.0f;
+    for (long k = 0; k * 1024 + t < nb; ++k) c += part[k * 1024 + t];
+    cc[t] = c;
+  }
+  return svl_tree(cc);
+}
+// VecSMultAddKernel_lattice: v = a1 * v + a2 * w, the first product fused
+void svl_axpby(float* v, float a1, const float* w, float a2, long n) {
+  for (long i = 0; i < n; ++i) v[i] = std::fma(a1, v[i], a2 * w[i]);
+}
+}  // namespace
+
+// Gratings::GPUCG_lattice (Gratings.cu:875-974) from x = 0: d = r = rhs,
+// delta = r . d, steps while count < max_iter and delta > end_res^2.
+uint32_t orc_svl_cg(const orc_svl* p, const float* rhs, float* x) {
+  const int X = (int)p->nx, Y = (int)p->ny, Z = (int)p->nz;
+  const long n = (long)X * Y * Z;
+  std::vector<float> d(rhs, rhs + n), r(rhs, rhs + n), q(n, 0.0f);
+  std::fill(x, x + n, 0.0f);
+  float delta_new = svl_dot(r.data(), d.data(), n);
+  const float term = p->end_res * p->end_res;
+  uint32_t it = 1;
+  while (it < p->max_iter && delta_new > term) {
+    svl_matvec(d.data(), q.data(), X, Y, Z);
+    const float dq = svl_dot(d.data(), q.data(), n);
+    const float alpha = delta_new / dq;
+    svl_axpby(x, 1.0f, d.data(), alpha, n);
+    svl_axpby(r.data(), 1.0f, q.data(), (float)(-1.0 * (double)alpha), n);
+    const float delta_old = delta_new;
+    delta_new = svl_dot(r.data(), r.data(), n);
+    const float beta = delta_new / delta_old;
+    svl_axpby(d.data(), beta, r.data(), 1.0f, n);
+    ++it;
+  }
+  return it;
+}
+
+// grating_kernel + svl_kernel (Gratings.cu:653-752) for m = 0 .. n_coeff-1: the
+// phase sampled at (u/2 + 1/2, ...) of the coarse grid as a clamped linear
+// texture (weights 0 or 1/2 per axis, x then y then z), exp(i phi), and
+// svl += cos(phi) c.x - sin(phi) c.y, the first product fused.
+void orc_svl_accumulate(const orc_svl* p, const float* phases, const float* coef, float* svl) {
+  const int X = (int)p->nx, Y = (int)p->ny, Z = (int)p->nz;
+  const long P = (long)X * Y * Z;
+  const int FX = 2 * X, FY = 2 * Y, FZ = 2 * Z;
+  for (int w = 0; w < FZ; ++w)
+    for (int v = 0; v < FY; ++v)
+      for (int u = 0; u < FX; ++u) {
+        const int i0 = u >> 1, j0 = v >> 1, k0 = w >> 1;
+        const int i1 = std::min(i0 + (u & 1), X - 1), j1 = std::min(j0 + (v & 1), Y - 1),
+                  k1 = std::min(k0 + (w & 1), Z - 1);
+        const float fx = (u & 1) ? 0.5f : 0.0f, fy = (v & 1) ? 0.5f : 0.0f, fz = (w & 1) ? 0.5f : 0.0f;
+        float& acc = svl[u + (long)FX * (v + (long)FY * w)];
+        for (uint32_t m = 0; m < p->n_coeff; ++m) {
+          const float* xm = phases + m * P;
+          auto at = [&](int i, int j, int k) { return xm[i + (long)X * (j + (long)Y * k)]; };
+          auto lx = [&](int j, int k) { return std::fma(fx, at(i1, j, k) - at(i0, j, k), at(i0, j, k)); };
+          const float c00 = lx(j0, k0), c10 = lx(j1, k0), c01 = lx(j0, k1), c11 = lx(j1, k1);
+          const float c0 = std::fma(fy, c10 - c00, c00), c1 = std::fma(fy, c11 - c01, c01);
+          const float ph = std::fma(fz, c1 - c0, c0);
+          acc = acc + std::fma(std::cos(ph), coef[2 * m], -(std::sin(ph) * coef[2 * m + 1]));
+        }
+      }
+}
+
 // create_lattice_kernel (src/lattice_files/Fft_lattice.cu:11-93): unit cell on
 // [-1, 1]^3 with the literal 3.14; the coordinate is formed in double and
 // rounded to float, and the products with 3.14 are double, rounded to float at

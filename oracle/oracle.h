@@ -99,6 +99,22 @@ uint64_t orc_mesh_retained(const orc_csg_point* acc, const float* field, uint32_
                            uint32_t nz, const float* voxel_size, const float* grid_center, float iso, float* pos,
                            float* norm, uint64_t capacity, uint64_t* active_out);
 
+/* Spatially variant lattice (src/lattice_files/Gratings.cu:100-1050,
+ * src/main.cu:3578-3711, 3904-4030). */
+typedef struct orc_svl {
+  uint32_t nx, ny, nz;
+  float dx, dy, dz;
+  uint32_t kind, period_type;
+  float period, period_x, period_y, period_z, lcon, lcon_1;
+  uint32_t sinewave_z, range, n_coeff, max_iter;
+  float end_res;
+} orc_svl;
+void orc_svl_dft(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t range, float* out);
+void orc_svl_rhs(const orc_svl* p, const float* period, uint32_t m, float* out);
+/* conjugate gradients from x = 0 on A x = rhs; returns the final step count */
+uint32_t orc_svl_cg(const orc_svl* p, const float* rhs, float* x);
+void orc_svl_accumulate(const orc_svl* p, const float* phases, const float* coef, float* svl);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,6 +22,7 @@
 // Use:  ref_runner <fatbin-dir> <variant sm103a|ptx89> <tables.bin> <job.bin> <out.bin>
 #include <cuda.h>
 
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -514,6 +515,130 @@ void run_retain(Reader& r, Writer& w, CUmodule mc, const Tables& T) {
   cuMemFree(d_pos); cuMemFree(d_norm); cuMemFree(c.d_compacted); cuMemFree(c.d_verts_scan);
 }
 
+// kind 8: the reference's spatially variant lattice (src/main.cu:3904-4030):
+// for coefficient m = 0 .. n-1 finding_phi_kernel, GPUCG_lattice (its host loop
+// restated, its kernels launched as it launches them, Gratings.cu:875-974),
+// the phase copied into a 3-D float array read through a linear-filtered
+// texture with the reference's descriptor (Interpolations.cu:79-107),
+// grating_kernel and svl_kernel.  Writes per m the right-hand side, the phase
+// and the step count, then the accumulated lattice.  The coefficients are an
+// input (the reference takes them from cuFFT).  Kind 9: the same run timed
+// (wall clock over the coefficient loop, nothing downloaded but the step counts).
+void run_svl(Reader& r, Writer& w, CUmodule gr, bool timing) {
+  int X = r.get<int32_t>(), Y = r.get<int32_t>(), Z = r.get<int32_t>();
+  float dx = r.get<float>(), dy = r.get<float>(), dz = r.get<float>();
+  char kind = (char)r.get<uint32_t>();
+  int ptype = r.get<int32_t>();
+  float per = r.get<float>(), px = r.get<float>(), py = r.get<float>(), pz = r.get<float>();
+  float lcon = r.get<float>(), lcon1 = r.get<float>();
+  bool sinez = r.get<uint32_t>() != 0;
+  int range = r.get<int32_t>();
+  uint32_t n = r.get<uint32_t>(), max_iter = r.get<uint32_t>();
+  float end_res = r.get<float>();
+  const size_t P = (size_t)X * Y * Z;
+  auto period = r.arr<float>(P);
+  const int wdt = 2 * range + 1;
+  auto coef = r.arr<float>(2 * (size_t)wdt * wdt * wdt);
+  CUdeviceptr d_phi = dalloc<float>(P), d_per = dupload(period), d_d = dalloc<float>(P), d_q = dalloc<float>(P),
+              d_res = dalloc<float>(P), d_coef = dupload(coef), d_svl = dalloc<float>(8 * P),
+              d_ga = dalloc<float>(16 * P);
+  const int nb = (int)(P / 1024) + ((P % 1024) ? 1 : 0);
+  CUdeviceptr d_red = dalloc<float>((size_t)nb);
+  CUDA_ARRAY3D_DESCRIPTOR ad;
+  std::memset(&ad, 0, sizeof(ad));
+  ad.Width = X; ad.Height = Y; ad.Depth = Z; ad.Format = CU_AD_FORMAT_FLOAT; ad.NumChannels = 1;
+  CUarray arr;
+  ck(cuArray3DCreate(&arr, &ad), "cuArray3DCreate");
+  CUDA_RESOURCE_DESC rd;
+  std::memset(&rd, 0, sizeof(rd));
+  rd.resType = CU_RESOURCE_TYPE_ARRAY;
+  rd.res.array.hArray = arr;
+  CUDA_TEXTURE_DESC td;
+  std::memset(&td, 0, sizeof(td));
+  td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = CU_TR_ADDRESS_MODE_WRAP;
+  td.filterMode = CU_TR_FILTER_MODE_LINEAR;
+  CUtexObject tex = 0;
+  ck(cuTexObjectCreate(&tex, &rd, &td, nullptr), "cuTexObjectCreate");
+  CUfunction k_phi = find_kernel(gr, "finding_phi_kernel"), k_mv = find_kernel(gr, "GPUMatvec_lattice_kernel"),
+             k_sc = find_kernel(gr, "GPUScalar_lattice_kernel"), k_red = find_kernel(gr, "Reduction_lattice"),
+             k_ax = find_kernel(gr, "VecSMultAddKernel_lattice"), k_gr = find_kernel(gr, "grating_kernel"),
+             k_svl = find_kernel(gr, "svl_kernel");
+  int Pi = (int)P;
+  const unsigned g1 = blocks_for(P, 1024);
+  auto dot = [&](CUdeviceptr a, CUdeviceptr b) {
+    void* as[] = {&d_red, &a, &b, &Pi};
+    launch(k_sc, g1, 1, 1, 1024, 1, 1, as);
+    void* ar[] = {&d_red, &d_red, const_cast<int*>(&nb)};
+    launch(k_red, 1, 1, 1, 1024, 1, 1, ar);
+    float v = 0;
+    ck(cuMemcpyDtoH(&v, d_red, sizeof(float)), "cuMemcpyDtoH");
+    ck(cuMemsetD8(d_red, 0, sizeof(float) * nb), "cuMemsetD8");
+    return v;
+  };
+  auto axpby = [&](CUdeviceptr v, float a1, CUdeviceptr wv, float a2) {
+    void* a[] = {&v, &a1, &wv, &a2, &X, &Y, &Z};
+    launch(k_ax, g1, 1, 1, 1024, 1, 1, a);
+  };
+  const auto t0 = std::chrono::steady_clock::now();
+  for (uint32_t m = 0; m < n; ++m) {
+    int i = (int)(m % wdt) - range, j = (int)((m / wdt) % wdt) - range, k = (int)(m / (wdt * wdt)) - range;
+    void* ap[] = {&d_phi, &d_per, &X, &Y, &Z, &i, &j, &k, &dx, &dy, &dz, &kind, &ptype, &per, &px, &py, &pz,
+                  &lcon, &lcon1, &sinez};
+    launch(k_phi, g1, 1, 1, 1024, 1, 1, ap);
+    if (!timing) w.arr(ddownload<float>(d_phi, P));
+    // GPUCG_lattice(d_phi, iter, 1, EndRes, FinalIter, FinalRes)
+    ck(cuMemcpyDtoD(d_d, d_phi, 4 * P), "cuMemcpyDtoD");
+    ck(cuMemcpyDtoD(d_res, d_phi, 4 * P), "cuMemcpyDtoD");
+    ck(cuMemsetD8(d_phi, 0, 4 * P), "cuMemsetD8");
+    ck(cuMemsetD8(d_q, 0, 4 * P), "cuMemsetD8");
+    (void)dot(d_res, d_res);
+    float delta_new = dot(d_res, d_d);
+    const float term = end_res * end_res;
+    uint32_t it = 1;
+    while (it < max_iter && delta_new > term) {
+      void* am[] = {&d_d, &d_q, &X, &Y, &Z};
+      launch(k_mv, g1, 1, 1, 1024, 1, 1, am);
+      const float tmp = dot(d_d, d_q);
+      const float alpha = delta_new / tmp;
+      axpby(d_phi, 1.0f, d_d, alpha);
+      axpby(d_res, 1.0f, d_q, (float)(-1.0 * alpha));
+      const float delta_old = delta_new;
+      delta_new = dot(d_res, d_res);
+      const float beta = delta_new / delta_old;
+      axpby(d_d, beta, d_res, 1.0f);
+      ++it;
+    }
+    if (!timing) w.arr(ddownload<float>(d_phi, P));
+    w.put<uint32_t>(it);
+    CUDA_MEMCPY3D cp;
+    std::memset(&cp, 0, sizeof(cp));
+    cp.srcMemoryType = CU_MEMORYTYPE_DEVICE;
+    cp.srcDevice = d_phi;
+    cp.srcPitch = 4 * (size_t)X;
+    cp.srcHeight = Y;
+    cp.dstMemoryType = CU_MEMORYTYPE_ARRAY;
+    cp.dstArray = arr;
+    cp.WidthInBytes = 4 * (size_t)X;
+    cp.Height = Y;
+    cp.Depth = Z;
+    ck(cuMemcpy3D(&cp), "cuMemcpy3D");
+    int X2 = 2 * X, Y2 = 2 * Y, Z2 = 2 * Z;
+    float dx2 = 0.5f * dx, dy2 = 0.5f * dy, dz2 = 0.5f * dz;
+    void* ag[] = {&d_ga, &X2, &Y2, &Z2, &dx2, &dy2, &dz2, &tex};
+    launch(k_gr, (unsigned)((X2 + 15) / 16), (unsigned)((Y2 + 15) / 16), (unsigned)((Z2 + 3) / 4), 16, 16, 4, ag);
+    int mi = (int)m;
+    void* as[] = {&d_svl, &d_ga, &X2, &Y2, &Z2, &mi, &d_coef};
+    launch(k_svl, blocks_for(8 * P, 1024), 1, 1, 1024, 1, 1, as);
+  }
+  ck(cuCtxSynchronize(), "cuCtxSynchronize");
+  const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (timing) w.put<double>(secs);
+  else w.arr(ddownload<float>(d_svl, 8 * P));
+  cuTexObjectDestroy(tex);
+  cuArrayDestroy(arr);
+  for (CUdeviceptr p : {d_phi, d_per, d_d, d_q, d_res, d_coef, d_svl, d_ga, d_red}) cuMemFree(p);
+}
+
 // kind 6: timing of the reference's plain marching-cubes kernels on one field.
 // Per repetition classifyVoxel_new, compactVoxels and
 // generateTriangles_lattice_kernel_3 are timed with events on a GB300, launched
@@ -636,6 +761,8 @@ int main(int argc, char** argv) {
       case 5: run_normalise_four(r, w, gr); break;
       case 6: run_mc_timing(r, w, mc, T); break;
       case 7: run_retain(r, w, mc, T); break;
+      case 8: run_svl(r, w, gr, false); break;
+      case 9: run_svl(r, w, gr, true); break;
       default: die("unknown job kind");
     }
   }
