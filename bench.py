@@ -198,6 +198,118 @@ def cpu_sample(threads, n=N_GRID, planes=256):
             "voxels_per_s": vox / (field_s + mesh_s)}
 
 
+def csg_scene(seed, n_prims=64, n_sub=8):
+    """Config C3: 64 seeded primitives (spheres r in [0.02, 0.15], z-axis capped
+    cylinders, axis boxes with half-extents in [0.02, 0.12]) at uniform centres
+    in [0, 1]^3, min-union with the last 8 subtracted."""
+    rng = np.random.default_rng(seed)
+    prims = []
+    for i in range(n_prims):
+        kind = int(rng.integers(0, 3))
+        c = rng.uniform(0, 1, 3).astype(np.float32)
+        op = 1 if i >= n_prims - n_sub else 0
+        if kind == 0:
+            prims.append(dict(kind=0, op=op, center=c, p=[rng.uniform(0.02, 0.15), 0.0]))
+        elif kind == 1:
+            r, hh = rng.uniform(0.02, 0.12, 2)
+            prims.append(dict(kind=1, op=op, center=c, v3=(0.0, 0.0, 1.0), p=[r, 0.0, 2 * hh]))
+        else:
+            prims.append(dict(kind=2, op=op, center=c, v3=(0.0, 0.0, 0.0), p=list(2 * rng.uniform(0.02, 0.12, 3))))
+    return prims
+
+
+def run_configs(ctx, steps, warmup, cpu=True):
+    """Configs C1 (128^3 uniform gyroid, period 32 voxels, over [0,1]^3) and C3
+    (384^3 CSG scene): field and fused mesh per step from CUDA events, and the
+    oracle on the host cores for the same config (all of C1; a centred slab of
+    64 planes of C3)."""
+    import torch
+
+    import oracle as O
+    from gpucadforam_gb300.mesher import Lattice, make_frame, make_grid, primitives_to_device
+
+    peak, _ = measured_peaks()
+    out = {}
+    threads = os.cpu_count() or 1
+    stream = torch.cuda.current_stream()
+    cs = C.c_void_p(stream.cuda_stream)
+    for name in ("C1", "C3"):
+        if name == "C1":
+            n = 128
+            lat = Lattice.from_numpy(0, (1, 1, 1), np.array([32.0], np.float32), np.zeros(3, np.float32),
+                                     np.zeros(1, np.float32), np.zeros(1, np.uint8), (0.0, 0.0, 0.0))
+            s = ctx.lattice_struct(lat)
+            field_call = lambda f: ctx.lib.gcm_field_lattice(ctx.h, C.byref(s), n, n, n, C.c_void_p(f.data_ptr()), cs)
+            desc = "uniform gyroid 128^3, period 32 voxels, over [0,1]^3, iso 0"
+        else:
+            n = 384
+            prims = csg_scene(SEED + 1)
+            d_prims = primitives_to_device(prims)
+            h = np.float32(1.0 / (n - 1))
+            frame = make_frame((0, 0, 0), (h, h, h))
+            field_call = lambda f: ctx.lib.gcm_field_csg(ctx.h, C.c_void_p(d_prims.data_ptr()), len(prims),
+                                                         C.byref(frame), n, n, n, C.c_void_p(f.data_ptr()), cs)
+            desc = "CSG 384^3: 64 seeded spheres / capped cylinders / boxes in [0,1]^3, 8 subtracted, iso 0"
+        vs = 1.0 / (n - 1)
+        grid = make_grid((n, n, n), (vs, vs, vs))
+        field = torch.empty((n, n, n), dtype=torch.float32, device="cuda")
+        ctx.check(field_call(field))
+        cnt = ctx.count_field(field, 0.0)
+        cap = max(cnt.total_verts, 1)
+        pos = torch.empty((cap, 4), device="cuda")
+        norm = torch.empty((cap, 4), device="cuda")
+        d_counts = torch.zeros(4, dtype=torch.int64, device="cuda")
+
+        def step(ev=None):
+            if ev:
+                ev[0].record(stream)
+            ctx.check(field_call(field))
+            if ev:
+                ev[1].record(stream)
+            ctx.check(ctx.lib.gcm_mesh_field_async(ctx.h, C.c_void_p(field.data_ptr()), C.byref(grid), 0.0,
+                                                   C.c_void_p(pos.data_ptr()), C.c_void_p(norm.data_ptr()), cap,
+                                                   C.c_void_p(d_counts.data_ptr()), cs))
+            if ev:
+                ev[2].record(stream)
+
+        for _ in range(warmup):
+            step()
+        torch.cuda.synchronize()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+        for k in range(steps):
+            step(evs[k])
+        torch.cuda.synchronize()
+        f_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in evs)
+        m_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in evs)
+        vox = (n - 1) ** 3
+        alg = 4 * n ** 3 + 32 * cnt.total_verts
+        r = {"workload": desc, "grid": [n, n, n], "verts": int(cnt.total_verts), "active_voxels": int(cnt.active_voxels),
+             "field_ms": f_ms, "mesh_ms": m_ms, "voxels_per_s": vox / ((f_ms + m_ms) / 1e3),
+             "tris_per_s": cnt.total_verts / 3 / ((f_ms + m_ms) / 1e3), "mesh_GBs": alg / (m_ms / 1e3) / 1e9,
+             "mesh_frac_of_measured": alg / (m_ms / 1e3) / 1e9 / peak}
+        if cpu:
+            t0 = time.perf_counter()
+            if name == "C1":
+                fo = O.lattice_field((n, n, n), 0, (1, 1, 1), np.array([32.0], np.float32), np.zeros(3, np.float32),
+                                     np.zeros(1, np.float32), np.zeros(1, np.uint8), (0.0, 0.0, 0.0), threads=threads)
+                planes = n
+            else:
+                planes = 64
+                z0 = (n - planes) // 2
+                fo = O.csg_field(prims, (n, n, planes), (0, 0, -z0), (h, h, h), threads=threads)
+            t1 = time.perf_counter()
+            tot, _, _, _ = O.mesh_field_omp(fo, (vs, vs, vs), (0, 0, 0), 0.0, 0, threads)
+            t2 = time.perf_counter()
+            O.mesh_field_omp(fo, (vs, vs, vs), (0, 0, 0), 0.0, tot, threads)
+            t3 = time.perf_counter()
+            cvox = (n - 1) ** 2 * (planes - 1)
+            r["cpu_baseline"] = {"value": cvox / ((t1 - t0) + (t3 - t2)), "unit": "voxels/s", "cores": threads,
+                                 "kind": "port", "sample": f"{planes} of {n} sample planes"}
+        out[name] = r
+        del field, pos, norm
+    return out
+
+
 def run_reference(args):
     world, rank, local, pg = dist_setup(args)
     if rank != 0:
@@ -519,6 +631,9 @@ def run_gcm(args):
     served = None
     if not args.no_served and rank == 0:
         served = run_served()
+    configs = None
+    if not args.no_configs:
+        configs = run_configs(ctx, args.steps, args.warmup, cpu=(rank == 0 and not args.no_cpu))
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -539,7 +654,7 @@ def run_gcm(args):
                              "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                              "algorithmic_bytes": mc_bytes, "traffic": traffic},
                 "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
-                "batched": batched, "served": served}
+                "batched": batched, "served": served, "configs": configs}
         print(json.dumps(line))
     ctx.close()
     if pg is not None:
@@ -559,6 +674,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-configs", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
