@@ -24,6 +24,14 @@ __device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); 
 // 1 Schwarz-P, 2 FRD, 3 IWP, 5 Schwarz-D (diamond), after
 // src/lattice_files/Fft_lattice.cu:59-85.
 __device__ __forceinline__ float tpms_sc(uint32_t type, float sX, float cX, float sY, float cY, float sZ, float cZ) {
+  if (type != 2 && type != 3) {
+    // gyroid, Schwarz-P and diamond (every other type) each with its own
+    // arithmetic, chosen without a branch
+    const float gy = fa(fa(fm(sX, cY), fm(sY, cZ)), fm(sZ, cX));
+    const float pp = fa(fa(cX, cY), cZ);
+    const float dd = fs(fm(fm(cX, cY), cZ), fm(fm(sX, sY), sZ));
+    return type == 0 ? gy : (type == 1 ? pp : dd);
+  }
   switch (type) {
     case 0: return fa(fa(fm(sX, cY), fm(sY, cZ)), fm(sZ, cX));
     case 1: return fa(fa(cX, cY), cZ);
@@ -41,12 +49,33 @@ __device__ __forceinline__ float tpms_sc(uint32_t type, float sX, float cX, floa
   }
 }
 
+// sin and cos: for |x| <= pi/4 their Taylor series to degree 11 and 12
+// (truncation below 2e-9 there) in Horner form, else sincosf.
+__device__ __forceinline__ void sincos_small(float x, float* s, float* c) {
+  if (fabsf(x) <= 0.78539818f) {
+    const float x2 = fm(x, x);
+    float ps = __fmaf_rn(x2, -2.5052108e-8f, 2.7557319e-6f);  // -1/11!, 1/9!
+    ps = __fmaf_rn(x2, ps, -1.9841270e-4f);                   // -1/7!
+    ps = __fmaf_rn(x2, ps, 8.3333333e-3f);                    // 1/5!
+    ps = __fmaf_rn(x2, ps, -1.6666667e-1f);                   // -1/3!
+    *s = __fmaf_rn(fm(x, x2), ps, x);
+    float pc = __fmaf_rn(x2, 2.0876757e-9f, -2.7557319e-7f);  // 1/12!, -1/10!
+    pc = __fmaf_rn(x2, pc, 2.4801587e-5f);                    // 1/8!
+    pc = __fmaf_rn(x2, pc, -1.3888889e-3f);                   // -1/6!
+    pc = __fmaf_rn(x2, pc, 4.1666667e-2f);                    // 1/4!
+    pc = __fmaf_rn(x2, pc, -0.5f);                            // -1/2!
+    *c = __fmaf_rn(x2, pc, 1.0f);
+  } else {
+    sincosf(x, s, c);
+  }
+}
+
 // Euler basis rows, ZYX convention of src/Modelling.cu:401-407.
 __device__ __forceinline__ void euler_rows(float ax, float ay, float az, float R[9]) {
   float sx, cx, sy, cy, sz, cz;
-  sincosf(ax, &sx, &cx);
-  sincosf(ay, &sy, &cy);
-  sincosf(az, &sz, &cz);
+  sincos_small(ax, &sx, &cx);
+  sincos_small(ay, &sy, &cy);
+  sincos_small(az, &sz, &cz);
   R[0] = fm(cz, cy);
   R[1] = fs(fm(fm(cz, sy), sx), fm(sz, cx));
   R[2] = fa(fm(fm(cz, sy), cx), fm(sz, sx));
