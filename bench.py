@@ -627,7 +627,7 @@ def run_gcm(args):
 
     batched = None
     if not args.no_batched:
-        batched = run_batched(ctx, args.steps, args.warmup)
+        batched = run_batched(ctx, args.steps, args.warmup, n_inst=args.batch_instances)
     served = None
     if not args.no_served and rank == 0:
         served = run_served()
@@ -675,6 +675,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
+    ap.add_argument("--batch-instances", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
