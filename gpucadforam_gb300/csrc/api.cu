@@ -614,7 +614,9 @@ gcm_status gcm_field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_
   p.ny = ny;
   p.nz = nz;
   p.out = d_out;
-  GCM_CUDA(ctx, gcm::launch_csg(p, row_blocks(ctx, ny, nz), static_cast<cudaStream_t>(stream)));
+  const uint32_t blocks =
+      (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(gcm::csg_tiles(nx, ny, nz), (uint64_t)ctx->sm_count * 4));
+  GCM_CUDA(ctx, gcm::launch_csg(p, blocks, static_cast<cudaStream_t>(stream)));
   count_launch(ctx, 1);
   return GCM_OK;
 }

@@ -495,28 +495,306 @@ __device__ float prim_eval(const PrimPre& P, float X, float Y, float Z) {
 
 }  // namespace
 
-constexpr int kMaxPrimsSmem = 256;
+// ---------------------------------------------------------------------------
+// Per-tile primitive culling.  The scene is evaluated in tiles of 32 x 8 x 4
+// samples.  For each tile every primitive gets an enclosure [L, U] of the
+// values the evaluation above produces at the tile's samples: each step of the
+// evaluation is a correctly rounded IEEE operation that is monotone in each
+// argument (products of two varying terms are taken at the interval corners),
+// so repeating the same operations on interval end points encloses the float
+// results themselves, not just the real-valued function.  A small slack
+// (2^-20 of the magnitudes involved, plus 1e-30) covers double-rounding
+// differences in the two double-precision cone expressions and flush-to-zero.
+//
+// A run of consecutive operations of one kind folds a multiset with min (or
+// max).  Within a union run with running upper bound M = min(hi(f), U_k), a
+// primitive with L_k > M is strictly above the run's result at every sample
+// of the tile, so dropping it changes no result bit (the minimum of the rest
+// is the same value; it is never a zero that could tie with another).  The
+// same holds mirrored for subtract (-g_k) and intersect runs.  The kept
+// primitives are evaluated in their original order.
+// ---------------------------------------------------------------------------
+namespace {
 
-__global__ void __launch_bounds__(256) csg_kernel(CsgParams p) {
-  __shared__ PrimPre s_pre[kMaxPrimsSmem];
-  const uint32_t n = p.n < kMaxPrimsSmem ? p.n : kMaxPrimsSmem;
-  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) prim_setup(p.prims[i], s_pre[i]);
-  __syncthreads();
-  const uint32_t rows = p.ny * p.nz;
-  for (uint32_t row = blockIdx.x; row < rows; row += gridDim.x) {
-    const uint32_t py = row % p.ny, pz = row / p.ny;
-    const float Y = fm(fs((float)py, p.origin[1]), p.spacing[1]);
-    const float Z = fm(fs((float)pz, p.origin[2]), p.spacing[2]);
-    float* out = p.out + (uint64_t)row * p.nx;
-    for (uint32_t px = threadIdx.x; px < p.nx; px += blockDim.x) {
-      const float X = fm(fs((float)px, p.origin[0]), p.spacing[0]);
-      float f = INFINITY;
-      for (uint32_t k = 0; k < n; ++k) {
-        const float g = prim_eval(s_pre[k], X, Y, Z);
-        const uint32_t op = s_pre[k].op;
-        f = op == 1 ? fmaxf(f, -g) : (op == 2 ? fmaxf(f, g) : fminf(f, g));
+struct Iv {
+  float lo, hi;
+};
+
+__device__ __forceinline__ Iv iv_abs(Iv a) {
+  if (a.lo >= 0.0f) return a;
+  if (a.hi <= 0.0f) return {-a.hi, -a.lo};
+  return {0.0f, fmaxf(-a.lo, a.hi)};
+}
+__device__ __forceinline__ Iv iv_sq(Iv a) {
+  const Iv m = iv_abs(a);
+  return {fm(m.lo, m.lo), fm(m.hi, m.hi)};
+}
+__device__ __forceinline__ Iv iv_mul_c(Iv a, float c) {
+  const float u = fm(a.lo, c), v = fm(a.hi, c);
+  return {fminf(u, v), fmaxf(u, v)};
+}
+__device__ __forceinline__ Iv iv_mul(Iv a, Iv b) {
+  const float p0 = fm(a.lo, b.lo), p1 = fm(a.lo, b.hi), p2 = fm(a.hi, b.lo), p3 = fm(a.hi, b.hi);
+  return {fminf(fminf(p0, p1), fminf(p2, p3)), fmaxf(fmaxf(p0, p1), fmaxf(p2, p3))};
+}
+__device__ __forceinline__ Iv iv_add3(Iv a, Iv b, Iv c) { return {fa(fa(a.lo, b.lo), c.lo), fa(fa(a.hi, b.hi), c.hi)}; }
+__device__ __forceinline__ Iv iv_sub(Iv a, Iv b) { return {fs(a.lo, b.hi), fs(a.hi, b.lo)}; }
+__device__ __forceinline__ Iv iv_subc(Iv a, float c) { return {fs(a.lo, c), fs(a.hi, c)}; }
+__device__ __forceinline__ Iv iv_neg(Iv a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ Iv iv_max(Iv a, Iv b) { return {fmaxf(a.lo, b.lo), fmaxf(a.hi, b.hi)}; }
+__device__ __forceinline__ float iv_mag(Iv a) { return fa(fabsf(a.lo), fabsf(a.hi)); }
+// Rotated coordinate: fa(fa(fm(x, r0), fm(y, r1)), fm(z, r2)).
+__device__ __forceinline__ Iv iv_row(const Iv w[3], const float* r) {
+  return iv_add3(iv_mul_c(w[0], r[0]), iv_mul_c(w[1], r[1]), iv_mul_c(w[2], r[2]));
+}
+// h of the cone kernels, in double as there: with g = (float)(b - hgt/2),
+// h = max((g - hgt/2) * 100, -(g + hgt/2) * 100).  The first piece increases
+// with b and the second decreases, so h over [b.lo, b.hi] lies between the
+// maxima of the pieces taken at opposite ends.
+__device__ __forceinline__ Iv cone_h_iv(Iv b, float hgt, float& mag) {
+  const float gl = (float)((double)b.lo - (double)hgt / 2.0), gh = (float)((double)b.hi - (double)hgt / 2.0);
+  const float p1l = (float)(((double)gl - (double)hgt / 2.0) * 100.0);
+  const float p1h = (float)(((double)gh - (double)hgt / 2.0) * 100.0);
+  const float p2l = (float)(((double)gh + (double)hgt / 2.0) * 100.0 * -1.0);
+  const float p2h = (float)(((double)gl + (double)hgt / 2.0) * 100.0 * -1.0);
+  mag = fa(mag, fa(fa(fabsf(p1l), fabsf(p1h)), fa(fabsf(p2l), fabsf(p2h))));
+  return {fmaxf(p1l, p2l), fmaxf(p1h, p2h)};
+}
+
+// Enclosure of prim_eval over the box [blo, bhi] of sample positions, or
+// (-inf, +inf) when any step is not finite.
+__device__ float2 prim_bounds(const PrimPre& P, const float* blo, const float* bhi) {
+  Iv w[3];
+  for (int a = 0; a < 3; ++a) w[a] = {fs(blo[a], P.c[a]), fs(bhi[a], P.c[a])};
+  float mag = fa(fa(iv_mag(w[0]), iv_mag(w[1])), iv_mag(w[2]));
+  Iv g;
+  switch (P.kind) {
+    case 0: {
+      const Iv x2 = iv_sq(w[0]), y2 = iv_sq(w[1]), z2 = iv_sq(w[2]);
+      const Iv d2 = iv_add3(x2, y2, z2);
+      const float r = P.p[0], t = P.p[1] * 0.5f;
+      if (P.flag) {
+        const float A = sqf(fs(r, t)), B = sqf(fa(r, t));
+        g = iv_max(iv_neg(iv_subc(d2, A)), iv_subc(d2, B));
+        mag = fa(mag, fa(A, B));
+      } else {
+        g = iv_subc(d2, sqf(r));
+        mag = fa(mag, sqf(r));
       }
-      out[px] = f;
+      mag = fa(mag, d2.hi);
+      break;
+    }
+    case 1: {
+      const float r = P.p[0], td = P.p[1] * 0.5f, tda = P.p[2] * 0.5f;
+      Iv v[3];
+      for (int a = 0; a < 3; ++a) v[a] = {fs(blo[a], P.end[a]), fs(bhi[a], P.end[a])};
+      const Iv dx = iv_sub(iv_mul(w[1], v[2]), iv_mul(w[2], v[1]));
+      const Iv dy = iv_sub(iv_mul(w[2], v[0]), iv_mul(w[0], v[2]));
+      const Iv dz = iv_sub(iv_mul(w[0], v[1]), iv_mul(w[1], v[0]));
+      const Iv s2 = iv_add3(iv_sq(dx), iv_sq(dy), iv_sq(dz));
+      const Iv e = {__fsqrt_rn(s2.lo), __fsqrt_rn(s2.hi)};
+      const Iv f = {__fdiv_rn(e.lo, P.dis), __fdiv_rn(e.hi, P.dis)};
+      const Iv ga = iv_row(w, P.axis);
+      const Iv fld1 = iv_max(iv_subc(ga, tda), iv_neg({fa(ga.lo, tda), fa(ga.hi, tda)}));
+      Iv fld2;
+      if (P.flag) fld2 = iv_max(iv_subc(f, fa(r, td)), iv_neg(iv_subc(f, fs(r, td))));
+      else fld2 = iv_subc(f, r);
+      g = iv_max(fld1, fld2);
+      mag = fa(fa(fa(mag, s2.hi), iv_mag(f)), fa(fa(iv_mag(ga), fabsf(r)), fa(fabsf(td), fabsf(tda))));
+      mag = fa(mag, fa(fa(iv_mag(v[0]), iv_mag(v[1])), iv_mag(v[2])));
+      break;
+    }
+    default: {
+      const Iv a = iv_row(w, P.R), b = iv_row(w, P.R + 3), cc = iv_row(w, P.R + 6);
+      mag = fa(mag, fa(fa(iv_mag(a), iv_mag(b)), iv_mag(cc)));
+      const Iv aa = iv_abs(a), ab = iv_abs(b), ac = iv_abs(cc);
+      switch (P.kind) {
+        case 2:
+          g = iv_max(iv_max(iv_subc(aa, P.p[0] * 0.5f), iv_subc(ab, P.p[1] * 0.5f)), iv_subc(ac, P.p[2] * 0.5f));
+          break;
+        case 3: {
+          const float wx = P.p[0] * 0.5f, wy = P.p[1] * 0.5f, wz = P.p[2] * 0.5f, th = P.p[3];
+          const Iv f11 = iv_subc(aa, wx), f12 = iv_subc(aa, fs(wx, th));
+          const Iv f21 = iv_subc(ab, wy), f22 = iv_subc(ab, fs(wy, th));
+          g = iv_max(iv_max(iv_max(f11, f21), iv_neg(iv_max(f12, f22))), iv_subc(ac, wz));
+          mag = fa(mag, fa(fa(fabsf(wx), fabsf(wy)), fa(fabsf(wz), fabsf(th))));
+          break;
+        }
+        case 4: {
+          const Iv s2 = {fa(sqf(aa.lo), sqf(ab.lo)), fa(sqf(aa.hi), sqf(ab.hi))};
+          const Iv side = {fs(P.p[0], __fsqrt_rn(s2.hi)), fs(P.p[0], __fsqrt_rn(s2.lo))};
+          const Iv q = iv_sq(side);
+          g = {fa(fs(sqf(ac.lo), sqf(P.p[1])), q.lo), fa(fs(sqf(ac.hi), sqf(P.p[1])), q.hi)};
+          mag = fa(fa(mag, s2.hi), fa(fa(q.hi, sqf(ac.hi)), sqf(P.p[1])));
+          break;
+        }
+        case 5: {
+          const float br = P.p[0], hgt = P.p[1];
+          const float k2 = sqf(__fdiv_rn(hgt, br));
+          const Iv q = {fm(fa(sqf(aa.lo), sqf(ac.lo)), k2), fm(fa(sqf(aa.hi), sqf(ac.hi)), k2)};
+          const Iv d = iv_sq(iv_subc(b, hgt));
+          const Iv f1 = {fs(q.lo, d.hi), fs(q.hi, d.lo)};
+          const Iv hh = cone_h_iv(b, hgt, mag);
+          g = iv_max(f1, hh);
+          mag = fa(mag, fa(fa(q.hi, d.hi), fabsf(k2)));
+          break;
+        }
+        case 6: {
+          const float tr = P.p[0], brr = P.p[1], hgt = P.p[2];
+          const float u1 = fm(__fdiv_rn(fs(hgt, b.lo), hgt), fs(brr, tr));
+          const float u2 = fm(__fdiv_rn(fs(hgt, b.hi), hgt), fs(brr, tr));
+          const Iv rd = {fminf(u1, u2), fmaxf(u1, u2)};
+          const Iv rrf = {fa(rd.lo, tr), fa(rd.hi, tr)};
+          const Iv m = iv_abs(rrf);
+          const Iv A = {fa(sqf(aa.lo), sqf(ac.lo)), fa(sqf(aa.hi), sqf(ac.hi))};
+          const Iv f1 = {(float)((double)A.lo - (double)m.hi * (double)m.hi),
+                         (float)((double)A.hi - (double)m.lo * (double)m.lo)};
+          g = iv_max(f1, cone_h_iv(b, hgt, mag));
+          mag = fa(mag, fa(A.hi, sqf(m.hi)));
+          break;
+        }
+        default: {
+          const float xwb = P.p[0] * 0.5f, xwt = P.p[1] * 0.5f, yh = P.p[2];
+          const float zwb = P.p[3] * 0.5f, zwt = P.p[4] * 0.5f;
+          const float r1 = __fdiv_rn(fs(yh, b.lo), yh), r2 = __fdiv_rn(fs(yh, b.hi), yh);
+          const Iv ratio = {fminf(r1, r2), fmaxf(r1, r2)};
+          const Iv xw0 = iv_mul_c(ratio, fs(xwb, xwt)), zw0 = iv_mul_c(ratio, fs(zwb, zwt));
+          const Iv xw = {fa(xw0.lo, xwt), fa(xw0.hi, xwt)}, zw = {fa(zw0.lo, zwt), fa(zw0.hi, zwt)};
+          const float hy = __fdiv_rn(yh, 2.0f);
+          const Iv f1 = iv_sub(aa, xw);
+          const Iv f2 = iv_subc(iv_abs(iv_subc(b, hy)), hy);
+          const Iv f3 = iv_sub(ac, zw);
+          g = iv_max(iv_max(f1, f2), f3);
+          mag = fa(fa(mag, fa(iv_mag(ratio), iv_mag(xw))), fa(fa(iv_mag(zw), fabsf(hy)), fa(fabsf(xwb), fabsf(zwb))));
+          break;
+        }
+      }
+    }
+  }
+  mag = fa(mag, iv_mag(g));
+  const float slack = fa(fm(mag, 0x1p-20f), 1e-30f);
+  if (!(fabsf(slack) <= FLT_MAX)) return make_float2(-INFINITY, INFINITY);
+  return make_float2(fs(g.lo, slack), fa(g.hi, slack));
+}
+
+__device__ __forceinline__ uint32_t csg_op(uint32_t op) { return op == 1 ? 1u : (op == 2 ? 2u : 0u); }
+
+// Picks the primitives of one tile that can change its samples (in order)
+// from their enclosures; one thread.
+__device__ uint32_t csg_cull(const PrimPre* pre, const float2* lu, uint32_t n, uint8_t* list) {
+  float flo = INFINITY, fhi = INFINITY;  // the running field starts at +inf
+  uint32_t cnt = 0;
+  uint32_t i = 0;
+  while (i < n) {
+    const uint32_t op = csg_op(pre[i].op);
+    uint32_t j = i + 1;
+    while (j < n && csg_op(pre[j].op) == op) ++j;
+    if (op == 0) {  // f = min(f, g)
+      float M = fhi;
+      for (uint32_t k = i; k < j; ++k) M = fminf(M, lu[k].y);
+      float lo = flo;
+      for (uint32_t k = i; k < j; ++k)
+        if (!(lu[k].x > M)) {
+          list[cnt++] = (uint8_t)k;
+          lo = fminf(lo, lu[k].x);
+        }
+      flo = lo;
+      fhi = M;
+    } else if (op == 1) {  // f = max(f, -g)
+      float m = flo;
+      for (uint32_t k = i; k < j; ++k) m = fmaxf(m, -lu[k].y);
+      float hi = fhi;
+      for (uint32_t k = i; k < j; ++k)
+        if (!(-lu[k].x < m)) {
+          list[cnt++] = (uint8_t)k;
+          hi = fmaxf(hi, -lu[k].x);
+        }
+      flo = m;
+      fhi = hi;
+    } else {  // f = max(f, g)
+      float m = flo;
+      for (uint32_t k = i; k < j; ++k) m = fmaxf(m, lu[k].x);
+      float hi = fhi;
+      for (uint32_t k = i; k < j; ++k)
+        if (!(lu[k].y < m)) {
+          list[cnt++] = (uint8_t)k;
+          hi = fmaxf(hi, lu[k].y);
+        }
+      flo = m;
+      fhi = hi;
+    }
+    i = j;
+  }
+  return cnt;
+}
+
+constexpr uint32_t kCsgTx = 32, kCsgTy = 8, kCsgTz = 4;  // 256 threads, 4 samples each along z
+
+__device__ __forceinline__ float csg_coord(uint32_t i, float o, float s) { return fm(fs((float)i, o), s); }
+
+}  // namespace
+
+__global__ void __launch_bounds__(256, 4) csg_kernel(CsgParams p) {
+  extern __shared__ __align__(16) unsigned char csg_smem[];
+  __shared__ uint32_t s_cnt;
+  const uint32_t n = p.n;  // at most 256 (checked by the caller)
+  PrimPre* s_pre = reinterpret_cast<PrimPre*>(csg_smem);
+  float2* s_lu = reinterpret_cast<float2*>(csg_smem + (size_t)n * sizeof(PrimPre));
+  uint8_t* s_list = reinterpret_cast<uint8_t*>(s_lu + n);
+  const uint32_t tid = threadIdx.x;
+  for (uint32_t i = tid; i < n; i += blockDim.x) prim_setup(p.prims[i], s_pre[i]);
+  __syncthreads();
+  const uint32_t tx = (p.nx + kCsgTx - 1) / kCsgTx, ty = (p.ny + kCsgTy - 1) / kCsgTy;
+  const uint32_t tz = (p.nz + kCsgTz - 1) / kCsgTz;
+  const uint64_t tiles = (uint64_t)tx * ty * tz;
+  const uint32_t lx = tid % kCsgTx, ly = tid / kCsgTx;
+  for (uint64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const uint32_t bx = (uint32_t)(t % tx), by = (uint32_t)((t / tx) % ty), bz = (uint32_t)(t / ((uint64_t)tx * ty));
+    const uint32_t x0 = bx * kCsgTx, y0 = by * kCsgTy, z0 = bz * kCsgTz;
+    {
+      const uint32_t i0[3] = {x0, y0, z0};
+      const uint32_t i1[3] = {min(x0 + kCsgTx - 1, p.nx - 1), min(y0 + kCsgTy - 1, p.ny - 1),
+                              min(z0 + kCsgTz - 1, p.nz - 1)};
+      float blo[3], bhi[3];
+      for (int a = 0; a < 3; ++a) {
+        // sample positions are monotone in the index
+        const float u = csg_coord(i0[a], p.origin[a], p.spacing[a]), v = csg_coord(i1[a], p.origin[a], p.spacing[a]);
+        blo[a] = fminf(u, v);
+        bhi[a] = fmaxf(u, v);
+        if (!(fabsf(u) <= FLT_MAX && fabsf(v) <= FLT_MAX)) {
+          blo[a] = -INFINITY;
+          bhi[a] = INFINITY;
+        }
+      }
+      for (uint32_t k = tid; k < n; k += blockDim.x) s_lu[k] = prim_bounds(s_pre[k], blo, bhi);
+    }
+    __syncthreads();
+    if (tid == 0) s_cnt = csg_cull(s_pre, s_lu, n, s_list);
+    __syncthreads();
+    const uint32_t cnt = s_cnt;
+    const uint32_t px = x0 + lx, py = y0 + ly;
+    const float X = csg_coord(px, p.origin[0], p.spacing[0]);
+    const float Y = csg_coord(py, p.origin[1], p.spacing[1]);
+    float Z[kCsgTz], f[kCsgTz];
+#pragma unroll
+    for (uint32_t q = 0; q < kCsgTz; ++q) {
+      Z[q] = csg_coord(z0 + q, p.origin[2], p.spacing[2]);
+      f[q] = INFINITY;
+    }
+    for (uint32_t j = 0; j < cnt; ++j) {
+      const PrimPre& P = s_pre[s_list[j]];
+      const uint32_t op = P.op;
+#pragma unroll
+      for (uint32_t q = 0; q < kCsgTz; ++q) {
+        const float g = prim_eval(P, X, Y, Z[q]);
+        f[q] = op == 1 ? fmaxf(f[q], -g) : (op == 2 ? fmaxf(f[q], g) : fminf(f[q], g));
+      }
+    }
+    if (px < p.nx && py < p.ny) {
+      float* out = p.out + ((uint64_t)z0 * p.ny + py) * p.nx + px;
+#pragma unroll
+      for (uint32_t q = 0; q < kCsgTz; ++q)
+        if (z0 + q < p.nz) out[(uint64_t)q * p.ny * p.nx] = f[q];
     }
   }
 }
@@ -603,8 +881,13 @@ cudaError_t launch_lattice_batch(const BatchLattice* inst, uint32_t n_inst, uint
   return cudaGetLastError();
 }
 
+uint64_t csg_tiles(uint32_t nx, uint32_t ny, uint32_t nz) {
+  return (uint64_t)((nx + kCsgTx - 1) / kCsgTx) * ((ny + kCsgTy - 1) / kCsgTy) * ((nz + kCsgTz - 1) / kCsgTz);
+}
+
 cudaError_t launch_csg(const CsgParams& p, uint32_t blocks, cudaStream_t st) {
-  csg_kernel<<<blocks, 256, 0, st>>>(p);
+  const size_t smem = (size_t)p.n * (sizeof(PrimPre) + sizeof(float2) + 1);
+  csg_kernel<<<blocks, 256, smem, st>>>(p);
   return cudaGetLastError();
 }
 
