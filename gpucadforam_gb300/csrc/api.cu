@@ -614,9 +614,7 @@ gcm_status gcm_field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_
   p.ny = ny;
   p.nz = nz;
   p.out = d_out;
-  const uint32_t blocks =
-      (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(gcm::csg_tiles(nx, ny, nz), (uint64_t)ctx->sm_count * 4));
-  GCM_CUDA(ctx, gcm::launch_csg(p, blocks, static_cast<cudaStream_t>(stream)));
+  GCM_CUDA(ctx, gcm::launch_csg(p, (uint32_t)ctx->sm_count, static_cast<cudaStream_t>(stream)));
   count_launch(ctx, 1);
   return GCM_OK;
 }

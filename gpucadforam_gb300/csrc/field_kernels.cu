@@ -418,77 +418,68 @@ __device__ void prim_setup(const gcm_primitive& q, PrimPre& o) {
   }
 }
 
-// Field of one primitive at scene point (X, Y, Z); src/Modelling.cu kernels.
-__device__ float prim_eval(const PrimPre& P, float X, float Y, float Z) {
-  switch (P.kind) {
-    case 0: {  // implicit_sphere_kernel :314-361
-      const float x = fs(X, P.c[0]), y = fs(Y, P.c[1]), z = fs(Z, P.c[2]);
-      const float r = P.p[0], t = P.p[1] * 0.5f;
-      const float d2 = fa(fa(sqf(x), sqf(y)), sqf(z));
-      if (P.flag) return fmaxf(-fs(d2, sqf(fs(r, t))), fs(d2, sqf(fa(r, t))));
-      return fs(d2, sqf(r));
-    }
-    case 1: {  // distance_from_line_kernel :244-302
-      const float r = P.p[0], td = P.p[1] * 0.5f, tda = P.p[2] * 0.5f;
-      const float w1x = fs(X, P.c[0]), w1y = fs(Y, P.c[1]), w1z = fs(Z, P.c[2]);
-      const float w2x = fs(X, P.end[0]), w2y = fs(Y, P.end[1]), w2z = fs(Z, P.end[2]);
-      const float dx = fs(fm(w1y, w2z), fm(w1z, w2y)), dy = fs(fm(w1z, w2x), fm(w1x, w2z)),
-                  dz = fs(fm(w1x, w2y), fm(w1y, w2x));
-      const float e = __fsqrt_rn(fa(fa(sqf(dx), sqf(dy)), sqf(dz)));
-      const float f = __fdiv_rn(e, P.dis);
-      const float g = fa(fa(fm(fs(X, P.c[0]), P.axis[0]), fm(fs(Y, P.c[1]), P.axis[1])), fm(fs(Z, P.c[2]), P.axis[2]));
-      const float fld1 = fmaxf(fs(g, tda), -fa(g, tda));
-      const float fld2 = P.flag ? fmaxf(fs(f, fa(r, td)), -fs(f, fs(r, td))) : fs(f, r);
-      return fmaxf(fld1, fld2);
-    }
-    default: {
-      const float x = fs(X, P.c[0]), y = fs(Y, P.c[1]), z = fs(Z, P.c[2]);
-      const float a = fa(fa(fm(x, P.R[0]), fm(y, P.R[1])), fm(z, P.R[2]));
-      const float b = fa(fa(fm(x, P.R[3]), fm(y, P.R[4])), fm(z, P.R[5]));
-      const float cc = fa(fa(fm(x, P.R[6]), fm(y, P.R[7])), fm(z, P.R[8]));
-      switch (P.kind) {
-        case 2: {  // implicit_cuboid_kernel :375-421
-          return fmaxf(fmaxf(fs(fabsf(a), P.p[0] * 0.5f), fs(fabsf(b), P.p[1] * 0.5f)), fs(fabsf(cc), P.p[2] * 0.5f));
-        }
-        case 3: {  // implicit_cuboid_shell_kernel :435-487
-          const float wx = P.p[0] * 0.5f, wy = P.p[1] * 0.5f, wz = P.p[2] * 0.5f, th = P.p[3];
-          const float f11 = fs(fabsf(a), wx), f12 = fs(fabsf(a), fs(wx, th));
-          const float f21 = fs(fabsf(b), wy), f22 = fs(fabsf(b), fs(wy, th));
-          return fmaxf(fmaxf(fmaxf(f11, f21), -fmaxf(f12, f22)), fs(fabsf(cc), wz));
-        }
-        case 4: {  // implicit_torus_kernel :569-616
-          const float side = fs(P.p[0], __fsqrt_rn(fa(sqf(a), sqf(b))));
-          return fa(fs(sqf(cc), sqf(P.p[1])), sqf(side));
-        }
-        case 5: {  // implicit_cone_kernel :631-683
-          const float br = P.p[0], hgt = P.p[1];
-          const float k2 = sqf(__fdiv_rn(hgt, br));
-          const float g = (float)((double)b - (double)hgt / 2.0);
-          const float h = (float)fmax(((double)g - (double)hgt / 2.0) * 100.0, ((double)g + (double)hgt / 2.0) * 100.0 * -1.0);
-          const float f1 = fs(fm(fa(sqf(a), sqf(cc)), k2), sqf(fs(b, hgt)));
-          return fmaxf(f1, h);
-        }
-        case 6: {  // implicit_cone_frustum_kernel :698-750
-          const float tr = P.p[0], brr = P.p[1], hgt = P.p[2];
-          const float rd = fm(__fdiv_rn(fs(hgt, b), hgt), fs(brr, tr));
-          const float g = (float)((double)b - (double)hgt / 2.0);
-          const float h = (float)fmax(((double)g - (double)hgt / 2.0) * 100.0, ((double)g + (double)hgt / 2.0) * 100.0 * -1.0);
-          const double rr = (double)fa(rd, tr);
-          const float f1 = (float)((double)fa(sqf(a), sqf(cc)) - rr * rr);
-          return fmaxf(f1, h);
-        }
-        default: {  // 7: implicit_pyramid_frustum_kernel :501-557
-          const float xwb = P.p[0] * 0.5f, xwt = P.p[1] * 0.5f, yh = P.p[2];
-          const float zwb = P.p[3] * 0.5f, zwt = P.p[4] * 0.5f;
-          const float ratio = __fdiv_rn(fs(yh, b), yh);
-          const float xw = fa(fm(ratio, fs(xwb, xwt)), xwt);
-          const float f1 = fs(fabsf(a), xw);
-          const float f2 = fs(fabsf(fs(b, __fdiv_rn(yh, 2.0f))), __fdiv_rn(yh, 2.0f));
-          const float zw = fa(fm(ratio, fs(zwb, zwt)), zwt);
-          const float f3 = fs(fabsf(cc), zw);
-          return fmaxf(fmaxf(f1, f2), f3);
-        }
-      }
+// Field of one primitive of kind K at scene point (X, Y, Z); src/Modelling.cu
+// kernels.  Kinds 7 and above are pyramid frustums.
+template <int K>
+__device__ __forceinline__ float prim_eval_k(const PrimPre& P, float X, float Y, float Z) {
+  if constexpr (K == 0) {  // implicit_sphere_kernel :314-361
+    const float x = fs(X, P.c[0]), y = fs(Y, P.c[1]), z = fs(Z, P.c[2]);
+    const float r = P.p[0], t = P.p[1] * 0.5f;
+    const float d2 = fa(fa(sqf(x), sqf(y)), sqf(z));
+    if (P.flag) return fmaxf(-fs(d2, sqf(fs(r, t))), fs(d2, sqf(fa(r, t))));
+    return fs(d2, sqf(r));
+  } else if constexpr (K == 1) {  // distance_from_line_kernel :244-302
+    const float r = P.p[0], td = P.p[1] * 0.5f, tda = P.p[2] * 0.5f;
+    const float w1x = fs(X, P.c[0]), w1y = fs(Y, P.c[1]), w1z = fs(Z, P.c[2]);
+    const float w2x = fs(X, P.end[0]), w2y = fs(Y, P.end[1]), w2z = fs(Z, P.end[2]);
+    const float dx = fs(fm(w1y, w2z), fm(w1z, w2y)), dy = fs(fm(w1z, w2x), fm(w1x, w2z)),
+                dz = fs(fm(w1x, w2y), fm(w1y, w2x));
+    const float e = __fsqrt_rn(fa(fa(sqf(dx), sqf(dy)), sqf(dz)));
+    const float f = __fdiv_rn(e, P.dis);
+    const float g = fa(fa(fm(fs(X, P.c[0]), P.axis[0]), fm(fs(Y, P.c[1]), P.axis[1])), fm(fs(Z, P.c[2]), P.axis[2]));
+    const float fld1 = fmaxf(fs(g, tda), -fa(g, tda));
+    const float fld2 = P.flag ? fmaxf(fs(f, fa(r, td)), -fs(f, fs(r, td))) : fs(f, r);
+    return fmaxf(fld1, fld2);
+  } else {
+    const float x = fs(X, P.c[0]), y = fs(Y, P.c[1]), z = fs(Z, P.c[2]);
+    const float a = fa(fa(fm(x, P.R[0]), fm(y, P.R[1])), fm(z, P.R[2]));
+    const float b = fa(fa(fm(x, P.R[3]), fm(y, P.R[4])), fm(z, P.R[5]));
+    const float cc = fa(fa(fm(x, P.R[6]), fm(y, P.R[7])), fm(z, P.R[8]));
+    if constexpr (K == 2) {  // implicit_cuboid_kernel :375-421
+      return fmaxf(fmaxf(fs(fabsf(a), P.p[0] * 0.5f), fs(fabsf(b), P.p[1] * 0.5f)), fs(fabsf(cc), P.p[2] * 0.5f));
+    } else if constexpr (K == 3) {  // implicit_cuboid_shell_kernel :435-487
+      const float wx = P.p[0] * 0.5f, wy = P.p[1] * 0.5f, wz = P.p[2] * 0.5f, th = P.p[3];
+      const float f11 = fs(fabsf(a), wx), f12 = fs(fabsf(a), fs(wx, th));
+      const float f21 = fs(fabsf(b), wy), f22 = fs(fabsf(b), fs(wy, th));
+      return fmaxf(fmaxf(fmaxf(f11, f21), -fmaxf(f12, f22)), fs(fabsf(cc), wz));
+    } else if constexpr (K == 4) {  // implicit_torus_kernel :569-616
+      const float side = fs(P.p[0], __fsqrt_rn(fa(sqf(a), sqf(b))));
+      return fa(fs(sqf(cc), sqf(P.p[1])), sqf(side));
+    } else if constexpr (K == 5) {  // implicit_cone_kernel :631-683
+      const float br = P.p[0], hgt = P.p[1];
+      const float k2 = sqf(__fdiv_rn(hgt, br));
+      const float g = (float)((double)b - (double)hgt / 2.0);
+      const float h = (float)fmax(((double)g - (double)hgt / 2.0) * 100.0, ((double)g + (double)hgt / 2.0) * 100.0 * -1.0);
+      const float f1 = fs(fm(fa(sqf(a), sqf(cc)), k2), sqf(fs(b, hgt)));
+      return fmaxf(f1, h);
+    } else if constexpr (K == 6) {  // implicit_cone_frustum_kernel :698-750
+      const float tr = P.p[0], brr = P.p[1], hgt = P.p[2];
+      const float rd = fm(__fdiv_rn(fs(hgt, b), hgt), fs(brr, tr));
+      const float g = (float)((double)b - (double)hgt / 2.0);
+      const float h = (float)fmax(((double)g - (double)hgt / 2.0) * 100.0, ((double)g + (double)hgt / 2.0) * 100.0 * -1.0);
+      const double rr = (double)fa(rd, tr);
+      const float f1 = (float)((double)fa(sqf(a), sqf(cc)) - rr * rr);
+      return fmaxf(f1, h);
+    } else {  // implicit_pyramid_frustum_kernel :501-557
+      const float xwb = P.p[0] * 0.5f, xwt = P.p[1] * 0.5f, yh = P.p[2];
+      const float zwb = P.p[3] * 0.5f, zwt = P.p[4] * 0.5f;
+      const float ratio = __fdiv_rn(fs(yh, b), yh);
+      const float xw = fa(fm(ratio, fs(xwb, xwt)), xwt);
+      const float f1 = fs(fabsf(a), xw);
+      const float f2 = fs(fabsf(fs(b, __fdiv_rn(yh, 2.0f))), __fdiv_rn(yh, 2.0f));
+      const float zw = fa(fm(ratio, fs(zwb, zwt)), zwt);
+      const float f3 = fs(fabsf(cc), zw);
+      return fmaxf(fmaxf(f1, f2), f3);
     }
   }
 }
@@ -679,76 +670,114 @@ __device__ float2 prim_bounds(const PrimPre& P, const float* blo, const float* b
 
 __device__ __forceinline__ uint32_t csg_op(uint32_t op) { return op == 1 ? 1u : (op == 2 ? 2u : 0u); }
 
-// Picks the primitives of one tile that can change its samples (in order)
-// from their enclosures; one thread.
-__device__ uint32_t csg_cull(const PrimPre* pre, const float2* lu, uint32_t n, uint8_t* list) {
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// One warp picks, in order, the primitives that can change the samples of its
+// tile, from their enclosures lu[] (x = L, y = U).  run_end[i] is the end of
+// the run of equal operations starting at i.  Returns the count; the indices
+// go to list[].
+__device__ uint32_t csg_cull_warp(const PrimPre* pre, const uint16_t* run_end, const float2* lu, uint32_t n,
+                                  uint8_t* list, uint32_t lane) {
   float flo = INFINITY, fhi = INFINITY;  // the running field starts at +inf
   uint32_t cnt = 0;
-  uint32_t i = 0;
-  while (i < n) {
-    const uint32_t op = csg_op(pre[i].op);
-    uint32_t j = i + 1;
-    while (j < n && csg_op(pre[j].op) == op) ++j;
-    if (op == 0) {  // f = min(f, g)
-      float M = fhi;
-      for (uint32_t k = i; k < j; ++k) M = fminf(M, lu[k].y);
-      float lo = flo;
-      for (uint32_t k = i; k < j; ++k)
-        if (!(lu[k].x > M)) {
-          list[cnt++] = (uint8_t)k;
-          lo = fminf(lo, lu[k].x);
+  const uint32_t below = (1u << lane) - 1u;
+  for (uint32_t i = 0; i < n;) {
+    const uint32_t j = run_end[i], op = csg_op(pre[i].op);
+    // union: items g_k, threshold M = min(hi f, U_k), drop L_k > M
+    // subtract: items -g_k in [-U_k, -L_k], threshold m = max(lo f, -U_k), drop -L_k < m
+    // intersect: items g_k, threshold m = max(lo f, L_k), drop U_k < m
+    float t = op == 0 ? fhi : flo;
+    for (uint32_t k = i + lane; k < j; k += 32) {
+      const float2 b = lu[k];
+      t = op == 0 ? fminf(t, b.y) : (op == 1 ? fmaxf(t, -b.y) : fmaxf(t, b.x));
+    }
+    t = op == 0 ? warp_min(t) : warp_max(t);
+    float e = op == 0 ? INFINITY : -INFINITY;  // new lower (union) or upper bound of the kept items
+    for (uint32_t base = i; base < j; base += 32) {
+      const uint32_t k = base + lane;
+      bool keep = false;
+      if (k < j) {
+        const float2 b = lu[k];
+        if (op == 0) {
+          keep = !(b.x > t);
+          if (keep) e = fminf(e, b.x);
+        } else if (op == 1) {
+          keep = !(-b.x < t);
+          if (keep) e = fmaxf(e, -b.x);
+        } else {
+          keep = !(b.y < t);
+          if (keep) e = fmaxf(e, b.y);
         }
-      flo = lo;
-      fhi = M;
-    } else if (op == 1) {  // f = max(f, -g)
-      float m = flo;
-      for (uint32_t k = i; k < j; ++k) m = fmaxf(m, -lu[k].y);
-      float hi = fhi;
-      for (uint32_t k = i; k < j; ++k)
-        if (!(-lu[k].x < m)) {
-          list[cnt++] = (uint8_t)k;
-          hi = fmaxf(hi, -lu[k].x);
-        }
-      flo = m;
-      fhi = hi;
-    } else {  // f = max(f, g)
-      float m = flo;
-      for (uint32_t k = i; k < j; ++k) m = fmaxf(m, lu[k].x);
-      float hi = fhi;
-      for (uint32_t k = i; k < j; ++k)
-        if (!(lu[k].y < m)) {
-          list[cnt++] = (uint8_t)k;
-          hi = fmaxf(hi, lu[k].y);
-        }
-      flo = m;
-      fhi = hi;
+      }
+      const uint32_t m = __ballot_sync(0xffffffffu, keep);
+      if (keep) list[cnt + __popc(m & below)] = (uint8_t)k;
+      cnt += __popc(m);
+    }
+    if (op == 0) {
+      flo = fminf(flo, warp_min(e));
+      fhi = t;
+    } else {
+      fhi = fmaxf(fhi, warp_max(e));
+      flo = t;
     }
     i = j;
   }
+  __syncwarp();
   return cnt;
 }
 
-constexpr uint32_t kCsgTx = 32, kCsgTy = 8, kCsgTz = 4;  // 256 threads, 4 samples each along z
+// A warp's tile: 32 samples along x (one per lane) by 4 rows (y) by 8 planes (z).
+constexpr uint32_t kCsgTx = 32, kCsgTy = 4, kCsgTz = 8, kCsgWarps = 8;
 
 __device__ __forceinline__ float csg_coord(uint32_t i, float o, float s) { return fm(fs((float)i, o), s); }
 
+__device__ __forceinline__ float csg_fold(uint32_t op, float f, float g) {
+  return op == 1 ? fmaxf(f, -g) : (op == 2 ? fmaxf(f, g) : fminf(f, g));
+}
+
+template <int K>
+__device__ __forceinline__ void csg_eval8(const PrimPre& P, uint32_t op, float X, float Y, const float (&Z)[kCsgTz],
+                                          float (&f)[kCsgTz]) {
+#pragma unroll
+  for (uint32_t q = 0; q < kCsgTz; ++q) f[q] = csg_fold(op, f[q], prim_eval_k<K>(P, X, Y, Z[q]));
+}
+
 }  // namespace
 
-__global__ void __launch_bounds__(256, 4) csg_kernel(CsgParams p) {
+__global__ void __launch_bounds__(kCsgWarps * 32) csg_kernel(CsgParams p) {
   extern __shared__ __align__(16) unsigned char csg_smem[];
-  __shared__ uint32_t s_cnt;
   const uint32_t n = p.n;  // at most 256 (checked by the caller)
   PrimPre* s_pre = reinterpret_cast<PrimPre*>(csg_smem);
   float2* s_lu = reinterpret_cast<float2*>(csg_smem + (size_t)n * sizeof(PrimPre));
-  uint8_t* s_list = reinterpret_cast<uint8_t*>(s_lu + n);
-  const uint32_t tid = threadIdx.x;
+  uint16_t* s_run = reinterpret_cast<uint16_t*>(s_lu + (size_t)kCsgWarps * n);
+  uint8_t* s_list = reinterpret_cast<uint8_t*>(s_run + n);
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   for (uint32_t i = tid; i < n; i += blockDim.x) prim_setup(p.prims[i], s_pre[i]);
+  if (tid == 0) {
+    for (uint32_t i = 0; i < n;) {
+      uint32_t j = i + 1;
+      while (j < n && csg_op(p.prims[j].op) == csg_op(p.prims[i].op)) ++j;
+      s_run[i] = (uint16_t)j;
+      i = j;
+    }
+  }
   __syncthreads();
+  float2* lu = s_lu + (size_t)warp * n;
+  uint8_t* list = s_list + (size_t)warp * n;
   const uint32_t tx = (p.nx + kCsgTx - 1) / kCsgTx, ty = (p.ny + kCsgTy - 1) / kCsgTy;
   const uint32_t tz = (p.nz + kCsgTz - 1) / kCsgTz;
   const uint64_t tiles = (uint64_t)tx * ty * tz;
-  const uint32_t lx = tid % kCsgTx, ly = tid / kCsgTx;
-  for (uint64_t t = blockIdx.x; t < tiles; t += gridDim.x) {
+  const uint64_t stride = (uint64_t)gridDim.x * kCsgWarps;
+  for (uint64_t t = (uint64_t)blockIdx.x * kCsgWarps + warp; t < tiles; t += stride) {
     const uint32_t bx = (uint32_t)(t % tx), by = (uint32_t)((t / tx) % ty), bz = (uint32_t)(t / ((uint64_t)tx * ty));
     const uint32_t x0 = bx * kCsgTx, y0 = by * kCsgTy, z0 = bz * kCsgTz;
     {
@@ -756,6 +785,7 @@ __global__ void __launch_bounds__(256, 4) csg_kernel(CsgParams p) {
       const uint32_t i1[3] = {min(x0 + kCsgTx - 1, p.nx - 1), min(y0 + kCsgTy - 1, p.ny - 1),
                               min(z0 + kCsgTz - 1, p.nz - 1)};
       float blo[3], bhi[3];
+#pragma unroll
       for (int a = 0; a < 3; ++a) {
         // sample positions are monotone in the index
         const float u = csg_coord(i0[a], p.origin[a], p.spacing[a]), v = csg_coord(i1[a], p.origin[a], p.spacing[a]);
@@ -766,36 +796,46 @@ __global__ void __launch_bounds__(256, 4) csg_kernel(CsgParams p) {
           bhi[a] = INFINITY;
         }
       }
-      for (uint32_t k = tid; k < n; k += blockDim.x) s_lu[k] = prim_bounds(s_pre[k], blo, bhi);
+      for (uint32_t k = lane; k < n; k += 32) lu[k] = prim_bounds(s_pre[k], blo, bhi);
     }
-    __syncthreads();
-    if (tid == 0) s_cnt = csg_cull(s_pre, s_lu, n, s_list);
-    __syncthreads();
-    const uint32_t cnt = s_cnt;
-    const uint32_t px = x0 + lx, py = y0 + ly;
+    __syncwarp();
+    const uint32_t cnt = csg_cull_warp(s_pre, s_run, lu, n, list, lane);
+    const uint32_t px = x0 + lane;
     const float X = csg_coord(px, p.origin[0], p.spacing[0]);
-    const float Y = csg_coord(py, p.origin[1], p.spacing[1]);
-    float Z[kCsgTz], f[kCsgTz];
+    float Z[kCsgTz];
 #pragma unroll
-    for (uint32_t q = 0; q < kCsgTz; ++q) {
-      Z[q] = csg_coord(z0 + q, p.origin[2], p.spacing[2]);
-      f[q] = INFINITY;
-    }
-    for (uint32_t j = 0; j < cnt; ++j) {
-      const PrimPre& P = s_pre[s_list[j]];
-      const uint32_t op = P.op;
+    for (uint32_t q = 0; q < kCsgTz; ++q) Z[q] = csg_coord(z0 + q, p.origin[2], p.spacing[2]);
+#pragma unroll 1
+    for (uint32_t r = 0; r < kCsgTy; ++r) {
+      const uint32_t py = y0 + r;
+      if (py >= p.ny) break;  // warp-uniform
+      const float Y = csg_coord(py, p.origin[1], p.spacing[1]);
+      float f[kCsgTz];
 #pragma unroll
-      for (uint32_t q = 0; q < kCsgTz; ++q) {
-        const float g = prim_eval(P, X, Y, Z[q]);
-        f[q] = op == 1 ? fmaxf(f[q], -g) : (op == 2 ? fmaxf(f[q], g) : fminf(f[q], g));
+      for (uint32_t q = 0; q < kCsgTz; ++q) f[q] = INFINITY;
+      for (uint32_t j = 0; j < cnt; ++j) {
+        const PrimPre& P = s_pre[list[j]];
+        const uint32_t op = P.op;
+        switch (P.kind) {
+          case 0: csg_eval8<0>(P, op, X, Y, Z, f); break;
+          case 1: csg_eval8<1>(P, op, X, Y, Z, f); break;
+          case 2: csg_eval8<2>(P, op, X, Y, Z, f); break;
+          case 3: csg_eval8<3>(P, op, X, Y, Z, f); break;
+          case 4: csg_eval8<4>(P, op, X, Y, Z, f); break;
+          case 5: csg_eval8<5>(P, op, X, Y, Z, f); break;
+          case 6: csg_eval8<6>(P, op, X, Y, Z, f); break;
+          default: csg_eval8<7>(P, op, X, Y, Z, f); break;
+        }
+      }
+      if (px < p.nx) {
+        float* out = p.out + ((uint64_t)z0 * p.ny + py) * p.nx + px;
+        const uint64_t plane = (uint64_t)p.ny * p.nx;
+#pragma unroll
+        for (uint32_t q = 0; q < kCsgTz; ++q)
+          if (z0 + q < p.nz) out[q * plane] = f[q];
       }
     }
-    if (px < p.nx && py < p.ny) {
-      float* out = p.out + ((uint64_t)z0 * p.ny + py) * p.nx + px;
-#pragma unroll
-      for (uint32_t q = 0; q < kCsgTz; ++q)
-        if (z0 + q < p.nz) out[(uint64_t)q * p.ny * p.nx] = f[q];
-    }
+    __syncwarp();  // lu[] and list[] are rewritten for the next tile
   }
 }
 
@@ -882,12 +922,27 @@ cudaError_t launch_lattice_batch(const BatchLattice* inst, uint32_t n_inst, uint
 }
 
 uint64_t csg_tiles(uint32_t nx, uint32_t ny, uint32_t nz) {
-  return (uint64_t)((nx + kCsgTx - 1) / kCsgTx) * ((ny + kCsgTy - 1) / kCsgTy) * ((nz + kCsgTz - 1) / kCsgTz);
+  const uint64_t t = (uint64_t)((nx + kCsgTx - 1) / kCsgTx) * ((ny + kCsgTy - 1) / kCsgTy) * ((nz + kCsgTz - 1) / kCsgTz);
+  return (t + kCsgWarps - 1) / kCsgWarps;  // CTAs that give every warp a tile
 }
 
-cudaError_t launch_csg(const CsgParams& p, uint32_t blocks, cudaStream_t st) {
-  const size_t smem = (size_t)p.n * (sizeof(PrimPre) + sizeof(float2) + 1);
-  csg_kernel<<<blocks, 256, smem, st>>>(p);
+cudaError_t launch_csg(const CsgParams& p, uint32_t sm_count, cudaStream_t st) {
+  const size_t smem = (size_t)p.n * (sizeof(PrimPre) + kCsgWarps * (sizeof(float2) + 1) + sizeof(uint16_t));
+  cudaError_t e = cudaSuccess;
+  if (smem > 48 * 1024) {
+    // up to 256 primitives take 52 KB; every caller sets the same value
+    int dev = 0, optin = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(csg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e != cudaSuccess) return e;
+  }
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, csg_kernel, kCsgWarps * 32, smem);
+  if (e != cudaSuccess) return e;
+  const uint64_t want = csg_tiles(p.nx, p.ny, p.nz), cap = (uint64_t)sm_count * (uint64_t)(per_sm > 0 ? per_sm : 1);
+  const uint32_t blocks = (uint32_t)(want < cap ? want : cap);
+  csg_kernel<<<blocks, kCsgWarps * 32, smem, st>>>(p);
   return cudaGetLastError();
 }
 

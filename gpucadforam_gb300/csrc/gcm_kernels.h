@@ -179,9 +179,10 @@ cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t pr
                            cudaStream_t st);
 cudaError_t launch_lattice_batch(const BatchLattice* inst, uint32_t n_inst, uint64_t total_rows, uint32_t blocks,
                                  cudaStream_t st);
-// CSG field over tiles of 32 x 8 x 4 samples, one tile per CTA at a time.
+// CSG field over tiles of 32 x 4 x 8 samples, one tile per warp at a time;
+// csg_tiles is the CTA count that gives every warp a tile.
 uint64_t csg_tiles(uint32_t nx, uint32_t ny, uint32_t nz);
-cudaError_t launch_csg(const CsgParams& p, uint32_t blocks, cudaStream_t st);
+cudaError_t launch_csg(const CsgParams& p, uint32_t sm_count, cudaStream_t st);
 cudaError_t launch_normalise(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, unsigned int* enc, float lo,
                              float hi, float* label, float* norm_field, uint32_t blocks, cudaStream_t st);
 
