@@ -735,8 +735,8 @@ __device__ uint32_t csg_cull_warp(const PrimPre* pre, const uint16_t* run_end, c
   return cnt;
 }
 
-// A warp's tile: 32 samples along x (one per lane) by 4 rows (y) by 8 planes (z).
-constexpr uint32_t kCsgTx = 32, kCsgTy = 4, kCsgTz = 8, kCsgWarps = 8;
+// A warp's tile: 32 samples along x (one per lane) by 8 rows (y) by 8 planes (z).
+constexpr uint32_t kCsgTx = 32, kCsgTy = 8, kCsgTz = 8, kCsgWarps = 8;
 
 __device__ __forceinline__ float csg_coord(uint32_t i, float o, float s) { return fm(fs((float)i, o), s); }
 
@@ -759,7 +759,8 @@ __global__ void __launch_bounds__(kCsgWarps * 32) csg_kernel(CsgParams p) {
   PrimPre* s_pre = reinterpret_cast<PrimPre*>(csg_smem);
   float2* s_lu = reinterpret_cast<float2*>(csg_smem + (size_t)n * sizeof(PrimPre));
   uint16_t* s_run = reinterpret_cast<uint16_t*>(s_lu + (size_t)kCsgWarps * n);
-  uint8_t* s_list = reinterpret_cast<uint8_t*>(s_run + n);
+  uint8_t* s_perm = reinterpret_cast<uint8_t*>(s_run + n);
+  uint8_t* s_list = s_perm + n;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   for (uint32_t i = tid; i < n; i += blockDim.x) prim_setup(p.prims[i], s_pre[i]);
   if (tid == 0) {
@@ -769,6 +770,11 @@ __global__ void __launch_bounds__(kCsgWarps * 32) csg_kernel(CsgParams p) {
       s_run[i] = (uint16_t)j;
       i = j;
     }
+    // enclosures are computed in kind order, so a warp's lanes mostly share a kind
+    uint32_t c = 0;
+    for (uint32_t kind = 0; kind < 8; ++kind)
+      for (uint32_t i = 0; i < n; ++i)
+        if (min(p.prims[i].kind, 7u) == kind) s_perm[c++] = (uint8_t)i;
   }
   __syncthreads();
   float2* lu = s_lu + (size_t)warp * n;
@@ -796,7 +802,10 @@ __global__ void __launch_bounds__(kCsgWarps * 32) csg_kernel(CsgParams p) {
           bhi[a] = INFINITY;
         }
       }
-      for (uint32_t k = lane; k < n; k += 32) lu[k] = prim_bounds(s_pre[k], blo, bhi);
+      for (uint32_t c = lane; c < n; c += 32) {
+        const uint32_t k = s_perm[c];
+        lu[k] = prim_bounds(s_pre[k], blo, bhi);
+      }
     }
     __syncwarp();
     const uint32_t cnt = csg_cull_warp(s_pre, s_run, lu, n, list, lane);
@@ -927,7 +936,7 @@ uint64_t csg_tiles(uint32_t nx, uint32_t ny, uint32_t nz) {
 }
 
 cudaError_t launch_csg(const CsgParams& p, uint32_t sm_count, cudaStream_t st) {
-  const size_t smem = (size_t)p.n * (sizeof(PrimPre) + kCsgWarps * (sizeof(float2) + 1) + sizeof(uint16_t));
+  const size_t smem = (size_t)p.n * (sizeof(PrimPre) + kCsgWarps * (sizeof(float2) + 1) + sizeof(uint16_t) + 1);
   cudaError_t e = cudaSuccess;
   if (smem > 48 * 1024) {
     // up to 256 primitives take 52 KB; every caller sets the same value
