@@ -122,6 +122,7 @@ PROTOTYPES = {
     "gcm_field_unit_cell": (I32, [P, U32, U32, U32, U32, P, P]),
     "gcm_field_lattice": (I32, [P, C.POINTER(GcmLattice), U32, U32, U32, P, P]),
     "gcm_mesh_lattice": (I32, [P, C.POINTER(GcmLattice), C.POINTER(GcmGrid), F32, P, P, U64, C.POINTER(GcmCounts), P]),
+    "gcm_mesh_lattice_async": (I32, [P, C.POINTER(GcmLattice), C.POINTER(GcmGrid), F32, P, P, U64, P, P]),
     "gcm_field_csg": (I32, [P, P, U32, C.POINTER(GcmFrame), U32, U32, U32, P, P]),
     "gcm_csg_retain": (I32, [P, P, P, U32, U32, U32, F32, U32, P]),
     "gcm_svl_coefficients": (I32, [P, U32, U32, U32, P, P]),

@@ -597,6 +597,27 @@ gcm_status gcm_mesh_lattice(gcm_ctx* ctx, const gcm_lattice* lattice, const gcm_
   return read_counts(ctx, used, h_counts, st);
 }
 
+gcm_status gcm_mesh_lattice_async(gcm_ctx* ctx, const gcm_lattice* lattice, const gcm_grid* grid, float iso,
+                                  float* d_pos, float* d_norm, uint64_t capacity, gcm_counts* d_counts,
+                                  gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_counts || (capacity && (!d_pos || !d_norm)))
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_mesh_lattice_async: NULL counts or outputs");
+  gcm_status s = check_grid(ctx, grid);
+  if (s) return s;
+  LatticeParams p;
+  s = lattice_params(ctx, lattice, grid->nx, grid->ny, grid->nz, &p);
+  if (s) return s;
+  const uint64_t n = (uint64_t)grid->nx * grid->ny * grid->nz;
+  s = ensure_buffer(ctx, &ctx->field_buf, &ctx->field_bytes, n * sizeof(float));
+  if (s) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  s = run_lattice(ctx, p, ctx->field_buf, st);
+  if (s) return s;
+  return mesh_core(ctx, ctx->field_buf, nullptr, grid, iso, 0, 0, kMeshPlain, 0, true, d_pos, d_norm, capacity,
+                   d_counts, st, nullptr);
+}
+
 gcm_status gcm_field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
                          uint32_t nx, uint32_t ny, uint32_t nz, float* d_out, gcm_stream stream) {
   if (!ctx) return GCM_ERR_INVALID_ARGUMENT;

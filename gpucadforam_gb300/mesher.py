@@ -196,6 +196,14 @@ class Context:
         self.check(rc, allow=(N.GCM_ERR_OUTPUT_OVERFLOW,) if allow_overflow or pos is None else ())
         return Counts(c.active_voxels, c.total_verts, c.status)
 
+    def mesh_lattice_async(self, lat, shape_zyx, iso, pos, norm, d_counts, voxel_size=(1, 1, 1),
+                           grid_center=(0, 0, 0), stream=None):
+        """Field + fused mesh, stream-ordered; counts go to d_counts (4 x int64 on the device)."""
+        s = self.lattice_struct(lat)
+        g = make_grid(shape_zyx, voxel_size, grid_center)
+        self.check(self.lib.gcm_mesh_lattice_async(self.h, C.byref(s), C.byref(g), float(iso), _ptr(pos), _ptr(norm),
+                                                   int(pos.shape[0]), _ptr(d_counts), _stream(stream)))
+
     def csg_field(self, prims_dev, n_prims, frame, shape_zyx, stream=None):
         nz, ny, nx = shape_zyx
         out = torch.empty((nz, ny, nx), dtype=torch.float32, device=f"cuda:{self.device}")

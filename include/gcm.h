@@ -203,6 +203,11 @@ gcm_status gcm_field_lattice(gcm_ctx* ctx, const gcm_lattice* lattice, uint32_t 
 /* Field evaluation + marching cubes (iso usually 0). */
 gcm_status gcm_mesh_lattice(gcm_ctx* ctx, const gcm_lattice* lattice, const gcm_grid* grid, float iso, float* d_pos,
                             float* d_norm, uint64_t capacity_verts, gcm_counts* h_counts, gcm_stream stream);
+/* Same, stream-ordered: counts land in d_counts (device), nothing syncs, so
+ * consecutive calls on one stream overlap with copies on other streams. */
+gcm_status gcm_mesh_lattice_async(gcm_ctx* ctx, const gcm_lattice* lattice, const gcm_grid* grid, float iso,
+                                  float* d_pos, float* d_norm, uint64_t capacity_verts, gcm_counts* d_counts,
+                                  gcm_stream stream);
 
 /* Primitive kinds (src/Modelling.cu): 0 sphere / sphere shell (flag) :314-361,
  * 1 capped cylinder / disc (flag) :244-302, 2 cuboid :375-421, 3 cuboid shell

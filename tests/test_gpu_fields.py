@@ -181,3 +181,36 @@ def test_lattice_mesh_equals_oracle_mc_of_device_field(ctx):
                 for dx in (0, 1):
                     nv |= m[dz:dz + n - 1, dy:dy + n - 1, dx:dx + n - 1].reshape(-1)
         assert nv[diff].all()
+
+
+def test_mesh_lattice_async_equals_sync(ctx):
+    """gcm_mesh_lattice_async: same vertices and counts as gcm_mesh_lattice, the
+    counts left on the device, for two calls in flight on one stream into
+    different buffers (the second reuses the context's field buffer)."""
+    from gpucadforam_gb300.mesher import Lattice
+
+    shapes = [(72, 80, 64), (64, 64, 64)]
+    lats = []
+    for k, shape in enumerate(shapes):
+        L = _graded(31 + k, 8, 0)
+        origin = tuple((d - 1) / 2 for d in shape[::-1])
+        lats.append(Lattice.from_numpy(0, L["ctrl"], L["period"], L["euler"], L["thickness"], L["types"], origin))
+    ref = []
+    for lat, shape in zip(lats, shapes):
+        cap = ctx.count_field(ctx.lattice_field(lat, shape), 0.0).total_verts
+        pos = torch.empty((cap, 4), device="cuda")
+        norm = torch.empty((cap, 4), device="cuda")
+        c = ctx.mesh_lattice(lat, shape, 0.0, pos=pos, norm=norm)
+        ref.append((c, host(pos), host(norm)))
+    outs = []
+    for (c, p, _), lat, shape in zip(ref, lats, shapes):
+        pos = torch.full((c.total_verts, 4), float("nan"), device="cuda")
+        norm = torch.full((c.total_verts, 4), float("nan"), device="cuda")
+        d_counts = torch.zeros(4, dtype=torch.int64, device="cuda")
+        ctx.mesh_lattice_async(lat, shape, 0.0, pos, norm, d_counts)
+        outs.append((pos, norm, d_counts))
+    torch.cuda.synchronize()
+    for (c, p, n), (pos, norm, d_counts) in zip(ref, outs):
+        dc = host(d_counts)
+        assert int(dc[0]) == c.active_voxels and int(dc[1]) == c.total_verts and int(dc[2]) == 0
+        assert host(pos).tobytes() == p.tobytes() and host(norm).tobytes() == n.tobytes()
