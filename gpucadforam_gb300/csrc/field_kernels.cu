@@ -226,43 +226,66 @@ __global__ void __launch_bounds__(256) lattice_prep_kernel(LatticeParams p, floa
 constexpr uint32_t kRowCx = 1024;   // control columns staged per row (PARAMS)
 constexpr uint32_t kBlendCx = 128;  // control columns staged per row (BLEND)
 
+// Up to kRowsIter consecutive rows share one staging pass and its two
+// barriers (as many as fit the 5 x kRowCx staging floats).  Control grids
+// wider than kRowCx columns read their columns directly (STAGED false).
+constexpr uint32_t kRowsIter = 4;
+
+template <bool STAGED>
 __global__ void __launch_bounds__(256) lattice_params_kernel(LatticeParams p) {
-  __shared__ float s_a[5][kRowCx];
-  __shared__ uint8_t s_t[kRowCx];
+  __shared__ float s_a[STAGED ? 5 * kRowCx : 1];
+  __shared__ uint8_t s_t[STAGED ? kRowCx : 1];
   const uint32_t c[3] = {p.cx, p.cy, p.cz};
   const uint32_t nc = p.cx * p.cy * p.cz;
   const float* arr[5] = {p.period, p.euler, p.euler ? p.euler + nc : nullptr,
                          p.euler ? p.euler + 2 * nc : nullptr, p.thickness};
-  const bool staged = p.cx <= kRowCx;
   const uint32_t rows = p.ny * p.nz;
-  for (uint32_t row = blockIdx.x; row < rows; row += gridDim.x) {
-    const uint32_t y = row % p.ny, z = row / p.ny;
-    const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
-    if (staged) {
-      __syncthreads();  // the previous row's readers are done
-      for (uint32_t i = threadIdx.x; i < 5 * p.cx; i += blockDim.x) {
-        const uint32_t k = i / p.cx, xc = i % p.cx;
-        s_a[k][xc] = column_yz(arr[k], (int)xc, ky, kz, c);
+  // rows per iteration: the staged columns of all of them fit s_a and s_t
+  const uint32_t R = STAGED ? max(1u, min(kRowsIter, kRowCx / p.cx)) : 1u;
+  const uint32_t groups = (rows + R - 1) / R;
+  for (uint32_t grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+    const uint32_t row0 = grp * R, nr = min(R, rows - row0);
+    if (STAGED) {
+      __syncthreads();  // the previous rows' readers are done
+      const uint32_t per_row = 5 * p.cx;
+      for (uint32_t i = threadIdx.x; i < nr * per_row; i += blockDim.x) {
+        const uint32_t r = i / per_row, k = (i - r * per_row) / p.cx, xc = i % p.cx;
+        const uint32_t row = row0 + r, y = row % p.ny, z = row / p.ny;
+        const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
+        s_a[i] = column_yz(arr[k], (int)xc, ky, kz, c);
       }
-      for (uint32_t xc = threadIdx.x; xc < p.cx; xc += blockDim.x)
-        s_t[xc] = __ldg(p.type + cidx((int)xc, ky.nearest, kz.nearest, c));
+      for (uint32_t i = threadIdx.x; i < nr * p.cx; i += blockDim.x) {
+        const uint32_t r = i / p.cx, xc = i - r * p.cx;
+        const uint32_t row = row0 + r, y = row % p.ny, z = row / p.ny;
+        const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
+        s_t[i] = __ldg(p.type + cidx((int)xc, ky.nearest, kz.nearest, c));
+      }
       __syncthreads();
     }
-    float* out = p.out + (uint64_t)row * p.nx;
-    for (uint32_t x = threadIdx.x; x < p.nx; x += blockDim.x) {
-      const AxisCell kx = locate1(x, c[0], p.scale[0]);
-      float v[5];
+    for (uint32_t r = 0; r < nr; ++r) {
+      const uint32_t row = row0 + r, y = row % p.ny, z = row / p.ny;
+      float* out = p.out + (uint64_t)row * p.nx;
+      for (uint32_t x = threadIdx.x; x < p.nx; x += blockDim.x) {
+        const AxisCell kx = locate1(x, c[0], p.scale[0]);
+        float v[5];
+        uint32_t type;
+        if (STAGED) {
+          const float* sa = s_a + r * 5 * p.cx;
 #pragma unroll
-      for (int k = 0; k < 5; ++k) {
-        const float a0 = staged ? s_a[k][kx.i0] : column_yz(arr[k], kx.i0, ky, kz, c);
-        const float a1 = staged ? s_a[k][kx.i1] : column_yz(arr[k], kx.i1, ky, kz, c);
-        v[k] = lerpf(a0, a1, kx.f);
+          for (int k = 0; k < 5; ++k) v[k] = lerpf(sa[k * p.cx + kx.i0], sa[k * p.cx + kx.i1], kx.f);
+          type = s_t[r * p.cx + kx.nearest];
+        } else {
+          const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
+#pragma unroll
+          for (int k = 0; k < 5; ++k)
+            v[k] = lerpf(column_yz(arr[k], kx.i0, ky, kz, c), column_yz(arr[k], kx.i1, ky, kz, c), kx.f);
+          type = __ldg(p.type + cidx(kx.nearest, ky.nearest, kz.nearest, c));
+        }
+        float R9[9];
+        euler_rows(v[1], v[2], v[3], R9);
+        const float q[3] = {fs((float)x, p.origin[0]), fs((float)y, p.origin[1]), fs((float)z, p.origin[2])};
+        out[x] = lattice_value(type, R9, __fdiv_rn(2.0f, v[0]), q, v[4]);
       }
-      const uint32_t type = staged ? s_t[kx.nearest] : __ldg(p.type + cidx(kx.nearest, ky.nearest, kz.nearest, c));
-      float R[9];
-      euler_rows(v[1], v[2], v[3], R);
-      const float q[3] = {fs((float)x, p.origin[0]), fs((float)y, p.origin[1]), fs((float)z, p.origin[2])};
-      out[x] = lattice_value(type, R, __fdiv_rn(2.0f, v[0]), q, v[4]);
     }
   }
 }
@@ -919,7 +942,8 @@ cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t pr
     q.blend = blend_buf;
     lattice_blend_kernel<<<blocks, 256, 0, st>>>(q);
   } else {
-    lattice_params_kernel<<<blocks, 256, 0, st>>>(p);
+    if (p.cx <= kRowCx) lattice_params_kernel<true><<<blocks, 256, 0, st>>>(p);
+    else lattice_params_kernel<false><<<blocks, 256, 0, st>>>(p);
   }
   return cudaGetLastError();
 }
