@@ -49,6 +49,7 @@ struct gcm_batch {
   gcm::BatchLattice* d_lat = nullptr;
   uint32_t n_params = 0;  // instances evaluated by the batched field kernel
   uint64_t param_rows = 0;
+  bool params_wide = false;  // some instance has more than GCM_BATCH_WARP_CX control columns
   std::vector<uint32_t> blend_ids;  // instances evaluated one by one (blend mode)
   float* blend_buf = nullptr;
   // tiles
@@ -143,8 +144,8 @@ gcm_status launch_fields(gcm_batch* b, cudaStream_t st) {
   if (b->n_params) {
     const uint32_t blocks =
         (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((b->param_rows + 7) / 8, (uint64_t)ctx->sm_count * 8));
-    GCM_CUDA(ctx, launch_lattice_batch(b->d_lat, b->n_params, b->param_rows, blocks, st));
-    count_launch(ctx, 1);
+    GCM_CUDA(ctx, launch_lattice_batch(b->d_lat, b->n_params, b->param_rows, blocks, b->params_wide, st));
+    count_launch(ctx, b->params_wide ? 2 : 1);
   }
   for (uint32_t i : b->blend_ids) {
     const gcm_batch_instance& I = b->inst[i];
@@ -302,6 +303,7 @@ gcm_status gcm_batch_create(gcm_ctx* ctx, const gcm_batch_instance* h_instances,
     p.nx = g.nx;
     p.ny = g.ny;
     p.nz = g.nz;
+    if (L.cx > GCM_BATCH_WARP_CX) b->params_wide = true;
     bl.row_begin = b->param_rows;
     b->param_rows += (uint64_t)g.ny * g.nz;
     lat.push_back(bl);

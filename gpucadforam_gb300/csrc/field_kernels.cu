@@ -348,8 +348,11 @@ __global__ void __launch_bounds__(256) lattice_blend_kernel(LatticeParams p) {
 // instances form one sequence; a warp takes one row (the rows of these grids
 // are short) and stages that row's y/z-interpolated control columns in its own
 // slice of shared memory.  Same arithmetic as lattice_params_kernel.
-constexpr uint32_t kWarpCx = 32;  // control columns staged per warp
+constexpr uint32_t kWarpCx = GCM_BATCH_WARP_CX;  // control columns staged per warp
 
+// STAGED: the rows of instances with at most kWarpCx control columns (the
+// other rows are skipped); the other form takes the wider ones.
+template <bool STAGED>
 __global__ void __launch_bounds__(256) lattice_params_batch_kernel(const BatchLattice* inst, uint32_t n_inst,
                                                                    uint64_t total_rows) {
   __shared__ float s_a[8][5][kWarpCx];
@@ -364,6 +367,7 @@ __global__ void __launch_bounds__(256) lattice_params_batch_kernel(const BatchLa
       else hi = mid - 1;
     }
     const LatticeParams& p = inst[lo].p;
+    if ((p.cx <= kWarpCx) != STAGED) continue;  // warp-uniform
     const uint32_t local = (uint32_t)(row - inst[lo].row_begin);
     const uint32_t y = local % p.ny, z = local / p.ny;
     const uint32_t c[3] = {p.cx, p.cy, p.cz};
@@ -371,9 +375,8 @@ __global__ void __launch_bounds__(256) lattice_params_batch_kernel(const BatchLa
     const float* arr[5] = {p.period, p.euler, p.euler ? p.euler + nc : nullptr,
                            p.euler ? p.euler + 2 * nc : nullptr, p.thickness};
     const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
-    const bool staged = p.cx <= kWarpCx;
     __syncwarp();
-    if (staged) {
+    if (STAGED) {
       for (uint32_t i = lane; i < 5 * p.cx; i += 32) {
         const uint32_t k = i / p.cx, xc = i % p.cx;
         s_a[wib][k][xc] = column_yz(arr[k], (int)xc, ky, kz, c);
@@ -382,21 +385,30 @@ __global__ void __launch_bounds__(256) lattice_params_batch_kernel(const BatchLa
     }
     __syncwarp();
     float* out = p.out + (uint64_t)local * p.nx;
-    for (uint32_t x = lane; x < p.nx; x += 32) {
-      const AxisCell kx = locate1(x, c[0], p.scale[0]);
-      float v[5];
+    if (STAGED) {
+      for (uint32_t x = lane; x < p.nx; x += 32) {
+        const AxisCell kx = locate1(x, c[0], p.scale[0]);
+        float v[5];
 #pragma unroll
-      for (int k = 0; k < 5; ++k) {
-        const float a0 = staged ? s_a[wib][k][kx.i0] : column_yz(arr[k], kx.i0, ky, kz, c);
-        const float a1 = staged ? s_a[wib][k][kx.i1] : column_yz(arr[k], kx.i1, ky, kz, c);
-        v[k] = lerpf(a0, a1, kx.f);
+        for (int k = 0; k < 5; ++k) v[k] = lerpf(s_a[wib][k][kx.i0], s_a[wib][k][kx.i1], kx.f);
+        float R[9];
+        euler_rows(v[1], v[2], v[3], R);
+        const float q[3] = {fs((float)x, p.origin[0]), fs((float)y, p.origin[1]), fs((float)z, p.origin[2])};
+        out[x] = lattice_value(s_t[wib][kx.nearest], R, __fdiv_rn(2.0f, v[0]), q, v[4]);
       }
-      const uint32_t type =
-          staged ? s_t[wib][kx.nearest] : __ldg(p.type + cidx(kx.nearest, ky.nearest, kz.nearest, c));
-      float R[9];
-      euler_rows(v[1], v[2], v[3], R);
-      const float q[3] = {fs((float)x, p.origin[0]), fs((float)y, p.origin[1]), fs((float)z, p.origin[2])};
-      out[x] = lattice_value(type, R, __fdiv_rn(2.0f, v[0]), q, v[4]);
+    } else {
+      for (uint32_t x = lane; x < p.nx; x += 32) {
+        const AxisCell kx = locate1(x, c[0], p.scale[0]);
+        float v[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k)
+          v[k] = lerpf(column_yz(arr[k], kx.i0, ky, kz, c), column_yz(arr[k], kx.i1, ky, kz, c), kx.f);
+        const uint32_t type = __ldg(p.type + cidx(kx.nearest, ky.nearest, kz.nearest, c));
+        float R[9];
+        euler_rows(v[1], v[2], v[3], R);
+        const float q[3] = {fs((float)x, p.origin[0]), fs((float)y, p.origin[1]), fs((float)z, p.origin[2])};
+        out[x] = lattice_value(type, R, __fdiv_rn(2.0f, v[0]), q, v[4]);
+      }
     }
   }
 }
@@ -949,8 +961,13 @@ cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t pr
 }
 
 cudaError_t launch_lattice_batch(const BatchLattice* inst, uint32_t n_inst, uint64_t total_rows, uint32_t blocks,
-                                 cudaStream_t st) {
-  lattice_params_batch_kernel<<<blocks, 256, 0, st>>>(inst, n_inst, total_rows);
+                                 bool any_wide, cudaStream_t st) {
+  lattice_params_batch_kernel<true><<<blocks, 256, 0, st>>>(inst, n_inst, total_rows);
+  if (any_wide) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    lattice_params_batch_kernel<false><<<blocks, 256, 0, st>>>(inst, n_inst, total_rows);
+  }
   return cudaGetLastError();
 }
 

@@ -177,9 +177,12 @@ cudaError_t launch_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t n
                              cudaStream_t st);
 cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t prep_blocks, uint32_t blocks,
                            cudaStream_t st);
+// Batched lattice fields: one launch for instances with at most
+// GCM_BATCH_WARP_CX control columns, a second one only when some are wider.
+#define GCM_BATCH_WARP_CX 32
 cudaError_t launch_lattice_batch(const BatchLattice* inst, uint32_t n_inst, uint64_t total_rows, uint32_t blocks,
-                                 cudaStream_t st);
-// CSG field over tiles of 32 x 4 x 8 samples, one tile per warp at a time;
+                                 bool any_wide, cudaStream_t st);
+// CSG field over tiles of 32 x 8 x 8 samples, one tile per warp at a time;
 // csg_tiles is the CTA count that gives every warp a tile.
 uint64_t csg_tiles(uint32_t nx, uint32_t ny, uint32_t nz);
 cudaError_t launch_csg(const CsgParams& p, uint32_t sm_count, cudaStream_t st);

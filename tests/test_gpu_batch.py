@@ -104,3 +104,37 @@ def test_single_grid_launch_shapes_are_identical(shape_):
     pos, norm, _ = c.mesh_field(f, 0.2)
     assert torch.equal(pos, ref_pos) and torch.equal(norm, ref_norm)
     c.close()
+
+
+def test_batch_with_wide_control_grid(ctx):
+    """An instance whose control grid has more columns than a warp stages
+    (40 > 32) goes through the second, unstaged batched field form; every
+    instance still equals its one-at-a-time mesh."""
+    from gpucadforam_gb300.mesher import Batch, Lattice, random_batch_lattices
+
+    lats, shapes = random_batch_lattices(3, seed=0xD4A + 9, dims=(24, 64))
+    rng = np.random.default_rng(5)
+    cw = (40, 6, 5)
+    nc = int(np.prod(cw))
+    shape = (48, 40, 90)
+    lats.insert(1, Lattice.from_numpy(0, cw, rng.uniform(12, 40, nc).astype(np.float32),
+                                      rng.uniform(-np.pi / 4, np.pi / 4, 3 * nc).astype(np.float32),
+                                      rng.uniform(-0.6, 0.6, nc).astype(np.float32),
+                                      rng.choice(np.array([0, 1, 5], np.uint8), nc),
+                                      origin=((shape[2] - 1) / 2, (shape[1] - 1) / 2, (shape[0] - 1) / 2)))
+    shapes.insert(1, shape)
+    b = Batch(ctx, lats, shapes)
+    try:
+        verts, active, tot = b.count()
+        pos, norm, offsets, counts = b.buffers(tot.total_verts)
+        b.mesh_async(pos, norm, offsets, counts)
+        torch.cuda.synchronize()
+        off = offsets.cpu().numpy().view(np.uint64)
+        for i, (lat, shp) in enumerate(zip(lats, shapes)):
+            ppos, pnorm, pc = _plain(ctx, lat, shp)
+            a, e = int(off[i]), int(off[i + 1])
+            assert e - a == pc.total_verts, i
+            assert pos[a:e].cpu().numpy().tobytes() == ppos.cpu().numpy().tobytes(), i
+            assert norm[a:e].cpu().numpy().tobytes() == pnorm.cpu().numpy().tobytes(), i
+    finally:
+        b.close()
