@@ -788,7 +788,7 @@ __device__ __forceinline__ void csg_eval8(const PrimPre& P, uint32_t op, float X
 
 }  // namespace
 
-__global__ void __launch_bounds__(kCsgWarps * 32) csg_kernel(CsgParams p) {
+__global__ void __launch_bounds__(kCsgWarps * 32, 4) csg_kernel(CsgParams p) {
   extern __shared__ __align__(16) unsigned char csg_smem[];
   const uint32_t n = p.n;  // at most 256 (checked by the caller)
   PrimPre* s_pre = reinterpret_cast<PrimPre*>(csg_smem);
