@@ -177,6 +177,22 @@ __global__ void __launch_bounds__(256) svl_rhs_kernel(SvlGeo g, const float* __r
   }
 }
 
+// floor(n / d) for n < 2^32 as the high half of n * m, m = ceil(2^64 / d):
+// the error term n * (m - 2^64 / d) / 2^64 stays below 2^-32 <= 1/d.
+struct FastDiv {
+  uint64_t m;
+  uint32_t d;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+  FastDiv f;
+  f.d = d;
+  f.m = d > 1 ? ~0ull / d + 1ull : 0ull;
+  return f;
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+  return f.d > 1 ? (uint32_t)__umul64hi((uint64_t)n, f.m) : n;
+}
+
 // A d at one control sample (GPUMatvec_lattice_kernel, Gratings.cu:420-597):
 // per axis the centre weight and the two neighbour terms of the reference's
 // boundary-dependent stencil; A_X = (wx + wy + wz) * d0 + the six neighbour
@@ -189,8 +205,10 @@ __device__ __forceinline__ void axis_terms(const float* dv, int c, int n, int st
   else { w = 0.5f; t2 = -0.25f * dv[-2 * stride]; t3 = -0.25f * dv[2 * stride]; }
 }
 
-__device__ __forceinline__ float matvec_at(const float* __restrict__ d, int tx, int X, int Y, int Z) {
-  const int xi = tx % X, yi = (tx % (X * Y)) / X, zi = tx / (X * Y);
+__device__ __forceinline__ float matvec_at(const float* __restrict__ d, int tx, int X, int Y, int Z, const FastDiv& dx,
+                                           const FastDiv& dxy) {
+  const int row = (int)fdiv((uint32_t)tx, dx), zi = (int)fdiv((uint32_t)tx, dxy);
+  const int xi = tx - row * X, yi = row - zi * Y;
   const float* dv = d + tx;
   float wx, x2, x3, wy, y2, y3, wz, z2, z3;
   axis_terms(dv, xi, X, 1, wx, x2, x3);
@@ -205,15 +223,32 @@ __device__ __forceinline__ float matvec_at(const float* __restrict__ d, int tx, 
 }
 
 // Tree reduction of one value per thread over a 1024-thread block
-// (GPUScalar_lattice_kernel, Gratings.cu:600-651); thread 0 returns the sum.
+// (GPUScalar_lattice_kernel, Gratings.cu:600-651): levels s = 512 .. 1 add
+// element t + s into element t.  The first five levels pair elements 32 w + l
+// across the warp index w (pairs (w, w + 16), (w, w + 8), ... for each lane
+// position l) and the last five pair the lane positions; here each is one
+// warp-shuffle tree, after a transpose through padded shared memory (element
+// 32 w + l at 33 w + l), so the same pairs are added in the same order with
+// two barriers instead of ten.  Thread 0 returns the sum.
+constexpr int kTreeSmem = kBlock + kBlock / 32 + 32;  // floats of shared memory a block_tree takes
+
 __device__ __forceinline__ float block_tree(float v, float* cc) {
-  cc[threadIdx.x] = v;
+  const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+  float* rr = cc + kBlock + kBlock / 32;
+  cc[threadIdx.x + w] = v;
   __syncthreads();
-  for (int s = kBlock / 2; s > 0; s /= 2) {
-    if ((int)threadIdx.x < s) cc[threadIdx.x] = __fadd_rn(cc[threadIdx.x], cc[threadIdx.x + s]);
-    __syncthreads();
+  float a = cc[w + 33u * lane];  // warp w now holds lane position w of every warp
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a = __fadd_rn(a, __shfl_down_sync(0xffffffffu, a, o));
+  if (lane == 0) rr[w] = a;
+  __syncthreads();
+  float sum = 0.0f;
+  if (w == 0) {
+    sum = rr[lane];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum = __fadd_rn(sum, __shfl_down_sync(0xffffffffu, sum, o));
   }
-  return cc[0];
+  return sum;
 }
 
 struct CgState {
@@ -225,15 +260,15 @@ struct CgState {
 // (grid: blocks x solves).
 __global__ void __launch_bounds__(kBlock) svl_matvec_kernel(const float* __restrict__ d, float* __restrict__ q,
                                                             float* __restrict__ part, const CgState* st, int X, int Y,
-                                                            int Z, uint64_t P, uint32_t nblk) {
-  __shared__ float cc[kBlock];
+                                                            int Z, FastDiv dx, FastDiv dxy, uint64_t P, uint32_t nblk) {
+  __shared__ float cc[kTreeSmem];
   const uint32_t b = blockIdx.y;
   if (!st[b].active) return;
   const uint64_t base = (uint64_t)b * P;
   const uint64_t t = (uint64_t)blockIdx.x * kBlock + threadIdx.x;
   float c = 0.0f;
   if (t < P) {
-    const float a = matvec_at(d + base, (int)t, X, Y, Z);
+    const float a = matvec_at(d + base, (int)t, X, Y, Z, dx, dxy);
     q[base + t] = a;
     c = __fmul_rn(d[base + t], a);
   }
@@ -248,7 +283,7 @@ __global__ void __launch_bounds__(kBlock) svl_matvec_kernel(const float* __restr
 // delta_new > term; kind 2 -> delta_new = r . d at the start.
 __global__ void __launch_bounds__(kBlock) svl_reduce_kernel(const float* __restrict__ part, CgState* st, uint32_t nblk,
                                                             uint32_t kind, uint32_t max_iter) {
-  __shared__ float cc[kBlock];
+  __shared__ float cc[kTreeSmem];
   const uint32_t b = blockIdx.x;
   if (kind != 2 && !st[b].active) return;
   const float* pb = part + (uint64_t)b * nblk;
@@ -277,7 +312,7 @@ __global__ void __launch_bounds__(kBlock) svl_update_kernel(float* __restrict__ 
                                                             const float* __restrict__ d, const float* __restrict__ q,
                                                             float* __restrict__ part, const CgState* st, uint64_t P,
                                                             uint32_t nblk) {
-  __shared__ float cc[kBlock];
+  __shared__ float cc[kTreeSmem];
   const uint32_t b = blockIdx.y;
   if (!st[b].active) return;
   const uint64_t base = (uint64_t)b * P;
@@ -328,7 +363,7 @@ __global__ void svl_start_kernel(CgState* st, uint32_t n, uint32_t max_iter, flo
 // Block partials of r . d for the starting delta (every solve).
 __global__ void __launch_bounds__(kBlock) svl_dot_kernel(const float* __restrict__ a, const float* __restrict__ bv,
                                                          float* __restrict__ part, uint64_t P, uint32_t nblk) {
-  __shared__ float cc[kBlock];
+  __shared__ float cc[kTreeSmem];
   const uint32_t b = blockIdx.y;
   const uint64_t base = (uint64_t)b * P;
   const uint64_t t = (uint64_t)blockIdx.x * kBlock + threadIdx.x;
@@ -494,7 +529,8 @@ gcm_status gcm_svl_lattice(gcm_ctx* ctx, const gcm_svl_params* prm, const float*
   if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaMemsetAsync(n_active, 0, sizeof(uint32_t), cap);
-    svl_matvec_kernel<<<gv, kBlock, 0, cap>>>(dd, q, part, cs, g.nx, g.ny, g.nz, P, nblk);
+    svl_matvec_kernel<<<gv, kBlock, 0, cap>>>(dd, q, part, cs, g.nx, g.ny, g.nz, make_fastdiv(p.nx),
+                                              make_fastdiv(p.nx * p.ny), P, nblk);
     svl_reduce_kernel<<<B, kBlock, 0, cap>>>(part, cs, nblk, 0, p.max_iter);
     svl_update_kernel<<<gv, kBlock, 0, cap>>>(x, r, dd, q, part, cs, P, nblk);
     svl_reduce_kernel<<<B, kBlock, 0, cap>>>(part, cs, nblk, 1, p.max_iter);
