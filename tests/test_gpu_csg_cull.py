@@ -136,3 +136,41 @@ def test_cull_c3_scene_full_size(ctx):
     frame = make_frame((0, 0, 0), (h, h, h))
     got = ctx.csg_field(primitives_to_device(prims), len(prims), frame, (n, n, n))
     _same(got, _fold(ctx, prims, frame, (n, n, n)))
+
+
+def test_unbounded_primitives_are_kept(ctx):
+    """Primitives whose enclosure is not finite (a centre at 1e30, a NaN
+    radius, a cone of zero base radius) get (-inf, +inf) and are evaluated
+    everywhere; as union members their NaN or infinite values leave the fold
+    as the full evaluation leaves it."""
+    from gpucadforam_gb300.mesher import make_frame, primitives_to_device
+
+    prims = _scene(21, 20, ops=(0, 1))
+    extra = [dict(kind=0, op=0, center=np.array([1e30, 0.5, 0.5], np.float32), p=[0.1, 0.0]),
+             dict(kind=0, op=0, center=np.array([0.5, 0.5, 0.5], np.float32), p=[float("nan"), 0.0]),
+             dict(kind=5, op=0, center=np.array([0.4, 0.6, 0.5], np.float32), v3=(0.3, 0.2, 0.1), p=[0.0, 0.2])]
+    prims = prims[:7] + extra + prims[7:]
+    shape = (33, 40, 48)
+    frame = make_frame((0.0, 0.0, 0.0), (1.0 / 39,) * 3)
+    got = ctx.csg_field(primitives_to_device(prims), len(prims), frame, shape)
+    _same(got, _fold(ctx, prims, frame, shape))
+
+
+def test_primitive_count_limits(ctx):
+    from gpucadforam_gb300 import _native as N
+    from gpucadforam_gb300.mesher import make_frame, primitives_to_device
+
+    import ctypes as C
+
+    prims = _scene(3, 257)
+    d = primitives_to_device(prims)
+    out = torch.empty((4, 4, 4), device="cuda")
+    frame = make_frame((0.0, 0.0, 0.0), (0.25,) * 3)
+    rc = ctx.lib.gcm_field_csg(ctx.h, C.c_void_p(d.data_ptr()), 257, C.byref(frame), 4, 4, 4,
+                               C.c_void_p(out.data_ptr()), None)
+    assert rc == N.GCM_ERR_NOT_SUPPORTED
+    rc = ctx.lib.gcm_field_csg(ctx.h, C.c_void_p(d.data_ptr()), 0, C.byref(frame), 4, 4, 4,
+                               C.c_void_p(out.data_ptr()), None)
+    assert rc == N.GCM_ERR_INVALID_ARGUMENT
+    got = ctx.csg_field(d, 256, frame, (4, 4, 4))  # the largest scene
+    _same(got, _fold(ctx, prims[:256], frame, (4, 4, 4)))

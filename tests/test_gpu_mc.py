@@ -120,6 +120,39 @@ def test_no_surface(ctx):
     assert cnt.total_verts == 0
 
 
+def test_iso_exactly_everywhere_is_outside(ctx):
+    """f == iso at every sample: no corner is inside (f < iso), no triangles."""
+    f = np.full((9, 10, 11), 0.25, np.float32)
+    cnt = ctx.count_field(dev(f), 0.25)
+    assert cnt.total_verts == 0 and cnt.active_voxels == 0
+
+
+def test_nan_and_inf_samples_vs_oracle(ctx):
+    """NaN samples are outside (f < iso is false); infinities are ordinary
+    corners whose edges interpolate to an end point or to NaN.  Counts and
+    cube indices are exact; positions and normals match bit for bit where
+    they are numbers and are NaN in the same places (NaN payloads differ
+    between the host's and the GPU's arithmetic)."""
+    rng = np.random.default_rng(77)
+    f = rng.standard_normal((23, 29, 37)).astype(np.float32)
+    flat = f.reshape(-1)
+    pick = rng.choice(flat.size, 400, replace=False)
+    flat[pick[:150]] = np.nan
+    flat[pick[150:280]] = np.inf
+    flat[pick[280:]] = -np.inf
+    pos, norm, cnt = ctx.mesh_field(dev(f), 0.0, (0.5, 1.0, 0.25), (0.0, 1.0, 0.0))
+    opos, onorm, oact = O.mesh(f, (0.5, 1.0, 0.25), (0.0, 1.0, 0.0), 0.0)
+    assert cnt.total_verts == len(opos) and cnt.active_voxels == oact
+    _, _, cube = ctx.classify(dev(f), 0.0)
+    _, _, ocube = O.mc_classify(f, 0.0)
+    assert np.array_equal(host(cube).reshape(-1), ocube.reshape(-1))
+    for got, ref in ((host(pos), opos), (host(norm), onorm)):
+        gn, rn = np.isnan(got), np.isnan(ref)
+        assert np.array_equal(gn, rn)
+        assert got[~gn].tobytes() == ref[~rn].tobytes()
+    assert np.isnan(host(pos)).any()  # the case does reach the NaN edges
+
+
 def test_overflow_reports_true_counts(ctx):
     f = _gyroid_c1(64, 16.0)
     full_pos, full_norm, full = ctx.mesh_field(dev(f), 0.0)
