@@ -226,66 +226,99 @@ __global__ void __launch_bounds__(256) lattice_prep_kernel(LatticeParams p, floa
 constexpr uint32_t kRowCx = 1024;   // control columns staged per row (PARAMS)
 constexpr uint32_t kBlendCx = 128;  // control columns staged per row (BLEND)
 
-// Up to kRowsIter consecutive rows share one staging pass and its two
-// barriers (as many as fit the 5 x kRowCx staging floats).  Control grids
-// wider than kRowCx columns read their columns directly (STAGED false).
+// Staged form: groups of R <= kRowsIter consecutive sample rows share one
+// staging pass and its two barriers (as many rows as fit the 5 x kRowCx
+// staging floats).  Each row's control columns are staged by its own share of
+// the threads, the rows' (y, z) step from group to group without a division,
+// and each sample column locates its x cell once for the group's rows.
 constexpr uint32_t kRowsIter = 4;
 
-template <bool STAGED>
-__global__ void __launch_bounds__(256) lattice_params_kernel(LatticeParams p) {
-  __shared__ float s_a[STAGED ? 5 * kRowCx : 1];
-  __shared__ uint8_t s_t[STAGED ? kRowCx : 1];
+__global__ void __launch_bounds__(256) lattice_staged_kernel(LatticeParams p) {
+  __shared__ float s_a[5 * kRowCx];
+  __shared__ uint8_t s_t[kRowCx];
+  __shared__ float2 s_q[kRowsIter];  // per row: y and z phase coordinates
   const uint32_t c[3] = {p.cx, p.cy, p.cz};
   const uint32_t nc = p.cx * p.cy * p.cz;
   const float* arr[5] = {p.period, p.euler, p.euler ? p.euler + nc : nullptr,
                          p.euler ? p.euler + 2 * nc : nullptr, p.thickness};
   const uint32_t rows = p.ny * p.nz;
-  // rows per iteration: the staged columns of all of them fit s_a and s_t
-  const uint32_t R = STAGED ? max(1u, min(kRowsIter, kRowCx / p.cx)) : 1u;
+  const uint32_t R = max(1u, min(kRowsIter, kRowCx / p.cx));
   const uint32_t groups = (rows + R - 1) / R;
+  const uint32_t tpr = blockDim.x / R;  // threads staging one row
+  const uint32_t my_r = threadIdx.x / tpr, my_j = threadIdx.x - my_r * tpr;
+  // (y, z) of the first row of this CTA's group and the step between its groups
+  const uint32_t first = blockIdx.x * R, step = gridDim.x * R;
+  uint32_t y0 = first % p.ny, z0 = first / p.ny;
+  const uint32_t sdy = step % p.ny, sdz = step / p.ny;
   for (uint32_t grp = blockIdx.x; grp < groups; grp += gridDim.x) {
     const uint32_t row0 = grp * R, nr = min(R, rows - row0);
-    if (STAGED) {
-      __syncthreads();  // the previous rows' readers are done
-      const uint32_t per_row = 5 * p.cx;
-      for (uint32_t i = threadIdx.x; i < nr * per_row; i += blockDim.x) {
-        const uint32_t r = i / per_row, k = (i - r * per_row) / p.cx, xc = i % p.cx;
-        const uint32_t row = row0 + r, y = row % p.ny, z = row / p.ny;
-        const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
-        s_a[i] = column_yz(arr[k], (int)xc, ky, kz, c);
-      }
-      for (uint32_t i = threadIdx.x; i < nr * p.cx; i += blockDim.x) {
-        const uint32_t r = i / p.cx, xc = i - r * p.cx;
-        const uint32_t row = row0 + r, y = row % p.ny, z = row / p.ny;
-        const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
-        s_t[i] = __ldg(p.type + cidx((int)xc, ky.nearest, kz.nearest, c));
-      }
-      __syncthreads();
-    }
-    for (uint32_t r = 0; r < nr; ++r) {
-      const uint32_t row = row0 + r, y = row % p.ny, z = row / p.ny;
-      float* out = p.out + (uint64_t)row * p.nx;
-      for (uint32_t x = threadIdx.x; x < p.nx; x += blockDim.x) {
-        const AxisCell kx = locate1(x, c[0], p.scale[0]);
-        float v[5];
-        uint32_t type;
-        if (STAGED) {
-          const float* sa = s_a + r * 5 * p.cx;
-#pragma unroll
-          for (int k = 0; k < 5; ++k) v[k] = lerpf(sa[k * p.cx + kx.i0], sa[k * p.cx + kx.i1], kx.f);
-          type = s_t[r * p.cx + kx.nearest];
-        } else {
-          const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
-#pragma unroll
-          for (int k = 0; k < 5; ++k)
-            v[k] = lerpf(column_yz(arr[k], kx.i0, ky, kz, c), column_yz(arr[k], kx.i1, ky, kz, c), kx.f);
-          type = __ldg(p.type + cidx(kx.nearest, ky.nearest, kz.nearest, c));
+    __syncthreads();  // the previous group's readers are done
+    if (my_r < nr) {
+      uint32_t y = y0, z = z0;
+      for (uint32_t r = 0; r < my_r; ++r)
+        if (++y == p.ny) {
+          y = 0;
+          ++z;
         }
+      const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
+      float* sa = s_a + my_r * 5 * p.cx;
+#pragma unroll
+      for (uint32_t k = 0; k < 5; ++k)
+        for (uint32_t xc = my_j; xc < p.cx; xc += tpr) sa[k * p.cx + xc] = column_yz(arr[k], (int)xc, ky, kz, c);
+      for (uint32_t xc = my_j; xc < p.cx; xc += tpr)
+        s_t[my_r * p.cx + xc] = __ldg(p.type + cidx((int)xc, ky.nearest, kz.nearest, c));
+      if (my_j == 0) s_q[my_r] = make_float2(fs((float)y, p.origin[1]), fs((float)z, p.origin[2]));
+    }
+    __syncthreads();
+    for (uint32_t x = threadIdx.x; x < p.nx; x += blockDim.x) {
+      const AxisCell kx = locate1(x, c[0], p.scale[0]);
+      const float qx = fs((float)x, p.origin[0]);
+      float* out = p.out + (uint64_t)row0 * p.nx + x;
+#pragma unroll 1
+      for (uint32_t r = 0; r < nr; ++r) {
+        const float* sa = s_a + r * 5 * p.cx;
+        float v[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) v[k] = lerpf(sa[k * p.cx + kx.i0], sa[k * p.cx + kx.i1], kx.f);
+        const uint32_t type = s_t[r * p.cx + kx.nearest];
         float R9[9];
         euler_rows(v[1], v[2], v[3], R9);
-        const float q[3] = {fs((float)x, p.origin[0]), fs((float)y, p.origin[1]), fs((float)z, p.origin[2])};
-        out[x] = lattice_value(type, R9, __fdiv_rn(2.0f, v[0]), q, v[4]);
+        const float2 qyz = s_q[r];
+        const float q[3] = {qx, qyz.x, qyz.y};
+        out[(uint64_t)r * p.nx] = lattice_value(type, R9, __fdiv_rn(2.0f, v[0]), q, v[4]);
       }
+    }
+    y0 += sdy;
+    z0 += sdz;
+    if (y0 >= p.ny) {
+      y0 -= p.ny;
+      ++z0;
+    }
+  }
+}
+
+// Control grids wider than kRowCx columns: every sample reads its columns.
+__global__ void __launch_bounds__(256) lattice_params_kernel(LatticeParams p) {
+  const uint32_t c[3] = {p.cx, p.cy, p.cz};
+  const uint32_t nc = p.cx * p.cy * p.cz;
+  const float* arr[5] = {p.period, p.euler, p.euler ? p.euler + nc : nullptr,
+                         p.euler ? p.euler + 2 * nc : nullptr, p.thickness};
+  const uint32_t rows = p.ny * p.nz;
+  for (uint32_t row = blockIdx.x; row < rows; row += gridDim.x) {
+    const uint32_t y = row % p.ny, z = row / p.ny;
+    const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
+    float* out = p.out + (uint64_t)row * p.nx;
+    for (uint32_t x = threadIdx.x; x < p.nx; x += blockDim.x) {
+      const AxisCell kx = locate1(x, c[0], p.scale[0]);
+      float v[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k)
+        v[k] = lerpf(column_yz(arr[k], kx.i0, ky, kz, c), column_yz(arr[k], kx.i1, ky, kz, c), kx.f);
+      const uint32_t type = __ldg(p.type + cidx(kx.nearest, ky.nearest, kz.nearest, c));
+      float R9[9];
+      euler_rows(v[1], v[2], v[3], R9);
+      const float q[3] = {fs((float)x, p.origin[0]), fs((float)y, p.origin[1]), fs((float)z, p.origin[2])};
+      out[x] = lattice_value(type, R9, __fdiv_rn(2.0f, v[0]), q, v[4]);
     }
   }
 }
@@ -954,8 +987,8 @@ cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t pr
     q.blend = blend_buf;
     lattice_blend_kernel<<<blocks, 256, 0, st>>>(q);
   } else {
-    if (p.cx <= kRowCx) lattice_params_kernel<true><<<blocks, 256, 0, st>>>(p);
-    else lattice_params_kernel<false><<<blocks, 256, 0, st>>>(p);
+    if (p.cx <= kRowCx) lattice_staged_kernel<<<blocks, 256, 0, st>>>(p);
+    else lattice_params_kernel<<<blocks, 256, 0, st>>>(p);
   }
   return cudaGetLastError();
 }
