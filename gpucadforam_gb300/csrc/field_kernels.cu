@@ -392,12 +392,16 @@ __global__ void __launch_bounds__(256) lattice_params_batch_kernel(const BatchLa
   __shared__ uint8_t s_t[8][kWarpCx];
   const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  uint32_t lo = 0;  // instance of the warp's row: rows only increase, so search only when it moves on
   for (uint64_t row = (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib; row < total_rows; row += warps) {
-    uint32_t lo = 0, hi = n_inst - 1;
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi + 1) / 2;
-      if (inst[mid].row_begin <= row) lo = mid;
-      else hi = mid - 1;
+    if (lo + 1 < n_inst && inst[lo + 1].row_begin <= row) {
+      uint32_t a = lo + 1, b = n_inst - 1;  // last instance with row_begin <= row
+      while (a < b) {
+        const uint32_t mid = (a + b + 1) / 2;
+        if (inst[mid].row_begin <= row) a = mid;
+        else b = mid - 1;
+      }
+      lo = a;
     }
     const LatticeParams& p = inst[lo].p;
     if ((p.cx <= kWarpCx) != STAGED) continue;  // warp-uniform
