@@ -310,6 +310,196 @@ def run_configs(ctx, steps, warmup, cpu=True):
     return out
 
 
+def run_rows(ctx, steps, warmup, cpu=True):
+    """The rows beside the hot path, each timed on the device (CUDA events on
+    the launching stream) with its algorithmic bytes, and the oracle's rate on
+    the host cores beside it:
+
+    * retained CSG editing: 8 sphere fields (6 united, 2 subtracted) folded into
+      a 256^3 accumulator (16 B read + 4 B field + 16 B written per sample and
+      fold), then the region mesh (16 B per sample read, 32 B per vertex);
+    * band mode: a 384^3 gyroid (period 32 voxels) normalised into label and
+      band field (4 B read twice, 8 B written per sample), then the band mesh
+      (8 B per sample read, 32 B per vertex), band [0.35, 0.65], iso 0.5;
+    * .obj export of the 128^3 gyroid mesh: GPU weld (call to counts on the
+      host) and the whole file written, against the oracle's restatement of
+      the reference's serial writer."""
+    import tempfile
+
+    import torch
+
+    import oracle as O
+    from gpucadforam_gb300 import _native as N
+    from gpucadforam_gb300.mesher import Lattice, make_frame, make_grid, primitives_to_device
+
+    peak, _ = measured_peaks()
+    threads = os.cpu_count() or 1
+    stream = torch.cuda.current_stream()
+    cs = C.c_void_p(stream.cuda_stream)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    out = {}
+
+    # ---- retained CSG editing
+    n = 256
+    rng = np.random.default_rng(SEED + 5)
+    h = np.float32(1.0 / (n - 1))
+    frame = make_frame((0, 0, 0), (h, h, h))
+    sph = [dict(kind=0, op=0, center=rng.uniform(0.2, 0.8, 3).astype(np.float32),
+                p=[float(rng.uniform(0.1, 0.25)), 0.0]) for _ in range(8)]
+    ops = ["union"] * 6 + ["subtract"] * 2
+    fields = [ctx.csg_field(primitives_to_device([q]), 1, frame, (n, n, n)) for q in sph]
+    acc = ctx.csg_accumulator((n, n, n))
+    for f, op in zip(fields, ops):
+        ctx.csg_retain(acc, f, op=op)
+    cap = ctx.count_retained(acc).total_verts
+    pos = torch.empty((max(cap, 1), 4), device="cuda")
+    norm = torch.empty((max(cap, 1), 4), device="cuda")
+    grid = make_grid((n, n, n))
+    gc = N.GcmCounts()
+    fold_ms, mesh_ms = [], []
+    for k in range(warmup + steps):
+        acc.zero_()
+        e = [ev() for _ in range(len(fields) + 2)]
+        e[0].record(stream)
+        for i, (f, op) in enumerate(zip(fields, ops)):
+            ctx.csg_retain(acc, f, op=op)
+            e[i + 1].record(stream)
+        ctx.check(ctx.lib.gcm_mesh_retained(ctx.h, C.c_void_p(acc.data_ptr()), None, 0, C.byref(grid), 0.0,
+                                            C.c_void_p(pos.data_ptr()), C.c_void_p(norm.data_ptr()), cap,
+                                            C.byref(gc), cs))
+        e[-1].record(stream)
+        torch.cuda.synchronize()
+        if k >= warmup:
+            fold_ms += [e[i].elapsed_time(e[i + 1]) for i in range(len(fields))]
+            mesh_ms.append(e[-2].elapsed_time(e[-1]))
+    P = n ** 3
+    f_ms, m_ms = statistics.mean(fold_ms), statistics.mean(mesh_ms)
+    r = {"workload": "8 sphere fields (6 united, 2 subtracted) folded into a 256^3 retained accumulator, then its "
+                     "region mesh", "grid": [n, n, n], "verts": int(gc.total_verts),
+         "fold_ms": f_ms, "fold_samples_per_s": P / (f_ms / 1e3), "fold_GBs": 36 * P / (f_ms / 1e3) / 1e9,
+         "fold_frac_of_measured": 36 * P / (f_ms / 1e3) / 1e9 / peak,
+         "mesh_ms": m_ms, "mesh_voxels_per_s": (n - 1) ** 3 / (m_ms / 1e3),
+         "mesh_GBs": (16 * P + 32 * int(gc.total_verts)) / (m_ms / 1e3) / 1e9,
+         "mesh_note": "gcm_mesh_retained returns counts to the host; its events include that sync"}
+    if cpu:
+        planes = 32
+        z0 = (n - planes) // 2
+        hf = [O.csg_field([q], (n, n, planes), (0, 0, -z0), (h, h, h), threads=threads) for q in sph]
+        hacc = O.csg_accumulator((planes, n, n))
+        t0 = time.perf_counter()
+        for f, op in zip(hf, ops):
+            O.csg_retain(hacc, f, op=op)
+        t1 = time.perf_counter()
+        O.mesh_retained(hacc, None, "union", (1, 1, 1), (0, 0, 0))
+        t2 = time.perf_counter()
+        r["cpu_baseline"] = {"fold_samples_per_s": len(hf) * n * n * planes / (t1 - t0) / len(hf),
+                             "mesh_voxels_per_s": (n - 1) ** 2 * (planes - 1) / (t2 - t1), "cores": 1,
+                             "kind": "port", "sample": f"{planes} of {n} sample planes (the oracle's retained kernels "
+                                                       f"are single-threaded)"}
+    out["retained_csg"] = r
+    del fields, acc, pos, norm
+
+    # ---- band mode
+    n = 384
+    lat = Lattice.from_numpy(0, (1, 1, 1), np.array([32.0], np.float32), np.zeros(3, np.float32),
+                             np.zeros(1, np.float32), np.zeros(1, np.uint8), (0.0, 0.0, 0.0))
+    f = ctx.lattice_field(lat, (n, n, n))
+    label = torch.empty_like(f)
+    nfield = torch.empty_like(f)
+    iso, lo, hi = 0.5, 0.35, 0.65
+    ctx.check(ctx.lib.gcm_normalise_band(ctx.h, C.c_void_p(f.data_ptr()), n, n, n, lo, hi,
+                                         C.c_void_p(label.data_ptr()), C.c_void_p(nfield.data_ptr()), None, cs))
+    cap = ctx.count_field(label, iso).total_verts
+    pos = torch.empty((max(cap, 1), 4), device="cuda")
+    norm = torch.empty((max(cap, 1), 4), device="cuda")
+    d_counts = torch.zeros(4, dtype=torch.int64, device="cuda")
+    grid = make_grid((n, n, n))
+    norm_ms, band_ms = [], []
+    for k in range(warmup + steps):
+        e = [ev() for _ in range(3)]
+        e[0].record(stream)
+        ctx.check(ctx.lib.gcm_normalise_band(ctx.h, C.c_void_p(f.data_ptr()), n, n, n, lo, hi,
+                                             C.c_void_p(label.data_ptr()), C.c_void_p(nfield.data_ptr()), None, cs))
+        e[1].record(stream)
+        ctx.check(ctx.lib.gcm_mesh_band_async(ctx.h, C.c_void_p(label.data_ptr()), C.c_void_p(nfield.data_ptr()),
+                                              C.byref(grid), iso, lo, hi, C.c_void_p(pos.data_ptr()),
+                                              C.c_void_p(norm.data_ptr()), cap, C.c_void_p(d_counts.data_ptr()), cs))
+        e[2].record(stream)
+        torch.cuda.synchronize()
+        if k >= warmup:
+            norm_ms.append(e[0].elapsed_time(e[1]))
+            band_ms.append(e[1].elapsed_time(e[2]))
+    P = n ** 3
+    nv = int(d_counts[1])
+    a_ms, b_ms = statistics.mean(norm_ms), statistics.mean(band_ms)
+    r = {"workload": "384^3 gyroid (period 32 voxels) normalised into a band [0.35, 0.65], iso 0.5, and meshed",
+         "grid": [n, n, n], "verts": nv, "normalise_ms": a_ms, "normalise_GBs": 16 * P / (a_ms / 1e3) / 1e9,
+         "normalise_frac_of_measured": 16 * P / (a_ms / 1e3) / 1e9 / peak,
+         "mesh_ms": b_ms, "mesh_voxels_per_s": (n - 1) ** 3 / (b_ms / 1e3),
+         "mesh_GBs": (8 * P + 32 * nv) / (b_ms / 1e3) / 1e9,
+         "mesh_frac_of_measured": (8 * P + 32 * nv) / (b_ms / 1e3) / 1e9 / peak}
+    if cpu:
+        planes = 64
+        z0 = (n - planes) // 2
+        hf = f[z0:z0 + planes].cpu().numpy()
+        t0 = time.perf_counter()
+        hl, hn, _ = O.normalise_band(hf, lo, hi)
+        t1 = time.perf_counter()
+        O.mesh_band(hl, hn, (1, 1, 1), (0, 0, 0), iso, lo, hi)
+        t2 = time.perf_counter()
+        r["cpu_baseline"] = {"normalise_samples_per_s": n * n * planes / (t1 - t0),
+                             "mesh_voxels_per_s": (n - 1) ** 2 * (planes - 1) / (t2 - t1), "cores": 1,
+                             "kind": "port", "sample": f"{planes} of {n} sample planes (the slab normalised on its "
+                                                       f"own range)"}
+    out["band"] = r
+    del f, label, nfield, pos, norm
+
+    # ---- .obj export
+    n = 128
+    lat = Lattice.from_numpy(0, (1, 1, 1), np.array([32.0], np.float32), np.zeros(3, np.float32),
+                             np.zeros(1, np.float32), np.zeros(1, np.uint8), (0.0, 0.0, 0.0))
+    f = ctx.lattice_field(lat, (n, n, n))
+    vs = 1.0 / (n - 1)
+    pos, _, cnt = ctx.mesh_field(f, 0.0, (vs, vs, vs))
+    V = int(cnt.total_verts)
+    nvo, nfo = C.c_uint64(0), C.c_uint64(0)
+    d_v = torch.empty((V, 3), dtype=torch.float32, device="cuda")
+    d_f = torch.empty((V // 3, 3), dtype=torch.int32, device="cuda")
+    weld_s, write_s = [], []
+    work = tempfile.mkdtemp(prefix="gcm_obj_")
+    path = os.path.join(work, "mesh.obj")
+    for k in range(warmup + steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.check(ctx.lib.gcm_weld_obj(ctx.h, C.c_void_p(pos.data_ptr()), V, C.c_void_p(d_v.data_ptr()), V,
+                                       C.c_void_p(d_f.data_ptr()), V // 3, C.byref(nvo), C.byref(nfo), cs))
+        t1 = time.perf_counter()
+        ctx.check(ctx.lib.gcm_write_obj(ctx.h, C.c_void_p(pos.data_ptr()), V, path.encode(), None, None, cs))
+        t2 = time.perf_counter()
+        if k >= warmup:
+            weld_s.append(t1 - t0)
+            write_s.append(t2 - t1)
+    w_s, wr_s = statistics.median(weld_s), statistics.median(write_s)
+    r = {"workload": "128^3 uniform gyroid mesh (period 32 voxels) welded and written as .obj", "verts": V,
+         "obj_vertices": int(nvo.value), "obj_faces": int(nfo.value), "file_bytes": os.path.getsize(path),
+         "weld_s": w_s, "weld_verts_per_s": V / w_s, "write_s": wr_s, "write_verts_per_s": V / wr_s}
+    if cpu:
+        hp = pos.cpu().numpy()
+        opath = os.path.join(work, "oracle.obj")
+        t0 = time.perf_counter()
+        O.write_obj(hp, opath)
+        t1 = time.perf_counter()
+        with open(path, "rb") as a, open(opath, "rb") as b:
+            r["identical_to_oracle"] = a.read() == b.read()
+        r["cpu_baseline"] = {"write_verts_per_s": V / (t1 - t0), "cores": 1, "kind": "port",
+                             "sample": "the whole mesh through the oracle's restatement of the reference's writer"}
+        os.remove(opath)
+    os.remove(path)
+    os.rmdir(work)
+    out["obj"] = r
+    return out
+
+
 def run_reference(args):
     world, rank, local, pg = dist_setup(args)
     if rank != 0:
@@ -653,6 +843,9 @@ def run_gcm(args):
     configs = None
     if not args.no_configs:
         configs = run_configs(ctx, args.steps, args.warmup, cpu=(rank == 0 and not args.no_cpu))
+    rows = None
+    if not args.no_rows:
+        rows = run_rows(ctx, args.steps, args.warmup, cpu=(rank == 0 and not args.no_cpu))
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -673,7 +866,7 @@ def run_gcm(args):
                              "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                              "algorithmic_bytes": mc_bytes, "traffic": traffic},
                 "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": int(launches),
-                "batched": batched, "served": served, "configs": configs}
+                "batched": batched, "served": served, "configs": configs, "rows": rows}
         print(json.dumps(line))
     ctx.close()
     if pg is not None:
@@ -694,6 +887,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
+    ap.add_argument("--no-rows", action="store_true", help="skip the retained-CSG, band and .obj lines")
     ap.add_argument("--batch-instances", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -119,6 +119,7 @@ PROTOTYPES = {
     "gcm_mc_generate": (I32, [P, P, C.POINTER(GcmGrid), F32, P, U64, P, P, P, U64, P]),
     "gcm_normalise_band": (I32, [P, P, U32, U32, U32, F32, F32, P, P, C.POINTER(F32), P]),
     "gcm_mesh_band": (I32, [P, P, P, C.POINTER(GcmGrid), F32, F32, F32, P, P, U64, C.POINTER(GcmCounts), P]),
+    "gcm_mesh_band_async": (I32, [P, P, P, C.POINTER(GcmGrid), F32, F32, F32, P, P, U64, P, P]),
     "gcm_field_unit_cell": (I32, [P, U32, U32, U32, U32, P, P]),
     "gcm_field_lattice": (I32, [P, C.POINTER(GcmLattice), U32, U32, U32, P, P]),
     "gcm_mesh_lattice": (I32, [P, C.POINTER(GcmLattice), C.POINTER(GcmGrid), F32, P, P, U64, C.POINTER(GcmCounts), P]),

@@ -357,6 +357,18 @@ gcm_status gcm_mesh_band(gcm_ctx* ctx, const float* d_label, const float* d_norm
   return read_counts(ctx, used, h_counts, st);
 }
 
+gcm_status gcm_mesh_band_async(gcm_ctx* ctx, const float* d_label, const float* d_norm_field, const gcm_grid* grid,
+                               float iso, float lo, float hi, float* d_pos, float* d_norm, uint64_t capacity,
+                               gcm_counts* d_counts, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_label || !d_norm_field || !d_counts || (capacity && (!d_pos || !d_norm)))
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_mesh_band_async: NULL argument");
+  gcm_status s = check_grid(ctx, grid);
+  if (s) return s;
+  return mesh_core(ctx, d_label, d_norm_field, grid, iso, lo, hi, kMeshBand, 0, true, d_pos, d_norm, capacity,
+                   d_counts, static_cast<cudaStream_t>(stream), nullptr);
+}
+
 // ------------------------------------------------------- retained CSG form
 
 gcm_status gcm_csg_retain(gcm_ctx* ctx, gcm_csg_point* d_acc, const float* d_field, uint32_t nx, uint32_t ny,
@@ -669,13 +681,10 @@ gcm_status gcm_normalise_band(gcm_ctx* ctx, const float* d_field, uint32_t nx, u
   if (s) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   unsigned int* enc = reinterpret_cast<unsigned int*>(static_cast<char*>(ctx->scratch) + 64);
-  // key(0.0f) = 0x80000000 for both min and max
-  const unsigned int init[2] = {0x80000000u, 0x80000000u};
-  GCM_CUDA(ctx, cudaMemcpyAsync(enc, init, sizeof(init), cudaMemcpyHostToDevice, st));
   const uint64_t n = (uint64_t)nx * ny * nz;
   GCM_CUDA(ctx, gcm::launch_normalise(d_field, nx, ny, nz, enc, lo, hi, d_label, d_norm_field,
                                        grid_blocks(ctx, n, 256, 4), st));
-  count_launch(ctx, 2);
+  count_launch(ctx, 3);
   if (h_minmax) {
     unsigned int k[2];
     GCM_CUDA(ctx, cudaMemcpyAsync(k, enc, sizeof(k), cudaMemcpyDeviceToHost, st));

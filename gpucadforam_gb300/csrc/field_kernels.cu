@@ -934,10 +934,29 @@ __device__ __forceinline__ float key2f(unsigned int k) {
   return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
+__global__ void minmax_init_kernel(unsigned int* enc) {
+  enc[0] = f2key(0.0f);
+  enc[1] = f2key(0.0f);
+}
+
 __global__ void __launch_bounds__(256) minmax_kernel(const float* f, uint64_t n, unsigned int* enc_min,
                                                      unsigned int* enc_max) {
   unsigned int lo = f2key(0.0f), hi = f2key(0.0f);
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+  uint64_t head = 0;  // samples before the first 16-byte boundary
+  if (((uintptr_t)f & 15u) == 0) {
+    // 16-byte loads: four samples per load
+    const float4* f4 = reinterpret_cast<const float4*>(f);
+    const uint64_t n4 = n / 4;
+    for (uint64_t i = tid; i < n4; i += stride) {
+      const float4 v = __ldg(f4 + i);
+      const unsigned int k0 = f2key(v.x), k1 = f2key(v.y), k2 = f2key(v.z), k3 = f2key(v.w);
+      lo = min(min(lo, min(k0, k1)), min(k2, k3));
+      hi = max(max(hi, max(k0, k1)), max(k2, k3));
+    }
+    head = 4 * n4;
+  }
+  for (uint64_t i = head + tid; i < n; i += stride) {
     const unsigned int k = f2key(__ldg(f + i));
     lo = min(lo, k);
     hi = max(hi, k);
@@ -952,23 +971,53 @@ __global__ void __launch_bounds__(256) minmax_kernel(const float* f, uint64_t n,
   }
 }
 
+// One warp per sample row: the row's (y, z) and boundary test once, then x,
+// four samples per 16-byte access where the rows allow it.
+__device__ __forceinline__ void band_sample(float v, float a, float b, float lo, float hi, bool edge, float& m,
+                                            float& k) {
+  k = __fdiv_rn(fs(v, a), fs(b, a));
+  if (edge) {
+    m = 0.0f;
+    k = 0.0f;
+  } else {
+    m = (k >= lo && k <= hi) ? 1.0f : 0.0f;
+  }
+}
+
 __global__ void __launch_bounds__(256) band_map_kernel(const float* f, uint32_t nx, uint32_t ny, uint32_t nz,
                                                        const unsigned int* enc, float lo, float hi, float* label,
                                                        float* norm_field) {
   const float a = key2f(enc[0]), b = key2f(enc[1]);
-  const uint64_t total = (uint64_t)nx * ny * nz;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t x = (uint32_t)(i % nx), y = (uint32_t)((i / nx) % ny), z = (uint32_t)(i / ((uint64_t)nx * ny));
-    float k = __fdiv_rn(fs(__ldg(f + i), a), fs(b, a));
-    float m;
-    if (x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 || z == nz - 1) {
-      m = 0.0f;
-      k = 0.0f;
+  const uint32_t rows = ny * nz, lane = threadIdx.x & 31u;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  const bool vec = (nx & 3u) == 0 && ((((uintptr_t)f) | ((uintptr_t)label) | ((uintptr_t)norm_field)) & 15u) == 0;
+  for (uint32_t row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < rows; row += warps) {
+    const uint32_t y = row % ny, z = row / ny;
+    const bool edge_row = y == 0 || y == ny - 1 || z == 0 || z == nz - 1;
+    const uint64_t base = (uint64_t)row * nx;
+    if (vec) {
+      const float4* f4 = reinterpret_cast<const float4*>(f + base);
+      float4* l4 = reinterpret_cast<float4*>(label + base);
+      float4* k4 = reinterpret_cast<float4*>(norm_field + base);
+      for (uint32_t x4 = lane; x4 < nx / 4; x4 += 32) {
+        const float4 v = __ldg(f4 + x4);
+        const uint32_t x = 4 * x4;
+        float4 m, k;
+        band_sample(v.x, a, b, lo, hi, edge_row || x == 0, m.x, k.x);
+        band_sample(v.y, a, b, lo, hi, edge_row, m.y, k.y);
+        band_sample(v.z, a, b, lo, hi, edge_row, m.z, k.z);
+        band_sample(v.w, a, b, lo, hi, edge_row || x + 3 == nx - 1, m.w, k.w);
+        l4[x4] = m;
+        k4[x4] = k;
+      }
     } else {
-      m = (k >= lo && k <= hi) ? 1.0f : 0.0f;
+      for (uint32_t x = lane; x < nx; x += 32) {
+        float m, k;
+        band_sample(__ldg(f + base + x), a, b, lo, hi, edge_row || x == 0 || x == nx - 1, m, k);
+        label[base + x] = m;
+        norm_field[base + x] = k;
+      }
     }
-    label[i] = m;
-    norm_field[i] = k;
   }
 }
 
@@ -1036,6 +1085,7 @@ cudaError_t launch_csg(const CsgParams& p, uint32_t sm_count, cudaStream_t st) {
 cudaError_t launch_normalise(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, unsigned int* enc, float lo,
                              float hi, float* label, float* norm_field, uint32_t blocks, cudaStream_t st) {
   const uint64_t n = (uint64_t)nx * ny * nz;
+  minmax_init_kernel<<<1, 1, 0, st>>>(enc);
   minmax_kernel<<<blocks, 256, 0, st>>>(f, n, enc, enc + 1);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;

@@ -131,10 +131,16 @@ __device__ __forceinline__ float3 edge_point_plain(const uint32_t g[3], const Fr
   return lerp3(corner_pos(g, fr, ka), corner_pos(g, fr, kb), t);
 }
 
+// The reference compares float differences against the double 0.0005
+// ((double)|d| < 0.0005).  float(0.0005) = 5.000000237e-4 is the smallest float
+// above 0.0005, so for every float d, |d| < float(0.0005) gives the same
+// answer (NaN included) without the FP64 pipe.
+constexpr float kSnap = 0.0005f;
+
 // Band edge point (vertexInterp2_new, src/MarchingCubes_kernel.cu:3593-3674):
 // endpoints with labels {0,1} are ordered so that f0 <= f1; the point snaps to
-// an endpoint within 0.0005 of a band edge (compared in double, as the
-// reference's double literal makes it) and otherwise lerps at the band edge
+// an endpoint within 0.0005 of a band edge (the reference's double comparison,
+// made exactly in float through kSnap) and otherwise lerps at the band edge
 // crossed.  Where the reference leaves t unset, t = 0.  `lab(k)` / `fv(k)`
 // return the label and the normalised field at corner k.
 template <class Lab, class Fv>
@@ -156,15 +162,15 @@ __device__ __forceinline__ float3 edge_point_band(const uint32_t g[3], const Fra
     for (int side = 0; side < 2; ++side) {
       const float lev = side ? hi : lo;
       if (!done && (f1 >= lev) && (f0 <= lev)) {
-        if ((double)fabsf(__fsub_rn(lev, f0)) < 0.0005) return pa;
-        if ((double)fabsf(__fsub_rn(lev, f1)) < 0.0005) return pb;
-        if ((double)fabsf(__fsub_rn(f1, f0)) < 0.0005) return pa;
+        if (fabsf(__fsub_rn(lev, f0)) < kSnap) return pa;
+        if (fabsf(__fsub_rn(lev, f1)) < kSnap) return pb;
+        if (fabsf(__fsub_rn(f1, f0)) < kSnap) return pa;
         t = __fdiv_rn(__fsub_rn(lev, f0), __fsub_rn(f1, f0));
         done = true;
       }
     }
     if (!done) {
-      if ((f1 == f0) && ((double)pa.z == 0.0)) t = 1.0f;
+      if ((f1 == f0) && (pa.z == 0.0f)) t = 1.0f;
       else if (f1 == f0) t = 0.0f;
     }
   }
@@ -175,32 +181,26 @@ __device__ __forceinline__ float3 edge_point_band(const uint32_t g[3], const Fra
 // (the same arithmetic and branch order as edge_point_band).
 __device__ __forceinline__ float3 edge_point_band_v(float id0, float id1, float f0, float f1, uint32_t ba, uint32_t bb,
                                                     const VoxelCorners& V, float lo, float hi) {
+  // The reference's branches as selects: the first band edge crossed (lo,
+  // then hi) decides the level; snapping returns an end point exactly; the
+  // interpolation is made with the same operations either way.
   const bool crossing = (id0 == 1.0f && id1 == 0.0f) || (id0 == 0.0f && id1 == 1.0f);
-  if (crossing && f1 < f0) {
-    const uint32_t tb = ba; ba = bb; bb = tb;
-    const float tf = f0; f0 = f1; f1 = tf;
-  }
-  const float3 pa = corner_sel(V, ba), pb = corner_sel(V, bb);
+  const bool swap = crossing && f1 < f0;
+  const uint32_t ua = swap ? bb : ba, ub = swap ? ba : bb;
+  const float g0 = swap ? f1 : f0, g1 = swap ? f0 : f1;
+  const float3 pa = corner_sel(V, ua), pb = corner_sel(V, ub);
+  const bool on_lo = (g1 >= lo) && (g0 <= lo), on_hi = (g1 >= hi) && (g0 <= hi);
+  const bool hit = crossing && (on_lo || on_hi);
+  const float lev = on_lo ? lo : hi;
+  const float d0 = __fsub_rn(lev, g0), d1 = __fsub_rn(lev, g1), dd = __fsub_rn(g1, g0);
+  const bool s0 = fabsf(d0) < kSnap, s1 = fabsf(d1) < kSnap, s2 = fabsf(dd) < kSnap;
   float t = 0.0f;
-  if (crossing) {
-    bool done = false;
-#pragma unroll
-    for (int side = 0; side < 2; ++side) {
-      const float lev = side ? hi : lo;
-      if (!done && (f1 >= lev) && (f0 <= lev)) {
-        if ((double)fabsf(__fsub_rn(lev, f0)) < 0.0005) return pa;
-        if ((double)fabsf(__fsub_rn(lev, f1)) < 0.0005) return pb;
-        if ((double)fabsf(__fsub_rn(f1, f0)) < 0.0005) return pa;
-        t = __fdiv_rn(__fsub_rn(lev, f0), __fsub_rn(f1, f0));
-        done = true;
-      }
-    }
-    if (!done) {
-      if ((f1 == f0) && ((double)pa.z == 0.0)) t = 1.0f;
-      else if (f1 == f0) t = 0.0f;
-    }
-  }
-  return lerp3(pa, pb, t);
+  if (hit) t = __fdiv_rn(d0, dd);
+  else if (crossing && g1 == g0) t = pa.z == 0.0f ? 1.0f : 0.0f;
+  const float3 p = lerp3(pa, pb, t);
+  if (hit && (s0 || (!s1 && s2))) return pa;
+  if (hit && !s0 && s1) return pb;
+  return p;
 }
 
 // Retained edge point (vertexInterp_primitive, src/MarchingCubes_kernel.cu:

@@ -153,6 +153,10 @@ gcm_status gcm_normalise_band(gcm_ctx* ctx, const float* d_field, uint32_t nx, u
 gcm_status gcm_mesh_band(gcm_ctx* ctx, const float* d_label, const float* d_norm_field, const gcm_grid* grid, float iso,
                          float band_lo, float band_hi, float* d_pos, float* d_norm, uint64_t capacity_verts,
                          gcm_counts* h_counts, gcm_stream stream);
+/* Same, stream-ordered: counts land in d_counts (device), nothing syncs. */
+gcm_status gcm_mesh_band_async(gcm_ctx* ctx, const float* d_label, const float* d_norm_field, const gcm_grid* grid,
+                               float iso, float band_lo, float band_hi, float* d_pos, float* d_norm,
+                               uint64_t capacity_verts, gcm_counts* d_counts, gcm_stream stream);
 
 /* ------------------------------------------------------------------ fields */
 
