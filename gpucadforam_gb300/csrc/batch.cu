@@ -488,6 +488,7 @@ gcm_status gcm_ctx_set_launch_shape(gcm_ctx* ctx, int threads, uint32_t tile_vox
                 tile_voxels);
   ctx->mesh_threads = threads;
   ctx->tile_voxels = tile_voxels;
+  ctx->shape_set = true;
   return GCM_OK;
 }
 

@@ -362,7 +362,8 @@ gcm_status gcm_batch_mesh_graph(gcm_batch* batch, float* d_pos, float* d_norm, u
 gcm_status gcm_batch_tune(gcm_batch* batch, float* d_pos, float* d_norm, uint64_t capacity_verts,
                           const char* cache_path, int* h_threads, uint32_t* h_tile_voxels, gcm_stream stream);
 /* Launch shape of the fused kernel for this context's single-grid calls:
- * CTA size (128 or 256) and voxels per tile. */
+ * CTA size (128 or 256) and voxels per tile.  Until it is set, the plain and
+ * retained forms use 128 threads x 1024 voxels and the band form 256 x 2048. */
 gcm_status gcm_ctx_set_launch_shape(gcm_ctx* ctx, int threads, uint32_t tile_voxels);
 
 /* ----------------------------------------------------------------- server */

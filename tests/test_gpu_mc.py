@@ -120,6 +120,22 @@ def test_no_surface(ctx):
     assert cnt.total_verts == 0
 
 
+def test_band_default_shape_equals_explicit(ctx):
+    """A context whose launch shape was never set meshes band fields with its
+    own default shape; the output equals that of the explicit shapes."""
+    from gpucadforam_gb300.mesher import Context
+
+    lab, nf, iso, lo, hi, vs, gc = band_case(MC, 0)
+    ref = ctx.mesh_band(dev(lab), dev(nf), iso, lo, hi, tuple(vs), tuple(gc))
+    fresh = Context(0)
+    try:
+        got = fresh.mesh_band(dev(lab), dev(nf), iso, lo, hi, tuple(vs), tuple(gc))
+    finally:
+        fresh.close()
+    assert got[2].total_verts == ref[2].total_verts
+    assert host(got[0]).tobytes() == host(ref[0]).tobytes() and host(got[1]).tobytes() == host(ref[1]).tobytes()
+
+
 def test_iso_exactly_everywhere_is_outside(ctx):
     """f == iso at every sample: no corner is inside (f < iso), no triangles."""
     f = np.full((9, 10, 11), 0.25, np.float32)
