@@ -220,9 +220,9 @@ __global__ void __launch_bounds__(256) lattice_prep_kernel(LatticeParams p, floa
   }
 }
 
-// Rows of samples are the unit of work: a CTA takes sample row (y, z), stages
-// per control column the row's y/z-interpolated parameters in shared memory,
-// and its threads cover x.  No 64-bit index arithmetic per sample.
+// Sample rows are the unit of work: a CTA takes sample rows (y, z), stages per
+// control column the rows' y/z-interpolated parameters in shared memory, and
+// its threads cover x.  No 64-bit index arithmetic per sample.
 constexpr uint32_t kRowCx = 1024;   // control columns staged per row (PARAMS)
 constexpr uint32_t kBlendCx = 128;  // control columns staged per row (BLEND)
 
@@ -624,7 +624,7 @@ __device__ __forceinline__ Iv cone_h_iv(Iv b, float hgt, float& mag) {
   return {fmaxf(p1l, p2l), fmaxf(p1h, p2h)};
 }
 
-// Enclosure of prim_eval over the box [blo, bhi] of sample positions, or
+// Enclosure of prim_eval_k over the box [blo, bhi] of sample positions, or
 // (-inf, +inf) when any step is not finite.
 __device__ float2 prim_bounds(const PrimPre& P, const float* blo, const float* bhi) {
   Iv w[3];
