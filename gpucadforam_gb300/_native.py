@@ -126,6 +126,7 @@ PROTOTYPES = {
     "gcm_mesh_lattice_async": (I32, [P, C.POINTER(GcmLattice), C.POINTER(GcmGrid), F32, P, P, U64, P, P]),
     "gcm_field_csg": (I32, [P, P, U32, C.POINTER(GcmFrame), U32, U32, U32, P, P]),
     "gcm_csg_retain": (I32, [P, P, P, U32, U32, U32, F32, U32, P]),
+    "gcm_csg_retain_band": (I32, [P, P, P, U32, U32, U32, F32, F32, F32, U32, P]),
     "gcm_svl_coefficients": (I32, [P, U32, U32, U32, P, P]),
     "gcm_svl_lattice": (I32, [P, C.POINTER(GcmSvlParams), P, P, P, P, P, P]),
     "gcm_mesh_retained": (I32, [P, P, P, U32, C.POINTER(GcmGrid), F32, P, P, U64, C.POINTER(GcmCounts), P]),

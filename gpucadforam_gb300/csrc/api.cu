@@ -385,8 +385,23 @@ gcm_status gcm_csg_retain(gcm_ctx* ctx, gcm_csg_point* d_acc, const float* d_fie
   if (op > GCM_CSG_INTERSECT) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_csg_retain: unknown op %u", (unsigned)op);
   if (nx == 0 || ny == 0 || nz == 0) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_csg_retain: empty grid");
   const uint64_t n = (uint64_t)nx * ny * nz;
-  GCM_CUDA(ctx, launch_csg_retain(d_acc, d_field, nx, ny, nz, iso, (uint32_t)op, grid_blocks(ctx, n, 256),
-                                  static_cast<cudaStream_t>(stream)));
+  GCM_CUDA(ctx, launch_csg_retain(d_acc, d_field, nx, ny, nz, iso, (uint32_t)op, false, 0.0f, 0.0f,
+                                  grid_blocks(ctx, n, 256), static_cast<cudaStream_t>(stream)));
+  count_launch(ctx, 1);
+  return GCM_OK;
+}
+
+gcm_status gcm_csg_retain_band(gcm_ctx* ctx, gcm_csg_point* d_acc, const float* d_lattice, uint32_t nx, uint32_t ny,
+                               uint32_t nz, float iso, float band_lo, float band_hi, gcm_csg_op op,
+                               gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_acc || !d_lattice) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_csg_retain_band: NULL argument");
+  if (op > GCM_CSG_INTERSECT)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_csg_retain_band: unknown op %u", (unsigned)op);
+  if (nx == 0 || ny == 0 || nz == 0) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_csg_retain_band: empty grid");
+  const uint64_t n = (uint64_t)nx * ny * nz;
+  GCM_CUDA(ctx, launch_csg_retain(d_acc, d_lattice, nx, ny, nz, iso, (uint32_t)op, true, band_lo, band_hi,
+                                  grid_blocks(ctx, n, 256), static_cast<cudaStream_t>(stream)));
   count_launch(ctx, 1);
   return GCM_OK;
 }

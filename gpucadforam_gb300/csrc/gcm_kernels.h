@@ -192,7 +192,7 @@ cudaError_t launch_normalise(const float* f, uint32_t nx, uint32_t ny, uint32_t 
 size_t mesh_smem_bytes(uint32_t nx, uint32_t rows, int mode);
 // Folds one primitive field into a retained accumulator (gcm_csg_point per sample).
 cudaError_t launch_csg_retain(gcm_csg_point* acc, const float* f, uint32_t nx, uint32_t ny, uint32_t nz, float iso,
-                              uint32_t op, uint32_t blocks, cudaStream_t st);
+                              uint32_t op, bool band, float iso1, float iso2, uint32_t blocks, cudaStream_t st);
 uint32_t scan_tile_elems();
 
 }  // namespace gcm

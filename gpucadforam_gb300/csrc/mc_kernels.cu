@@ -834,25 +834,49 @@ namespace {
 // crossing fraction t = (iso - f) / (f' - f) replaces a non-positive stored
 // fraction or is averaged with a positive one.  Like the reference, the last
 // sample of the grid is left as it is.
+// classify_copy_Voxel (src/MarchingCubes_kernel.cu:158-447): static mode (the
+// field is the object) or, with `band`, the lattice-band mode (dynamic = true:
+// the open band iso1 < f < iso2 is the object, the crossing fraction is taken
+// at iso1, else at iso2, and the difference pairs the band with the old
+// outside as the reference does).
 __global__ void __launch_bounds__(256) csg_retain_kernel(gcm_csg_point* __restrict__ acc, const float* __restrict__ f,
-                                                         uint32_t nx, uint32_t ny, uint32_t nz, float iso, uint32_t op) {
+                                                         uint32_t nx, uint32_t ny, uint32_t nz, float iso, uint32_t op,
+                                                         bool band, float iso1, float iso2) {
   const uint64_t plane = (uint64_t)nx * ny, total = plane * nz;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i + 1 < total;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t x = (uint32_t)(i % nx), y = (uint32_t)((i / nx) % ny), z = (uint32_t)(i / plane);
     gcm_csg_point pt = acc[i];
     const float v = __ldg(f + i);
-    const bool in_v = v < iso, in_a = (float)pt.val < iso;
+    const bool in_a = (float)pt.val < iso;
     bool inside;
-    if (op == GCM_CSG_SUBTRACT) inside = (v >= iso) && in_a;
-    else if (op == GCM_CSG_INTERSECT) inside = in_v && in_a;
-    else inside = in_v || in_a;
+    if (band) {
+      const bool in_b = (v > iso1) && (v < iso2);
+      if (op == GCM_CSG_SUBTRACT) inside = in_b && !in_a;
+      else if (op == GCM_CSG_INTERSECT) inside = in_b && in_a;
+      else inside = in_b || in_a;
+    } else {
+      const bool in_v = v < iso;
+      if (op == GCM_CSG_SUBTRACT) inside = (v >= iso) && in_a;
+      else if (op == GCM_CSG_INTERSECT) inside = in_v && in_a;
+      else inside = in_v || in_a;
+    }
     pt.val = inside ? -1 : 1;
+    auto crosses = [&](float w, float lev) { return (w < lev && v >= lev) || (w >= lev && v < lev); };
     auto fold = [&](float& ts, float w) {
-      if ((w < iso && v >= iso) || (w >= iso && v < iso)) {
-        const float t = __fdiv_rn(__fsub_rn(iso, v), __fsub_rn(w, v));
-        ts = ts > 0.0f ? __fmul_rn(__fadd_rn(ts, t), 0.5f) : t;
+      float lev;
+      if (!band) {
+        if (!crosses(w, iso)) return;
+        lev = iso;
+      } else if (crosses(w, iso1)) {
+        lev = iso1;
+      } else if (crosses(w, iso2)) {
+        lev = iso2;
+      } else {
+        return;
       }
+      const float t = __fdiv_rn(__fsub_rn(lev, v), __fsub_rn(w, v));
+      ts = ts > 0.0f ? __fmul_rn(__fadd_rn(ts, t), 0.5f) : t;
     };
     if (x + 1 < nx) fold(pt.t_x, __ldg(f + i + 1));
     if (y + 1 < ny) fold(pt.t_y, __ldg(f + i + nx));
@@ -933,8 +957,8 @@ cudaError_t launch_batch_mesh(bool emit, int threads, const BatchMeshParams& p, 
 }
 
 cudaError_t launch_csg_retain(gcm_csg_point* acc, const float* f, uint32_t nx, uint32_t ny, uint32_t nz, float iso,
-                              uint32_t op, uint32_t blocks, cudaStream_t st) {
-  csg_retain_kernel<<<blocks, 256, 0, st>>>(acc, f, nx, ny, nz, iso, op);
+                              uint32_t op, bool band, float iso1, float iso2, uint32_t blocks, cudaStream_t st) {
+  csg_retain_kernel<<<blocks, 256, 0, st>>>(acc, f, nx, ny, nz, iso, op, band, iso1, iso2);
   return cudaGetLastError();
 }
 

@@ -247,11 +247,17 @@ class Context:
         as an (nz, ny, nx, 4) int32 tensor (the fractions are float bits)."""
         return torch.zeros((*shape_zyx, 4), dtype=torch.int32, device=f"cuda:{self.device}")
 
-    def csg_retain(self, acc, field, op="union", iso=0.0, stream=None):
+    def csg_retain(self, acc, field, op="union", iso=0.0, band=None, stream=None):
+        """Fold a field (or, with band = (lo, hi), a lattice band) into acc."""
         nz, ny, nx = field.shape
         assert tuple(acc.shape[:3]) == (nz, ny, nx) and acc.shape[3] == 4
-        self.check(self.lib.gcm_csg_retain(self.h, _ptr(acc), _ptr(field), nx, ny, nz, float(iso),
-                                           self.CSG_OPS.get(op, op), _stream(stream)))
+        if band is None:
+            self.check(self.lib.gcm_csg_retain(self.h, _ptr(acc), _ptr(field), nx, ny, nz, float(iso),
+                                               self.CSG_OPS.get(op, op), _stream(stream)))
+        else:
+            self.check(self.lib.gcm_csg_retain_band(self.h, _ptr(acc), _ptr(field), nx, ny, nz, float(iso),
+                                                    float(band[0]), float(band[1]), self.CSG_OPS.get(op, op),
+                                                    _stream(stream)))
 
     def count_retained(self, acc, field=None, op="union", iso=0.0, stream=None) -> Counts:
         g = make_grid(acc.shape[:3])

@@ -266,6 +266,14 @@ typedef struct gcm_csg_point {
  * has the accumulator's nx*ny*nz samples; the reference folds at iso 0. */
 gcm_status gcm_csg_retain(gcm_ctx* ctx, gcm_csg_point* d_acc, const float* d_field, uint32_t nx, uint32_t ny,
                           uint32_t nz, float iso, gcm_csg_op op, gcm_stream stream);
+/* Folds a lattice band instead (classify_copy_Voxel with dynamic = true,
+ * src/MarchingCubes_kernel.cu:158-447; its `fixed` flag is not read): the
+ * object is band_lo < lattice < band_hi, each edge's fraction is where the
+ * lattice crosses band_lo, else band_hi; difference marks band samples that
+ * the model does not hold, as the reference's kernel does. */
+gcm_status gcm_csg_retain_band(gcm_ctx* ctx, gcm_csg_point* d_acc, const float* d_lattice, uint32_t nx, uint32_t ny,
+                               uint32_t nz, float iso, float band_lo, float band_hi, gcm_csg_op op,
+                               gcm_stream stream);
 /* Mesh of the accumulator, one fused pass (Isosurface::computeIsosurface,
  * src/Isosurface.cu:44-135, with classifyVoxel and
  * generateTriangles_lattice_kernel, src/MarchingCubes_kernel.cu:869-1052,

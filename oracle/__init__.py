@@ -74,6 +74,8 @@ def lib():
         L.orc_write_obj.argtypes = [F32P, C.c_uint64, C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.orc_write_obj.restype = C.c_int
         L.orc_csg_retain.argtypes = [C.c_void_p, F32P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32]
+        L.orc_csg_retain_band.argtypes = [C.c_void_p, F32P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, C.c_float,
+                                          C.c_float, C.c_uint32]
         L.orc_mesh_retained.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                         F32P, F32P, C.c_float, C.c_void_p, C.c_void_p, C.c_uint64,
                                         C.POINTER(C.c_uint64)]
@@ -300,13 +302,19 @@ def csg_accumulator(shape_zyx):
     return np.zeros((*shape_zyx, 4), np.int32)
 
 
-def csg_retain(acc, field, op="union", iso=0.0):
-    """classify_copy_Voxel static mode (src/MarchingCubes_kernel.cu:158-447), in place."""
+def csg_retain(acc, field, op="union", iso=0.0, band=None):
+    """classify_copy_Voxel (src/MarchingCubes_kernel.cu:158-447), in place: the
+    static mode, or with band = (iso1, iso2) the lattice-band mode with field
+    as the lattice."""
     assert acc.dtype == np.int32 and acc.flags.c_contiguous and acc.shape[3] == 4
     field = np.ascontiguousarray(field, np.float32)
     nz, ny, nx = field.shape
     assert acc.shape[:3] == field.shape
-    lib().orc_csg_retain(acc.ctypes.data, field, nx, ny, nz, iso, CSG_OPS.get(op, op))
+    if band is None:
+        lib().orc_csg_retain(acc.ctypes.data, field, nx, ny, nz, iso, CSG_OPS.get(op, op))
+    else:
+        lib().orc_csg_retain_band(acc.ctypes.data, field, nx, ny, nz, iso, float(band[0]), float(band[1]),
+                                  CSG_OPS.get(op, op))
     return acc
 
 

@@ -726,6 +726,44 @@ void orc_csg_retain(orc_csg_point* acc, const float* f, uint32_t nx, uint32_t ny
   }
 }
 
+// classify_copy_Voxel, lattice-band ("dynamic") mode (src/MarchingCubes_kernel.cu:
+// 158-447 with dynamic = true; its `fixed` flag is not read): the object is the
+// open band iso1 < L < iso2 of the lattice field L.  Union: band or old inside;
+// difference: band and old outside (the kernel's own pairing, :206-215);
+// intersection: band and old inside.  On each +x, +y, +z edge the fraction is
+// taken where L crosses iso1, else where it crosses iso2 (the same crossing
+// test and fraction as the static mode, per band edge), and replaces or is
+// averaged with the stored one.
+void orc_csg_retain_band(orc_csg_point* acc, const float* lat, uint32_t nx, uint32_t ny, uint32_t nz, float iso,
+                         float iso1, float iso2, uint32_t op) {
+  const uint64_t plane = (uint64_t)nx * ny, total = plane * nz;
+  for (uint64_t i = 0; i + 1 < total; ++i) {
+    const uint32_t x = (uint32_t)(i % nx), y = (uint32_t)((i / nx) % ny), z = (uint32_t)(i / plane);
+    orc_csg_point pt = acc[i];
+    const float v = lat[i];
+    const bool band = (v > iso1) && (v < iso2);
+    bool inside;
+    if (op == 1) inside = band && ((float)pt.val >= iso);
+    else if (op == 2) inside = band && ((float)pt.val < iso);
+    else inside = band || ((float)pt.val < iso);
+    pt.val = inside ? -1 : 1;
+    const uint64_t stride[3] = {1, nx, plane};
+    const bool has[3] = {x + 1 < nx, y + 1 < ny, z + 1 < nz};
+    for (int a = 0; a < 3; ++a) {
+      if (!has[a]) continue;
+      const float w = lat[i + stride[a]];
+      auto crosses = [&](float lev) { return (w < lev && v >= lev) || (w >= lev && v < lev); };
+      float lev;
+      if (crosses(iso1)) lev = iso1;
+      else if (crosses(iso2)) lev = iso2;
+      else continue;
+      const float t = (lev - v) / (w - v);
+      pt.t[a] = pt.t[a] > 0 ? (float)((double)(pt.t[a] + t) * 0.5) : t;
+    }
+    acc[i] = pt;
+  }
+}
+
 // Meshes of the accumulator: classifyVoxel and generateTriangles_lattice_kernel
 // (src/MarchingCubes_kernel.cu:869-1052, 1865-2200) in their make_region mode
 // (field == NULL) and their plain primitive mode (fixed = dynamic = false): the

@@ -93,6 +93,9 @@ typedef struct orc_csg_point {
 } orc_csg_point;
 void orc_csg_retain(orc_csg_point* acc, const float* field, uint32_t nx, uint32_t ny, uint32_t nz, float iso,
                     uint32_t op);
+/* The same fold with the open band iso1 < lattice < iso2 as the object. */
+void orc_csg_retain_band(orc_csg_point* acc, const float* lattice, uint32_t nx, uint32_t ny, uint32_t nz, float iso,
+                         float iso1, float iso2, uint32_t op);
 /* field NULL: region mesh; else the accumulator combined with field by op.
  * Returns the vertex total; writes the triangles whose vertices fit. */
 uint64_t orc_mesh_retained(const orc_csg_point* acc, const float* field, uint32_t op, uint32_t nx, uint32_t ny,

@@ -442,7 +442,10 @@ void run_normalise_four(Reader& r, Writer& w, CUmodule gr) {
 // scans, compactVoxels, generateTriangles_lattice_kernel, in the make_region
 // mode (mode 0) or the plain primitive mode with one more primitive field
 // (mode 1).  Unused field arguments get zeroed buffers (the kernels read them).
-void run_retain(Reader& r, Writer& w, CUmodule mc, const Tables& T) {
+// kind 10 is kind 7 with, per fold, the mode (0 static, 1 lattice band) and
+// the band edges iso1, iso2 before the field; a band fold passes the field as
+// classify_copy_Voxel's vol_lattice with dynamic = true.
+void run_retain(Reader& r, Writer& w, CUmodule mc, const Tables& T, bool banded) {
   U3 g{r.get<uint32_t>(), r.get<uint32_t>(), r.get<uint32_t>()};
   float iso = r.get<float>();
   F3 vs{r.get<float>(), r.get<float>(), r.get<float>()};
@@ -456,11 +459,18 @@ void run_retain(Reader& r, Writer& w, CUmodule mc, const Tables& T) {
   CUfunction k_fold = find_kernel(mc, "classify_copy_Voxel");
   for (uint32_t i = 0; i < n_folds; ++i) {
     uint32_t op = r.get<uint32_t>();
+    bool dynamic = false;
+    float iso1 = 0.0f, iso2 = 0.0f;
+    if (banded) {
+      dynamic = r.get<uint32_t>() != 0;
+      iso1 = r.get<float>();
+      iso2 = r.get<float>();
+    }
     auto f = r.arr<float>(P);
     CUdeviceptr d_f = dupload(f);
-    bool fixed = false, dynamic = false, ou = op == 0, od = op == 1, oi = op == 2;
-    float iso1 = 0.0f, iso2 = 0.0f;
-    void* a[] = {&d_verts, &d_acc, &d_f, &d_zero, &fixed, &dynamic, &iso1, &iso2, &g, &shift, &mask, &nvox,
+    bool fixed = false, ou = op == 0, od = op == 1, oi = op == 2;
+    CUdeviceptr d_two = dynamic ? d_zero : d_f, d_lat = dynamic ? d_f : d_zero;
+    void* a[] = {&d_verts, &d_acc, &d_two, &d_lat, &fixed, &dynamic, &iso1, &iso2, &g, &shift, &mask, &nvox,
                  &vs, &iso, const_cast<CUtexObject*>(&T.nverts_tex), &ou, &od, &oi};
     launch(k_fold, blocks_for(P, 1024), 1, 1, 1024, 1, 1, a);
     cuMemFree(d_f);
@@ -760,7 +770,8 @@ int main(int argc, char** argv) {
       case 4: run_primitive(r, w, mdl); break;
       case 5: run_normalise_four(r, w, gr); break;
       case 6: run_mc_timing(r, w, mc, T); break;
-      case 7: run_retain(r, w, mc, T); break;
+      case 7: run_retain(r, w, mc, T, false); break;
+      case 10: run_retain(r, w, mc, T, true); break;
       case 8: run_svl(r, w, gr, false); break;
       case 9: run_svl(r, w, gr, true); break;
       default: die("unknown job kind");

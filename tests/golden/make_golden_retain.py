@@ -9,8 +9,10 @@ Each case folds a seeded sequence of primitive fields into a zeroed
 grid_points accumulator with the reference's classify_copy_Voxel
 (src/MarchingCubes_kernel.cu:158-447) and meshes it with its classifyVoxel,
 compactVoxels and generateTriangles_lattice_kernel (:869-1052, :1594-1608,
-:1865-2200), in the region mode or with one more primitive field (job kind 7
-of oracle/ref/ref_runner.cpp).  Both reference build variants (sm103a SASS and
+:1865-2200), in the region mode or with one more primitive field (job kind 10
+of oracle/ref/ref_runner.cpp).  A fold is static (the field is the object) or
+a lattice band (classify_copy_Voxel's dynamic mode: the open band
+iso1 < field < iso2 is the object).  Both reference build variants (sm103a SASS and
 the Makefile's compute_89 PTX) must agree bit for bit; the sm103a outputs are
 written to ``golden_retain.npz`` with the inputs.
 """
@@ -48,8 +50,16 @@ def box(n, c, h):
                       np.abs(z - c[2]) - h[2]).astype(np.float32)
 
 
+def gyroid(n, period):
+    x, y, z = _grid(n)
+    k = 2.0 * np.pi / period
+    x, y, z = (k * x.astype(np.float64), k * y.astype(np.float64), k * z.astype(np.float64))
+    return (np.sin(x) * np.cos(y) + np.sin(y) * np.cos(z) + np.sin(z) * np.cos(x)).astype(np.float32)
+
+
 def cases():
-    """(name, n, iso, vs, gc, folds [(op, field)], mode, preview op, preview field)."""
+    """(name, n, iso, vs, gc, folds [(op, field) or (op, field, (iso1, iso2))],
+    mode, preview op, preview field)."""
     rng = np.random.default_rng(0xD4A7)
     out = []
     n = (20, 18, 16)
@@ -78,16 +88,52 @@ def cases():
     out.append(("random_region", n, 0.0, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), folds, 0, "union", None))
     out.append(("random_preview", n, 0.0, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), folds[:3], 1, "intersect",
                 rng.uniform(-1, 1, n[::-1]).astype(np.float32)))
+    # lattice-band folds (the dynamic mode)
+    n = (24, 22, 20)
+    g = gyroid(n, 10.0)
+    a = sphere(n, (9.3, 10.1, 8.6), 6.2)
+    c = sphere(n, (14.5, 9.2, 11.1), 4.1)
+    b = box(n, (12.2, 11.4, 9.3), (5.6, 4.9, 6.1))
+    e = sphere(n, (8.6, 12.3, 10.4), 4.3)
+    out.append(("band_region", n, 0.0, (0.5, 0.5, 0.5), (0.0, 0.0, 0.0),
+                [("union", a), ("union", g, (-0.35, 0.35)), ("subtract", c)], 0, "union", None))
+    out.append(("band_diff_preview", n, 0.0, (0.5, 0.5, 0.5), (0.0, 0.0, 0.0),
+                [("union", b), ("subtract", g, (-0.3, 0.3))], 1, "union", e))
+    out.append(("band_intersect_region", n, 0.0, (1.0, 1.0, 1.0), (1.0, -2.0, 0.5),
+                [("union", sphere(n, (12.0, 11.0, 10.0), 9.5)), ("intersect", g, (-0.5, 0.5))], 0, "union", None))
+    # integer lattice values: samples exactly at the band edges, crossings onto them
+    n = (14, 13, 12)
+    x, y, z = _grid(n)
+    gi = (np.mod(x + 2 * y + 3 * z, 5.0) - 2.0).astype(np.float32)
+    out.append(("band_exact", n, 0.0, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0),
+                [("union", sphere(n, (6, 6, 5), 4)), ("union", gi, (-1.0, 1.0)), ("subtract", gi, (0.0, 2.0))], 0,
+                "union", None))
+    # random fields, static and band folds mixed
+    n = (17, 15, 13)
+    folds = []
+    for k in range(6):
+        op = ["union", "subtract", "intersect"][int(rng.integers(0, 3))]
+        f = rng.uniform(-1, 1, n[::-1]).astype(np.float32)
+        folds.append((op, f, (-0.25, 0.3)) if k % 2 else (op, f))
+    out.append(("band_random_region", n, 0.0, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), folds, 0, "union", None))
+    out.append(("band_random_preview", n, 0.0, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), folds[:4], 1, "subtract",
+                rng.uniform(-1, 1, n[::-1]).astype(np.float32)))
     return out
+
+
+def fold_band(fold):
+    """(dynamic, iso1, iso2) of a fold tuple."""
+    return (1, float(fold[2][0]), float(fold[2][1])) if len(fold) > 2 else (0, 0.0, 0.0)
 
 
 def build_job():
     parts, meta = [], []
     for name, n, iso, vs, gc, folds, mode, pop, pf in cases():
-        b = MG._p("I", 7) + MG._p("3I", *n) + MG._p("f", iso) + MG._p("3f", *vs) + MG._p("3f", *gc)
+        b = MG._p("I", 10) + MG._p("3I", *n) + MG._p("f", iso) + MG._p("3f", *vs) + MG._p("3f", *gc)
         b += MG._p("I", len(folds))
-        for op, f in folds:
-            b += MG._p("I", OPS[op]) + f.astype("<f4").tobytes()
+        for fold in folds:
+            dyn, i1, i2 = fold_band(fold)
+            b += MG._p("I", OPS[fold[0]]) + MG._p("I", dyn) + MG._p("2f", i1, i2) + fold[1].astype("<f4").tobytes()
         b += MG._p("2I", mode, OPS[pop])
         if mode == 1:
             b += pf.astype("<f4").tobytes()
@@ -100,7 +146,7 @@ def parse(blob, meta):
     B = MG.Buf(blob)
     res = []
     for c in meta:
-        assert int(B.u32()) == 7
+        assert int(B.u32()) == 10
         P = c["n"][0] * c["n"][1] * c["n"][2]
         r = dict(meta=c, acc=B.arr(np.int32, 4 * P).reshape(*c["n"][::-1], 4))
         nvox, act, tot = int(B.u32()), int(B.u32()), int(B.u32())
@@ -143,8 +189,9 @@ def main():
         pre = f"case{i}/"
         d[pre + "params"] = np.array([*c["n"], c["iso"], *c["vs"], *c["gc"], c["mode"], OPS[c["pop"]]], np.float64)
         d[pre + "name"] = np.array(c["name"])
-        d[pre + "fold_ops"] = np.array([OPS[op] for op, _ in c["folds"]], np.int32)
-        d[pre + "fold_fields"] = np.stack([f for _, f in c["folds"]])
+        d[pre + "fold_ops"] = np.array([OPS[fold[0]] for fold in c["folds"]], np.int32)
+        d[pre + "fold_fields"] = np.stack([fold[1] for fold in c["folds"]])
+        d[pre + "fold_band"] = np.array([fold_band(fold) for fold in c["folds"]], np.float32)
         if c["pf"] is not None:
             d[pre + "preview_field"] = c["pf"]
         for k in ("acc", "verts", "occ", "compacted", "pos", "norm"):

@@ -31,8 +31,8 @@ def test_retained_matches_reference(ctx, i):
     R = golden("golden_retain.npz")
     pre, n, iso, vs, gc, folds, pf, pop = case(i)
     acc = ctx.csg_accumulator(n[::-1])
-    for op, f in folds:
-        ctx.csg_retain(acc, dev(f), OPS[int(op)], iso)
+    for op, f, band in folds:
+        ctx.csg_retain(acc, dev(f), OPS[int(op)], iso, band=band)
     assert acc.cpu().numpy().tobytes() == R[pre + "acc"].tobytes()
     pos, norm, cnt = ctx.mesh_retained(acc, None if pf is None else dev(pf), pop, iso, vs, gc)
     assert cnt.active_voxels == len(R[pre + "compacted"])
@@ -86,3 +86,30 @@ def test_retained_rejects_misaligned_accumulator(ctx):
     rc = ctx.lib.gcm_count_retained(ctx.h, C.c_void_p(bad.data_ptr()), None, 0, C.byref(g), 0.0, C.byref(c),
                                     C.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == N.GCM_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("shape", [(33, 29, 41), (2, 3, 70), (96, 80, 72)])
+@pytest.mark.parametrize("op", ["union", "subtract", "intersect"])
+def test_band_folds_vs_oracle(ctx, shape, op):
+    """Lattice-band folds (the reference's dynamic mode) on ragged grids: the
+    accumulator and the region mesh equal the oracle's bit for bit."""
+    rng = np.random.default_rng(sum(shape) + len(op) + 7)
+    nz, ny, nx = shape
+    z, y, x = np.meshgrid(np.arange(nz, dtype=np.float64), np.arange(ny, dtype=np.float64),
+                          np.arange(nx, dtype=np.float64), indexing="ij")
+    k = 2 * np.pi / rng.uniform(6, 14)
+    gyr = (np.sin(k * x) * np.cos(k * y) + np.sin(k * y) * np.cos(k * z) + np.sin(k * z) * np.cos(k * x)).astype(np.float32)
+    c = rng.uniform(0, 1, 3) * np.array([nx, ny, nz])
+    r = 0.4 * min(nx, ny, nz) + 1.0
+    sph = ((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2 - r * r).astype(np.float32)
+    folds = [("union", sph, None), (op, gyr, (-0.3, 0.35)), ("union", gyr + 0.5, (0.0, 0.4))]
+    acc_o = O.csg_accumulator(shape)
+    acc_g = ctx.csg_accumulator(shape)
+    for fop, f, band in folds:
+        O.csg_retain(acc_o, f, fop, 0.0, band=band)
+        ctx.csg_retain(acc_g, dev(f), fop, 0.0, band=band)
+    assert acc_g.cpu().numpy().tobytes() == acc_o.tobytes()
+    opos, onorm, oact = O.mesh_retained(acc_o, None, "union", (1, 1, 1), (0, 0, 0))
+    pos, norm, cnt = ctx.mesh_retained(acc_g, None, "union", 0.0)
+    assert cnt.active_voxels == oact and cnt.total_verts == len(opos)
+    assert pos.cpu().numpy().tobytes() == opos.tobytes() and norm.cpu().numpy().tobytes() == onorm.tobytes()

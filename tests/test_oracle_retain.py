@@ -22,7 +22,10 @@ def case(i):
     p = R[pre + "params"]
     n = tuple(int(v) for v in p[:3])
     iso, vs, gc, mode, pop = float(p[3]), tuple(p[4:7]), tuple(p[7:10]), int(p[10]), int(p[11])
-    folds = list(zip(R[pre + "fold_ops"], R[pre + "fold_fields"]))
+    bands = R[pre + "fold_band"] if pre + "fold_band" in R.files else np.zeros((len(R[pre + "fold_ops"]), 3))
+    # (op, field, band): band (iso1, iso2) for a lattice-band fold, else None
+    folds = [(op, f, (float(b[1]), float(b[2])) if b[0] else None)
+             for op, f, b in zip(R[pre + "fold_ops"], R[pre + "fold_fields"], bands)]
     pf = R[pre + "preview_field"] if mode == 1 else None
     return pre, n, iso, vs, gc, folds, pf, OPS[pop]
 
@@ -31,9 +34,13 @@ def case(i):
 def test_accumulator_bit_exact(i):
     pre, n, iso, vs, gc, folds, pf, pop = case(i)
     acc = O.csg_accumulator(n[::-1])
-    for op, f in folds:
-        O.csg_retain(acc, f, OPS[int(op)], iso)
+    for op, f, band in folds:
+        O.csg_retain(acc, f, OPS[int(op)], iso, band=band)
     assert acc.tobytes() == R[pre + "acc"].tobytes()
+
+
+def test_fixtures_hold_band_folds():
+    assert any(b is not None for i in range(n_cases()) for _, _, b in case(i)[5])
 
 
 @pytest.mark.parametrize("i", range(n_cases()))
