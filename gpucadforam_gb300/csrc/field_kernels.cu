@@ -835,18 +835,21 @@ __global__ void __launch_bounds__(kCsgWarps * 32, 4) csg_kernel(CsgParams p) {
   uint8_t* s_list = s_perm + n;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   for (uint32_t i = tid; i < n; i += blockDim.x) prim_setup(p.prims[i], s_pre[i]);
-  if (tid == 0) {
-    for (uint32_t i = 0; i < n;) {
-      uint32_t j = i + 1;
-      while (j < n && csg_op(p.prims[j].op) == csg_op(p.prims[i].op)) ++j;
-      s_run[i] = (uint16_t)j;
-      i = j;
+  __syncthreads();
+  for (uint32_t i = tid; i < n; i += blockDim.x) {
+    const uint32_t op = csg_op(s_pre[i].op), kind = min(s_pre[i].kind, 7u);
+    // end of the run of equal operations that starts here (read only at run starts)
+    uint32_t j = i + 1;
+    while (j < n && csg_op(s_pre[j].op) == op) ++j;
+    s_run[i] = (uint16_t)j;
+    // place in kind order, so that a warp's lanes mostly share a kind when
+    // they compute enclosures
+    uint32_t rank = 0;
+    for (uint32_t k = 0; k < n; ++k) {
+      const uint32_t kk = min(s_pre[k].kind, 7u);
+      rank += (kk < kind || (kk == kind && k < i)) ? 1u : 0u;
     }
-    // enclosures are computed in kind order, so a warp's lanes mostly share a kind
-    uint32_t c = 0;
-    for (uint32_t kind = 0; kind < 8; ++kind)
-      for (uint32_t i = 0; i < n; ++i)
-        if (min(p.prims[i].kind, 7u) == kind) s_perm[c++] = (uint8_t)i;
+    s_perm[rank] = (uint8_t)i;
   }
   __syncthreads();
   float2* lu = s_lu + (size_t)warp * n;
