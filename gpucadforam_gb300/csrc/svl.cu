@@ -308,6 +308,11 @@ __global__ void __launch_bounds__(kBlock) svl_reduce_kernel(const float* __restr
 // x = 1 x + alpha d, r = 1 r + (-alpha) q (VecSMultAddKernel_lattice,
 // Gratings.cu:77-97: a1 * V + a2 * W, the first product fused with the sum of
 // the second), and the block partials of r . r.
+__device__ __forceinline__ float upd_x(float x, float alpha, float d) { return __fmaf_rn(1.0f, x, __fmul_rn(alpha, d)); }
+__device__ __forceinline__ float upd_r(float r, float alpha, float q) {
+  return __fmaf_rn(1.0f, r, __fmul_rn(-alpha, q));
+}
+
 __global__ void __launch_bounds__(kBlock) svl_update_kernel(float* __restrict__ x, float* __restrict__ r,
                                                             const float* __restrict__ d, const float* __restrict__ q,
                                                             float* __restrict__ part, const CgState* st, uint64_t P,
@@ -320,8 +325,8 @@ __global__ void __launch_bounds__(kBlock) svl_update_kernel(float* __restrict__ 
   const float alpha = st[b].alpha;
   float c = 0.0f;
   if (t < P) {
-    x[base + t] = __fmaf_rn(1.0f, x[base + t], __fmul_rn(alpha, d[base + t]));
-    const float rv = __fmaf_rn(1.0f, r[base + t], __fmul_rn(-alpha, q[base + t]));
+    x[base + t] = upd_x(x[base + t], alpha, d[base + t]);
+    const float rv = upd_r(r[base + t], alpha, q[base + t]);
     r[base + t] = rv;
     c = __fmul_rn(rv, rv);
   }
@@ -329,16 +334,79 @@ __global__ void __launch_bounds__(kBlock) svl_update_kernel(float* __restrict__ 
   if (threadIdx.x == 0) part[(uint64_t)b * nblk + blockIdx.x] = s;
 }
 
+// The same with 16-byte accesses (P a multiple of 4): a block of 256 threads
+// covers the reference's 1024-element reduction block, thread i holding
+// elements 4i .. 4i+3.  The tree pairs element t with t + s for s = 512 .. 1,
+// which is: across the 8 warps (s = 512, 256, 128), across lanes
+// (s = 64 .. 4, shuffles) and inside a thread's four (s = 2, 1).
+constexpr int kBlock4 = kBlock / 4;
+
+__global__ void __launch_bounds__(kBlock4) svl_update4_kernel(float4* __restrict__ x, float4* __restrict__ r,
+                                                              const float4* __restrict__ d,
+                                                              const float4* __restrict__ q, float* __restrict__ part,
+                                                              const CgState* st, uint64_t P4, uint32_t nblk) {
+  __shared__ float4 cc[kBlock4];
+  const uint32_t b = blockIdx.y;
+  if (!st[b].active) return;
+  const uint64_t base = (uint64_t)b * P4;
+  const uint64_t t = (uint64_t)blockIdx.x * kBlock4 + threadIdx.x;
+  const float alpha = st[b].alpha;
+  float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (t < P4) {
+    const float4 xv = x[base + t], dv = d[base + t], rv0 = r[base + t], qv = q[base + t];
+    x[base + t] = make_float4(upd_x(xv.x, alpha, dv.x), upd_x(xv.y, alpha, dv.y), upd_x(xv.z, alpha, dv.z),
+                              upd_x(xv.w, alpha, dv.w));
+    const float4 rv = make_float4(upd_r(rv0.x, alpha, qv.x), upd_r(rv0.y, alpha, qv.y), upd_r(rv0.z, alpha, qv.z),
+                                  upd_r(rv0.w, alpha, qv.w));
+    r[base + t] = rv;
+    c = make_float4(__fmul_rn(rv.x, rv.x), __fmul_rn(rv.y, rv.y), __fmul_rn(rv.z, rv.z), __fmul_rn(rv.w, rv.w));
+  }
+  cc[threadIdx.x] = c;
+  __syncthreads();
+  if (threadIdx.x >= 32) return;
+  const uint32_t lane = threadIdx.x;
+  auto add4 = [](float4 u, float4 v) {
+    return make_float4(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y), __fadd_rn(u.z, v.z), __fadd_rn(u.w, v.w));
+  };
+  float4 v[8];
+#pragma unroll
+  for (int w = 0; w < 8; ++w) v[w] = cc[32 * w + lane];
+#pragma unroll
+  for (int h = 4; h > 0; h >>= 1)
+#pragma unroll
+    for (int w = 0; w < h; ++w) v[w] = add4(v[w], v[w + h]);
+  float4 a = v[0];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float4 o4 = make_float4(__shfl_down_sync(0xffffffffu, a.x, o), __shfl_down_sync(0xffffffffu, a.y, o),
+                                  __shfl_down_sync(0xffffffffu, a.z, o), __shfl_down_sync(0xffffffffu, a.w, o));
+    a = add4(a, o4);
+  }
+  if (lane == 0) part[(uint64_t)b * nblk + blockIdx.x] = __fadd_rn(__fadd_rn(a.x, a.z), __fadd_rn(a.y, a.w));
+}
+
 // d = beta d + 1 r, and the decision to take another step
 // (the while condition of GPUCG_lattice, Gratings.cu:910-969).
+__device__ __forceinline__ float dir_d(float beta, float d, float r) { return __fmaf_rn(beta, d, __fmul_rn(1.0f, r)); }
+
 __global__ void __launch_bounds__(256) svl_dir_kernel(float* __restrict__ d, const float* __restrict__ r, CgState* st,
                                                       uint64_t P, uint32_t max_iter) {
   const uint32_t b = blockIdx.y;
   if (!st[b].active) return;
   const uint64_t base = (uint64_t)b * P;
   const float beta = st[b].beta;
+  if ((P & 3u) == 0) {
+    float4* d4 = reinterpret_cast<float4*>(d + base);
+    const float4* r4 = reinterpret_cast<const float4*>(r + base);
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < P / 4; t += (uint64_t)gridDim.x * blockDim.x) {
+      const float4 dv = d4[t], rv = r4[t];
+      d4[t] = make_float4(dir_d(beta, dv.x, rv.x), dir_d(beta, dv.y, rv.y), dir_d(beta, dv.z, rv.z),
+                          dir_d(beta, dv.w, rv.w));
+    }
+    return;
+  }
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < P; t += (uint64_t)gridDim.x * blockDim.x)
-    d[base + t] = __fmaf_rn(beta, d[base + t], __fmul_rn(1.0f, r[base + t]));
+    d[base + t] = dir_d(beta, d[base + t], r[base + t]);
 }
 
 __global__ void svl_decide_kernel(CgState* st, uint32_t n, uint32_t max_iter, uint32_t* n_active) {
@@ -532,7 +600,12 @@ gcm_status gcm_svl_lattice(gcm_ctx* ctx, const gcm_svl_params* prm, const float*
     svl_matvec_kernel<<<gv, kBlock, 0, cap>>>(dd, q, part, cs, g.nx, g.ny, g.nz, make_fastdiv(p.nx),
                                               make_fastdiv(p.nx * p.ny), P, nblk);
     svl_reduce_kernel<<<B, kBlock, 0, cap>>>(part, cs, nblk, 0, p.max_iter);
-    svl_update_kernel<<<gv, kBlock, 0, cap>>>(x, r, dd, q, part, cs, P, nblk);
+    if ((P & 3u) == 0)
+      svl_update4_kernel<<<gv, kBlock4, 0, cap>>>(reinterpret_cast<float4*>(x), reinterpret_cast<float4*>(r),
+                                                 reinterpret_cast<const float4*>(dd),
+                                                 reinterpret_cast<const float4*>(q), part, cs, P / 4, nblk);
+    else
+      svl_update_kernel<<<gv, kBlock, 0, cap>>>(x, r, dd, q, part, cs, P, nblk);
     svl_reduce_kernel<<<B, kBlock, 0, cap>>>(part, cs, nblk, 1, p.max_iter);
     svl_dir_kernel<<<dim3(grid_blocks(ctx, P, 256, 4), B), 256, 0, cap>>>(dd, r, cs, P, p.max_iter);
     svl_decide_kernel<<<(B + 127) / 128, 128, 0, cap>>>(cs, B, p.max_iter, n_active);

@@ -49,7 +49,7 @@ def test_coefficients_match_oracle_dft(ctx):
     assert np.abs(got - G["coef"]).max() < 2e-7
 
 
-@pytest.mark.parametrize("shape", [(32, 24, 16), (20, 12, 9)])
+@pytest.mark.parametrize("shape", [(32, 24, 16), (20, 12, 9), (9, 7, 5)])  # the last: P not a multiple of 4
 def test_svl_vs_oracle(ctx, shape):
     p = O.svl_params(shape, "n", 1, 8.0, (7.0, 9.5, 6.0), n_coeff=40)
     coef = G["coef"]
