@@ -197,12 +197,16 @@ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
 // per axis the centre weight and the two neighbour terms of the reference's
 // boundary-dependent stencil; A_X = (wx + wy + wz) * d0 + the six neighbour
 // terms, left to right, the first addition fused with the product.
+// The five cases (c = 0, 1, n-2, n-1, interior; n >= 4) as selects of the
+// neighbour offsets and weights, so boundary lanes do not diverge: each term
+// is a neighbour times -1 or -0.25 (exact), as in the case-by-case form.
 __device__ __forceinline__ void axis_terms(const float* dv, int c, int n, int stride, float& w, float& t2, float& t3) {
-  if (c == 0) { w = 1.25f; t2 = -dv[stride]; t3 = -0.25f * dv[2 * stride]; }
-  else if (c == 1) { w = 1.25f; t2 = -dv[-stride]; t3 = -0.25f * dv[2 * stride]; }
-  else if (c == n - 2) { w = 1.25f; t2 = -0.25f * dv[-2 * stride]; t3 = -dv[stride]; }
-  else if (c == n - 1) { w = 1.25f; t2 = -0.25f * dv[-2 * stride]; t3 = -dv[-stride]; }
-  else { w = 0.5f; t2 = -0.25f * dv[-2 * stride]; t3 = -0.25f * dv[2 * stride]; }
+  const bool lo = c <= 1, hi = !lo && c >= n - 2;
+  const int o2 = c == 0 ? stride : (c == 1 ? -stride : -2 * stride);
+  const int o3 = lo ? 2 * stride : (c == n - 2 ? stride : (c == n - 1 ? -stride : 2 * stride));
+  w = (lo || hi) ? 1.25f : 0.5f;
+  t2 = (lo ? -1.0f : -0.25f) * dv[o2];
+  t3 = (hi ? -1.0f : -0.25f) * dv[o3];
 }
 
 __device__ __forceinline__ float matvec_at(const float* __restrict__ d, int tx, int X, int Y, int Z, const FastDiv& dx,
