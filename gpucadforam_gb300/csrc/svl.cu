@@ -280,6 +280,107 @@ __global__ void __launch_bounds__(kBlock) svl_matvec_kernel(const float* __restr
   if (threadIdx.x == 0) part[(uint64_t)b * nblk + blockIdx.x] = s;
 }
 
+// Neighbour offsets and weights along one axis for sample position c (the
+// selects of axis_terms), for the four-sample form.
+struct AxisCase {
+  int o2, o3;
+  float w, k2, k3;
+};
+__device__ __forceinline__ AxisCase axis_case(int c, int n) {
+  const bool lo = c <= 1, hi = !lo && c >= n - 2;
+  AxisCase a;
+  a.o2 = c == 0 ? 1 : (c == 1 ? -1 : -2);
+  a.o3 = lo ? 2 : (c == n - 2 ? 1 : (c == n - 1 ? -1 : 2));
+  a.w = (lo || hi) ? 1.25f : 0.5f;
+  a.k2 = lo ? -1.0f : -0.25f;
+  a.k3 = hi ? -1.0f : -0.25f;
+  return a;
+}
+
+__device__ __forceinline__ float f4c(const float4& v, int j) { return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w)); }
+
+// Block tree of four values per thread over a 256-thread block with the
+// reference's pairs for its 1024 elements (see svl_update4_kernel); thread 0
+// returns the sum.
+__device__ __forceinline__ float block_tree4(float4 c, float4* cc) {
+  cc[threadIdx.x] = c;
+  __syncthreads();
+  if (threadIdx.x >= 32) return 0.0f;
+  const uint32_t lane = threadIdx.x;
+  auto add4 = [](float4 u, float4 v) {
+    return make_float4(__fadd_rn(u.x, v.x), __fadd_rn(u.y, v.y), __fadd_rn(u.z, v.z), __fadd_rn(u.w, v.w));
+  };
+  float4 v[8];
+#pragma unroll
+  for (int w = 0; w < 8; ++w) v[w] = cc[32 * w + lane];
+#pragma unroll
+  for (int h = 4; h > 0; h >>= 1)
+#pragma unroll
+    for (int w = 0; w < h; ++w) v[w] = add4(v[w], v[w + h]);
+  float4 a = v[0];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float4 o4 = make_float4(__shfl_down_sync(0xffffffffu, a.x, o), __shfl_down_sync(0xffffffffu, a.y, o),
+                                  __shfl_down_sync(0xffffffffu, a.z, o), __shfl_down_sync(0xffffffffu, a.w, o));
+    a = add4(a, o4);
+  }
+  return __fadd_rn(__fadd_rn(a.x, a.z), __fadd_rn(a.y, a.w));
+}
+
+// q = A d and the block partials of d . q, four consecutive samples of one
+// row per thread (X a multiple of 4): the x neighbours come from the 12
+// values d[t-4 .. t+7] (three 16-byte loads; the outer two are needed, and
+// read, only away from the row ends), the y and z neighbours from two 16-byte
+// loads per axis.  Same terms, same order as matvec_at.
+__global__ void __launch_bounds__(kBlock / 4) svl_matvec4_kernel(const float* __restrict__ d, float* __restrict__ q,
+                                                                 float* __restrict__ part, const CgState* st, int X,
+                                                                 int Y, int Z, FastDiv dx, FastDiv dxy, uint64_t P,
+                                                                 uint32_t nblk) {
+  __shared__ float4 cc[kBlock / 4];
+  const uint32_t b = blockIdx.y;
+  if (!st[b].active) return;
+  const uint64_t base = (uint64_t)b * P;
+  const uint64_t t = 4ull * ((uint64_t)blockIdx.x * (kBlock / 4) + threadIdx.x);
+  float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (t < P) {
+    const float* dv = d + base + t;
+    const int row = (int)fdiv((uint32_t)t, dx), zi = (int)fdiv((uint32_t)t, dxy);
+    const int x0 = (int)t - row * X, yi = row - zi * Y, XY = X * Y;
+    const float4 mid = *reinterpret_cast<const float4*>(dv);
+    const float4 left = x0 > 0 ? *reinterpret_cast<const float4*>(dv - 4) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float4 right = x0 + 4 < X ? *reinterpret_cast<const float4*>(dv + 4) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    auto win = [&](int k) {  // d[t + k - 4], k in [0, 12)
+      return k < 4 ? f4c(left, k) : (k < 8 ? f4c(mid, k - 4) : f4c(right, k - 8));
+    };
+    const AxisCase ay = axis_case(yi, Y), az = axis_case(zi, Z);
+    const float4 y2v = *reinterpret_cast<const float4*>(dv + ay.o2 * X);
+    const float4 y3v = *reinterpret_cast<const float4*>(dv + ay.o3 * X);
+    const float4 z2v = *reinterpret_cast<const float4*>(dv + (int64_t)az.o2 * XY);
+    const float4 z3v = *reinterpret_cast<const float4*>(dv + (int64_t)az.o3 * XY);
+    float a[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const AxisCase ax = axis_case(x0 + j, X);
+      // the x neighbours at offsets o2, o3 in {-2, -1, +1, +2}, as selects
+      const float n2 = ax.o2 == 1 ? win(5 + j) : (ax.o2 == -1 ? win(3 + j) : win(2 + j));
+      const float n3 = ax.o3 == 2 ? win(6 + j) : (ax.o3 == 1 ? win(5 + j) : win(3 + j));
+      const float x2 = ax.k2 * n2, x3 = ax.k3 * n3;
+      const float y2 = ay.k2 * f4c(y2v, j), y3 = ay.k3 * f4c(y3v, j);
+      const float z2 = az.k2 * f4c(z2v, j), z3 = az.k3 * f4c(z3v, j);
+      float s = __fmaf_rn(__fadd_rn(__fadd_rn(ax.w, ay.w), az.w), f4c(mid, j), x2);
+      s = __fadd_rn(s, x3);
+      s = __fadd_rn(s, y2);
+      s = __fadd_rn(s, y3);
+      s = __fadd_rn(s, z2);
+      a[j] = __fadd_rn(s, z3);
+    }
+    *reinterpret_cast<float4*>(q + base + t) = make_float4(a[0], a[1], a[2], a[3]);
+    c = make_float4(__fmul_rn(mid.x, a[0]), __fmul_rn(mid.y, a[1]), __fmul_rn(mid.z, a[2]), __fmul_rn(mid.w, a[3]));
+  }
+  const float s = block_tree4(c, cc);
+  if (threadIdx.x == 0) part[(uint64_t)b * nblk + blockIdx.x] = s;
+}
+
 // Final reduction of a solve's block partials (Reduction_lattice,
 // Gratings.cu:22-75), then the scalar step: kind 0 -> alpha = delta_new /
 // (d . q); kind 1 -> delta_old = delta_new, delta_new = r . r,
@@ -601,8 +702,12 @@ gcm_status gcm_svl_lattice(gcm_ctx* ctx, const gcm_svl_params* prm, const float*
   if (e == cudaSuccess) e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaMemsetAsync(n_active, 0, sizeof(uint32_t), cap);
-    svl_matvec_kernel<<<gv, kBlock, 0, cap>>>(dd, q, part, cs, g.nx, g.ny, g.nz, make_fastdiv(p.nx),
-                                              make_fastdiv(p.nx * p.ny), P, nblk);
+    if ((p.nx & 3u) == 0)
+      svl_matvec4_kernel<<<gv, kBlock / 4, 0, cap>>>(dd, q, part, cs, g.nx, g.ny, g.nz, make_fastdiv(p.nx),
+                                                     make_fastdiv(p.nx * p.ny), P, nblk);
+    else
+      svl_matvec_kernel<<<gv, kBlock, 0, cap>>>(dd, q, part, cs, g.nx, g.ny, g.nz, make_fastdiv(p.nx),
+                                                make_fastdiv(p.nx * p.ny), P, nblk);
     svl_reduce_kernel<<<B, kBlock, 0, cap>>>(part, cs, nblk, 0, p.max_iter);
     if ((P & 3u) == 0)
       svl_update4_kernel<<<gv, kBlock4, 0, cap>>>(reinterpret_cast<float4*>(x), reinterpret_cast<float4*>(r),
