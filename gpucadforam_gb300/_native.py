@@ -131,6 +131,8 @@ PROTOTYPES = {
     "gcm_svl_lattice": (I32, [P, C.POINTER(GcmSvlParams), P, P, P, P, P, P]),
     "gcm_mesh_retained": (I32, [P, P, P, U32, C.POINTER(GcmGrid), F32, P, P, U64, C.POINTER(GcmCounts), P]),
     "gcm_count_retained": (I32, [P, P, P, U32, C.POINTER(GcmGrid), F32, C.POINTER(GcmCounts), P]),
+    "gcm_mesh_lattice_preview": (I32, [P, P, P, P, U32, C.POINTER(GcmGrid), F32, F32, F32, P, P, U64,
+                                      C.POINTER(GcmCounts), P]),
     "gcm_test_lookback_stall": (I32, [P, U32, U32, U64, P, P]),
     "gcm_batch_create": (I32, [P, P, U32, C.POINTER(P)]),
     "gcm_batch_destroy": (I32, [P]),

@@ -439,6 +439,31 @@ gcm_status gcm_count_retained(gcm_ctx* ctx, const gcm_csg_point* d_acc, const fl
                        h_counts, stream);
 }
 
+gcm_status gcm_mesh_lattice_preview(gcm_ctx* ctx, const gcm_csg_point* d_acc, const float* d_field,
+                                    const float* d_lattice, gcm_csg_op op, const gcm_grid* grid, float iso,
+                                    float band_lo, float band_hi, float* d_pos, float* d_norm, uint64_t capacity,
+                                    gcm_counts* h_counts, gcm_stream stream) {
+  static const char* who = "gcm_mesh_lattice_preview";
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_lattice || !h_counts || (d_acc != nullptr) == (d_field != nullptr) || (capacity && (!d_pos || !d_norm)))
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT,
+                "%s: needs a lattice, counts, and exactly one of the accumulator or a primitive field", who);
+  if (d_acc && (reinterpret_cast<uintptr_t>(d_acc) & 15u) != 0)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "%s: the accumulator must be 16-byte aligned", who);
+  if (op > GCM_CSG_INTERSECT) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "%s: unknown op %u", who, (unsigned)op);
+  gcm_status s = check_grid(ctx, grid);
+  if (s) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  gcm_counts* used = nullptr;
+  const int mode = d_acc ? kMeshLatDynamic : kMeshLatFixed;
+  const float* f = d_acc ? reinterpret_cast<const float*>(d_acc) : d_field;
+  const bool emit = capacity > 0;
+  s = mesh_core(ctx, f, d_lattice, grid, iso, band_lo, band_hi, mode, (uint32_t)op, emit, emit ? d_pos : nullptr,
+                emit ? d_norm : nullptr, emit ? capacity : 0, nullptr, st, &used);
+  if (s) return s;
+  return read_counts(ctx, used, h_counts, st);
+}
+
 // ------------------------------------------------------------ staged form
 
 gcm_status gcm_mc_classify(gcm_ctx* ctx, const float* d_field, const gcm_grid* grid, float iso, uint32_t* d_verts,

@@ -203,6 +203,44 @@ __device__ __forceinline__ float3 edge_point_band_v(float id0, float id1, float 
   return p;
 }
 
+// Lattice "fixed" preview edge point (vertexInterp_new, src/MarchingCubes_kernel.cu:
+// 1728-1790): fractions where the primitive field f crosses iso and where the
+// lattice L crosses lo and hi (strict on the lower side), combined as the
+// reference does; (t1 + t) * 0.5 runs in double there, which rounds to the
+// same float as the float product.
+__device__ __forceinline__ float3 edge_point_latfixed(float iso, float lo, float hi, float3 pa, float3 pb, float f0,
+                                                      float f1, float l0, float l1) {
+  float t1 = 0.0f, t2 = 0.0f, t3 = 0.0f;
+  if (((f0 < iso) && (f1 >= iso)) || ((f1 < iso) && (f0 >= iso))) t1 = __fdiv_rn(__fsub_rn(iso, f0), __fsub_rn(f1, f0));
+  if (((l0 < lo) && (l1 >= lo)) || ((l1 < lo) && (l0 >= lo))) t2 = __fdiv_rn(__fsub_rn(lo, l0), __fsub_rn(l1, l0));
+  if (((l0 < hi) && (l1 >= hi)) || ((l1 < hi) && (l0 >= hi))) t3 = __fdiv_rn(__fsub_rn(hi, l0), __fsub_rn(l1, l0));
+  float t = 0.0f;
+  if ((t1 > 0.0f) && (t2 > 0.0f) && (t3 == 0.0f)) t = __fmul_rn(__fadd_rn(t1, t2), 0.5f);
+  else if ((t1 > 0.0f) && (t3 > 0.0f) && (t2 == 0.0f)) t = __fmul_rn(__fadd_rn(t1, t3), 0.5f);
+  else if ((t1 > 0.0f) && (t2 == 0.0f) && (t3 == 0.0f)) t = t1;
+  else if ((t2 > 0.0f) && (t1 == 0.0f) && (t3 == 0.0f)) t = t2;
+  else if ((t3 > 0.0f) && (t1 == 0.0f) && (t2 == 0.0f)) t = t3;
+  return lerp3(pa, pb, t);
+}
+
+// Lattice "dynamic" preview edge point (vertexInterp_primitive_one,
+// src/MarchingCubes_kernel.cu:1676-1726): the stored fraction t1 of the edge's
+// lower corner combined with where the lattice crosses lo, then (overriding
+// where it applies) with where it crosses hi; inclusive crossing tests.
+__device__ __forceinline__ float3 edge_point_latdyn(float lo, float hi, float3 p0, float3 p1, float l0, float l1,
+                                                    float t1) {
+  float t2 = 0.0f, t3 = 0.0f, t = 0.0f;
+  if (((l1 >= lo) && (l0 <= lo)) || ((l0 >= lo) && (l1 <= lo))) t2 = __fdiv_rn(__fsub_rn(lo, l0), __fsub_rn(l1, l0));
+  if ((t1 > 0.0f) && (t2 > 0.0f)) t = __fmul_rn(__fadd_rn(t1, t2), 0.5f);
+  else if ((t1 > 0.0f) && (t2 == 0.0f)) t = t1;
+  else if ((t2 > 0.0f) && (t1 == 0.0f)) t = t2;
+  if (((l1 >= hi) && (l0 <= hi)) || ((l0 >= hi) && (l1 <= hi))) t3 = __fdiv_rn(__fsub_rn(hi, l0), __fsub_rn(l1, l0));
+  if ((t1 > 0.0f) && (t3 > 0.0f)) t = __fmul_rn(__fadd_rn(t1, t3), 0.5f);
+  else if ((t1 > 0.0f) && (t3 == 0.0f)) t = t1;
+  else if ((t3 > 0.0f) && (t1 == 0.0f)) t = t3;
+  return lerp3(p0, p1, t);
+}
+
 // Retained edge point (vertexInterp_primitive, src/MarchingCubes_kernel.cu:
 // 1640-1672): the crossing fraction t2 of the fed field on the edge (inclusive
 // tests on both sides), averaged with the accumulated fraction t1 when both

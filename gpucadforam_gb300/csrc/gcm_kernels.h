@@ -28,10 +28,27 @@ namespace gcm {
 // field + normalised field), and the two meshes of a retained primitive
 // accumulator (gcm_csg_point): its region alone, or its preview combined
 // with a fed primitive field.
-enum MeshMode : int { kMeshPlain = 0, kMeshBand = 1, kMeshRegion = 2, kMeshPreview = 3 };
-__host__ __device__ constexpr bool mode_has_g(int mode) { return mode == kMeshBand || mode == kMeshPreview; }
+// The lattice previews of the retained editor: a primitive field with a lattice
+// band ("fixed"), or the accumulator with a lattice band ("dynamic").
+enum MeshMode : int {
+  kMeshPlain = 0,
+  kMeshBand = 1,
+  kMeshRegion = 2,
+  kMeshPreview = 3,
+  kMeshLatFixed = 4,
+  kMeshLatDynamic = 5
+};
+__host__ __device__ constexpr bool mode_has_g(int mode) {
+  return mode == kMeshBand || mode == kMeshPreview || mode == kMeshLatFixed || mode == kMeshLatDynamic;
+}
 // floats per sample of the classify input (accumulator records are 4 words)
-__host__ __device__ constexpr uint32_t mode_fw(int mode) { return mode >= kMeshRegion ? 4u : 1u; }
+__host__ __device__ constexpr uint32_t mode_fw(int mode) {
+  return (mode == kMeshRegion || mode == kMeshPreview || mode == kMeshLatDynamic) ? 4u : 1u;
+}
+// edges run from the lower corner and carry the stored fraction's offset
+__host__ __device__ constexpr bool mode_lower_edges(int mode) { return mode_fw(mode) == 4u; }
+// generateTriangles_lattice_kernel's normals: calcNormal(v0, v2, v1), w = 0.5
+__host__ __device__ constexpr bool mode_retained_normal(int mode) { return mode >= kMeshRegion; }
 
 // Most voxels in one tile (the triangle list keeps a voxel's index within its
 // tile in 16 bits), as a row limit for rows of vx voxels.

@@ -201,11 +201,27 @@ struct WindowCursor {
 // accumulated sign combined with the fed field (classifyVoxel,
 // src/MarchingCubes_kernel.cu:869-1052): union (val < iso) | (f < iso),
 // difference (f >= iso) & (val < iso), intersection (val < iso) & (f < iso).
+// Lattice previews (the same kernel with `fixed` or `dynamic` set), with the
+// open band lo < L < hi of the lattice field L in g: fixed combines the fed
+// primitive field f with the band (difference (f >= iso) & band); dynamic
+// combines the accumulated sign with it (difference (val < iso) & (L < lo |
+// L > hi), as the reference pairs it).
 template <int MODE>
-__device__ __forceinline__ bool corner_inside(float fval, float gval, uint32_t op, float iso) {
+__device__ __forceinline__ bool corner_inside(float fval, float gval, uint32_t op, float iso, float lo, float hi) {
   if (MODE == kMeshPlain || MODE == kMeshBand) return fval < iso;
+  if (MODE == kMeshLatFixed) {
+    const bool band = (gval > lo) && (gval < hi);
+    if (op == GCM_CSG_SUBTRACT) return (fval >= iso) && band;
+    if (op == GCM_CSG_INTERSECT) return (fval < iso) && band;
+    return (fval < iso) || band;
+  }
   const bool a = (float)__float_as_int(fval) < iso;
   if (MODE == kMeshRegion) return a;
+  if (MODE == kMeshLatDynamic) {
+    if (op == GCM_CSG_SUBTRACT) return a && ((gval < lo) || (gval > hi));
+    if (op == GCM_CSG_INTERSECT) return a && (gval > lo) && (gval < hi);
+    return a || ((gval > lo) && (gval < hi));
+  }
   if (op == GCM_CSG_SUBTRACT) return (gval >= iso) && a;
   if (op == GCM_CSG_INTERSECT) return a && (gval < iso);
   return a || (gval < iso);
@@ -239,7 +255,7 @@ __device__ __forceinline__ void tile_classify(const TileGeom& tg, const MeshLayo
     // the lower coordinate (generateTriangles_lattice_kernel,
     // src/MarchingCubes_kernel.cu:2087-2098).
     const uint32_t e = threadIdx.x - (THREADS - 12);
-    const bool retained = MODE == kMeshRegion || MODE == kMeshPreview;
+    const bool retained = mode_lower_edges(MODE);
     const uint32_t dplane = L.plane_stride + (retained ? n1 - n0 : m1 - m0);
     auto off = [&](uint32_t k) {
       return 4u * ((uint32_t)corner_z((int)k) * dplane + (uint32_t)corner_y((int)k) * nx + (uint32_t)corner_x((int)k));
@@ -274,7 +290,7 @@ __device__ __forceinline__ void tile_classify(const TileGeom& tg, const MeshLayo
       const float* c1 = P.f1 + m1 + W * (r * nx + x);
       const float c[8] = {a[0], a[W], a[W * (nx + 1)], a[W * nx], c1[0], c1[W], c1[W * (nx + 1)], c1[W * nx]};
       float gv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      if (MODE == kMeshPreview) {
+      if (MODE == kMeshPreview || MODE == kMeshLatFixed || MODE == kMeshLatDynamic) {
         const float* ga = P.g0 + n0 + r * nx + x;
         const float* gb = P.g1 + n1 + r * nx + x;
         gv[0] = ga[0]; gv[1] = ga[1]; gv[2] = ga[nx + 1]; gv[3] = ga[nx];
@@ -282,7 +298,7 @@ __device__ __forceinline__ void tile_classify(const TileGeom& tg, const MeshLayo
       }
       uint32_t ci = 0;
 #pragma unroll
-      for (int k = 0; k < 8; ++k) ci |= (uint32_t)corner_inside<MODE>(c[k], gv[k], tg.op, tg.iso) << k;
+      for (int k = 0; k < 8; ++k) ci |= (uint32_t)corner_inside<MODE>(c[k], gv[k], tg.op, tg.iso, tg.lo, tg.hi) << k;
       s_cube[r * vx + x] = (uint8_t)ci;
       nt = (uint32_t)(s_tri[ci] & 0xFu);
     }
@@ -328,7 +344,7 @@ template <int MODE, int THREADS>
 __device__ __forceinline__ void tile_emit(const TileGeom& tg, uint64_t t, const MeshLayout& L, unsigned char* smem,
                                           const EmitTarget& out, TileOut& res) {
   constexpr uint32_t kWarps = THREADS / 32;
-  constexpr bool kRetained = MODE == kMeshRegion || MODE == kMeshPreview;
+  constexpr bool kRetained = mode_retained_normal(MODE);
   const uint64_t* s_tri = reinterpret_cast<const uint64_t*>(smem);
   const Planes P = planes_of(smem, L);
   const uint8_t* s_cube = smem + L.cube_off;
@@ -434,6 +450,12 @@ __device__ __forceinline__ void tile_emit(const TileGeom& tg, uint64_t t, const 
           } else if (MODE == kMeshPreview) {
             vtx[m] = edge_point_retained(tg.iso, corner_sel(V, ba), corner_sel(V, bb), at(Gv, oa), at(Gv, ob),
                                          at(Av, (uint32_t)te[1]));
+          } else if (MODE == kMeshLatFixed) {
+            vtx[m] = edge_point_latfixed(tg.iso, tg.lo, tg.hi, corner_sel(V, ba), corner_sel(V, bb), at(Fv, oa),
+                                         at(Fv, ob), at(Gv, oa), at(Gv, ob));
+          } else if (MODE == kMeshLatDynamic) {
+            vtx[m] = edge_point_latdyn(tg.lo, tg.hi, corner_sel(V, ba), corner_sel(V, bb), at(Gv, oa), at(Gv, ob),
+                                       at(Av, (uint32_t)te[1]));
           } else {
             vtx[m] = edge_point_plain_v(at(Fv, oa), at(Fv, ob), corner_sel(V, ba), corner_sel(V, bb), tg.iso);
           }
@@ -896,6 +918,8 @@ MeshFn mesh_fn_t(int mode, bool emit) {
     case kMeshBand: return mesh_fn_e<kMeshBand, T>(emit);
     case kMeshRegion: return mesh_fn_e<kMeshRegion, T>(emit);
     case kMeshPreview: return mesh_fn_e<kMeshPreview, T>(emit);
+    case kMeshLatFixed: return mesh_fn_e<kMeshLatFixed, T>(emit);
+    case kMeshLatDynamic: return mesh_fn_e<kMeshLatDynamic, T>(emit);
     default: return mesh_fn_e<kMeshPlain, T>(emit);
   }
 }

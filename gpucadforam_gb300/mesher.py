@@ -283,6 +283,24 @@ class Context:
         n = int(c.total_verts)
         return pos[:n], norm[:n], Counts(c.active_voxels, c.total_verts, c.status)
 
+    def mesh_lattice_preview(self, lattice, band, acc=None, field=None, op="union", iso=0.0, voxel_size=(1, 1, 1),
+                             grid_center=(0, 0, 0), stream=None):
+        """Lattice preview mesh: with field the "fixed" form (field and the
+        lattice band), with acc the "dynamic" form (model and band)."""
+        g = make_grid(lattice.shape, voxel_size, grid_center)
+        c = N.GcmCounts()
+        opn = self.CSG_OPS.get(op, op)
+        args = (self.h, _ptr(acc), _ptr(field), _ptr(lattice), opn, C.byref(g), float(iso), float(band[0]),
+                float(band[1]))
+        self.check(self.lib.gcm_mesh_lattice_preview(*args, None, None, 0, C.byref(c), _stream(stream)))
+        cap = int(c.total_verts)
+        pos = torch.empty((max(cap, 1), 4), dtype=torch.float32, device=lattice.device)
+        norm = torch.empty((max(cap, 1), 4), dtype=torch.float32, device=lattice.device)
+        self.check(self.lib.gcm_mesh_lattice_preview(*args, _ptr(pos), _ptr(norm), max(cap, 1), C.byref(c),
+                                                     _stream(stream)))
+        n = int(c.total_verts)
+        return pos[:n], norm[:n], Counts(c.active_voxels, c.total_verts, c.status)
+
     def mesh_csg(self, prims_dev, n_prims, frame, shape_zyx, iso, voxel_size=(1, 1, 1), grid_center=(0, 0, 0),
                  pos=None, norm=None, stream=None, allow_overflow=False):
         g = make_grid(shape_zyx, voxel_size, grid_center)

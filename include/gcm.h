@@ -290,6 +290,19 @@ gcm_status gcm_mesh_retained(gcm_ctx* ctx, const gcm_csg_point* d_acc, const flo
 /* Counting pass of gcm_mesh_retained. */
 gcm_status gcm_count_retained(gcm_ctx* ctx, const gcm_csg_point* d_acc, const float* d_field, gcm_csg_op op,
                               const gcm_grid* grid, float iso, gcm_counts* h_counts, gcm_stream stream);
+/* The editor's lattice previews (classifyVoxel and
+ * generateTriangles_lattice_kernel with `fixed` or `dynamic` set,
+ * src/MarchingCubes_kernel.cu:869-1052, 1865-2200): with d_field (d_acc NULL)
+ * a primitive field combined by op with the open band band_lo < lattice <
+ * band_hi, vertices by vertexInterp_new (:1728-1790); with d_acc (d_field
+ * NULL) the accumulated model combined with that band (its difference keeps
+ * lattice < band_lo or > band_hi), vertices by vertexInterp_primitive_one
+ * (:1676-1726).  Normals calcNormal(v0, v2, v1) with w = 0.5.  capacity 0
+ * counts only. */
+gcm_status gcm_mesh_lattice_preview(gcm_ctx* ctx, const gcm_csg_point* d_acc, const float* d_field,
+                                    const float* d_lattice, gcm_csg_op op, const gcm_grid* grid, float iso,
+                                    float band_lo, float band_hi, float* d_pos, float* d_norm,
+                                    uint64_t capacity_verts, gcm_counts* h_counts, gcm_stream stream);
 
 /* ------------------------------------------------- spatially variant lattices */
 

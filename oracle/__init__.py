@@ -80,6 +80,11 @@ def lib():
                                         F32P, F32P, C.c_float, C.c_void_p, C.c_void_p, C.c_uint64,
                                         C.POINTER(C.c_uint64)]
         L.orc_mesh_retained.restype = C.c_uint64
+        L.orc_mesh_lattice_preview.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                               C.c_uint32, C.c_uint32, C.c_uint32, F32P, F32P, C.c_float, C.c_float,
+                                               C.c_float, C.c_void_p, C.c_void_p, C.c_uint64,
+                                               C.POINTER(C.c_uint64)]
+        L.orc_mesh_lattice_preview.restype = C.c_uint64
         L.orc_svl_dft.argtypes = [F32P, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, F32P]
         L.orc_svl_rhs.argtypes = [C.POINTER(OrcSvl), C.c_void_p, C.c_uint32, F32P]
         L.orc_svl_cg.argtypes = [C.POINTER(OrcSvl), F32P, F32P]
@@ -332,6 +337,27 @@ def mesh_retained(acc, field, op, vs, gc, iso=0.0):
     norm = np.zeros((max(total, 1), 4), np.float32)
     L.orc_mesh_retained(acc.ctypes.data, gp, CSG_OPS.get(op, op), nx, ny, nz, _f3(vs), _f3(gc), iso,
                         pos.ctypes.data, norm.ctypes.data, total, C.byref(act))
+    return pos[:total], norm[:total], int(act.value)
+
+
+def mesh_lattice_preview(acc, field, lattice, band, op, vs, gc, iso=0.0):
+    """Lattice preview mesh: with field (the primitive field; acc unused) the
+    "fixed" form, with field None the "dynamic" form over acc; band = (iso1,
+    iso2) on the lattice.  Returns (pos, norm, active_voxels)."""
+    nz, ny, nx = lattice.shape
+    lat = np.ascontiguousarray(lattice, np.float32)
+    f = None if field is None else np.ascontiguousarray(field, np.float32)
+    a = np.ascontiguousarray(acc) if acc is not None else np.zeros((nz, ny, nx, 4), np.int32)
+    mode = 2 if f is not None else 3
+    L = lib()
+    act = C.c_uint64(0)
+    fp = None if f is None else f.ctypes.data
+    args = (a.ctypes.data, fp, lat.ctypes.data, mode, CSG_OPS.get(op, op), nx, ny, nz, _f3(vs), _f3(gc), iso,
+            float(band[0]), float(band[1]))
+    total = L.orc_mesh_lattice_preview(*args, None, None, 0, C.byref(act))
+    pos = np.zeros((max(total, 1), 4), np.float32)
+    norm = np.zeros((max(total, 1), 4), np.float32)
+    L.orc_mesh_lattice_preview(*args, pos.ctypes.data, norm.ctypes.data, total, C.byref(act))
     return pos[:total], norm[:total], int(act.value)
 
 

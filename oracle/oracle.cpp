@@ -852,6 +852,120 @@ uint64_t orc_mesh_retained(const orc_csg_point* acc, const float* g, uint32_t op
   return total;
 }
 
+// The lattice previews of classifyVoxel and generateTriangles_lattice_kernel
+// (src/MarchingCubes_kernel.cu:869-1052, 1865-2200) with `fixed` (mode 2: the
+// primitive field f with the open lattice band iso1 < L < iso2; classic edge
+// direction; vertexInterp_new :1728-1790) or `dynamic` (mode 3: the
+// accumulated sign with the band, its difference keeping L < iso1 or L > iso2;
+// edges from the lower corner; vertexInterp_primitive_one :1676-1726) set;
+// normals calcNormal(v0, v2, v1) with w = 0.5.
+static float preview_t_fixed(float iso, float i1, float i2, float f0, float f1, float f2, float f3) {
+  float t1 = 0.0f, t2 = 0.0f, t3 = 0.0f;
+  if (((f0 < iso) && (f1 >= iso)) || ((f1 < iso) && (f0 >= iso))) t1 = (iso - f0) / (f1 - f0);
+  if (((f2 < i1) && (f3 >= i1)) || ((f3 < i1) && (f2 >= i1))) t2 = (i1 - f2) / (f3 - f2);
+  if (((f2 < i2) && (f3 >= i2)) || ((f3 < i2) && (f2 >= i2))) t3 = (i2 - f2) / (f3 - f2);
+  if ((t1 > 0.0f) && (t2 > 0.0f) && (t3 == 0.0f)) return (float)((double)(t1 + t2) * 0.5);
+  if ((t1 > 0.0f) && (t3 > 0.0f) && (t2 == 0.0f)) return (float)((double)(t1 + t3) * 0.5);
+  if ((t1 > 0.0f) && (t2 == 0.0f) && (t3 == 0.0f)) return t1;
+  if ((t2 > 0.0f) && (t1 == 0.0f) && (t3 == 0.0f)) return t2;
+  if ((t3 > 0.0f) && (t1 == 0.0f) && (t2 == 0.0f)) return t3;
+  return 0.0f;
+}
+
+static float preview_t_dynamic(float i1, float i2, float f0, float f1, float t1) {
+  float t2 = 0.0f, t3 = 0.0f, t = 0.0f;
+  if (((f1 >= i1) && (f0 <= i1)) || ((f0 >= i1) && (f1 <= i1))) t2 = (i1 - f0) / (f1 - f0);
+  if ((t1 > 0) && (t2 > 0)) t = (float)((double)(t1 + t2) * 0.5);
+  else if ((t1 > 0) && (t2 == 0)) t = t1;
+  else if ((t2 > 0) && (t1 == 0)) t = t2;
+  if (((f1 >= i2) && (f0 <= i2)) || ((f0 >= i2) && (f1 <= i2))) t3 = (i2 - f0) / (f1 - f0);
+  if ((t1 > 0) && (t3 > 0)) t = (float)((double)(t1 + t3) * 0.5);
+  else if ((t1 > 0) && (t3 == 0)) t = t1;
+  else if ((t3 > 0) && (t1 == 0)) t = t3;
+  return t;
+}
+
+uint64_t orc_mesh_lattice_preview(const orc_csg_point* acc, const float* f, const float* L, uint32_t mode,
+                                  uint32_t op, uint32_t nx, uint32_t ny, uint32_t nz, const float* vs,
+                                  const float* gc, float iso, float iso1, float iso2, float* pos, float* norm,
+                                  uint64_t capacity, uint64_t* active_out) {
+  const bool fixed = mode == 2;
+  const uint64_t nvox = (uint64_t)(nx - 1) * (ny - 1) * (nz - 1);
+  auto inside = [&](uint64_t i) {
+    const bool band = (L[i] > iso1) && (L[i] < iso2);
+    if (fixed) {
+      if (op == 1) return (f[i] >= iso) && band;
+      if (op == 2) return (f[i] < iso) && band;
+      return (f[i] < iso) || band;
+    }
+    const bool a = (float)acc[i].val < iso;
+    if (op == 1) return a && ((L[i] < iso1) || (L[i] > iso2));
+    if (op == 2) return a && band;
+    return a || band;
+  };
+  auto cube = [&](uint32_t x, uint32_t y, uint32_t z) {
+    unsigned ci = 0;
+    for (int k = 0; k < 8; ++k)
+      ci |= (unsigned)inside(pidx(x + gcm::kCornerX[k], y + gcm::kCornerY[k], z + gcm::kCornerZ[k], nx, ny)) << k;
+    return ci;
+  };
+  std::vector<uint64_t> scan(nvox);
+  uint64_t total = 0, active = 0;
+  for (uint64_t v = 0; v < nvox; ++v) {
+    uint32_t x, y, z;
+    voxel_pos(v, nx, ny, x, y, z);
+    const unsigned n = kNumVerts(cube(x, y, z));
+    scan[v] = total;
+    total += n;
+    active += n > 0;
+  }
+  if (active_out) *active_out = active;
+  const Arith A = decode(orc_default_arith());
+  for (uint64_t v = 0; v < nvox; ++v) {
+    uint32_t gp[3];
+    voxel_pos(v, nx, ny, gp[0], gp[1], gp[2]);
+    const unsigned ci = cube(gp[0], gp[1], gp[2]);
+    const uint64_t row = gcm::kTriRows[ci];
+    const unsigned nv = kNumVerts(ci);
+    for (unsigned j = 0; j < nv; j += 3) {
+      float vv[3][3];
+      for (int m = 0; m < 3; ++m) {
+        const int e = (int)gcm::tri_edge(row, j + m);
+        int lo = gcm::kEdgeA[e], up = gcm::kEdgeB[e];
+        int axis = 0;
+        {
+          const int olo[3] = {gcm::kCornerX[lo], gcm::kCornerY[lo], gcm::kCornerZ[lo]};
+          const int oup[3] = {gcm::kCornerX[up], gcm::kCornerY[up], gcm::kCornerZ[up]};
+          for (int a = 0; a < 3; ++a)
+            if (olo[a] != oup[a]) axis = a;
+          if (!fixed && olo[axis] > oup[axis]) std::swap(lo, up);  // dynamic: from the lower corner
+        }
+        const int o0[3] = {gcm::kCornerX[lo], gcm::kCornerY[lo], gcm::kCornerZ[lo]};
+        const int o1[3] = {gcm::kCornerX[up], gcm::kCornerY[up], gcm::kCornerZ[up]};
+        const uint64_t p0 = pidx(gp[0] + o0[0], gp[1] + o0[1], gp[2] + o0[2], nx, ny);
+        const uint64_t p1 = pidx(gp[0] + o1[0], gp[1] + o1[1], gp[2] + o1[2], nx, ny);
+        const float t = fixed ? preview_t_fixed(iso, iso1, iso2, f[p0], f[p1], L[p0], L[p1])
+                              : preview_t_dynamic(iso1, iso2, L[p0], L[p1], acc[p0].t[axis]);
+        for (int a = 0; a < 3; ++a) {
+          const float d = (float)gp[a] - gc[a];
+          vv[m][a] = lerp_axis(d, vs[a], o0[a], o1[a], t, A);
+        }
+      }
+      float n[3];
+      normal_of(vv[0], vv[2], vv[1], A.cross, n);
+      const uint64_t idx = scan[v] + j;
+      if (idx + 3 > capacity) continue;
+      for (int m = 0; m < 3; ++m) {
+        float* P = pos + 4 * (idx + m);
+        float* N = norm + 4 * (idx + m);
+        P[0] = vv[m][0]; P[1] = vv[m][1]; P[2] = vv[m][2]; P[3] = 1.0f;
+        N[0] = n[0]; N[1] = n[1]; N[2] = n[2]; N[3] = 0.5f;
+      }
+    }
+  }
+  return total;
+}
+
 // ---- spatially variant lattices ---------------------------------------------------
 
 // Coefficient m's frequencies: k outer, j, i inner over [-range, range]

@@ -101,6 +101,12 @@ void orc_csg_retain_band(orc_csg_point* acc, const float* lattice, uint32_t nx, 
 uint64_t orc_mesh_retained(const orc_csg_point* acc, const float* field, uint32_t op, uint32_t nx, uint32_t ny,
                            uint32_t nz, const float* voxel_size, const float* grid_center, float iso, float* pos,
                            float* norm, uint64_t capacity, uint64_t* active_out);
+/* Lattice previews: mode 2 combines the primitive field with the open band
+ * iso1 < lattice < iso2, mode 3 the accumulator with that band. */
+uint64_t orc_mesh_lattice_preview(const orc_csg_point* acc, const float* field, const float* lattice, uint32_t mode,
+                                  uint32_t op, uint32_t nx, uint32_t ny, uint32_t nz, const float* voxel_size,
+                                  const float* grid_center, float iso, float iso1, float iso2, float* pos, float* norm,
+                                  uint64_t capacity, uint64_t* active_out);
 
 /* Spatially variant lattice (src/lattice_files/Gratings.cu:100-1050,
  * src/main.cu:3578-3711, 3904-4030). */

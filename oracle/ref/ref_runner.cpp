@@ -475,16 +475,25 @@ void run_retain(Reader& r, Writer& w, CUmodule mc, const Tables& T, bool banded)
     launch(k_fold, blocks_for(P, 1024), 1, 1, 1024, 1, 1, a);
     cuMemFree(d_f);
   }
+  // mesh mode: 0 region, 1 primitive preview (field), and in kind 10 also
+  // 2 lattice "fixed" (band edges, field, lattice) and 3 lattice "dynamic"
+  // (band edges, lattice): classifyVoxel / generateTriangles_lattice_kernel
+  // with fixed or dynamic set
   uint32_t mode = r.get<uint32_t>(), pop = r.get<uint32_t>();
-  CUdeviceptr d_dyn = d_zero;
-  if (mode == 1) d_dyn = dupload(r.arr<float>(P));
-  bool ou = pop == 0, od = pop == 1, oi = pop == 2, prim = true, topo = false, lat = false, fixed = false,
-       dynamic = false, region = mode == 0;
   float iso1 = 0.0f, iso2 = 0.0f;
+  if (banded && mode >= 2) {
+    iso1 = r.get<float>();
+    iso2 = r.get<float>();
+  }
+  CUdeviceptr d_dyn = d_zero, d_lat = d_zero;
+  if (mode == 1 || mode == 2) d_dyn = dupload(r.arr<float>(P));
+  if (banded && mode >= 2) d_lat = dupload(r.arr<float>(P));
+  bool ou = pop == 0, od = pop == 1, oi = pop == 2, prim = mode <= 1, topo = false, lat = mode >= 2,
+       fixed = mode == 2, dynamic = mode == 3, region = mode == 0;
   CUdeviceptr d_occ = dalloc<uint32_t>(nvox);
   CUfunction k_cls = find_kernel(mc, "classifyVoxel");
   {
-    void* a[] = {&d_zero, &g, &d_verts, &d_occ, &d_acc, &d_dyn, &d_zero, &d_zero, &g, &shift, &mask, &nvox,
+    void* a[] = {&d_zero, &g, &d_verts, &d_occ, &d_acc, &d_dyn, &d_zero, &d_lat, &g, &shift, &mask, &nvox,
                  &iso1, &iso2, &vs, &iso, const_cast<CUtexObject*>(&T.nverts_tex), &ou, &od, &oi, &prim, &topo,
                  &lat, &fixed, &dynamic, &region};
     launch(k_cls, blocks_for(nvox, 1024), 1, 1, 1024, 1, 1, a);
@@ -512,7 +521,7 @@ void run_retain(Reader& r, Writer& w, CUmodule mc, const Tables& T, bool banded)
     CUfunction k = find_kernel(mc, "generateTriangles_lattice_kernel");
     void* a[] = {&d_pos, &d_norm, &c.d_compacted, &c.d_verts_scan, &g, &shift, &mask, &vs, &gc, &iso,
                  &c.active, &maxv, const_cast<CUtexObject*>(&T.tri_tex), const_cast<CUtexObject*>(&T.nverts_tex),
-                 &c.total, &d_acc, &d_dyn, &d_zero, &d_zero, &iso1, &iso2, &d_verts, &ou, &od, &oi, &prim, &topo,
+                 &c.total, &d_acc, &d_dyn, &d_zero, &d_lat, &iso1, &iso2, &d_verts, &ou, &od, &oi, &prim, &topo,
                  &lat, &fixed, &dynamic, &region};
     launch(k, blocks_for(c.active, 32), 1, 1, 32, 1, 1, a);
   }
@@ -521,6 +530,7 @@ void run_retain(Reader& r, Writer& w, CUmodule mc, const Tables& T, bool banded)
   w.arr(ddownload<float>(d_pos, 4ull * c.total));
   w.arr(ddownload<float>(d_norm, 4ull * c.total));
   if (d_dyn != d_zero) cuMemFree(d_dyn);
+  if (d_lat != d_zero) cuMemFree(d_lat);
   cuMemFree(d_acc); cuMemFree(d_zero); cuMemFree(d_verts); cuMemFree(d_occ); cuMemFree(d_occ_scan);
   cuMemFree(d_pos); cuMemFree(d_norm); cuMemFree(c.d_compacted); cuMemFree(c.d_verts_scan);
 }

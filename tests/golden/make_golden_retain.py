@@ -12,7 +12,11 @@ compactVoxels and generateTriangles_lattice_kernel (:869-1052, :1594-1608,
 :1865-2200), in the region mode or with one more primitive field (job kind 10
 of oracle/ref/ref_runner.cpp).  A fold is static (the field is the object) or
 a lattice band (classify_copy_Voxel's dynamic mode: the open band
-iso1 < field < iso2 is the object).  Both reference build variants (sm103a SASS and
+iso1 < field < iso2 is the object).  Meshes: the region (mode 0), the model
+with one more primitive field (mode 1), and the lattice previews of
+classifyVoxel / generateTriangles_lattice_kernel with `fixed` (mode 2: a
+primitive field with the lattice band) or `dynamic` (mode 3: the model with
+the lattice band) set.  Both reference build variants (sm103a SASS and
 the Makefile's compute_89 PTX) must agree bit for bit; the sm103a outputs are
 written to ``golden_retain.npz`` with the inputs.
 """
@@ -118,6 +122,26 @@ def cases():
     out.append(("band_random_region", n, 0.0, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), folds, 0, "union", None))
     out.append(("band_random_preview", n, 0.0, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), folds[:4], 1, "subtract",
                 rng.uniform(-1, 1, n[::-1]).astype(np.float32)))
+    # lattice previews: mode 2 ("fixed": a primitive field with the lattice
+    # band) and mode 3 ("dynamic": the accumulated model with the lattice band)
+    n = (24, 22, 20)
+    g = gyroid(n, 10.0)
+    a = sphere(n, (9.3, 10.1, 8.6), 6.2)
+    c = sphere(n, (14.5, 9.2, 11.1), 4.1)
+    e = sphere(n, (11.6, 12.3, 10.4), 5.3)
+    for op in ("union", "subtract", "intersect"):
+        out.append((f"latfixed_{op}", n, 0.0, (0.5, 0.5, 0.5), (0.0, 0.0, 0.0), [("union", a)], 2, op, e, g,
+                    (-0.35, 0.35)))
+        out.append((f"latdyn_{op}", n, 0.0, (0.5, 0.5, 0.5), (1.0, 0.0, -0.5), [("union", a), ("subtract", c)], 3,
+                    op, None, g, (-0.3, 0.3)))
+    n = (14, 13, 12)
+    x, y, z = _grid(n)
+    gi = (np.mod(x + 2 * y + 3 * z, 5.0) - 2.0).astype(np.float32)
+    s1 = sphere(n, (6, 6, 5), 4)
+    out.append(("latfixed_exact", n, 0.0, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), [("union", s1)], 2, "union",
+                sphere(n, (7, 6, 6), 3), gi, (-1.0, 1.0)))
+    out.append(("latdyn_exact", n, 0.0, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), [("union", s1), ("union", gi, (0.0, 2.0))],
+                3, "subtract", None, gi, (-1.0, 1.0)))
     return out
 
 
@@ -128,17 +152,24 @@ def fold_band(fold):
 
 def build_job():
     parts, meta = [], []
-    for name, n, iso, vs, gc, folds, mode, pop, pf in cases():
+    for case in cases():
+        name, n, iso, vs, gc, folds, mode, pop, pf = case[:9]
+        lat, lband = (case[9], case[10]) if len(case) > 9 else (None, None)
         b = MG._p("I", 10) + MG._p("3I", *n) + MG._p("f", iso) + MG._p("3f", *vs) + MG._p("3f", *gc)
         b += MG._p("I", len(folds))
         for fold in folds:
             dyn, i1, i2 = fold_band(fold)
             b += MG._p("I", OPS[fold[0]]) + MG._p("I", dyn) + MG._p("2f", i1, i2) + fold[1].astype("<f4").tobytes()
         b += MG._p("2I", mode, OPS[pop])
-        if mode == 1:
+        if mode >= 2:
+            b += MG._p("2f", *lband)
+        if mode in (1, 2):
             b += pf.astype("<f4").tobytes()
+        if mode >= 2:
+            b += lat.astype("<f4").tobytes()
         parts.append(b)
-        meta.append(dict(name=name, n=n, iso=iso, vs=vs, gc=gc, folds=folds, mode=mode, pop=pop, pf=pf))
+        meta.append(dict(name=name, n=n, iso=iso, vs=vs, gc=gc, folds=folds, mode=mode, pop=pop, pf=pf, lat=lat,
+                         lband=lband))
     return MG._p("I", MG.MAGIC) + MG._p("I", len(parts)) + b"".join(parts), meta
 
 
@@ -194,6 +225,9 @@ def main():
         d[pre + "fold_band"] = np.array([fold_band(fold) for fold in c["folds"]], np.float32)
         if c["pf"] is not None:
             d[pre + "preview_field"] = c["pf"]
+        if c["lat"] is not None:
+            d[pre + "lattice"] = c["lat"]
+            d[pre + "lattice_band"] = np.array(c["lband"], np.float32)
         for k in ("acc", "verts", "occ", "compacted", "pos", "norm"):
             d[pre + k] = r[k]
     np.savez_compressed(os.path.join(args.out, "golden_retain.npz"), **d)

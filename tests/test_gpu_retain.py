@@ -7,7 +7,7 @@ import torch
 
 import oracle as O
 from tests.helpers import golden
-from tests.test_oracle_retain import OPS, case, n_cases
+from tests.test_oracle_retain import OPS, case, n_cases, preview
 
 pytestmark = pytest.mark.gpu
 
@@ -34,7 +34,13 @@ def test_retained_matches_reference(ctx, i):
     for op, f, band in folds:
         ctx.csg_retain(acc, dev(f), OPS[int(op)], iso, band=band)
     assert acc.cpu().numpy().tobytes() == R[pre + "acc"].tobytes()
-    pos, norm, cnt = ctx.mesh_retained(acc, None if pf is None else dev(pf), pop, iso, vs, gc)
+    mode, lat, band = preview(i)
+    if mode >= 2:
+        pos, norm, cnt = ctx.mesh_lattice_preview(dev(lat), band, acc=acc if mode == 3 else None,
+                                                  field=dev(pf) if mode == 2 else None, op=pop, iso=iso,
+                                                  voxel_size=vs, grid_center=gc)
+    else:
+        pos, norm, cnt = ctx.mesh_retained(acc, None if pf is None else dev(pf), pop, iso, vs, gc)
     assert cnt.active_voxels == len(R[pre + "compacted"])
     assert pos.cpu().numpy().tobytes() == R[pre + "pos"].tobytes()
     assert norm.cpu().numpy().tobytes() == R[pre + "norm"].tobytes()
@@ -111,5 +117,38 @@ def test_band_folds_vs_oracle(ctx, shape, op):
     assert acc_g.cpu().numpy().tobytes() == acc_o.tobytes()
     opos, onorm, oact = O.mesh_retained(acc_o, None, "union", (1, 1, 1), (0, 0, 0))
     pos, norm, cnt = ctx.mesh_retained(acc_g, None, "union", 0.0)
+    assert cnt.active_voxels == oact and cnt.total_verts == len(opos)
+    assert pos.cpu().numpy().tobytes() == opos.tobytes() and norm.cpu().numpy().tobytes() == onorm.tobytes()
+
+
+@pytest.mark.parametrize("shape", [(33, 29, 41), (2, 3, 70), (64, 48, 40)])
+@pytest.mark.parametrize("op", ["union", "subtract", "intersect"])
+@pytest.mark.parametrize("form", ["fixed", "dynamic"])
+def test_lattice_preview_vs_oracle(ctx, shape, op, form):
+    """The editor's lattice previews on ragged grids: counts, positions and
+    normals equal the oracle's bit for bit."""
+    rng = np.random.default_rng(sum(shape) + len(op) + len(form))
+    nz, ny, nx = shape
+    z, y, x = np.meshgrid(np.arange(nz, dtype=np.float64), np.arange(ny, dtype=np.float64),
+                          np.arange(nx, dtype=np.float64), indexing="ij")
+    k = 2 * np.pi / rng.uniform(6, 14)
+    lat = (np.sin(k * x) * np.cos(k * y) + np.sin(k * y) * np.cos(k * z) + np.sin(k * z) * np.cos(k * x)).astype(np.float32)
+    c = rng.uniform(0, 1, 3) * np.array([nx, ny, nz])
+    r = 0.4 * min(nx, ny, nz) + 1.0
+    sph = ((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2 - r * r).astype(np.float32)
+    band = (-0.3, 0.35)
+    vs, gc = (0.5, 1.0, 0.25), (1.0, 0.0, -2.0)
+    if form == "fixed":
+        opos, onorm, oact = O.mesh_lattice_preview(None, sph, lat, band, op, vs, gc)
+        pos, norm, cnt = ctx.mesh_lattice_preview(dev(lat), band, field=dev(sph), op=op, voxel_size=vs,
+                                                  grid_center=gc)
+    else:
+        acc_o = O.csg_accumulator(shape)
+        acc_g = ctx.csg_accumulator(shape)
+        for f, b in ((sph, None), (lat + 0.5, (0.0, 0.4))):
+            O.csg_retain(acc_o, f, "union", 0.0, band=b)
+            ctx.csg_retain(acc_g, dev(f), "union", 0.0, band=b)
+        opos, onorm, oact = O.mesh_lattice_preview(acc_o, None, lat, band, op, vs, gc)
+        pos, norm, cnt = ctx.mesh_lattice_preview(dev(lat), band, acc=acc_g, op=op, voxel_size=vs, grid_center=gc)
     assert cnt.active_voxels == oact and cnt.total_verts == len(opos)
     assert pos.cpu().numpy().tobytes() == opos.tobytes() and norm.cpu().numpy().tobytes() == onorm.tobytes()
