@@ -860,7 +860,7 @@ def run_gcm(args):
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded control grid)",
                 "config": workload_config(n), "tris_per_s": tris, "verts_per_step": cap,
                 "active_voxels": cnt.active_voxels,
-                "kernels_ms": {"lattice_params_kernel": statistics.mean(field_ms),
+                "kernels_ms": {"lattice_rows_kernel": statistics.mean(field_ms),
                                "mc_mesh_kernel": statistics.mean(mc_ms)},
                 "roofline": {"bound": "hbm", "kernel": "mc_mesh_kernel", "achieved": achieved, "peak": peak,
                              "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,

@@ -615,10 +615,11 @@ static gcm_status run_lattice(gcm_ctx* ctx, LatticeParams& p, float* d_out, cuda
     const uint64_t nc = (uint64_t)p.cx * p.cy * p.cz;
     gcm_status s = ensure_buffer(ctx, &ctx->blend_buf, &ctx->blend_bytes, nc * 12 * sizeof(float));
     if (s) return s;
-    GCM_CUDA(ctx, gcm::launch_lattice(p, ctx->blend_buf, grid_blocks(ctx, nc, 256), row_blocks(ctx, p.ny, p.nz), st));
+    GCM_CUDA(ctx, gcm::launch_lattice(p, ctx->blend_buf, grid_blocks(ctx, nc, 256), row_blocks(ctx, p.ny, p.nz),
+                                      (uint32_t)ctx->sm_count, st));
     count_launch(ctx, 2);
   } else {
-    GCM_CUDA(ctx, gcm::launch_lattice(p, nullptr, 0, row_blocks(ctx, p.ny, p.nz), st));
+    GCM_CUDA(ctx, gcm::launch_lattice(p, nullptr, 0, row_blocks(ctx, p.ny, p.nz), (uint32_t)ctx->sm_count, st));
     count_launch(ctx, 1);
   }
   return GCM_OK;

@@ -142,8 +142,9 @@ gcm_status make_plan(gcm_batch* b, int threads, uint32_t tile_voxels) {
 gcm_status launch_fields(gcm_batch* b, cudaStream_t st) {
   gcm_ctx* ctx = b->ctx;
   if (b->n_params) {
-    const uint32_t blocks =
-        (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((b->param_rows + 7) / 8, (uint64_t)ctx->sm_count * 8));
+    // about 8 rows per warp (8 warps per CTA): many CTAs rather than one
+    // resident wave, so the block scheduler balances the SMs
+    const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((b->param_rows + 63) / 64, 1u << 30));
     GCM_CUDA(ctx, launch_lattice_batch(b->d_lat, b->n_params, b->param_rows, blocks, b->params_wide, st));
     count_launch(ctx, b->params_wide ? 2 : 1);
   }
@@ -170,7 +171,7 @@ gcm_status launch_fields(gcm_batch* b, cudaStream_t st) {
     p.out = b->field + b->field_off[i];
     const uint64_t nc = (uint64_t)p.cx * p.cy * p.cz;
     const uint32_t rows = std::max<uint32_t>(1, std::min<uint32_t>(n[1] * n[2], (uint32_t)ctx->sm_count * 8));
-    GCM_CUDA(ctx, launch_lattice(p, b->blend_buf, grid_blocks(ctx, nc, 256), rows, st));
+    GCM_CUDA(ctx, launch_lattice(p, b->blend_buf, grid_blocks(ctx, nc, 256), rows, (uint32_t)ctx->sm_count, st));
     count_launch(ctx, 2);
   }
   return GCM_OK;

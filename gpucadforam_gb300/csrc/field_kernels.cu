@@ -5,6 +5,8 @@
 // explicit IEEE intrinsics, so the only difference from a correctly rounded
 // evaluation is the accuracy of the CUDA trig functions.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <float.h>
 #include <math.h>
 #include <stdint.h>
@@ -220,84 +222,103 @@ __global__ void __launch_bounds__(256) lattice_prep_kernel(LatticeParams p, floa
   }
 }
 
-// Sample rows are the unit of work: a CTA takes sample rows (y, z), stages per
-// control column the rows' y/z-interpolated parameters in shared memory, and
-// its threads cover x.  No 64-bit index arithmetic per sample.
-constexpr uint32_t kRowCx = 1024;   // control columns staged per row (PARAMS)
-constexpr uint32_t kBlendCx = 128;  // control columns staged per row (BLEND)
+// Sample rows are the unit of work.  PARAMS mode: a warp takes R consecutive
+// sample rows (y, z), stages per control column the rows' y/z-interpolated
+// parameters and the nearest types in its own slice of shared memory (warp
+// syncs only, no CTA barrier), and each lane then evaluates two samples of a
+// row (x and x + 32) per step, which gives the compiler two independent
+// chains.  One row group per warp and many CTAs rather than a persistent grid:
+// the block scheduler balances the SMs.  No 64-bit index arithmetic per sample.
+constexpr uint32_t kBlendCx = 128;        // control columns staged per row (BLEND)
+constexpr uint32_t kRowWarps = 8;         // warps per CTA of lattice_rows_kernel
+constexpr size_t kRowSmem = 48 * 1024;    // shared memory of one such CTA, at most
 
-// Staged form: groups of R <= kRowsIter consecutive sample rows share one
-// staging pass and its two barriers (as many rows as fit the 5 x kRowCx
-// staging floats).  Each row's control columns are staged by its own share of
-// the threads, the rows' (y, z) step from group to group without a division,
-// and each sample column locates its x cell once for the group's rows.
-constexpr uint32_t kRowsIter = 4;
+// Floats of one warp's slice: R rows x 5 parameters x cx columns, the rows'
+// (y, z) phase coordinates, then R x cx type bytes.
+__host__ __device__ constexpr uint32_t row_slice_floats(uint32_t R, uint32_t cx) {
+  return R * 5 * cx + 2 * R + (R * cx + 3) / 4;
+}
 
-__global__ void __launch_bounds__(256) lattice_staged_kernel(LatticeParams p) {
-  __shared__ float s_a[5 * kRowCx];
-  __shared__ uint8_t s_t[kRowCx];
-  __shared__ float2 s_q[kRowsIter];  // per row: y and z phase coordinates
+namespace {
+
+// One staged sample: x-interpolation of the row's five staged parameters,
+// rotation, phase, TPMS value.
+__device__ __forceinline__ float staged_sample(const float* __restrict__ s, const uint8_t* __restrict__ t,
+                                               uint32_t cx, const AxisCell& kx, float qx, float qy, float qz) {
+  float v[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) v[k] = lerpf(s[k * cx + kx.i0], s[k * cx + kx.i1], kx.f);
+  float R9[9];
+  euler_rows(v[1], v[2], v[3], R9);
+  const float q[3] = {qx, qy, qz};
+  return lattice_value(t[kx.nearest], R9, __fdiv_rn(2.0f, v[0]), q, v[4]);
+}
+
+}  // namespace
+
+template <uint32_t R>
+__global__ void __launch_bounds__(256, 4) lattice_rows_kernel(LatticeParams p) {
+  extern __shared__ float s_rows[];
+  const uint32_t cx = p.cx;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  float* sa = s_rows + warp * row_slice_floats(R, cx);
+  float* sq = sa + R * 5 * cx;
+  uint8_t* st = reinterpret_cast<uint8_t*>(sq + 2 * R);
   const uint32_t c[3] = {p.cx, p.cy, p.cz};
   const uint32_t nc = p.cx * p.cy * p.cz;
   const float* arr[5] = {p.period, p.euler, p.euler ? p.euler + nc : nullptr,
                          p.euler ? p.euler + 2 * nc : nullptr, p.thickness};
   const uint32_t rows = p.ny * p.nz;
-  const uint32_t R = max(1u, min(kRowsIter, kRowCx / p.cx));
   const uint32_t groups = (rows + R - 1) / R;
-  const uint32_t tpr = blockDim.x / R;  // threads staging one row
-  const uint32_t my_r = threadIdx.x / tpr, my_j = threadIdx.x - my_r * tpr;
-  // (y, z) of the first row of this CTA's group and the step between its groups
-  const uint32_t first = blockIdx.x * R, step = gridDim.x * R;
-  uint32_t y0 = first % p.ny, z0 = first / p.ny;
-  const uint32_t sdy = step % p.ny, sdz = step / p.ny;
-  for (uint32_t grp = blockIdx.x; grp < groups; grp += gridDim.x) {
-    const uint32_t row0 = grp * R, nr = min(R, rows - row0);
-    __syncthreads();  // the previous group's readers are done
-    if (my_r < nr) {
-      uint32_t y = y0, z = z0;
-      for (uint32_t r = 0; r < my_r; ++r)
-        if (++y == p.ny) {
-          y = 0;
-          ++z;
-        }
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t g = blockIdx.x * (blockDim.x >> 5) + warp; g < groups; g += warps) {
+    const uint32_t row0 = g * R, nr = min(R, rows - row0);
+    __syncwarp();  // the warp's previous group is read
+    uint32_t y = row0 % p.ny, z = row0 / p.ny;
+    for (uint32_t r = 0; r < nr; ++r) {
       const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
-      float* sa = s_a + my_r * 5 * p.cx;
 #pragma unroll
       for (uint32_t k = 0; k < 5; ++k)
-        for (uint32_t xc = my_j; xc < p.cx; xc += tpr) sa[k * p.cx + xc] = column_yz(arr[k], (int)xc, ky, kz, c);
-      for (uint32_t xc = my_j; xc < p.cx; xc += tpr)
-        s_t[my_r * p.cx + xc] = __ldg(p.type + cidx((int)xc, ky.nearest, kz.nearest, c));
-      if (my_j == 0) s_q[my_r] = make_float2(fs((float)y, p.origin[1]), fs((float)z, p.origin[2]));
-    }
-    __syncthreads();
-    for (uint32_t x = threadIdx.x; x < p.nx; x += blockDim.x) {
-      const AxisCell kx = locate1(x, c[0], p.scale[0]);
-      const float qx = fs((float)x, p.origin[0]);
-      float* out = p.out + (uint64_t)row0 * p.nx + x;
-#pragma unroll 1
-      for (uint32_t r = 0; r < nr; ++r) {
-        const float* sa = s_a + r * 5 * p.cx;
-        float v[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) v[k] = lerpf(sa[k * p.cx + kx.i0], sa[k * p.cx + kx.i1], kx.f);
-        const uint32_t type = s_t[r * p.cx + kx.nearest];
-        float R9[9];
-        euler_rows(v[1], v[2], v[3], R9);
-        const float2 qyz = s_q[r];
-        const float q[3] = {qx, qyz.x, qyz.y};
-        out[(uint64_t)r * p.nx] = lattice_value(type, R9, __fdiv_rn(2.0f, v[0]), q, v[4]);
+        for (uint32_t xc = lane; xc < cx; xc += 32) sa[(r * 5 + k) * cx + xc] = column_yz(arr[k], (int)xc, ky, kz, c);
+      for (uint32_t xc = lane; xc < cx; xc += 32)
+        st[r * cx + xc] = __ldg(p.type + cidx((int)xc, ky.nearest, kz.nearest, c));
+      if (lane == 0) {
+        sq[2 * r] = fs((float)y, p.origin[1]);
+        sq[2 * r + 1] = fs((float)z, p.origin[2]);
+      }
+      if (++y == p.ny) {
+        y = 0;
+        ++z;
       }
     }
-    y0 += sdy;
-    z0 += sdz;
-    if (y0 >= p.ny) {
-      y0 -= p.ny;
-      ++z0;
+    __syncwarp();
+    for (uint32_t x0 = lane; x0 < p.nx; x0 += 64) {
+      const uint32_t x1 = x0 + 32;
+      const AxisCell k0 = locate1(x0, c[0], p.scale[0]);
+      const float q0 = fs((float)x0, p.origin[0]);
+      float* out = p.out + (uint64_t)row0 * p.nx + x0;
+      if (x0 - lane + 32 < p.nx) {  // warp-uniform: the second segment holds samples
+        const AxisCell k1 = locate1(min(x1, p.nx - 1), c[0], p.scale[0]);
+        const float q1 = fs((float)x1, p.origin[0]);
+#pragma unroll 1
+        for (uint32_t r = 0; r < nr; ++r) {
+          const float* s = sa + r * 5 * cx;
+          const uint8_t* t = st + r * cx;
+          const float v0 = staged_sample(s, t, cx, k0, q0, sq[2 * r], sq[2 * r + 1]);
+          const float v1 = staged_sample(s, t, cx, k1, q1, sq[2 * r], sq[2 * r + 1]);
+          out[(uint64_t)r * p.nx] = v0;
+          if (x1 < p.nx) out[(uint64_t)r * p.nx + 32] = v1;
+        }
+      } else {
+#pragma unroll 1
+        for (uint32_t r = 0; r < nr; ++r)
+          out[(uint64_t)r * p.nx] = staged_sample(sa + r * 5 * cx, st + r * cx, cx, k0, q0, sq[2 * r], sq[2 * r + 1]);
+      }
     }
   }
 }
 
-// Control grids wider than kRowCx columns: every sample reads its columns.
+// Control grids too wide for a warp's slice of one row: every sample reads its columns.
 __global__ void __launch_bounds__(256) lattice_params_kernel(LatticeParams p) {
   const uint32_t c[3] = {p.cx, p.cy, p.cz};
   const uint32_t nc = p.cx * p.cy * p.cz;
@@ -386,7 +407,7 @@ constexpr uint32_t kWarpCx = GCM_BATCH_WARP_CX;  // control columns staged per w
 // STAGED: the rows of instances with at most kWarpCx control columns (the
 // other rows are skipped); the other form takes the wider ones.
 template <bool STAGED>
-__global__ void __launch_bounds__(256) lattice_params_batch_kernel(const BatchLattice* inst, uint32_t n_inst,
+__global__ void __launch_bounds__(256, 4) lattice_params_batch_kernel(const BatchLattice* inst, uint32_t n_inst,
                                                                    uint64_t total_rows) {
   __shared__ float s_a[8][5][kWarpCx];
   __shared__ uint8_t s_t[8][kWarpCx];
@@ -423,15 +444,20 @@ __global__ void __launch_bounds__(256) lattice_params_batch_kernel(const BatchLa
     __syncwarp();
     float* out = p.out + (uint64_t)local * p.nx;
     if (STAGED) {
-      for (uint32_t x = lane; x < p.nx; x += 32) {
-        const AxisCell kx = locate1(x, c[0], p.scale[0]);
-        float v[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) v[k] = lerpf(s_a[wib][k][kx.i0], s_a[wib][k][kx.i1], kx.f);
-        float R[9];
-        euler_rows(v[1], v[2], v[3], R);
-        const float q[3] = {fs((float)x, p.origin[0]), fs((float)y, p.origin[1]), fs((float)z, p.origin[2])};
-        out[x] = lattice_value(s_t[wib][kx.nearest], R, __fdiv_rn(2.0f, v[0]), q, v[4]);
+      const float qy = fs((float)y, p.origin[1]), qz = fs((float)z, p.origin[2]);
+      for (uint32_t x0 = lane; x0 < p.nx; x0 += 64) {  // two samples per lane per step
+        const uint32_t x1 = x0 + 32;
+        const AxisCell k0 = locate1(x0, c[0], p.scale[0]);
+        const float q0 = fs((float)x0, p.origin[0]);
+        if (x0 - lane + 32 < p.nx) {  // warp-uniform: the second segment holds samples
+          const AxisCell k1 = locate1(min(x1, p.nx - 1), c[0], p.scale[0]);
+          const float v0 = staged_sample(&s_a[wib][0][0], s_t[wib], kWarpCx, k0, q0, qy, qz);
+          const float v1 = staged_sample(&s_a[wib][0][0], s_t[wib], kWarpCx, k1, fs((float)x1, p.origin[0]), qy, qz);
+          out[x0] = v0;
+          if (x1 < p.nx) out[x1] = v1;
+        } else {
+          out[x0] = staged_sample(&s_a[wib][0][0], s_t[wib], kWarpCx, k0, q0, qy, qz);
+        }
       }
     } else {
       for (uint32_t x = lane; x < p.nx; x += 32) {
@@ -1033,8 +1059,27 @@ cudaError_t launch_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t n
   return cudaGetLastError();
 }
 
+// Rows per warp for lattice_rows_kernel: the most of {8, 4, 2, 1} whose slices
+// fit kRowSmem and that still leave 32 warps of row groups per SM; 0 when not
+// even one row's slice fits (the unstaged kernel then runs).
+uint32_t lattice_rows_per_warp(uint32_t cx, uint32_t rows, uint32_t sm_count) {
+  for (uint32_t R = 8; R >= 1; R /= 2) {
+    if ((size_t)kRowWarps * row_slice_floats(R, cx) * sizeof(float) > kRowSmem) continue;
+    if (R == 1 || (uint64_t)(rows + R - 1) / R >= (uint64_t)sm_count * 32) return R;
+  }
+  return 0;
+}
+
+template <uint32_t R>
+static void launch_rows(const LatticeParams& p, cudaStream_t st) {
+  const uint64_t groups = ((uint64_t)p.ny * p.nz + R - 1) / R;
+  const uint32_t blocks = (uint32_t)std::min<uint64_t>((groups + kRowWarps - 1) / kRowWarps, 1u << 30);
+  const size_t smem = (size_t)kRowWarps * row_slice_floats(R, p.cx) * sizeof(float);
+  lattice_rows_kernel<R><<<blocks, kRowWarps * 32, smem, st>>>(p);
+}
+
 cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t prep_blocks, uint32_t blocks,
-                           cudaStream_t st) {
+                           uint32_t sm_count, cudaStream_t st) {
   if (p.mode == 1) {
     lattice_prep_kernel<<<prep_blocks, 256, 0, st>>>(p, blend_buf);
     cudaError_t e = cudaGetLastError();
@@ -1043,8 +1088,13 @@ cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t pr
     q.blend = blend_buf;
     lattice_blend_kernel<<<blocks, 256, 0, st>>>(q);
   } else {
-    if (p.cx <= kRowCx) lattice_staged_kernel<<<blocks, 256, 0, st>>>(p);
-    else lattice_params_kernel<<<blocks, 256, 0, st>>>(p);
+    switch (lattice_rows_per_warp(p.cx, p.ny * p.nz, sm_count)) {
+      case 8: launch_rows<8>(p, st); break;
+      case 4: launch_rows<4>(p, st); break;
+      case 2: launch_rows<2>(p, st); break;
+      case 1: launch_rows<1>(p, st); break;
+      default: lattice_params_kernel<<<blocks, 256, 0, st>>>(p);
+    }
   }
   return cudaGetLastError();
 }

@@ -192,8 +192,10 @@ cudaError_t launch_lookback_stall(uint32_t ntiles, uint32_t stall, uint64_t wait
 
 cudaError_t launch_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t nz, float* out, uint32_t blocks,
                              cudaStream_t st);
+// PARAMS mode picks its kernel from the control-grid width (sm_count sizes the
+// row groups); blocks is the grid of the blend and unstaged forms.
 cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t prep_blocks, uint32_t blocks,
-                           cudaStream_t st);
+                           uint32_t sm_count, cudaStream_t st);
 // Batched lattice fields: one launch for instances with at most
 // GCM_BATCH_WARP_CX control columns, a second one only when some are wider.
 #define GCM_BATCH_WARP_CX 32
