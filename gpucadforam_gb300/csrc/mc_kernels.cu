@@ -28,11 +28,15 @@ namespace gcm {
 namespace {
 
 
-// Register cap per CTA size: resident CTAs per SM the kernel is compiled for.
+// Register cap per CTA size: resident CTAs per SM the kernel is compiled for,
+// 64 registers for both sizes.  128-thread CTAs: 8, the count the default
+// tile's shared memory allows at 512^3 (a cap of 10, 48 registers, spills and
+// measured 3% slower there); 256-thread CTAs: 4 (the band form's default
+// tiles fit 3 per SM).
 #ifndef GCM_MESH_MIN_BLOCKS
-#define GCM_MESH_MIN_BLOCKS 5
+#define GCM_MESH_MIN_BLOCKS 4
 #endif
-constexpr int mesh_min_blocks(int threads) { return threads >= 256 ? GCM_MESH_MIN_BLOCKS : 2 * GCM_MESH_MIN_BLOCKS; }
+constexpr int mesh_min_blocks(int threads) { return threads >= 256 ? GCM_MESH_MIN_BLOCKS : 8; }
 
 __host__ __device__ inline uint32_t align16(uint32_t x) { return (x + 15u) & ~15u; }
 
@@ -371,11 +375,16 @@ __device__ __forceinline__ void tile_emit(const TileGeom& tg, uint64_t t, const 
         row = s_tri[s_cube[v]];
         nt = (uint32_t)(row & 0xFu);
       }
-      if (__ballot_sync(0xffffffffu, nt) == 0) continue;
-      const uint32_t first = s_win[w] + warp_incl_scan(nt) - nt;
-      for (uint32_t j = 0; j < nt; ++j) {
-        const uint32_t u = first + j - base;
-        if (u < n) s_list[u] = list_entry(v, tri_edges3(row, j));
+      const uint32_t most = __reduce_max_sync(0xffffffffu, nt);
+      if (most == 0) continue;
+      const uint32_t first = s_win[w] + warp_incl_scan(nt) - nt - base;  // wraps below base
+      // unrolled over the (at most 5) triangles of a voxel, so every edge group
+      // is a constant shift; the warp stops after its largest count
+#pragma unroll
+      for (uint32_t j = 0; j < 5; ++j) {
+        if (j >= most) break;
+        const uint32_t u = first + j;
+        if (j < nt && u < n) s_list[u] = list_entry(v, tri_edges3(row, j));
       }
     }
   };
