@@ -223,47 +223,55 @@ __global__ void __launch_bounds__(256) lattice_prep_kernel(LatticeParams p, floa
 }
 
 // Sample rows are the unit of work.  PARAMS mode: a warp takes R consecutive
-// sample rows (y, z), stages per control column the rows' y/z-interpolated
-// parameters and the nearest types in its own slice of shared memory (warp
-// syncs only, no CTA barrier), and each lane then evaluates two samples of a
-// row (x and x + 32) per step, which gives the compiler two independent
-// chains.  One row group per warp and many CTAs rather than a persistent grid:
-// the block scheduler balances the SMs.  No 64-bit index arithmetic per sample.
+// sample rows (y, z) and stages, per control cell i of each row, one 48-byte
+// record in its own slice of shared memory (warp syncs only, no CTA barrier):
+// the five y/z-interpolated parameters at column i and their differences to
+// column i + 1, and the types of both columns.  A sample then reads its cell's
+// record with three 16-byte loads and interpolates each parameter with one
+// FMA (lerp(u, v, t) = fma(t, v - u, u), the same rounding as computing the
+// difference per sample).  Each lane evaluates two samples of a row (x and
+// x + 32) per step, which gives the compiler two independent chains.  One row
+// group per warp and many CTAs rather than a persistent grid: the block
+// scheduler balances the SMs.  No 64-bit index arithmetic per sample.
 constexpr uint32_t kBlendCx = 128;        // control columns staged per row (BLEND)
 constexpr uint32_t kRowWarps = 8;         // warps per CTA of lattice_rows_kernel
 constexpr size_t kRowSmem = 48 * 1024;    // shared memory of one such CTA, at most
 
-// Floats of one warp's slice: R rows x 5 parameters x cx columns, the rows'
-// (y, z) phase coordinates, then R x cx type bytes.
-__host__ __device__ constexpr uint32_t row_slice_floats(uint32_t R, uint32_t cx) {
-  return R * 5 * cx + 2 * R + (R * cx + 3) / 4;
-}
+// Cells of a row: cx - 1 (one for a single control column).
+__host__ __device__ constexpr uint32_t row_cells(uint32_t cx) { return cx > 1 ? cx - 1 : 1; }
+
+// 16-byte words of one warp's slice: R rows x cells x 3 record words, then one
+// word per row holding its (y, z) phase coordinates.
+__host__ __device__ constexpr uint32_t row_slice_words(uint32_t R, uint32_t cx) { return R * row_cells(cx) * 3 + R; }
 
 namespace {
 
-// One staged sample: x-interpolation of the row's five staged parameters,
-// rotation, phase, TPMS value.
-__device__ __forceinline__ float staged_sample(const float* __restrict__ s, const uint8_t* __restrict__ t,
-                                               uint32_t cx, const AxisCell& kx, float qx, float qy, float qz) {
-  float v[5];
-#pragma unroll
-  for (int k = 0; k < 5; ++k) v[k] = lerpf(s[k * cx + kx.i0], s[k * cx + kx.i1], kx.f);
+// One staged sample of lattice_rows_kernel from its cell's record: rotation,
+// phase, TPMS value.  The nearest control column is the cell's first or
+// second column.
+__device__ __forceinline__ float record_sample(const float4* __restrict__ rec, const AxisCell& kx, float qx,
+                                               float2 qyz) {
+  const float4* r = rec + 3 * kx.i0;
+  const float4 a = r[0], b = r[1], c = r[2];
+  const float f = kx.f;
+  const float period = __fmaf_rn(f, a.y, a.x), ex = __fmaf_rn(f, a.w, a.z), ey = __fmaf_rn(f, b.y, b.x),
+              ez = __fmaf_rn(f, b.w, b.z), thick = __fmaf_rn(f, c.y, c.x);
+  const uint32_t type = __float_as_uint(kx.nearest == kx.i0 ? c.z : c.w);
   float R9[9];
-  euler_rows(v[1], v[2], v[3], R9);
-  const float q[3] = {qx, qy, qz};
-  return lattice_value(t[kx.nearest], R9, __fdiv_rn(2.0f, v[0]), q, v[4]);
+  euler_rows(ex, ey, ez, R9);
+  const float q[3] = {qx, qyz.x, qyz.y};
+  return lattice_value(type, R9, __fdiv_rn(2.0f, period), q, thick);
 }
 
 }  // namespace
 
 template <uint32_t R>
 __global__ void __launch_bounds__(256, 4) lattice_rows_kernel(LatticeParams p) {
-  extern __shared__ float s_rows[];
-  const uint32_t cx = p.cx;
+  extern __shared__ float4 s_rows[];
+  const uint32_t cx = p.cx, cells = row_cells(cx);
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-  float* sa = s_rows + warp * row_slice_floats(R, cx);
-  float* sq = sa + R * 5 * cx;
-  uint8_t* st = reinterpret_cast<uint8_t*>(sq + 2 * R);
+  float4* rec = s_rows + warp * row_slice_words(R, cx);
+  float4* sq = rec + R * cells * 3;
   const uint32_t c[3] = {p.cx, p.cy, p.cz};
   const uint32_t nc = p.cx * p.cy * p.cz;
   const float* arr[5] = {p.period, p.euler, p.euler ? p.euler + nc : nullptr,
@@ -277,15 +285,22 @@ __global__ void __launch_bounds__(256, 4) lattice_rows_kernel(LatticeParams p) {
     uint32_t y = row0 % p.ny, z = row0 / p.ny;
     for (uint32_t r = 0; r < nr; ++r) {
       const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
+      for (uint32_t i = lane; i < cells; i += 32) {
+        const int i1 = cx > 1 ? (int)i + 1 : 0;
+        float u[5], d[5];
 #pragma unroll
-      for (uint32_t k = 0; k < 5; ++k)
-        for (uint32_t xc = lane; xc < cx; xc += 32) sa[(r * 5 + k) * cx + xc] = column_yz(arr[k], (int)xc, ky, kz, c);
-      for (uint32_t xc = lane; xc < cx; xc += 32)
-        st[r * cx + xc] = __ldg(p.type + cidx((int)xc, ky.nearest, kz.nearest, c));
-      if (lane == 0) {
-        sq[2 * r] = fs((float)y, p.origin[1]);
-        sq[2 * r + 1] = fs((float)z, p.origin[2]);
+        for (uint32_t k = 0; k < 5; ++k) {
+          u[k] = column_yz(arr[k], (int)i, ky, kz, c);
+          d[k] = fs(column_yz(arr[k], i1, ky, kz, c), u[k]);
+        }
+        const uint32_t t0 = __ldg(p.type + cidx((int)i, ky.nearest, kz.nearest, c));
+        const uint32_t t1 = __ldg(p.type + cidx(i1, ky.nearest, kz.nearest, c));
+        float4* w = rec + (r * cells + i) * 3;
+        w[0] = make_float4(u[0], d[0], u[1], d[1]);
+        w[1] = make_float4(u[2], d[2], u[3], d[3]);
+        w[2] = make_float4(u[4], d[4], __uint_as_float(t0), __uint_as_float(t1));
       }
+      if (lane == 0) sq[r] = make_float4(fs((float)y, p.origin[1]), fs((float)z, p.origin[2]), 0.0f, 0.0f);
       if (++y == p.ny) {
         y = 0;
         ++z;
@@ -302,17 +317,19 @@ __global__ void __launch_bounds__(256, 4) lattice_rows_kernel(LatticeParams p) {
         const float q1 = fs((float)x1, p.origin[0]);
 #pragma unroll 1
         for (uint32_t r = 0; r < nr; ++r) {
-          const float* s = sa + r * 5 * cx;
-          const uint8_t* t = st + r * cx;
-          const float v0 = staged_sample(s, t, cx, k0, q0, sq[2 * r], sq[2 * r + 1]);
-          const float v1 = staged_sample(s, t, cx, k1, q1, sq[2 * r], sq[2 * r + 1]);
+          const float4* rr = rec + r * cells * 3;
+          const float4 qr = sq[r];
+          const float v0 = record_sample(rr, k0, q0, make_float2(qr.x, qr.y));
+          const float v1 = record_sample(rr, k1, q1, make_float2(qr.x, qr.y));
           out[(uint64_t)r * p.nx] = v0;
           if (x1 < p.nx) out[(uint64_t)r * p.nx + 32] = v1;
         }
       } else {
 #pragma unroll 1
-        for (uint32_t r = 0; r < nr; ++r)
-          out[(uint64_t)r * p.nx] = staged_sample(sa + r * 5 * cx, st + r * cx, cx, k0, q0, sq[2 * r], sq[2 * r + 1]);
+        for (uint32_t r = 0; r < nr; ++r) {
+          const float4 qr = sq[r];
+          out[(uint64_t)r * p.nx] = record_sample(rec + r * cells * 3, k0, q0, make_float2(qr.x, qr.y));
+        }
       }
     }
   }
@@ -401,7 +418,8 @@ __global__ void __launch_bounds__(256) lattice_blend_kernel(LatticeParams p) {
 // Batched graded lattices (GCM_GRADE_PARAMS): the sample rows of all
 // instances form one sequence; a warp takes one row (the rows of these grids
 // are short) and stages that row's y/z-interpolated control columns in its own
-// slice of shared memory.  Same arithmetic as lattice_params_kernel.
+// slice of shared memory as lattice_rows_kernel's cell records.  Same
+// arithmetic as lattice_params_kernel.
 constexpr uint32_t kWarpCx = GCM_BATCH_WARP_CX;  // control columns staged per warp
 
 // STAGED: the rows of instances with at most kWarpCx control columns (the
@@ -409,8 +427,7 @@ constexpr uint32_t kWarpCx = GCM_BATCH_WARP_CX;  // control columns staged per w
 template <bool STAGED>
 __global__ void __launch_bounds__(256, 4) lattice_params_batch_kernel(const BatchLattice* inst, uint32_t n_inst,
                                                                    uint64_t total_rows) {
-  __shared__ float s_a[8][5][kWarpCx];
-  __shared__ uint8_t s_t[8][kWarpCx];
+  __shared__ float4 s_rec[8][3 * kWarpCx];  // per warp: the row's cell records (lattice_rows_kernel's form)
   const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
   uint32_t lo = 0;  // instance of the warp's row: rows only increase, so search only when it moves on
@@ -435,28 +452,38 @@ __global__ void __launch_bounds__(256, 4) lattice_params_batch_kernel(const Batc
     const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
     __syncwarp();
     if (STAGED) {
-      for (uint32_t i = lane; i < 5 * p.cx; i += 32) {
-        const uint32_t k = i / p.cx, xc = i % p.cx;
-        s_a[wib][k][xc] = column_yz(arr[k], (int)xc, ky, kz, c);
+      for (uint32_t i = lane; i < row_cells(p.cx); i += 32) {
+        const int i1 = p.cx > 1 ? (int)i + 1 : 0;
+        float u[5], d[5];
+#pragma unroll
+        for (uint32_t k = 0; k < 5; ++k) {
+          u[k] = column_yz(arr[k], (int)i, ky, kz, c);
+          d[k] = fs(column_yz(arr[k], i1, ky, kz, c), u[k]);
+        }
+        const uint32_t t0 = __ldg(p.type + cidx((int)i, ky.nearest, kz.nearest, c));
+        const uint32_t t1 = __ldg(p.type + cidx(i1, ky.nearest, kz.nearest, c));
+        float4* w = &s_rec[wib][3 * i];
+        w[0] = make_float4(u[0], d[0], u[1], d[1]);
+        w[1] = make_float4(u[2], d[2], u[3], d[3]);
+        w[2] = make_float4(u[4], d[4], __uint_as_float(t0), __uint_as_float(t1));
       }
-      for (uint32_t xc = lane; xc < p.cx; xc += 32) s_t[wib][xc] = __ldg(p.type + cidx((int)xc, ky.nearest, kz.nearest, c));
     }
     __syncwarp();
     float* out = p.out + (uint64_t)local * p.nx;
     if (STAGED) {
-      const float qy = fs((float)y, p.origin[1]), qz = fs((float)z, p.origin[2]);
+      const float2 qyz = make_float2(fs((float)y, p.origin[1]), fs((float)z, p.origin[2]));
       for (uint32_t x0 = lane; x0 < p.nx; x0 += 64) {  // two samples per lane per step
         const uint32_t x1 = x0 + 32;
         const AxisCell k0 = locate1(x0, c[0], p.scale[0]);
         const float q0 = fs((float)x0, p.origin[0]);
         if (x0 - lane + 32 < p.nx) {  // warp-uniform: the second segment holds samples
           const AxisCell k1 = locate1(min(x1, p.nx - 1), c[0], p.scale[0]);
-          const float v0 = staged_sample(&s_a[wib][0][0], s_t[wib], kWarpCx, k0, q0, qy, qz);
-          const float v1 = staged_sample(&s_a[wib][0][0], s_t[wib], kWarpCx, k1, fs((float)x1, p.origin[0]), qy, qz);
+          const float v0 = record_sample(s_rec[wib], k0, q0, qyz);
+          const float v1 = record_sample(s_rec[wib], k1, fs((float)x1, p.origin[0]), qyz);
           out[x0] = v0;
           if (x1 < p.nx) out[x1] = v1;
         } else {
-          out[x0] = staged_sample(&s_a[wib][0][0], s_t[wib], kWarpCx, k0, q0, qy, qz);
+          out[x0] = record_sample(s_rec[wib], k0, q0, qyz);
         }
       }
     } else {
@@ -1064,7 +1091,7 @@ cudaError_t launch_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t n
 // even one row's slice fits (the unstaged kernel then runs).
 uint32_t lattice_rows_per_warp(uint32_t cx, uint32_t rows, uint32_t sm_count) {
   for (uint32_t R = 8; R >= 1; R /= 2) {
-    if ((size_t)kRowWarps * row_slice_floats(R, cx) * sizeof(float) > kRowSmem) continue;
+    if ((size_t)kRowWarps * row_slice_words(R, cx) * sizeof(float4) > kRowSmem) continue;
     if (R == 1 || (uint64_t)(rows + R - 1) / R >= (uint64_t)sm_count * 32) return R;
   }
   return 0;
@@ -1074,7 +1101,7 @@ template <uint32_t R>
 static void launch_rows(const LatticeParams& p, cudaStream_t st) {
   const uint64_t groups = ((uint64_t)p.ny * p.nz + R - 1) / R;
   const uint32_t blocks = (uint32_t)std::min<uint64_t>((groups + kRowWarps - 1) / kRowWarps, 1u << 30);
-  const size_t smem = (size_t)kRowWarps * row_slice_floats(R, p.cx) * sizeof(float);
+  const size_t smem = (size_t)kRowWarps * row_slice_words(R, p.cx) * sizeof(float4);
   lattice_rows_kernel<R><<<blocks, kRowWarps * 32, smem, st>>>(p);
 }
 
