@@ -283,6 +283,30 @@ __device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v) {
   return v;
 }
 
+// Lanes below this one, as a mask.
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Bit planes of per-lane counts below 8 (three ballots): a lane's exclusive
+// prefix is sum_k 2^k popc(plane_k & lanes below), the warp's total
+// sum_k 2^k popc(plane_k).
+struct CountPlanes {
+  uint32_t b0, b1, b2;
+};
+__device__ __forceinline__ CountPlanes count_planes(uint32_t v) {
+  return {__ballot_sync(0xffffffffu, v & 1u), __ballot_sync(0xffffffffu, v & 2u), __ballot_sync(0xffffffffu, v & 4u)};
+}
+__device__ __forceinline__ uint32_t planes_total(const CountPlanes& c) {
+  return (uint32_t)__popc(c.b0) + 2u * (uint32_t)__popc(c.b1) + 4u * (uint32_t)__popc(c.b2);
+}
+__device__ __forceinline__ uint32_t planes_excl(const CountPlanes& c) {
+  const uint32_t lt = lanemask_lt();
+  return (uint32_t)__popc(c.b0 & lt) + 2u * (uint32_t)__popc(c.b1 & lt) + 4u * (uint32_t)__popc(c.b2 & lt);
+}
+
 __device__ __forceinline__ uint32_t warp_sum_u32(uint32_t v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

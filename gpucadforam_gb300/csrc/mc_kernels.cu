@@ -306,8 +306,10 @@ __device__ __forceinline__ void tile_classify(const TileGeom& tg, const MeshLayo
       s_cube[r * vx + x] = (uint8_t)ci;
       nt = (uint32_t)(s_tri[ci] & 0xFu);
     }
-    my_active += __popc(__ballot_sync(0xffffffffu, nt > 0));
-    const uint32_t wsum = warp_sum_u32(nt);
+    // triangle counts are 0..5: the window's total from three ballots
+    const CountPlanes cp = count_planes(nt);
+    my_active += __popc(cp.b0 | cp.b1 | cp.b2);
+    const uint32_t wsum = planes_total(cp);
     if (lane == 0) s_win[w] = wsum;
   }
   if (lane == 0 && my_active) atomicAdd(&res.active, my_active);
@@ -377,7 +379,7 @@ __device__ __forceinline__ void tile_emit(const TileGeom& tg, uint64_t t, const 
       }
       const uint32_t most = __reduce_max_sync(0xffffffffu, nt);
       if (most == 0) continue;
-      const uint32_t first = s_win[w] + warp_incl_scan(nt) - nt - base;  // wraps below base
+      const uint32_t first = s_win[w] + planes_excl(count_planes(nt)) - base;  // wraps below base
       // unrolled over the (at most 5) triangles of a voxel, so every edge group
       // is a constant shift; the warp stops after its largest count
 #pragma unroll

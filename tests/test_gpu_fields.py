@@ -102,6 +102,38 @@ def test_graded_lattice_vs_oracle(ctx, mode, shape):
     assert err.max() < 4e-5, err.max()
 
 
+@pytest.mark.parametrize("shape,ctrl", [
+    ((200, 200, 64), (16, 16, 16)),   # 40,000 sample rows: 8 rows per warp
+    ((150, 150, 64), (16, 16, 16)),   # 22,500 rows: 4 per warp
+    ((110, 110, 70), (16, 16, 16)),   # 12,100 rows: 2 per warp; rows of 70 end on a single-sample step
+    ((40, 40, 100), (16, 16, 16)),    # 1,600 rows: 1 per warp; a ragged second segment
+    ((24, 20, 300), (64, 4, 4)),      # 64 control columns: one row's records per warp fit
+    ((12, 10, 500), (200, 3, 3)),     # 200 control columns: the unstaged kernel
+])
+def test_graded_lattice_kernel_forms_vs_oracle(ctx, shape, ctrl):
+    """Each staged form of the PARAMS field kernel (rows per warp picked from
+    the row count and the control-grid width) and the unstaged kernel agree
+    with the FP32 oracle to the trig tolerance."""
+    from gpucadforam_gb300.mesher import Lattice
+
+    nz, ny, nx = shape
+    rng = np.random.default_rng(sum(shape) + sum(ctrl))
+    n = ctrl[0] * ctrl[1] * ctrl[2]
+    period = rng.uniform(16, 64, n).astype(np.float32)
+    euler = rng.uniform(-np.pi / 4, np.pi / 4, 3 * n).astype(np.float32)
+    thick = rng.uniform(-0.6, 0.6, n).astype(np.float32)
+    types = rng.choice(np.array([0, 1, 2, 3, 5], np.uint8), n)
+    origin = ((nx - 1) / 2, (ny - 1) / 2, (nz - 1) / 2)
+    lat = Lattice.from_numpy(0, ctrl, period, euler, thick, types, origin)
+    got = host(ctx.lattice_field(lat, shape))
+    ref32 = O.lattice_field((nx, ny, nz), 0, ctrl, period, euler, thick, types, origin)
+    # as in the test above: an ulp of a rotation entry moves the phase by
+    # |q| * 2/period * ulp, so the absolute bound grows with the largest |q|
+    qmax = float(np.linalg.norm(np.array([nx, ny, nz], np.float64) / 2))
+    err = np.abs(got.reshape(-1).astype(np.float64) - ref32.reshape(-1).astype(np.float64))
+    assert err.max() < 2e-5 * max(1.0, qmax / 84), err.max()
+
+
 def test_c1_uniform_gyroid_fp64(ctx):
     from gpucadforam_gb300.mesher import Lattice
 
