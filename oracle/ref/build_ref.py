@@ -8,7 +8,7 @@ working tree).  Outputs:
 * ``oracle/_ref/ref_<name>_sm103a.fatbin`` - device code compiled for sm_103a;
 * ``oracle/_ref/ref_<name>_ptx89.fatbin``  - device code as the reference's own
   Makefile ships it (``-gencode arch=compute_89,code=compute_89``, PTX only, JIT
-  compiled by the driver at load time), Makefile:46-48;
+  compiled by the CUDA driver at load time), Makefile:46-48;
 * ``tests/golden/ref_tables.bin`` - the reference's tables.h data, dumped by a tiny
   host program (``oracle/ref/dump_tables.cpp``);
 * ``oracle/_ref/obj_ref_writer`` - the reference's own ``.obj`` writer
