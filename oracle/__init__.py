@@ -1,8 +1,8 @@
 """ctypes front end of the CPU oracle (oracle/oracle.cpp).
 
 TEST INFRASTRUCTURE ONLY.  Imported by tests/, ``__graft_entry__.smoke()`` and
-the CPU-baseline leg of ``bench.py`` as the checker; the product package never
-imports it.  Every function mirrors one reference routine; see oracle.cpp for
+the CPU-baseline leg of ``bench.py``, to check and time against; the product
+package never imports it.  Every function mirrors one reference routine; see oracle.cpp for
 the file:line each one restates.
 """
 from __future__ import annotations

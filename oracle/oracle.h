@@ -1,6 +1,6 @@
 // CPU oracle for the field -> mesh path.  TEST INFRASTRUCTURE ONLY: the tests,
-// the smoke check and bench.py's CPU-baseline leg call it as the checker; the
-// product never links, loads or falls back to it.
+// the smoke check and bench.py's CPU-baseline leg call it to check and time
+// against; the product never links, loads or falls back to it.
 //
 // Each function restates one piece of the reference (DESIGN4ADDITIVE/GPUCADforAM)
 // and cites the file:line it follows.  Grid conventions are the reference's:
