@@ -452,20 +452,26 @@ __global__ void __launch_bounds__(256, 4) lattice_params_batch_kernel(const Batc
     const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
     __syncwarp();
     if (STAGED) {
-      for (uint32_t i = lane; i < row_cells(p.cx); i += 32) {
-        const int i1 = p.cx > 1 ? (int)i + 1 : 0;
-        float u[5], d[5];
+      // one control column per lane (at most kWarpCx = 32 of them); a cell's
+      // second column is the next lane's (a single column is its own)
+      const bool has_col = lane < p.cx;
+      float u[5], v[5];
 #pragma unroll
-        for (uint32_t k = 0; k < 5; ++k) {
-          u[k] = column_yz(arr[k], (int)i, ky, kz, c);
-          d[k] = fs(column_yz(arr[k], i1, ky, kz, c), u[k]);
-        }
-        const uint32_t t0 = __ldg(p.type + cidx((int)i, ky.nearest, kz.nearest, c));
-        const uint32_t t1 = __ldg(p.type + cidx(i1, ky.nearest, kz.nearest, c));
-        float4* w = &s_rec[wib][3 * i];
-        w[0] = make_float4(u[0], d[0], u[1], d[1]);
-        w[1] = make_float4(u[2], d[2], u[3], d[3]);
-        w[2] = make_float4(u[4], d[4], __uint_as_float(t0), __uint_as_float(t1));
+      for (uint32_t k = 0; k < 5; ++k) u[k] = has_col ? column_yz(arr[k], (int)lane, ky, kz, c) : 0.0f;
+      const uint32_t t0 = has_col ? __ldg(p.type + cidx((int)lane, ky.nearest, kz.nearest, c)) : 0u;
+      uint32_t t1 = __shfl_down_sync(0xffffffffu, t0, 1);
+#pragma unroll
+      for (uint32_t k = 0; k < 5; ++k) v[k] = __shfl_down_sync(0xffffffffu, u[k], 1);
+      if (p.cx == 1) {
+#pragma unroll
+        for (uint32_t k = 0; k < 5; ++k) v[k] = u[k];
+        t1 = t0;
+      }
+      if (lane < row_cells(p.cx)) {
+        float4* w = &s_rec[wib][3 * lane];
+        w[0] = make_float4(u[0], fs(v[0], u[0]), u[1], fs(v[1], u[1]));
+        w[1] = make_float4(u[2], fs(v[2], u[2]), u[3], fs(v[3], u[3]));
+        w[2] = make_float4(u[4], fs(v[4], u[4]), __uint_as_float(t0), __uint_as_float(t1));
       }
     }
     __syncwarp();
