@@ -360,7 +360,9 @@ void format_faces(const uint32_t* f, uint64_t b, uint64_t e, std::string& out) {
 template <class Fmt, class T>
 bool write_lines(FILE* fp, const T* data, uint64_t count, Fmt fmt) {
   const unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
-  const uint64_t block = 1ull << 20;  // lines per parallel block
+  // lines per thread and pass: the count spread over the threads, at least
+  // 4096 (thread start-up) and at most 2^20 (64 MB of text per thread buffer)
+  const uint64_t block = std::min<uint64_t>(1ull << 20, std::max<uint64_t>(4096, (count + nt - 1) / nt));
   std::vector<std::string> bufs(nt);
   for (uint64_t b0 = 0; b0 < count; b0 += block * nt) {
     std::vector<std::thread> th;
