@@ -138,3 +138,38 @@ def test_batch_with_wide_control_grid(ctx):
             assert norm[a:e].cpu().numpy().tobytes() == pnorm.cpu().numpy().tobytes(), i
     finally:
         b.close()
+
+
+@pytest.mark.parametrize("cw", [(1, 1, 1), (2, 2, 2), (32, 3, 2), (31, 1, 4)])
+def test_batch_staged_control_grid_edges(ctx, cw):
+    """The staged batched field form holds one control column per lane and
+    takes each cell's second column from the next lane: a single column (its
+    own), two columns, and 31 or 32 columns (every lane holding one) must
+    give each instance its one-at-a-time mesh bit for bit."""
+    from gpucadforam_gb300.mesher import Batch, Lattice, random_batch_lattices
+
+    lats, shapes = random_batch_lattices(2, seed=0xD4A + 11, dims=(24, 56))
+    rng = np.random.default_rng(sum(cw))
+    nc = int(np.prod(cw))
+    shape = (36, 30, 75)
+    lats.insert(1, Lattice.from_numpy(0, cw, rng.uniform(12, 40, nc).astype(np.float32),
+                                      rng.uniform(-np.pi / 4, np.pi / 4, 3 * nc).astype(np.float32),
+                                      rng.uniform(-0.6, 0.6, nc).astype(np.float32),
+                                      rng.choice(np.array([0, 1, 2, 3, 5], np.uint8), nc),
+                                      origin=((shape[2] - 1) / 2, (shape[1] - 1) / 2, (shape[0] - 1) / 2)))
+    shapes.insert(1, shape)
+    b = Batch(ctx, lats, shapes)
+    try:
+        verts, active, tot = b.count()
+        pos, norm, offsets, counts = b.buffers(tot.total_verts)
+        b.mesh_async(pos, norm, offsets, counts)
+        torch.cuda.synchronize()
+        off = offsets.cpu().numpy().view(np.uint64)
+        for i, (lat, shp) in enumerate(zip(lats, shapes)):
+            ppos, pnorm, pc = _plain(ctx, lat, shp)
+            a, e = int(off[i]), int(off[i + 1])
+            assert e - a == pc.total_verts, i
+            assert pos[a:e].cpu().numpy().tobytes() == ppos.cpu().numpy().tobytes(), i
+            assert norm[a:e].cpu().numpy().tobytes() == pnorm.cpu().numpy().tobytes(), i
+    finally:
+        b.close()
