@@ -144,7 +144,7 @@ gcm_status launch_fields(gcm_batch* b, cudaStream_t st) {
   if (b->n_params) {
     // about 8 rows per warp (8 warps per CTA): many CTAs rather than one
     // resident wave, so the block scheduler balances the SMs
-    const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((b->param_rows + 63) / 64, 1u << 30));
+    const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((b->param_rows + 63) / 64, 1u << 26));
     GCM_CUDA(ctx, launch_lattice_batch(b->d_lat, b->n_params, b->param_rows, blocks, b->params_wide, st));
     count_launch(ctx, b->params_wide ? 2 : 1);
   }

@@ -1106,7 +1106,9 @@ uint32_t lattice_rows_per_warp(uint32_t cx, uint32_t rows, uint32_t sm_count) {
 template <uint32_t R>
 static void launch_rows(const LatticeParams& p, cudaStream_t st) {
   const uint64_t groups = ((uint64_t)p.ny * p.nz + R - 1) / R;
-  const uint32_t blocks = (uint32_t)std::min<uint64_t>((groups + kRowWarps - 1) / kRowWarps, 1u << 30);
+  // at most 2^26 CTAs, so the kernel's 32-bit warp stride cannot wrap (the
+  // group loop covers the rest)
+  const uint32_t blocks = (uint32_t)std::min<uint64_t>((groups + kRowWarps - 1) / kRowWarps, 1u << 26);
   const size_t smem = (size_t)kRowWarps * row_slice_words(R, p.cx) * sizeof(float4);
   lattice_rows_kernel<R><<<blocks, kRowWarps * 32, smem, st>>>(p);
 }
