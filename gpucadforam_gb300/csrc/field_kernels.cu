@@ -51,33 +51,44 @@ __device__ __forceinline__ float tpms_sc(uint32_t type, float sX, float cX, floa
   }
 }
 
-// sin and cos: for |x| <= pi/4 their Taylor series to degree 11 and 12
-// (truncation below 2e-9 there) in Horner form, else sincosf.
+// sin and cos for |x| <= pi/4: their Taylor series to degree 11 and 12
+// (truncation below 2e-9 there) in Horner form.
+__device__ __forceinline__ void sincos_taylor(float x, float* s, float* c) {
+  const float x2 = fm(x, x);
+  float ps = __fmaf_rn(x2, -2.5052108e-8f, 2.7557319e-6f);  // -1/11!, 1/9!
+  ps = __fmaf_rn(x2, ps, -1.9841270e-4f);                   // -1/7!
+  ps = __fmaf_rn(x2, ps, 8.3333333e-3f);                    // 1/5!
+  ps = __fmaf_rn(x2, ps, -1.6666667e-1f);                   // -1/3!
+  *s = __fmaf_rn(fm(x, x2), ps, x);
+  float pc = __fmaf_rn(x2, 2.0876757e-9f, -2.7557319e-7f);  // 1/12!, -1/10!
+  pc = __fmaf_rn(x2, pc, 2.4801587e-5f);                    // 1/8!
+  pc = __fmaf_rn(x2, pc, -1.3888889e-3f);                   // -1/6!
+  pc = __fmaf_rn(x2, pc, 4.1666667e-2f);                    // 1/4!
+  pc = __fmaf_rn(x2, pc, -0.5f);                            // -1/2!
+  *c = __fmaf_rn(x2, pc, 1.0f);
+}
+
+// sin and cos: the Taylor series above for |x| <= pi/4, else sincosf.
 __device__ __forceinline__ void sincos_small(float x, float* s, float* c) {
-  if (fabsf(x) <= 0.78539818f) {
-    const float x2 = fm(x, x);
-    float ps = __fmaf_rn(x2, -2.5052108e-8f, 2.7557319e-6f);  // -1/11!, 1/9!
-    ps = __fmaf_rn(x2, ps, -1.9841270e-4f);                   // -1/7!
-    ps = __fmaf_rn(x2, ps, 8.3333333e-3f);                    // 1/5!
-    ps = __fmaf_rn(x2, ps, -1.6666667e-1f);                   // -1/3!
-    *s = __fmaf_rn(fm(x, x2), ps, x);
-    float pc = __fmaf_rn(x2, 2.0876757e-9f, -2.7557319e-7f);  // 1/12!, -1/10!
-    pc = __fmaf_rn(x2, pc, 2.4801587e-5f);                    // 1/8!
-    pc = __fmaf_rn(x2, pc, -1.3888889e-3f);                   // -1/6!
-    pc = __fmaf_rn(x2, pc, 4.1666667e-2f);                    // 1/4!
-    pc = __fmaf_rn(x2, pc, -0.5f);                            // -1/2!
-    *c = __fmaf_rn(x2, pc, 1.0f);
-  } else {
-    sincosf(x, s, c);
-  }
+  if (fabsf(x) <= 0.78539818f) sincos_taylor(x, s, c);
+  else sincosf(x, s, c);
 }
 
 // Euler basis rows, ZYX convention of src/Modelling.cu:401-407.
 __device__ __forceinline__ void euler_rows(float ax, float ay, float az, float R[9]) {
   float sx, cx, sy, cy, sz, cz;
-  sincos_small(ax, &sx, &cx);
-  sincos_small(ay, &sy, &cy);
-  sincos_small(az, &sz, &cz);
+  constexpr float kQuarter = 0.78539818f;
+  if (fabsf(ax) <= kQuarter && fabsf(ay) <= kQuarter && fabsf(az) <= kQuarter) {
+    // one test for the three angles (false for NaN, which takes the
+    // per-angle path): the same values as sincos_small gives each of them
+    sincos_taylor(ax, &sx, &cx);
+    sincos_taylor(ay, &sy, &cy);
+    sincos_taylor(az, &sz, &cz);
+  } else {
+    sincos_small(ax, &sx, &cx);
+    sincos_small(ay, &sy, &cy);
+    sincos_small(az, &sz, &cz);
+  }
   R[0] = fm(cz, cy);
   R[1] = fs(fm(fm(cz, sy), sx), fm(sz, cx));
   R[2] = fa(fm(fm(cz, sy), cx), fm(sz, sx));
