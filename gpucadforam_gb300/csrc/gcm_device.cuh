@@ -307,12 +307,6 @@ __device__ __forceinline__ uint32_t planes_excl(const CountPlanes& c) {
   return (uint32_t)__popc(c.b0 & lt) + 2u * (uint32_t)__popc(c.b1 & lt) + 4u * (uint32_t)__popc(c.b2 & lt);
 }
 
-__device__ __forceinline__ uint32_t warp_sum_u32(uint32_t v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
 __device__ __forceinline__ uint64_t global_timer_ns() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
