@@ -20,7 +20,7 @@ REPO = os.path.dirname(HERE)
 
 SOURCES = ["mc_kernels.cu", "field_kernels.cu", "api.cu", "mesh_noalloc.cu", "obj_writer.cu", "batch.cu", "server.cu",
            "svl.cu"]
-HEADERS = ["gcm_device.cuh", "gcm_kernels.h", "mc_tables.h", "gcm_ctx.h", "pool.h"]
+HEADERS = ["gcm_device.cuh", "gcm_kernels.h", "mc_tables.h", "angle_table.h", "gcm_ctx.h", "pool.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]

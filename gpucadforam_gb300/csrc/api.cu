@@ -613,7 +613,7 @@ static gcm_status run_lattice(gcm_ctx* ctx, LatticeParams& p, float* d_out, cuda
   p.out = d_out;
   if (p.mode == GCM_GRADE_BLEND) {
     const uint64_t nc = (uint64_t)p.cx * p.cy * p.cz;
-    gcm_status s = ensure_buffer(ctx, &ctx->blend_buf, &ctx->blend_bytes, nc * 12 * sizeof(float));
+    gcm_status s = ensure_buffer(ctx, &ctx->blend_buf, &ctx->blend_bytes, nc * GCM_BLEND_WORDS * sizeof(float));
     if (s) return s;
     GCM_CUDA(ctx, gcm::launch_lattice(p, ctx->blend_buf, grid_blocks(ctx, nc, 256), row_blocks(ctx, p.ny, p.nz),
                                       (uint32_t)ctx->sm_count, st));

@@ -321,7 +321,7 @@ gcm_status gcm_batch_create(gcm_ctx* ctx, const gcm_batch_instance* h_instances,
   if (e == cudaSuccess && !lat.empty())
     e = cudaMemcpy(b->d_lat, lat.data(), sizeof(BatchLattice) * lat.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess && max_blend_ctrl)
-    e = cudaMalloc(reinterpret_cast<void**>(&b->blend_buf), max_blend_ctrl * 12 * sizeof(float));
+    e = cudaMalloc(reinterpret_cast<void**>(&b->blend_buf), max_blend_ctrl * GCM_BLEND_WORDS * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&b->d_inst), sizeof(uint64_t) * (3 * (size_t)n + 1));
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&b->d_counts_internal), sizeof(gcm_counts));
   if (e != cudaSuccess) s = cuda_fail(ctx, e, "gcm_batch_create allocation");

@@ -11,6 +11,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "angle_table.h"
 #include "gcm_device.cuh"
 #include "gcm_kernels.h"
 
@@ -100,16 +101,164 @@ __device__ __forceinline__ void euler_rows(float ax, float ay, float az, float R
   R[8] = fm(cy, cx);
 }
 
-// One lattice: phase X = (R q) * h in half-turns (h = 2 / period).
-__device__ __forceinline__ float lattice_value(uint32_t type, const float R[9], float h, const float q[3],
-                                               float thick) {
+// ---------------------------------------------------------------------------
+// Compensated FP32 arithmetic of the graded lattices.  The phase X of a 512^3
+// lattice reaches ~55 half-turns, where one float ulp is 4e-6 half-turns; so
+// the parameters, 2/period, the sines and cosines of the Euler angles, the
+// rotation and the phase are carried as pairs of floats (hi + lo, ~40 bits)
+// and X is reduced mod 2 before its own sin/cos.  Every step is an IEEE float
+// add, sub, mul, fma or div in a fixed order (explicit intrinsics, nothing
+// contracted), with double add/mul/div/rint only for angles outside
+// [-3.156, 3.156]; a CPU restatement of the same sequence gives the same bits.
+// ---------------------------------------------------------------------------
+struct PF {
+  float h, l;
+};
+
+__device__ __forceinline__ float fmaf_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// s + e = a + b exactly (Knuth's branch-free two-sum).
+__device__ __forceinline__ PF two_sum(float a, float b) {
+  const float s = fa(a, b), bb = fs(s, a);
+  return {s, fa(fs(a, fs(s, bb)), fs(b, bb))};
+}
+__device__ __forceinline__ PF pf_diff(PF b, PF a) {
+  const PF d = two_sum(b.h, -a.h);
+  return {d.h, fa(d.l, fs(b.l, a.l))};
+}
+// u + t * d
+__device__ __forceinline__ PF pf_at(PF u, PF d, float t) {
+  const float p = fm(t, d.h);
+  float pe = fmaf_(t, d.h, -p);
+  pe = fmaf_(t, d.l, pe);
+  const PF s = two_sum(u.h, p);
+  return {s.h, fa(fa(s.l, pe), u.l)};
+}
+__device__ __forceinline__ PF pf_lerp(PF a, PF b, float t) { return pf_at(a, pf_diff(b, a), t); }
+__device__ __forceinline__ PF pf_mulf(PF a, float f) {
+  const float p = fm(a.h, f);
+  float pe = fmaf_(a.h, f, -p);
+  pe = fmaf_(a.l, f, pe);
+  return {p, pe};
+}
+__device__ __forceinline__ PF pf_mul(PF a, PF b) {
+  const float p = fm(a.h, b.h);
+  float pe = fmaf_(a.h, b.h, -p);
+  pe = fmaf_(a.h, b.l, pe);
+  pe = fmaf_(a.l, b.h, pe);
+  return {p, pe};
+}
+__device__ __forceinline__ PF pf_add(PF a, PF b) {
+  const PF s = two_sum(a.h, b.h);
+  return {s.h, fa(s.l, fa(a.l, b.l))};
+}
+__device__ __forceinline__ PF pf_neg(PF a) { return {-a.h, -a.l}; }
+// 2 / P: the correctly rounded quotient and its remainder term
+__device__ __forceinline__ PF pf_two_over(PF P) {
+  const float hh = __fdiv_rn(2.0f, P.h);
+  float r = fmaf_(-hh, P.h, 2.0f);
+  r = fmaf_(-hh, P.l, r);
+  return {hh, fm(r, fm(0.5f, hh))};
+}
+
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23: adding it rounds to an integer
+constexpr uint32_t kAngleRows = 2 * GCM_ANGLE_K + 1;
+
+// sin and cos of an angle pair: the table's sin/cos(k/32) pair nearest the
+// angle, corrected by the Taylor series of the remainder d (|d| <= 1/64, terms
+// to d^4), renormalised so that later products drop only lo * lo terms.
+__device__ __forceinline__ void pf_sincos(PF a, const float4* __restrict__ tab, PF& s, PF& c) {
+  if (!(fabsf(a.h) <= (float)GCM_ANGLE_K / GCM_ANGLE_STEP_INV)) {
+    // rare: reduce by 2 pi in double (NaN and infinities stay NaN)
+    const double two_pi = 6.283185307179586;
+    double A = __dadd_rn((double)a.h, (double)a.l);
+    const double m = rint(__ddiv_rn(A, two_pi));
+    A = __dsub_rn(A, __dmul_rn(m, two_pi));
+    a.h = __double2float_rn(A);
+    a.l = __double2float_rn(__dsub_rn(A, (double)a.h));
+  }
+  const float t = fmaf_(a.h, (float)GCM_ANGLE_STEP_INV, kMagic);
+  const float kf = fs(t, kMagic);
+  const int k = min(max(__float_as_int(t) - __float_as_int(kMagic), -GCM_ANGLE_K), GCM_ANGLE_K);
+  float d = fmaf_(kf, -1.0f / GCM_ANGLE_STEP_INV, a.h);
+  d = fa(d, a.l);
+  const float4 e = tab[k + GCM_ANGLE_K];
+  const float d2 = fm(d, d), d3 = fm(d2, d);
+  const float sd = fmaf_(d3, -0x1.555556p-3f, d);
+  const float cm1 = fm(d2, fmaf_(d2, 0x1.555556p-5f, -0.5f));
+  float sl = fmaf_(e.x, cm1, e.y);
+  sl = fmaf_(e.z, sd, sl);
+  sl = fmaf_(e.w, sd, sl);
+  float cl = fmaf_(e.z, cm1, e.w);
+  cl = fmaf_(-e.x, sd, cl);
+  cl = fmaf_(-e.y, sd, cl);
+  s = two_sum(e.x, sl);
+  c = two_sum(e.z, cl);
+}
+
+// X mod 2 (half-turns) as one float.
+__device__ __forceinline__ float pf_reduce(PF X) {
+  const float t = fmaf_(X.h, 0.5f, kMagic);
+  const float kf = fs(t, kMagic);
+  return fa(fmaf_(kf, -2.0f, X.h), X.l);
+}
+
+// sin(pi r), cos(pi r): quarter turn j = rint(2r), u = r - j/2 (|u| <= 1/4),
+// Taylor polynomials of sin(pi u) to u^9 and cos(pi u) to u^10.
+__device__ __forceinline__ void sincospi_taylor(float r, float& s, float& c) {
+  const float t = fmaf_(r, 2.0f, kMagic);
+  const float jf = fs(t, kMagic);
+  const int j = __float_as_int(t) & 3;
+  const float u = fmaf_(jf, -0.5f, r);
+  const float z = fm(u, u);
+  float ps = fmaf_(z, GCM_SINPI_C9, GCM_SINPI_C7);
+  ps = fmaf_(z, ps, GCM_SINPI_C5);
+  ps = fmaf_(z, ps, GCM_SINPI_C3);
+  ps = fmaf_(z, ps, GCM_SINPI_C1);
+  const float sn = fm(u, ps);
+  float pc = fmaf_(z, GCM_COSPI_C10, GCM_COSPI_C8);
+  pc = fmaf_(z, pc, GCM_COSPI_C6);
+  pc = fmaf_(z, pc, GCM_COSPI_C4);
+  pc = fmaf_(z, pc, GCM_COSPI_C2);
+  const float cs = fmaf_(z, pc, 1.0f);
+  const bool swap = (j & 1) != 0;
+  const float a = swap ? cs : sn, b = swap ? sn : cs;
+  s = (j == 0 || j == 1) ? a : -a;
+  c = (j == 0 || j == 3) ? b : -b;
+}
+
+__device__ __forceinline__ float tpms_of_phase(uint32_t type, const float r[3], float thick) {
   float s[3], c[3];
 #pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    const float X = fm(__fmaf_rn(R[3 * r + 2], q[2], __fmaf_rn(R[3 * r + 1], q[1], fm(R[3 * r], q[0]))), h);
-    sincospif(X, &s[r], &c[r]);
-  }
+  for (int k = 0; k < 3; ++k) sincospi_taylor(r[k], s[k], c[k]);
   return fs(tpms_sc(type, s[0], c[0], s[1], c[1], s[2], c[2]), thick);
+}
+
+// PARAMS phase: q rotated about x, then y, then z (the rows of Modelling.cu:
+// 401-407 applied one axis at a time), scaled by 2/P, reduced mod 2.
+__device__ __forceinline__ void params_phase(PF P, PF ax, PF ay, PF az, const float q[3],
+                                             const float4* __restrict__ tab, float r[3]) {
+  PF sx, cx, sy, cy, sz, cz;
+  pf_sincos(ax, tab, sx, cx);
+  pf_sincos(ay, tab, sy, cy);
+  pf_sincos(az, tab, sz, cz);
+  const PF v1 = pf_add(pf_mulf(cx, q[1]), pf_neg(pf_mulf(sx, q[2])));
+  const PF v2 = pf_add(pf_mulf(sx, q[1]), pf_mulf(cx, q[2]));
+  const PF w0 = pf_add(pf_mulf(cy, q[0]), pf_mul(sy, v2));
+  const PF w2 = pf_add(pf_mul(cy, v2), pf_neg(pf_mulf(sy, q[0])));
+  const PF X0 = pf_add(pf_mul(cz, w0), pf_neg(pf_mul(sz, v1)));
+  const PF X1 = pf_add(pf_mul(sz, w0), pf_mul(cz, v1));
+  const PF H = pf_two_over(P);
+  r[0] = pf_reduce(pf_mul(X0, H));
+  r[1] = pf_reduce(pf_mul(X1, H));
+  r[2] = pf_reduce(pf_mul(w2, H));
+}
+
+// The angle table, copied into shared memory by every graded-lattice CTA.
+__device__ const float4 kAngleTable[kAngleRows] = {GCM_ANGLE_TABLE_ROWS};
+
+__device__ __forceinline__ void load_angle_table(float4* s_tab) {
+  for (uint32_t i = threadIdx.x; i < kAngleRows; i += blockDim.x) s_tab[i] = kAngleTable[i];
 }
 
 // Control-grid cell of one sample coordinate along one axis: the cell index
@@ -216,73 +365,155 @@ __global__ void __launch_bounds__(256) unit_cell_kernel(uint32_t type, uint32_t 
 // Graded lattices.
 // ---------------------------------------------------------------------------
 
-// Blend mode setup: per control point the rotation rows, 2/period, thickness
-// and type, 12 words each.
+// Blend mode setup: per control point M = R * (2 / period) in double from the
+// angle table's sin/cos pairs (rotation rows of Modelling.cu:401-407), each
+// entry split into a float pair, then thickness and type:
+// GCM_BLEND_WORDS = 20 words (M[r][j] hi, lo at 2 (3r + j)).
 __global__ void __launch_bounds__(256) lattice_prep_kernel(LatticeParams p, float* blend_out) {
   const uint32_t n = p.cx * p.cy * p.cz;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    float R[9];
-    const float ax = p.euler ? p.euler[i] : 0.0f, ay = p.euler ? p.euler[n + i] : 0.0f,
-                az = p.euler ? p.euler[2 * n + i] : 0.0f;
-    euler_rows(ax, ay, az, R);
-    float* o = blend_out + 12 * (uint64_t)i;
-    for (int k = 0; k < 9; ++k) o[k] = R[k];
-    o[9] = __fdiv_rn(2.0f, p.period[i]);
-    o[10] = p.thickness ? p.thickness[i] : 0.0f;
-    o[11] = __uint_as_float((uint32_t)p.type[i]);
+    const float ang[3] = {p.euler ? p.euler[i] : 0.0f, p.euler ? p.euler[n + i] : 0.0f,
+                          p.euler ? p.euler[2 * n + i] : 0.0f};
+    double S[3], C[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      PF s, c;
+      pf_sincos({ang[a], 0.0f}, kAngleTable, s, c);
+      S[a] = __dadd_rn((double)s.h, (double)s.l);
+      C[a] = __dadd_rn((double)c.h, (double)c.l);
+    }
+    const double sx = S[0], cx = C[0], sy = S[1], cy = C[1], sz = S[2], cz = C[2];
+    double R[9];
+    R[0] = __dmul_rn(cz, cy);
+    R[1] = __dsub_rn(__dmul_rn(__dmul_rn(cz, sy), sx), __dmul_rn(sz, cx));
+    R[2] = __dadd_rn(__dmul_rn(__dmul_rn(cz, sy), cx), __dmul_rn(sz, sx));
+    R[3] = __dmul_rn(sz, cy);
+    R[4] = __dadd_rn(__dmul_rn(__dmul_rn(sz, sy), sx), __dmul_rn(cz, cx));
+    R[5] = __dsub_rn(__dmul_rn(__dmul_rn(sz, sy), cx), __dmul_rn(cz, sx));
+    R[6] = -sy;
+    R[7] = __dmul_rn(cy, sx);
+    R[8] = __dmul_rn(cy, cx);
+    const double H = __ddiv_rn(2.0, (double)p.period[i]);
+    float* o = blend_out + GCM_BLEND_WORDS * (uint64_t)i;
+    for (int k = 0; k < 9; ++k) {
+      const double m = __dmul_rn(R[k], H);
+      const float hi = __double2float_rn(m);
+      o[2 * k] = hi;
+      o[2 * k + 1] = __double2float_rn(__dsub_rn(m, (double)hi));
+    }
+    o[18] = p.thickness ? p.thickness[i] : 0.0f;
+    o[19] = __uint_as_float((uint32_t)p.type[i]);
   }
 }
 
 // Sample rows are the unit of work.  PARAMS mode: a warp takes R consecutive
-// sample rows (y, z) and stages, per control cell i of each row, one 48-byte
-// record in its own slice of shared memory (warp syncs only, no CTA barrier):
-// the five y/z-interpolated parameters at column i and their differences to
-// column i + 1, and the types of both columns.  A sample then reads its cell's
-// record with three 16-byte loads and interpolates each parameter with one
-// FMA (lerp(u, v, t) = fma(t, v - u, u), the same rounding as computing the
-// difference per sample).  Each lane evaluates two samples of a row (x and
-// x + 32) per step, which gives the compiler two independent chains.  One row
-// group per warp and many CTAs rather than a persistent grid: the block
-// scheduler balances the SMs.  No 64-bit index arithmetic per sample.
+// sample rows (y, z) and stages, per control cell i of each row, one 80-byte
+// record in its own slice of shared memory (warp syncs only): for period and
+// the three Euler angles the y/z-interpolated value at column i and its
+// difference to column i + 1 as float pairs, then thickness (value and
+// difference) and the types of both columns.  A sample reads its cell's
+// record with five 16-byte loads and finishes each parameter with one
+// compensated step u + fx * d.  Each lane evaluates two samples of a row (x
+// and x + 32) per step.  One row group per warp and many CTAs rather than a
+// persistent grid: the block scheduler balances the SMs.
 constexpr uint32_t kBlendCx = 128;        // control columns staged per row (BLEND)
 constexpr uint32_t kRowWarps = 8;         // warps per CTA of lattice_rows_kernel
 constexpr size_t kRowSmem = 48 * 1024;    // shared memory of one such CTA, at most
+constexpr uint32_t kRecWords = 5;         // 16-byte words of one cell record
 
 // Cells of a row: cx - 1 (one for a single control column).
 __host__ __device__ constexpr uint32_t row_cells(uint32_t cx) { return cx > 1 ? cx - 1 : 1; }
 
-// 16-byte words of one warp's slice: R rows x cells x 3 record words, then one
-// word per row holding its (y, z) phase coordinates.
-__host__ __device__ constexpr uint32_t row_slice_words(uint32_t R, uint32_t cx) { return R * row_cells(cx) * 3 + R; }
+// 16-byte words of one warp's slice: R rows x cells x kRecWords record words,
+// then one word per row holding its (y, z) phase coordinates.
+__host__ __device__ constexpr uint32_t row_slice_words(uint32_t R, uint32_t cx) {
+  return R * row_cells(cx) * kRecWords + R;
+}
+// dynamic shared memory of lattice_rows_kernel: the angle table, then the slices
+__host__ __device__ constexpr size_t row_smem_bytes(uint32_t R, uint32_t cx) {
+  return (kAngleRows + (size_t)kRowWarps * row_slice_words(R, cx)) * sizeof(float4);
+}
 
 namespace {
 
-// One staged sample of lattice_rows_kernel from its cell's record: rotation,
-// phase, TPMS value.  The nearest control column is the cell's first or
-// second column.
+// Compensated trilinear interpolation of one control array at column xc of
+// the sample row's (y, z) cell, y first, then z: pairs all the way.
+__device__ __forceinline__ PF column_pf(const float* __restrict__ a, int xc, const AxisCell& ky, const AxisCell& kz,
+                                        const uint32_t c[3]) {
+  if (!a) return {0.0f, 0.0f};
+  const PF A = pf_lerp({__ldg(a + cidx(xc, ky.i0, kz.i0, c)), 0.0f}, {__ldg(a + cidx(xc, ky.i1, kz.i0, c)), 0.0f},
+                       ky.f);
+  const PF B = pf_lerp({__ldg(a + cidx(xc, ky.i0, kz.i1, c)), 0.0f}, {__ldg(a + cidx(xc, ky.i1, kz.i1, c)), 0.0f},
+                       ky.f);
+  return pf_lerp(A, B, kz.f);
+}
+
+// Writes one cell record: columns i and i1 of the row (y, z) of cells ky, kz.
+__device__ __forceinline__ void write_record(float4* w, const float* const arr[5], const uint8_t* __restrict__ type,
+                                             int i, int i1, const AxisCell& ky, const AxisCell& kz,
+                                             const uint32_t c[3]) {
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k) {
+    const PF u = column_pf(arr[k], i, ky, kz, c);
+    const PF d = pf_diff(column_pf(arr[k], i1, ky, kz, c), u);
+    w[k] = make_float4(u.h, u.l, d.h, d.l);
+  }
+  const float tu = column_yz(arr[4], i, ky, kz, c);
+  const float td = fs(column_yz(arr[4], i1, ky, kz, c), tu);
+  const uint32_t t0 = __ldg(type + cidx(i, ky.nearest, kz.nearest, c));
+  const uint32_t t1 = __ldg(type + cidx(i1, ky.nearest, kz.nearest, c));
+  w[4] = make_float4(tu, td, __uint_as_float(t0), __uint_as_float(t1));
+}
+
+// One staged sample from its cell's record: parameters, phase, TPMS value.
+// The nearest control column is the cell's first or second column.
 __device__ __forceinline__ float record_sample(const float4* __restrict__ rec, const AxisCell& kx, float qx,
-                                               float2 qyz) {
-  const float4* r = rec + 3 * kx.i0;
-  const float4 a = r[0], b = r[1], c = r[2];
+                                               float2 qyz, const float4* __restrict__ tab) {
+  const float4* r = rec + kRecWords * kx.i0;
+  const float4 a = r[0], b = r[1], c = r[2], d = r[3], e = r[4];
   const float f = kx.f;
-  const float period = __fmaf_rn(f, a.y, a.x), ex = __fmaf_rn(f, a.w, a.z), ey = __fmaf_rn(f, b.y, b.x),
-              ez = __fmaf_rn(f, b.w, b.z), thick = __fmaf_rn(f, c.y, c.x);
-  const uint32_t type = __float_as_uint(kx.nearest == kx.i0 ? c.z : c.w);
-  float R9[9];
-  euler_rows(ex, ey, ez, R9);
+  const PF P = pf_at({a.x, a.y}, {a.z, a.w}, f), ex = pf_at({b.x, b.y}, {b.z, b.w}, f),
+           ey = pf_at({c.x, c.y}, {c.z, c.w}, f), ez = pf_at({d.x, d.y}, {d.z, d.w}, f);
+  const float thick = fmaf_(f, e.y, e.x);
+  const uint32_t type = __float_as_uint(kx.nearest == kx.i0 ? e.z : e.w);
   const float q[3] = {qx, qyz.x, qyz.y};
-  return lattice_value(type, R9, __fdiv_rn(2.0f, period), q, thick);
+  float rr[3];
+  params_phase(P, ex, ey, ez, q, tab, rr);
+  return tpms_of_phase(type, rr, thick);
+}
+
+// One unstaged sample: the same values as record_sample from the global arrays.
+__device__ __forceinline__ float params_sample(const float* const arr[5], const uint8_t* __restrict__ type,
+                                               const AxisCell& kx, const AxisCell& ky, const AxisCell& kz,
+                                               const uint32_t c[3], const float q[3],
+                                               const float4* __restrict__ tab) {
+  PF v[4];
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k) {
+    const PF u = column_pf(arr[k], kx.i0, ky, kz, c);
+    v[k] = pf_at(u, pf_diff(column_pf(arr[k], kx.i1, ky, kz, c), u), kx.f);
+  }
+  const float tu = column_yz(arr[4], kx.i0, ky, kz, c);
+  const float thick = fmaf_(kx.f, fs(column_yz(arr[4], kx.i1, ky, kz, c), tu), tu);
+  const uint32_t t = __ldg(type + cidx(kx.nearest, ky.nearest, kz.nearest, c));
+  float rr[3];
+  params_phase(v[0], v[1], v[2], v[3], q, tab, rr);
+  return tpms_of_phase(t, rr, thick);
 }
 
 }  // namespace
 
 template <uint32_t R>
 __global__ void __launch_bounds__(256, 4) lattice_rows_kernel(LatticeParams p) {
-  extern __shared__ float4 s_rows[];
+  extern __shared__ float4 s_dyn[];
+  float4* s_tab = s_dyn;
+  float4* s_rows = s_dyn + kAngleRows;
+  load_angle_table(s_tab);
+  __syncthreads();
   const uint32_t cx = p.cx, cells = row_cells(cx);
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
   float4* rec = s_rows + warp * row_slice_words(R, cx);
-  float4* sq = rec + R * cells * 3;
+  float4* sq = rec + R * cells * kRecWords;
   const uint32_t c[3] = {p.cx, p.cy, p.cz};
   const uint32_t nc = p.cx * p.cy * p.cz;
   const float* arr[5] = {p.period, p.euler, p.euler ? p.euler + nc : nullptr,
@@ -296,21 +527,8 @@ __global__ void __launch_bounds__(256, 4) lattice_rows_kernel(LatticeParams p) {
     uint32_t y = row0 % p.ny, z = row0 / p.ny;
     for (uint32_t r = 0; r < nr; ++r) {
       const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
-      for (uint32_t i = lane; i < cells; i += 32) {
-        const int i1 = cx > 1 ? (int)i + 1 : 0;
-        float u[5], d[5];
-#pragma unroll
-        for (uint32_t k = 0; k < 5; ++k) {
-          u[k] = column_yz(arr[k], (int)i, ky, kz, c);
-          d[k] = fs(column_yz(arr[k], i1, ky, kz, c), u[k]);
-        }
-        const uint32_t t0 = __ldg(p.type + cidx((int)i, ky.nearest, kz.nearest, c));
-        const uint32_t t1 = __ldg(p.type + cidx(i1, ky.nearest, kz.nearest, c));
-        float4* w = rec + (r * cells + i) * 3;
-        w[0] = make_float4(u[0], d[0], u[1], d[1]);
-        w[1] = make_float4(u[2], d[2], u[3], d[3]);
-        w[2] = make_float4(u[4], d[4], __uint_as_float(t0), __uint_as_float(t1));
-      }
+      for (uint32_t i = lane; i < cells; i += 32)
+        write_record(rec + (r * cells + i) * kRecWords, arr, p.type, (int)i, cx > 1 ? (int)i + 1 : 0, ky, kz, c);
       if (lane == 0) sq[r] = make_float4(fs((float)y, p.origin[1]), fs((float)z, p.origin[2]), 0.0f, 0.0f);
       if (++y == p.ny) {
         y = 0;
@@ -328,10 +546,10 @@ __global__ void __launch_bounds__(256, 4) lattice_rows_kernel(LatticeParams p) {
         const float q1 = fs((float)x1, p.origin[0]);
 #pragma unroll 1
         for (uint32_t r = 0; r < nr; ++r) {
-          const float4* rr = rec + r * cells * 3;
+          const float4* rr = rec + r * cells * kRecWords;
           const float4 qr = sq[r];
-          const float v0 = record_sample(rr, k0, q0, make_float2(qr.x, qr.y));
-          const float v1 = record_sample(rr, k1, q1, make_float2(qr.x, qr.y));
+          const float v0 = record_sample(rr, k0, q0, make_float2(qr.x, qr.y), s_tab);
+          const float v1 = record_sample(rr, k1, q1, make_float2(qr.x, qr.y), s_tab);
           out[(uint64_t)r * p.nx] = v0;
           if (x1 < p.nx) out[(uint64_t)r * p.nx + 32] = v1;
         }
@@ -339,7 +557,7 @@ __global__ void __launch_bounds__(256, 4) lattice_rows_kernel(LatticeParams p) {
 #pragma unroll 1
         for (uint32_t r = 0; r < nr; ++r) {
           const float4 qr = sq[r];
-          out[(uint64_t)r * p.nx] = record_sample(rec + r * cells * 3, k0, q0, make_float2(qr.x, qr.y));
+          out[(uint64_t)r * p.nx] = record_sample(rec + r * cells * kRecWords, k0, q0, make_float2(qr.x, qr.y), s_tab);
         }
       }
     }
@@ -348,6 +566,9 @@ __global__ void __launch_bounds__(256, 4) lattice_rows_kernel(LatticeParams p) {
 
 // Control grids too wide for a warp's slice of one row: every sample reads its columns.
 __global__ void __launch_bounds__(256) lattice_params_kernel(LatticeParams p) {
+  __shared__ float4 s_tab[kAngleRows];
+  load_angle_table(s_tab);
+  __syncthreads();
   const uint32_t c[3] = {p.cx, p.cy, p.cz};
   const uint32_t nc = p.cx * p.cy * p.cz;
   const float* arr[5] = {p.period, p.euler, p.euler ? p.euler + nc : nullptr,
@@ -359,22 +580,26 @@ __global__ void __launch_bounds__(256) lattice_params_kernel(LatticeParams p) {
     float* out = p.out + (uint64_t)row * p.nx;
     for (uint32_t x = threadIdx.x; x < p.nx; x += blockDim.x) {
       const AxisCell kx = locate1(x, c[0], p.scale[0]);
-      float v[5];
-#pragma unroll
-      for (int k = 0; k < 5; ++k)
-        v[k] = lerpf(column_yz(arr[k], kx.i0, ky, kz, c), column_yz(arr[k], kx.i1, ky, kz, c), kx.f);
-      const uint32_t type = __ldg(p.type + cidx(kx.nearest, ky.nearest, kz.nearest, c));
-      float R9[9];
-      euler_rows(v[1], v[2], v[3], R9);
       const float q[3] = {fs((float)x, p.origin[0]), fs((float)y, p.origin[1]), fs((float)z, p.origin[2])};
-      out[x] = lattice_value(type, R9, __fdiv_rn(2.0f, v[0]), q, v[4]);
+      out[x] = params_sample(arr, p.type, kx, ky, kz, c, q, s_tab);
     }
   }
 }
 
+namespace {
+
+// BLEND mode: phase of one corner lattice, X_r = M_r0 q0 + K_r with
+// K_r = M_r1 q1 + M_r2 q2 (constant along a sample row).
+__device__ __forceinline__ PF blend_k(const float* __restrict__ rec, uint32_t r, float q1, float q2) {
+  return pf_add(pf_mulf({rec[6 * r + 2], rec[6 * r + 3]}, q1), pf_mulf({rec[6 * r + 4], rec[6 * r + 5]}, q2));
+}
+
+}  // namespace
+
 __global__ void __launch_bounds__(256) lattice_blend_kernel(LatticeParams p) {
-  // records of the 4 (y, z) corner rows of the current sample row, per control column
-  __shared__ float s_rec[4][kBlendCx][12];
+  // per (y, z) corner row of the current sample row and control column:
+  // M_r0 pairs (3), K_r pairs (3), thickness, type
+  __shared__ float4 s_rec[4][kBlendCx][4];
   const uint32_t c[3] = {p.cx, p.cy, p.cz};
   const bool staged = p.cx <= kBlendCx;
   const uint32_t rows = p.ny * p.nz;
@@ -394,11 +619,24 @@ __global__ void __launch_bounds__(256) lattice_blend_kernel(LatticeParams p) {
 #pragma unroll
       for (int dy = 0; dy < 2; ++dy) wyz[2 * dz + dy] = fm(axis_weight(ky, c[1], dy), axis_weight(kz, c[2], dz));
     if (staged) {
-      __syncthreads();
-      for (uint32_t i = threadIdx.x; i < 4 * p.cx * 12; i += blockDim.x) {
-        const uint32_t corner = i / (p.cx * 12), rem = i % (p.cx * 12), xc = rem / 12, w = rem % 12;
+      __syncthreads();  // the previous row's records are read
+      for (uint32_t i = threadIdx.x; i < 4 * p.cx; i += blockDim.x) {
+        const uint32_t corner = i / p.cx, xc = i % p.cx;
         const int dy = corner & 1, dz = corner >> 1;
-        s_rec[corner][xc][w] = __ldg(p.blend + 12 * (uint64_t)cidx((int)xc, gy[dy], gz[dz], c) + w);
+        const float* rec = p.blend + GCM_BLEND_WORDS * (uint64_t)cidx((int)xc, gy[dy], gz[dz], c);
+        float m[6];
+#pragma unroll
+        for (uint32_t r = 0; r < 3; ++r) {
+          m[2 * r] = __ldg(rec + 6 * r);
+          m[2 * r + 1] = __ldg(rec + 6 * r + 1);
+        }
+        const PF K0 = blend_k(rec, 0, qy[dy], qz[dz]), K1 = blend_k(rec, 1, qy[dy], qz[dz]),
+                 K2 = blend_k(rec, 2, qy[dy], qz[dz]);
+        float4* w = s_rec[corner][xc];
+        w[0] = make_float4(m[0], m[1], m[2], m[3]);
+        w[1] = make_float4(m[4], m[5], K0.h, K0.l);
+        w[2] = make_float4(K1.h, K1.l, K2.h, K2.l);
+        w[3] = make_float4(__ldg(rec + 18), __ldg(rec + 19), 0.0f, 0.0f);
       }
       __syncthreads();
     }
@@ -412,14 +650,35 @@ __global__ void __launch_bounds__(256) lattice_blend_kernel(LatticeParams p) {
         const int dx = corner & 1, dy = (corner >> 1) & 1, dz = corner >> 2;
         const float w = fm(axis_weight(kx, c[0], dx), wyz[2 * dz + dy]);
         if (w == 0.0f) continue;
-        const float q[3] = {fs((float)x, c[0] > 1 ? fm((float)gx[dx], p.anchor[0]) : 0.0f), qy[dy], qz[dz]};
-        const float* rec = staged ? &s_rec[2 * dz + dy][gx[dx]][0]
-                                  : p.blend + 12 * (uint64_t)cidx(gx[dx], gy[dy], gz[dz], c);
-        float R[9];
-#pragma unroll
-        for (int r = 0; r < 9; ++r) R[r] = rec[r];
-        const float v = lattice_value(__float_as_uint(rec[11]), R, rec[9], q, rec[10]);
-        acc = __fmaf_rn(w, v, acc);
+        const float q0 = fs((float)x, c[0] > 1 ? fm((float)gx[dx], p.anchor[0]) : 0.0f);
+        PF M0, M1, M2, K0, K1, K2;
+        float thick;
+        uint32_t type;
+        if (staged) {
+          const float4* s = s_rec[2 * dz + dy][gx[dx]];
+          const float4 a = s[0], b = s[1], e = s[2], f = s[3];
+          M0 = {a.x, a.y};
+          M1 = {a.z, a.w};
+          M2 = {b.x, b.y};
+          K0 = {b.z, b.w};
+          K1 = {e.x, e.y};
+          K2 = {e.z, e.w};
+          thick = f.x;
+          type = __float_as_uint(f.y);
+        } else {
+          const float* rec = p.blend + GCM_BLEND_WORDS * (uint64_t)cidx(gx[dx], gy[dy], gz[dz], c);
+          M0 = {__ldg(rec + 0), __ldg(rec + 1)};
+          M1 = {__ldg(rec + 6), __ldg(rec + 7)};
+          M2 = {__ldg(rec + 12), __ldg(rec + 13)};
+          K0 = blend_k(rec, 0, qy[dy], qz[dz]);
+          K1 = blend_k(rec, 1, qy[dy], qz[dz]);
+          K2 = blend_k(rec, 2, qy[dy], qz[dz]);
+          thick = __ldg(rec + 18);
+          type = __float_as_uint(__ldg(rec + 19));
+        }
+        const float r[3] = {pf_reduce(pf_add(pf_mulf(M0, q0), K0)), pf_reduce(pf_add(pf_mulf(M1, q0), K1)),
+                            pf_reduce(pf_add(pf_mulf(M2, q0), K2))};
+        acc = fmaf_(w, tpms_of_phase(type, r, thick), acc);
       }
       out[x] = acc;
     }
@@ -428,9 +687,8 @@ __global__ void __launch_bounds__(256) lattice_blend_kernel(LatticeParams p) {
 
 // Batched graded lattices (GCM_GRADE_PARAMS): the sample rows of all
 // instances form one sequence; a warp takes one row (the rows of these grids
-// are short) and stages that row's y/z-interpolated control columns in its own
-// slice of shared memory as lattice_rows_kernel's cell records.  Same
-// arithmetic as lattice_params_kernel.
+// are short) and stages that row's cell records in its own slice of shared
+// memory as lattice_rows_kernel does.  Same values as the single-grid kernels.
 constexpr uint32_t kWarpCx = GCM_BATCH_WARP_CX;  // control columns staged per warp
 
 // STAGED: the rows of instances with at most kWarpCx control columns (the
@@ -438,7 +696,10 @@ constexpr uint32_t kWarpCx = GCM_BATCH_WARP_CX;  // control columns staged per w
 template <bool STAGED>
 __global__ void __launch_bounds__(256, 4) lattice_params_batch_kernel(const BatchLattice* inst, uint32_t n_inst,
                                                                    uint64_t total_rows) {
-  __shared__ float4 s_rec[8][3 * kWarpCx];  // per warp: the row's cell records (lattice_rows_kernel's form)
+  __shared__ float4 s_rec[8][kRecWords * kWarpCx];  // per warp: the row's cell records
+  __shared__ float4 s_tab[kAngleRows];
+  load_angle_table(s_tab);
+  __syncthreads();
   const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
   uint32_t lo = 0;  // instance of the warp's row: rows only increase, so search only when it moves on
@@ -466,23 +727,32 @@ __global__ void __launch_bounds__(256, 4) lattice_params_batch_kernel(const Batc
       // one control column per lane (at most kWarpCx = 32 of them); a cell's
       // second column is the next lane's (a single column is its own)
       const bool has_col = lane < p.cx;
-      float u[5], v[5];
+      const int col = has_col ? (int)lane : 0;
+      PF u[4];
 #pragma unroll
-      for (uint32_t k = 0; k < 5; ++k) u[k] = has_col ? column_yz(arr[k], (int)lane, ky, kz, c) : 0.0f;
-      const uint32_t t0 = has_col ? __ldg(p.type + cidx((int)lane, ky.nearest, kz.nearest, c)) : 0u;
+      for (uint32_t k = 0; k < 4; ++k) u[k] = column_pf(arr[k], col, ky, kz, c);
+      const float tu = column_yz(arr[4], col, ky, kz, c);
+      const uint32_t t0 = __ldg(p.type + cidx(col, ky.nearest, kz.nearest, c));
+      PF v[4];
+#pragma unroll
+      for (uint32_t k = 0; k < 4; ++k)
+        v[k] = {__shfl_down_sync(0xffffffffu, u[k].h, 1), __shfl_down_sync(0xffffffffu, u[k].l, 1)};
+      float tv = __shfl_down_sync(0xffffffffu, tu, 1);
       uint32_t t1 = __shfl_down_sync(0xffffffffu, t0, 1);
-#pragma unroll
-      for (uint32_t k = 0; k < 5; ++k) v[k] = __shfl_down_sync(0xffffffffu, u[k], 1);
       if (p.cx == 1) {
 #pragma unroll
-        for (uint32_t k = 0; k < 5; ++k) v[k] = u[k];
+        for (uint32_t k = 0; k < 4; ++k) v[k] = u[k];
+        tv = tu;
         t1 = t0;
       }
       if (lane < row_cells(p.cx)) {
-        float4* w = &s_rec[wib][3 * lane];
-        w[0] = make_float4(u[0], fs(v[0], u[0]), u[1], fs(v[1], u[1]));
-        w[1] = make_float4(u[2], fs(v[2], u[2]), u[3], fs(v[3], u[3]));
-        w[2] = make_float4(u[4], fs(v[4], u[4]), __uint_as_float(t0), __uint_as_float(t1));
+        float4* w = &s_rec[wib][kRecWords * lane];
+#pragma unroll
+        for (uint32_t k = 0; k < 4; ++k) {
+          const PF d = pf_diff(v[k], u[k]);
+          w[k] = make_float4(u[k].h, u[k].l, d.h, d.l);
+        }
+        w[4] = make_float4(tu, fs(tv, tu), __uint_as_float(t0), __uint_as_float(t1));
       }
     }
     __syncwarp();
@@ -495,26 +765,19 @@ __global__ void __launch_bounds__(256, 4) lattice_params_batch_kernel(const Batc
         const float q0 = fs((float)x0, p.origin[0]);
         if (x0 - lane + 32 < p.nx) {  // warp-uniform: the second segment holds samples
           const AxisCell k1 = locate1(min(x1, p.nx - 1), c[0], p.scale[0]);
-          const float v0 = record_sample(s_rec[wib], k0, q0, qyz);
-          const float v1 = record_sample(s_rec[wib], k1, fs((float)x1, p.origin[0]), qyz);
+          const float v0 = record_sample(s_rec[wib], k0, q0, qyz, s_tab);
+          const float v1 = record_sample(s_rec[wib], k1, fs((float)x1, p.origin[0]), qyz, s_tab);
           out[x0] = v0;
           if (x1 < p.nx) out[x1] = v1;
         } else {
-          out[x0] = record_sample(s_rec[wib], k0, q0, qyz);
+          out[x0] = record_sample(s_rec[wib], k0, q0, qyz, s_tab);
         }
       }
     } else {
       for (uint32_t x = lane; x < p.nx; x += 32) {
         const AxisCell kx = locate1(x, c[0], p.scale[0]);
-        float v[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k)
-          v[k] = lerpf(column_yz(arr[k], kx.i0, ky, kz, c), column_yz(arr[k], kx.i1, ky, kz, c), kx.f);
-        const uint32_t type = __ldg(p.type + cidx(kx.nearest, ky.nearest, kz.nearest, c));
-        float R[9];
-        euler_rows(v[1], v[2], v[3], R);
         const float q[3] = {fs((float)x, p.origin[0]), fs((float)y, p.origin[1]), fs((float)z, p.origin[2])};
-        out[x] = lattice_value(type, R, __fdiv_rn(2.0f, v[0]), q, v[4]);
+        out[x] = params_sample(arr, p.type, kx, ky, kz, c, q, s_tab);
       }
     }
   }
@@ -1108,7 +1371,7 @@ cudaError_t launch_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t n
 // even one row's slice fits (the unstaged kernel then runs).
 uint32_t lattice_rows_per_warp(uint32_t cx, uint32_t rows, uint32_t sm_count) {
   for (uint32_t R = 8; R >= 1; R /= 2) {
-    if ((size_t)kRowWarps * row_slice_words(R, cx) * sizeof(float4) > kRowSmem) continue;
+    if (row_smem_bytes(R, cx) > kRowSmem) continue;
     if (R == 1 || (uint64_t)(rows + R - 1) / R >= (uint64_t)sm_count * 32) return R;
   }
   return 0;
@@ -1120,8 +1383,7 @@ static void launch_rows(const LatticeParams& p, cudaStream_t st) {
   // at most 2^26 CTAs, so the kernel's 32-bit warp stride cannot wrap (the
   // group loop covers the rest)
   const uint32_t blocks = (uint32_t)std::min<uint64_t>((groups + kRowWarps - 1) / kRowWarps, 1u << 26);
-  const size_t smem = (size_t)kRowWarps * row_slice_words(R, p.cx) * sizeof(float4);
-  lattice_rows_kernel<R><<<blocks, kRowWarps * 32, smem, st>>>(p);
+  lattice_rows_kernel<R><<<blocks, kRowWarps * 32, row_smem_bytes(R, p.cx), st>>>(p);
 }
 
 cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t prep_blocks, uint32_t blocks,

@@ -139,6 +139,9 @@ struct ScanParams {
   uint64_t wait_ns;
 };
 
+// Words per control point of the blend-mode setup buffer.
+#define GCM_BLEND_WORDS 20
+
 // Graded lattice, device form of gcm_lattice.
 struct LatticeParams {
   uint32_t mode;
@@ -147,7 +150,8 @@ struct LatticeParams {
   const float* euler;  // [3][n] or null
   const float* thickness;
   const uint8_t* type;
-  const float* blend;  // blend mode: per control point R[9], 2/period, thickness, type (12 words)
+  const float* blend;  // blend mode: per control point GCM_BLEND_WORDS words (R * 2/period as float pairs,
+                       // thickness, type)
   float origin[3];
   float scale[3];   // control coordinate per voxel: (c-1)/(n-1)
   float anchor[3];  // voxel spacing of control points: (n-1)/(c-1)

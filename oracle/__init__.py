@@ -65,6 +65,8 @@ def lib():
         L.orc_lattice_field.argtypes = [C.POINTER(OrcLattice), C.c_uint32, C.c_uint32, C.c_uint32, F32P, C.c_int]
         L.orc_lattice_field_slab.argtypes = [C.POINTER(OrcLattice), C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                              C.c_uint32, F32P, C.c_int]
+        L.orc_lattice_field64_slab.argtypes = [C.POINTER(OrcLattice), C.c_uint32, C.c_uint32, C.c_uint32,
+                                               C.c_uint32, C.c_uint32, F64P, C.c_int]
         L.orc_lattice_field64.argtypes = [C.POINTER(OrcLattice), C.c_uint32, C.c_uint32, C.c_uint32, F64P, C.c_int]
         L.orc_csg_field.argtypes = [C.POINTER(OrcPrim), C.c_uint32, F32P, F32P, C.c_uint32, C.c_uint32, C.c_uint32,
                                     F32P, C.c_int]
@@ -245,14 +247,18 @@ def lattice_field(n, mode, ctrl, period, euler=None, thickness=None, types=None,
 
 
 def lattice_slab(n, z0, nplanes, mode, ctrl, period, euler=None, thickness=None, types=None, origin=(0, 0, 0),
-                 threads=0):
+                 threads=0, fp64=False):
     """Planes z0..z0+nplanes-1 of the nx*ny*nz lattice field (same control mapping)."""
     nx, ny, nz = n
     if types is None:
         types = np.zeros(int(np.prod(ctrl)), np.uint8)
     s, keep = _lattice_struct(mode, ctrl, period, euler, thickness, types, origin)
-    out = np.zeros(nx * ny * nplanes, np.float32)
-    lib().orc_lattice_field_slab(C.byref(s), nx, ny, nz, z0, nplanes, out, threads)
+    if fp64:
+        out = np.zeros(nx * ny * nplanes, np.float64)
+        lib().orc_lattice_field64_slab(C.byref(s), nx, ny, nz, z0, nplanes, out, threads)
+    else:
+        out = np.zeros(nx * ny * nplanes, np.float32)
+        lib().orc_lattice_field_slab(C.byref(s), nx, ny, nz, z0, nplanes, out, threads)
     del keep
     return out.reshape(nplanes, ny, nx)
 

@@ -14,7 +14,8 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
 SOURCES = [os.path.join(HERE, "oracle.cpp")]
 DEPS = SOURCES + [os.path.join(HERE, "oracle.h"),
-                  os.path.join(os.path.dirname(HERE), "gpucadforam_gb300", "csrc", "mc_tables.h")]
+                  os.path.join(os.path.dirname(HERE), "gpucadforam_gb300", "csrc", "mc_tables.h"),
+                  os.path.join(os.path.dirname(HERE), "gpucadforam_gb300", "csrc", "angle_table.h")]
 
 
 def build(force: bool = False) -> str:

@@ -21,6 +21,7 @@
 #include <omp.h>
 #endif
 
+#include "../gpucadforam_gb300/csrc/angle_table.h"
 #include "../gpucadforam_gb300/csrc/mc_tables.h"
 
 namespace {
@@ -214,12 +215,6 @@ void euler_rows(T ax, T ay, T az, T R[9]) {
   R[6] = -sy;     R[7] = cy * sx;                R[8] = cy * cx;
 }
 
-inline void sincospi32(float x, float& s, float& c) {
-  // Reference sin(pi x) / cos(pi x) of an FP32 argument, rounded from FP64.
-  const double a = M_PI * (double)x;
-  s = (float)std::sin(a);
-  c = (float)std::cos(a);
-}
 inline void sincospi64(double x, double& s, double& c) {
   // Exact reduction of x to [-1, 1] half-turns before the FP64 trig.
   double r = x - 2.0 * std::nearbyint(x * 0.5);
@@ -312,20 +307,213 @@ double trilinear64(const float* a, const Cell& k, const uint32_t c[3]) {
 }
 
 // Phase of one lattice in half-turns: X = R q * (2 / period).
-float lattice_value32(unsigned type, const float R[9], float h, const float q[3], float thick) {
-  float X[3];
-  for (int r = 0; r < 3; ++r) X[r] = std::fma(R[3 * r + 2], q[2], std::fma(R[3 * r + 1], q[1], R[3 * r] * q[0])) * h;
-  float s[3], c[3];
-  for (int r = 0; r < 3; ++r) sincospi32(X[r], s[r], c[r]);
-  return tpms_from_sc<float>(type, s[0], c[0], s[1], c[1], s[2], c[2]) - thick;
-}
-
 double lattice_value64(unsigned type, const double R[9], double h, const double q[3], double thick) {
   double X[3];
   for (int r = 0; r < 3; ++r) X[r] = (R[3 * r] * q[0] + R[3 * r + 1] * q[1] + R[3 * r + 2] * q[2]) * h;
   double s[3], c[3];
   for (int r = 0; r < 3; ++r) sincospi64(X[r], s[r], c[r]);
   return tpms_from_sc<double>(type, s[0], c[0], s[1], c[1], s[2], c[2]) - thick;
+}
+
+// ---- compensated FP32 arithmetic of the graded lattices ---------------------------
+//
+// The GPU evaluates the graded lattices with pairs of floats (hi + lo) from the
+// parameter interpolation through the reduced phase, so that the phase X (up to
+// ~55 half-turns at 512^3) keeps ~40 bits instead of 24.  Every step below is an
+// IEEE float operation (add, sub, mul, fma, div) in a fixed order, plus double
+// add/mul/div/rint on the rare path of angles outside [-3.156, 3.156]; this is a
+// separate restatement of that sequence, so its results equal the kernels' bit
+// for bit.  Angles go through a table of sin/cos(k/32) pairs
+// (gpucadforam_gb300/csrc/angle_table.h, generated from decimal Taylor series);
+// sin(pi r) and cos(pi r) of the reduced phase are their Taylor polynomials.
+struct PF {
+  float h, l;
+};
+
+inline PF two_sum(float a, float b) {
+  const float s = a + b, bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+inline PF pf_diff(PF b, PF a) {
+  const PF d = two_sum(b.h, -a.h);
+  return {d.h, d.l + (b.l - a.l)};
+}
+// u + t * d
+inline PF pf_at(PF u, PF d, float t) {
+  const float p = t * d.h;
+  float pe = std::fma(t, d.h, -p);
+  pe = std::fma(t, d.l, pe);
+  const PF s = two_sum(u.h, p);
+  return {s.h, (s.l + pe) + u.l};
+}
+inline PF pf_lerp(PF a, PF b, float t) { return pf_at(a, pf_diff(b, a), t); }
+inline PF pf_mulf(PF a, float f) {
+  const float p = a.h * f;
+  float pe = std::fma(a.h, f, -p);
+  pe = std::fma(a.l, f, pe);
+  return {p, pe};
+}
+inline PF pf_mul(PF a, PF b) {
+  const float p = a.h * b.h;
+  float pe = std::fma(a.h, b.h, -p);
+  pe = std::fma(a.h, b.l, pe);
+  pe = std::fma(a.l, b.h, pe);
+  return {p, pe};
+}
+inline PF pf_add(PF a, PF b) {
+  const PF s = two_sum(a.h, b.h);
+  return {s.h, s.l + (a.l + b.l)};
+}
+inline PF pf_neg(PF a) { return {-a.h, -a.l}; }
+// 2 / P
+inline PF pf_two_over(PF P) {
+  const float hh = 2.0f / P.h;
+  float r = std::fma(-hh, P.h, 2.0f);
+  r = std::fma(-hh, P.l, r);
+  return {hh, r * (0.5f * hh)};
+}
+
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23: adding it rounds to an integer
+inline int32_t fbits(float f) {
+  int32_t i;
+  std::memcpy(&i, &f, 4);
+  return i;
+}
+
+const float kAngleTab[][4] = {GCM_ANGLE_TABLE_ROWS};
+
+// sin and cos of the angle a (a pair) as pairs: table entry at k/32 nearest a,
+// corrected by the Taylor series of the remainder (|d| <= 1/64).
+inline void pf_sincos(PF a, PF& s, PF& c) {
+  if (!(std::fabs(a.h) <= (float)GCM_ANGLE_K / GCM_ANGLE_STEP_INV)) {
+    const double two_pi = 6.283185307179586;
+    double A = (double)a.h + (double)a.l;
+    const double m = std::rint(A / two_pi);
+    A = A - m * two_pi;
+    a.h = (float)A;
+    a.l = (float)(A - (double)a.h);
+  }
+  const float t = std::fma(a.h, (float)GCM_ANGLE_STEP_INV, kMagic);
+  const float kf = t - kMagic;
+  int k = fbits(t) - fbits(kMagic);
+  k = std::min(std::max(k, -GCM_ANGLE_K), GCM_ANGLE_K);
+  float d = std::fma(kf, -1.0f / GCM_ANGLE_STEP_INV, a.h);
+  d = d + a.l;
+  const float* e = kAngleTab[k + GCM_ANGLE_K];
+  const float d2 = d * d, d3 = d2 * d;
+  const float sd = std::fma(d3, -0x1.555556p-3f, d);
+  const float cm1 = d2 * std::fma(d2, 0x1.555556p-5f, -0.5f);
+  float sl = std::fma(e[0], cm1, e[1]);
+  sl = std::fma(e[2], sd, sl);
+  sl = std::fma(e[3], sd, sl);
+  float cl = std::fma(e[2], cm1, e[3]);
+  cl = std::fma(-e[0], sd, cl);
+  cl = std::fma(-e[1], sd, cl);
+  // renormalised, so that products drop only terms of order lo * lo
+  s = two_sum(e[0], sl);
+  c = two_sum(e[2], cl);
+}
+
+// X mod 2 (half-turns) as one float.
+inline float pf_reduce(PF X) {
+  const float t = std::fma(X.h, 0.5f, kMagic);
+  const float kf = t - kMagic;
+  const float r = std::fma(kf, -2.0f, X.h);
+  return r + X.l;
+}
+
+// sin(pi r), cos(pi r): quarter-turn j = rint(2r), u = r - j/2, Taylor polynomials in u.
+inline void sincospi_taylor(float r, float& s, float& c) {
+  const float t = std::fma(r, 2.0f, kMagic);
+  const float jf = t - kMagic;
+  const int j = fbits(t) & 3;
+  const float u = std::fma(jf, -0.5f, r);
+  const float z = u * u;
+  float ps = std::fma(z, GCM_SINPI_C9, GCM_SINPI_C7);
+  ps = std::fma(z, ps, GCM_SINPI_C5);
+  ps = std::fma(z, ps, GCM_SINPI_C3);
+  ps = std::fma(z, ps, GCM_SINPI_C1);
+  const float sn = u * ps;
+  float pc = std::fma(z, GCM_COSPI_C10, GCM_COSPI_C8);
+  pc = std::fma(z, pc, GCM_COSPI_C6);
+  pc = std::fma(z, pc, GCM_COSPI_C4);
+  pc = std::fma(z, pc, GCM_COSPI_C2);
+  const float cs = std::fma(z, pc, 1.0f);
+  switch (j) {
+    case 0: s = sn; c = cs; break;
+    case 1: s = cs; c = -sn; break;
+    case 2: s = -sn; c = -cs; break;
+    default: s = -cs; c = sn; break;
+  }
+}
+
+inline float tpms_of_phase(unsigned type, const float r[3], float thick) {
+  float s[3], c[3];
+  for (int k = 0; k < 3; ++k) sincospi_taylor(r[k], s[k], c[k]);
+  return tpms_from_sc<float>(type, s[0], c[0], s[1], c[1], s[2], c[2]) - thick;
+}
+
+// PARAMS mode: one parameter's compensated trilinear value, y first, then z,
+// then x (as trilinear64), with the x step as record + fraction.
+PF trilinear_pf(const float* a, const Cell& k, const uint32_t c[3]) {
+  if (!a) return {0.0f, 0.0f};
+  const int x1 = c[0] > 1 ? k.i0[0] + 1 : 0, y1 = c[1] > 1 ? k.i0[1] + 1 : 0, z1 = c[2] > 1 ? k.i0[2] + 1 : 0;
+  const int y0 = k.i0[1], z0 = k.i0[2];
+  auto col = [&](int xc) {
+    const PF A = pf_lerp({a[cidx(xc, y0, z0, c)], 0.0f}, {a[cidx(xc, y1, z0, c)], 0.0f}, k.f[1]);
+    const PF B = pf_lerp({a[cidx(xc, y0, z1, c)], 0.0f}, {a[cidx(xc, y1, z1, c)], 0.0f}, k.f[1]);
+    return pf_lerp(A, B, k.f[2]);
+  };
+  return pf_lerp(col(k.i0[0]), col(x1), k.f[0]);
+}
+
+// PARAMS mode phase: q rotated by Rx, Ry, Rz in turn (the rows of Modelling.cu:
+// 401-407 applied one axis at a time), scaled by 2/P, reduced mod 2.
+void params_phase(PF P, PF ax, PF ay, PF az, const float q[3], float r[3]) {
+  PF sx, cx, sy, cy, sz, cz;
+  pf_sincos(ax, sx, cx);
+  pf_sincos(ay, sy, cy);
+  pf_sincos(az, sz, cz);
+  const PF v1 = pf_add(pf_mulf(cx, q[1]), pf_neg(pf_mulf(sx, q[2])));
+  const PF v2 = pf_add(pf_mulf(sx, q[1]), pf_mulf(cx, q[2]));
+  const PF w0 = pf_add(pf_mulf(cy, q[0]), pf_mul(sy, v2));
+  const PF w2 = pf_add(pf_mul(cy, v2), pf_neg(pf_mulf(sy, q[0])));
+  const PF X0 = pf_add(pf_mul(cz, w0), pf_neg(pf_mul(sz, v1)));
+  const PF X1 = pf_add(pf_mul(sz, w0), pf_mul(cz, v1));
+  const PF H = pf_two_over(P);
+  r[0] = pf_reduce(pf_mul(X0, H));
+  r[1] = pf_reduce(pf_mul(X1, H));
+  r[2] = pf_reduce(pf_mul(w2, H));
+}
+
+// BLEND mode per control point: M = R * (2 / period) in double from the table's
+// sin/cos pairs, each entry split into a float pair (row-major M[r][j]).
+void blend_matrix(float ax, float ay, float az, float period, PF M[9]) {
+  PF s[3], c[3];
+  pf_sincos({ax, 0.0f}, s[0], c[0]);
+  pf_sincos({ay, 0.0f}, s[1], c[1]);
+  pf_sincos({az, 0.0f}, s[2], c[2]);
+  const double sx = (double)s[0].h + (double)s[0].l, cx = (double)c[0].h + (double)c[0].l;
+  const double sy = (double)s[1].h + (double)s[1].l, cy = (double)c[1].h + (double)c[1].l;
+  const double sz = (double)s[2].h + (double)s[2].l, cz = (double)c[2].h + (double)c[2].l;
+  double R[9];
+  R[0] = cz * cy; R[1] = (cz * sy) * sx - sz * cx; R[2] = (cz * sy) * cx + sz * sx;
+  R[3] = sz * cy; R[4] = (sz * sy) * sx + cz * cx; R[5] = (sz * sy) * cx - cz * sx;
+  R[6] = -sy;     R[7] = cy * sx;                  R[8] = cy * cx;
+  const double H = 2.0 / (double)period;
+  for (int i = 0; i < 9; ++i) {
+    const double m = R[i] * H;
+    M[i].h = (float)m;
+    M[i].l = (float)(m - (double)M[i].h);
+  }
+}
+
+// BLEND mode phase of one corner lattice: X_r = M_r0 q0 + (M_r1 q1 + M_r2 q2).
+void blend_phase(const PF M[9], const float q[3], float r[3]) {
+  for (int i = 0; i < 3; ++i) {
+    const PF K = pf_add(pf_mulf(M[3 * i + 1], q[1]), pf_mulf(M[3 * i + 2], q[2]));
+    r[i] = pf_reduce(pf_add(pf_mulf(M[3 * i], q[0]), K));
+  }
 }
 
 template <bool F64, class Out>
@@ -336,12 +524,12 @@ void lattice_field_impl(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t
   const float s[3] = {ctrl_scale(c[0], nx), ctrl_scale(c[1], ny), ctrl_scale(c[2], nz)};
   const uint64_t nctrl = (uint64_t)c[0] * c[1] * c[2];
   // Per-control-point rotation rows (blend mode), from the control Euler angles.
-  std::vector<float> R32(9 * nctrl);
+  std::vector<PF> M32(9 * nctrl);
   std::vector<double> R64(9 * nctrl);
   for (uint64_t i = 0; i < nctrl; ++i) {
     const float ax = L->euler ? L->euler[i] : 0.f, ay = L->euler ? L->euler[nctrl + i] : 0.f,
                 az = L->euler ? L->euler[2 * nctrl + i] : 0.f;
-    euler_rows<float>(ax, ay, az, &R32[9 * i]);
+    if (L->mode == 1) blend_matrix(ax, ay, az, L->period[i], &M32[9 * i]);
     euler_rows<double>(ax, ay, az, &R64[9 * i]);
   }
   const int nt = set_threads(threads);
@@ -357,15 +545,15 @@ void lattice_field_impl(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t
       const uint64_t ni = cidx(k.nearest[0], k.nearest[1], k.nearest[2], c);
       const unsigned type = L->type[ni];
       if (!F64) {
-        const float P = trilinear32(L->period, k, c);
-        const float ax = trilinear32(L->euler, k, c);
-        const float ay = trilinear32(L->euler ? L->euler + nctrl : nullptr, k, c);
-        const float az = trilinear32(L->euler ? L->euler + 2 * nctrl : nullptr, k, c);
+        const PF P = trilinear_pf(L->period, k, c);
+        const PF ax = trilinear_pf(L->euler, k, c);
+        const PF ay = trilinear_pf(L->euler ? L->euler + nctrl : nullptr, k, c);
+        const PF az = trilinear_pf(L->euler ? L->euler + 2 * nctrl : nullptr, k, c);
         const float th = trilinear32(L->thickness, k, c);
-        float R[9];
-        euler_rows<float>(ax, ay, az, R);
         const float q[3] = {(float)p[0] - L->origin[0], (float)p[1] - L->origin[1], (float)p[2] - L->origin[2]};
-        out[i] = (Out)lattice_value32(type, R, 2.0f / P, q, th);
+        float r[3];
+        params_phase(P, ax, ay, az, q, r);
+        out[i] = (Out)tpms_of_phase(type, r, th);
       } else {
         const double P = trilinear64(L->period, k, c);
         const double ax = trilinear64(L->euler, k, c);
@@ -396,8 +584,9 @@ void lattice_field_impl(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t
           const float w = wa[0] * (wa[1] * wa[2]);
           if (w == 0.0f) continue;
           const uint64_t ci = cidx(g[0], g[1], g[2], c);
-          const float v = lattice_value32(L->type[ci], &R32[9 * ci], 2.0f / L->period[ci], q,
-                                          L->thickness ? L->thickness[ci] : 0.0f);
+          float r[3];
+          blend_phase(&M32[9 * ci], q, r);
+          const float v = tpms_of_phase(L->type[ci], r, L->thickness ? L->thickness[ci] : 0.0f);
           acc = std::fma(w, v, acc);
         }
         out[i] = (Out)acc;
@@ -410,7 +599,9 @@ void lattice_field_impl(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t
           for (int a = 0; a < 3; ++a) {
             g[a] = c[a] > 1 ? k.i0[a] + d[a] : 0;
             wa[a] = (c[a] > 1) ? (d[a] ? (double)k.f[a] : 1.0 - (double)k.f[a]) : (d[a] ? 0.0 : 1.0);
-            const double anchor = c[a] > 1 ? (double)g[a] * ((double)(n[a] - 1) / (double)(c[a] - 1)) : 0.0;
+            // the anchor positions are FP32 numbers (a modelling decision shared by
+            // both precisions, like the cell fractions)
+            const double anchor = c[a] > 1 ? (double)((float)g[a] * ((float)(n[a] - 1) / (float)(c[a] - 1))) : 0.0;
             q[a] = (double)p[a] - anchor;
           }
           const double w = wa[0] * (wa[1] * wa[2]);
@@ -1249,6 +1440,10 @@ void orc_lattice_field64(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_
 void orc_lattice_field_slab(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t z0,
                             uint32_t nplanes, float* out, int threads) {
   lattice_field_impl<false>(L, nx, ny, nz, out, threads, z0, nplanes);
+}
+void orc_lattice_field64_slab(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t z0,
+                            uint32_t nplanes, double* out, int threads) {
+  lattice_field_impl<true>(L, nx, ny, nz, out, threads, z0, nplanes);
 }
 
 void orc_csg_field(const orc_prim* prims, uint32_t n, const float* origin, const float* spacing, uint32_t nx,

@@ -47,7 +47,9 @@ void orc_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t nz, float* 
 void orc_primitive(uint32_t kind, int nx, int ny, int nz, float dx, float dy, float dz, const float* center,
                    const float* v3, const float* p, uint32_t flag, float* out);
 
-// Graded lattice, see oracle.cpp for the exact formulation.
+// Graded lattice, see oracle.cpp for the exact formulation.  The float forms
+// restate the GPU's compensated arithmetic (pairs of floats through the reduced
+// phase); the double forms are the accuracy reference.
 typedef struct orc_lattice {
   uint32_t mode;  // 0 = trilinear parameters, 1 = trilinear blend of per-control-point fields
   uint32_t cx, cy, cz;
@@ -62,6 +64,8 @@ void orc_lattice_field64(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_
 // Planes z0 .. z0+nplanes-1 of the same nx*ny*nz field.
 void orc_lattice_field_slab(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t z0,
                             uint32_t nplanes, float* out, int threads);
+void orc_lattice_field64_slab(const orc_lattice* L, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t z0,
+                              uint32_t nplanes, double* out, int threads);
 
 // CSG scene of primitives: f = op_n(...op_1(op_0(+inf, g_0), g_1)..., g_n).
 typedef struct orc_prim {

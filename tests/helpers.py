@@ -50,3 +50,13 @@ def assert_field_close(got, ref, k_rel=4, k_scale=8):
     bad = err > tol
     assert not bad.any(), (f"{bad.sum()} of {ref.size} values out of tolerance; worst err {err.max():.3e} "
                            f"at {int(err.argmax())} (ref {ref[err.argmax()]!r}, got {got[err.argmax()]!r})")
+
+
+def assert_rel_close(got, ref64, rel):
+    """|got - ref| <= rel * max(1, |ref|): relative to the value, with the
+    field's unit scale as the floor (a field near its zero set has no
+    meaningful relative error)."""
+    got = np.asarray(got, np.float64).reshape(-1)
+    ref64 = np.asarray(ref64, np.float64).reshape(-1)
+    err = np.abs(got - ref64) / np.maximum(1.0, np.abs(ref64))
+    assert err.max() <= rel, f"worst relative error {err.max():.3e} at {int(err.argmax())}"

@@ -1,16 +1,16 @@
 """GPU parity of the field kernels, through the C ABI.
 
 Unit cells and primitives against the reference's own kernels (fixtures);
-graded lattices and CSG scenes against the FP32 oracle (same operation order,
-so only the trig implementations differ) and the FP64 oracle.  Tolerances are
-written in each test.
+graded lattices bit for bit against the oracle's restatement of the kernels'
+compensated float arithmetic and within 1e-5 relative of the FP64 oracle; CSG
+scenes against the FP32 and FP64 oracles.  Tolerances are written in each test.
 """
 import numpy as np
 import pytest
 import torch
 
 import oracle as O
-from tests.helpers import assert_field_close, golden, n_cases
+from tests.helpers import assert_field_close, assert_rel_close, golden, n_cases
 
 pytestmark = pytest.mark.gpu
 
@@ -90,16 +90,10 @@ def test_graded_lattice_vs_oracle(ctx, mode, shape):
     ref32 = O.lattice_field((nx, ny, nz), mode, L["ctrl"], L["period"], L["euler"], L["thickness"], L["types"], origin)
     ref64 = O.lattice_field((nx, ny, nz), mode, L["ctrl"], L["period"], L["euler"], L["thickness"], L["types"], origin,
                             fp64=True)
-    # FP32 oracle: identical operation order, different sin/cos implementations
-    # (CUDA sincosf/sincospif within 2 ulp).  An ulp of difference in a rotation
-    # entry moves the phase by |q| * 2/period * ulp, |q| <= 84 voxels here, so
-    # the bound is absolute: 2e-5.
-    err32 = np.abs(got.astype(np.float64) - ref32.astype(np.float64))
-    assert err32.max() < 2e-5, err32.max()
-    # FP64 oracle: the FP32 phase carries ~1 ulp of |X| (half-turns); with the
-    # phase magnitude below 2^6 here that bounds the field error by 4e-5 absolute
-    err = np.abs(got.astype(np.float64) - ref64)
-    assert err.max() < 4e-5, err.max()
+    # the oracle restates the kernels' compensated float arithmetic step for step
+    assert got.tobytes() == ref32.tobytes()
+    # FP64 oracle: within 1e-5 relative, |f - f64| <= 1e-5 * max(1, |f64|)
+    assert_rel_close(got, ref64, 1e-5)
 
 
 @pytest.mark.parametrize("shape,ctrl", [
@@ -127,11 +121,9 @@ def test_graded_lattice_kernel_forms_vs_oracle(ctx, shape, ctrl):
     lat = Lattice.from_numpy(0, ctrl, period, euler, thick, types, origin)
     got = host(ctx.lattice_field(lat, shape))
     ref32 = O.lattice_field((nx, ny, nz), 0, ctrl, period, euler, thick, types, origin)
-    # as in the test above: an ulp of a rotation entry moves the phase by
-    # |q| * 2/period * ulp, so the absolute bound grows with the largest |q|
-    qmax = float(np.linalg.norm(np.array([nx, ny, nz], np.float64) / 2))
-    err = np.abs(got.reshape(-1).astype(np.float64) - ref32.reshape(-1).astype(np.float64))
-    assert err.max() < 2e-5 * max(1.0, qmax / 84), err.max()
+    assert got.tobytes() == ref32.tobytes()
+    ref64 = O.lattice_field((nx, ny, nz), 0, ctrl, period, euler, thick, types, origin, fp64=True)
+    assert_rel_close(got, ref64, 1e-5)
 
 
 def test_c1_uniform_gyroid_fp64(ctx):
@@ -182,7 +174,7 @@ def test_csg_scene_vs_oracle(ctx):
 def test_lattice_mesh_equals_oracle_mc_of_device_field(ctx):
     """End to end: the fused lattice mesher's output equals marching cubes (oracle)
     of the field the device evaluated; cube indices of that field differ from the
-    FP64 field's only where |f - iso| < 4e-5 (the stated field tolerance)."""
+    FP64 field's only where |f - iso| < 1e-5 (the stated field tolerance)."""
     from gpucadforam_gb300.mesher import Lattice
 
     n = 80
@@ -205,7 +197,7 @@ def test_lattice_mesh_equals_oracle_mc_of_device_field(ctx):
     diff = c32 != c64
     if diff.any():
         # every differing voxel has a corner within tolerance of the isovalue
-        near = np.abs(f64) < 4e-5
+        near = np.abs(f64) < 1e-5
         nv = np.zeros(c32.shape, bool)
         m = near
         for dz in (0, 1):

@@ -192,31 +192,6 @@ def test_repeat_runs_identical_and_count_matches(ctx):
     assert c.total_verts == a[2].total_verts and c.active_voxels == a[2].active_voxels
 
 
-def test_full_size_512_properties(ctx):
-    """512^3 graded field: emit total == count total, scan of the staged counts
-    agrees, and every vertex lies inside the grid box."""
-    n = 512
-    rng = np.random.default_rng(0xD4A + 2)
-    C = 16
-    period = rng.uniform(16, 64, C ** 3).astype(np.float32)
-    euler = rng.uniform(-np.pi / 4, np.pi / 4, 3 * C ** 3).astype(np.float32)
-    th = rng.uniform(-0.6, 0.6, C ** 3).astype(np.float32)
-    types = rng.choice(np.array([0, 1, 5], np.uint8), C ** 3)
-    from gpucadforam_gb300.mesher import Lattice
-
-    lat = Lattice.from_numpy(0, (C, C, C), period, euler, th, types, origin=((n - 1) / 2,) * 3)
-    field = ctx.lattice_field(lat, (n, n, n))
-    cnt = ctx.count_field(field, 0.0)
-    verts, occ, _ = ctx.classify(field, 0.0)
-    _, total = ctx.scan(verts)
-    _, active = ctx.scan(occ)
-    assert total == cnt.total_verts and active == cnt.active_voxels
-    pos, norm, c2 = ctx.mesh_field(field, 0.0)
-    assert c2.total_verts == cnt.total_verts
-    assert float(pos[:, :3].min()) >= 0.0 and float(pos[:, :3].max()) <= n - 1
-    assert bool((pos[:, 3] == 1.0).all()) and bool((norm[:, 3] == 0.0).all())
-
-
 def test_lookback_wait_runs_out_and_context_survives(ctx):
     import ctypes as C
     from gpucadforam_gb300 import _native as N
