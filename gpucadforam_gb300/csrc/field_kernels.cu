@@ -167,16 +167,23 @@ constexpr uint32_t kAngleRows = 2 * GCM_ANGLE_K + 1;
 // sin and cos of an angle pair: the table's sin/cos(k/32) pair nearest the
 // angle, corrected by the Taylor series of the remainder d (|d| <= 1/64, terms
 // to d^4), renormalised so that later products drop only lo * lo terms.
-__device__ __forceinline__ void pf_sincos(PF a, const float4* __restrict__ tab, PF& s, PF& c) {
-  if (!(fabsf(a.h) <= (float)GCM_ANGLE_K / GCM_ANGLE_STEP_INV)) {
-    // rare: reduce by 2 pi in double (NaN and infinities stay NaN)
-    const double two_pi = 6.283185307179586;
-    double A = __dadd_rn((double)a.h, (double)a.l);
-    const double m = rint(__ddiv_rn(A, two_pi));
-    A = __dsub_rn(A, __dmul_rn(m, two_pi));
-    a.h = __double2float_rn(A);
-    a.l = __double2float_rn(__dsub_rn(A, (double)a.h));
-  }
+constexpr float kAngleMax = (float)GCM_ANGLE_K / GCM_ANGLE_STEP_INV;  // the table's reach
+
+__device__ __forceinline__ bool angle_in_table(PF a) { return fabsf(a.h) <= kAngleMax; }
+
+// Angles beyond the table (rare): reduced by 2 pi in double (NaN and
+// infinities stay NaN).
+__device__ __noinline__ PF reduce_angle(PF a) {
+  const double two_pi = 6.283185307179586;
+  double A = __dadd_rn((double)a.h, (double)a.l);
+  const double m = rint(__ddiv_rn(A, two_pi));
+  A = __dsub_rn(A, __dmul_rn(m, two_pi));
+  const float h = __double2float_rn(A);
+  return {h, __double2float_rn(__dsub_rn(A, (double)h))};
+}
+
+// Table part of pf_sincos, for an angle within the table's reach.
+__device__ __forceinline__ void pf_sincos_table(PF a, const float4* __restrict__ tab, PF& s, PF& c) {
   const float t = fmaf_(a.h, (float)GCM_ANGLE_STEP_INV, kMagic);
   const float kf = fs(t, kMagic);
   const int k = min(max(__float_as_int(t) - __float_as_int(kMagic), -GCM_ANGLE_K), GCM_ANGLE_K);
@@ -194,6 +201,11 @@ __device__ __forceinline__ void pf_sincos(PF a, const float4* __restrict__ tab, 
   cl = fmaf_(-e.y, sd, cl);
   s = two_sum(e.x, sl);
   c = two_sum(e.z, cl);
+}
+
+__device__ __forceinline__ void pf_sincos(PF a, const float4* __restrict__ tab, PF& s, PF& c) {
+  if (!angle_in_table(a)) a = reduce_angle(a);
+  pf_sincos_table(a, tab, s, c);
 }
 
 // X mod 2 (half-turns) as one float.
@@ -221,10 +233,12 @@ __device__ __forceinline__ void sincospi_taylor(float r, float& s, float& c) {
   pc = fmaf_(z, pc, GCM_COSPI_C4);
   pc = fmaf_(z, pc, GCM_COSPI_C2);
   const float cs = fmaf_(z, pc, 1.0f);
+  // quarter turns: (s, c) = (sn, cs), (cs, -sn), (-sn, -cs), (-cs, sn); the
+  // negations as sign-bit flips
   const bool swap = (j & 1) != 0;
   const float a = swap ? cs : sn, b = swap ? sn : cs;
-  s = (j == 0 || j == 1) ? a : -a;
-  c = (j == 0 || j == 3) ? b : -b;
+  s = __int_as_float(__float_as_int(a) ^ ((j & 2) << 30));
+  c = __int_as_float(__float_as_int(b) ^ (((j + 1) & 2) << 30));
 }
 
 __device__ __forceinline__ float tpms_of_phase(uint32_t type, const float r[3], float thick) {
@@ -239,9 +253,14 @@ __device__ __forceinline__ float tpms_of_phase(uint32_t type, const float r[3], 
 __device__ __forceinline__ void params_phase(PF P, PF ax, PF ay, PF az, const float q[3],
                                              const float4* __restrict__ tab, float r[3]) {
   PF sx, cx, sy, cy, sz, cz;
-  pf_sincos(ax, tab, sx, cx);
-  pf_sincos(ay, tab, sy, cy);
-  pf_sincos(az, tab, sz, cz);
+  if (!(angle_in_table(ax) && angle_in_table(ay) && angle_in_table(az))) {  // false for NaN too
+    if (!angle_in_table(ax)) ax = reduce_angle(ax);
+    if (!angle_in_table(ay)) ay = reduce_angle(ay);
+    if (!angle_in_table(az)) az = reduce_angle(az);
+  }
+  pf_sincos_table(ax, tab, sx, cx);
+  pf_sincos_table(ay, tab, sy, cy);
+  pf_sincos_table(az, tab, sz, cz);
   const PF v1 = pf_add(pf_mulf(cx, q[1]), pf_neg(pf_mulf(sx, q[2])));
   const PF v2 = pf_add(pf_mulf(sx, q[1]), pf_mulf(cx, q[2]));
   const PF w0 = pf_add(pf_mulf(cy, q[0]), pf_mul(sy, v2));
@@ -424,10 +443,12 @@ constexpr uint32_t kRecWords = 5;         // 16-byte words of one cell record
 // Cells of a row: cx - 1 (one for a single control column).
 __host__ __device__ constexpr uint32_t row_cells(uint32_t cx) { return cx > 1 ? cx - 1 : 1; }
 
-// 16-byte words of one warp's slice: R rows x cells x kRecWords record words,
-// then one word per row holding its (y, z) phase coordinates.
+// 16-byte words of one warp's slice: R rows x (cells + 1) record slots (the
+// extra slot holds the last control column while the records are formed), then
+// one word per row holding its (y, z) phase coordinates and y, z.
+__host__ __device__ constexpr uint32_t row_slots(uint32_t cx) { return row_cells(cx) + 1; }
 __host__ __device__ constexpr uint32_t row_slice_words(uint32_t R, uint32_t cx) {
-  return R * row_cells(cx) * kRecWords + R;
+  return R * row_slots(cx) * kRecWords + R;
 }
 // dynamic shared memory of lattice_rows_kernel: the angle table, then the slices
 __host__ __device__ constexpr size_t row_smem_bytes(uint32_t R, uint32_t cx) {
@@ -448,21 +469,46 @@ __device__ __forceinline__ PF column_pf(const float* __restrict__ a, int xc, con
   return pf_lerp(A, B, kz.f);
 }
 
-// Writes one cell record: columns i and i1 of the row (y, z) of cells ky, kz.
-__device__ __forceinline__ void write_record(float4* w, const float* const arr[5], const uint8_t* __restrict__ type,
-                                             int i, int i1, const AxisCell& ky, const AxisCell& kz,
-                                             const uint32_t c[3]) {
+// Staging of one warp's rows, in two passes over all (row, column) pairs so
+// that every lane has work.  Pass 1 writes, in slot col of row r, the
+// y/z-interpolated values of control column col (the four float pairs, the
+// thickness) and its type; pass 2 turns slot i into the record of cell i by
+// adding the differences to slot i + 1 (a single column is its own second
+// column).  The records are those of one cell at a time: u, v - u.
+__device__ __forceinline__ void stage_columns(float4* rec, const float4* sq, uint32_t nr, uint32_t lane,
+                                              const float* const arr[5], const uint8_t* __restrict__ type,
+                                              const LatticeParams& p, const uint32_t c[3]) {
+  const uint32_t cx = c[0], slots = row_slots(cx);
+  for (uint32_t j = lane; j < nr * cx; j += 32) {
+    const uint32_t r = j / cx, col = j - r * cx;
+    const float4 qr = sq[r];
+    const AxisCell ky = locate1(__float_as_uint(qr.z), c[1], p.scale[1]);
+    const AxisCell kz = locate1(__float_as_uint(qr.w), c[2], p.scale[2]);
+    float4* w = rec + (r * slots + col) * kRecWords;
 #pragma unroll
-  for (uint32_t k = 0; k < 4; ++k) {
-    const PF u = column_pf(arr[k], i, ky, kz, c);
-    const PF d = pf_diff(column_pf(arr[k], i1, ky, kz, c), u);
-    w[k] = make_float4(u.h, u.l, d.h, d.l);
+    for (uint32_t k = 0; k < 4; ++k) {
+      const PF u = column_pf(arr[k], (int)col, ky, kz, c);
+      *reinterpret_cast<float2*>(w + k) = make_float2(u.h, u.l);
+    }
+    w[4].x = column_yz(arr[4], (int)col, ky, kz, c);
+    w[4].z = __uint_as_float((uint32_t)__ldg(type + cidx((int)col, ky.nearest, kz.nearest, c)));
   }
-  const float tu = column_yz(arr[4], i, ky, kz, c);
-  const float td = fs(column_yz(arr[4], i1, ky, kz, c), tu);
-  const uint32_t t0 = __ldg(type + cidx(i, ky.nearest, kz.nearest, c));
-  const uint32_t t1 = __ldg(type + cidx(i1, ky.nearest, kz.nearest, c));
-  w[4] = make_float4(tu, td, __uint_as_float(t0), __uint_as_float(t1));
+  __syncwarp();
+  const uint32_t cells = row_cells(cx);
+  for (uint32_t j = lane; j < nr * cells; j += 32) {
+    const uint32_t r = j / cells, i = j - r * cells;
+    float4* w0 = rec + (r * slots + i) * kRecWords;
+    const float4* w1 = cx > 1 ? w0 + kRecWords : w0;
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) {
+      const float2 u = *reinterpret_cast<const float2*>(w0 + k), v = *reinterpret_cast<const float2*>(w1 + k);
+      const PF d = pf_diff({v.x, v.y}, {u.x, u.y});
+      *reinterpret_cast<float2*>(reinterpret_cast<float*>(w0 + k) + 2) = make_float2(d.h, d.l);
+    }
+    const float tu = w0[4].x, tv = w1[4].x, t1 = w1[4].z;
+    w0[4].y = fs(tv, tu);
+    w0[4].w = t1;
+  }
 }
 
 // One staged sample from its cell's record: parameters, phase, TPMS value.
@@ -503,17 +549,23 @@ __device__ __forceinline__ float params_sample(const float* const arr[5], const 
 
 }  // namespace
 
+// CTAs per SM the register budget of lattice_rows_kernel is sized for.
+#ifndef GCM_LATTICE_ROWS_MIN_CTAS
+#define GCM_LATTICE_ROWS_MIN_CTAS 4
+#endif
+
 template <uint32_t R>
-__global__ void __launch_bounds__(256, 4) lattice_rows_kernel(LatticeParams p) {
+__global__ void __launch_bounds__(256, GCM_LATTICE_ROWS_MIN_CTAS) lattice_rows_kernel(LatticeParams p) {
   extern __shared__ float4 s_dyn[];
   float4* s_tab = s_dyn;
   float4* s_rows = s_dyn + kAngleRows;
   load_angle_table(s_tab);
   __syncthreads();
-  const uint32_t cx = p.cx, cells = row_cells(cx);
+  const uint32_t cx = p.cx;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+  const uint32_t slots = row_slots(cx);
   float4* rec = s_rows + warp * row_slice_words(R, cx);
-  float4* sq = rec + R * cells * kRecWords;
+  float4* sq = rec + R * slots * kRecWords;
   const uint32_t c[3] = {p.cx, p.cy, p.cz};
   const uint32_t nc = p.cx * p.cy * p.cz;
   const float* arr[5] = {p.period, p.euler, p.euler ? p.euler + nc : nullptr,
@@ -524,17 +576,13 @@ __global__ void __launch_bounds__(256, 4) lattice_rows_kernel(LatticeParams p) {
   for (uint32_t g = blockIdx.x * (blockDim.x >> 5) + warp; g < groups; g += warps) {
     const uint32_t row0 = g * R, nr = min(R, rows - row0);
     __syncwarp();  // the warp's previous group is read
-    uint32_t y = row0 % p.ny, z = row0 / p.ny;
-    for (uint32_t r = 0; r < nr; ++r) {
-      const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
-      for (uint32_t i = lane; i < cells; i += 32)
-        write_record(rec + (r * cells + i) * kRecWords, arr, p.type, (int)i, cx > 1 ? (int)i + 1 : 0, ky, kz, c);
-      if (lane == 0) sq[r] = make_float4(fs((float)y, p.origin[1]), fs((float)z, p.origin[2]), 0.0f, 0.0f);
-      if (++y == p.ny) {
-        y = 0;
-        ++z;
-      }
+    if (lane < nr) {
+      const uint32_t y = (row0 + lane) % p.ny, z = (row0 + lane) / p.ny;
+      sq[lane] = make_float4(fs((float)y, p.origin[1]), fs((float)z, p.origin[2]), __uint_as_float(y),
+                             __uint_as_float(z));
     }
+    __syncwarp();
+    stage_columns(rec, sq, nr, lane, arr, p.type, p, c);
     __syncwarp();
     for (uint32_t x0 = lane; x0 < p.nx; x0 += 64) {
       const uint32_t x1 = x0 + 32;
@@ -546,7 +594,7 @@ __global__ void __launch_bounds__(256, 4) lattice_rows_kernel(LatticeParams p) {
         const float q1 = fs((float)x1, p.origin[0]);
 #pragma unroll 1
         for (uint32_t r = 0; r < nr; ++r) {
-          const float4* rr = rec + r * cells * kRecWords;
+          const float4* rr = rec + r * slots * kRecWords;
           const float4 qr = sq[r];
           const float v0 = record_sample(rr, k0, q0, make_float2(qr.x, qr.y), s_tab);
           const float v1 = record_sample(rr, k1, q1, make_float2(qr.x, qr.y), s_tab);
@@ -557,7 +605,7 @@ __global__ void __launch_bounds__(256, 4) lattice_rows_kernel(LatticeParams p) {
 #pragma unroll 1
         for (uint32_t r = 0; r < nr; ++r) {
           const float4 qr = sq[r];
-          out[(uint64_t)r * p.nx] = record_sample(rec + r * cells * kRecWords, k0, q0, make_float2(qr.x, qr.y), s_tab);
+          out[(uint64_t)r * p.nx] = record_sample(rec + r * slots * kRecWords, k0, q0, make_float2(qr.x, qr.y), s_tab);
         }
       }
     }
