@@ -309,6 +309,14 @@ gcm_status gcm_ctx_set_wait_limit(gcm_ctx* ctx, uint64_t ns) {
 
 uint64_t gcm_ctx_launch_count(const gcm_ctx* ctx) { return ctx ? ctx->launches.load() : 0; }
 
+gcm_status gcm_ctx_set_primitive_arith(gcm_ctx* ctx, gcm_prim_arith arith) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (arith != GCM_PRIM_ARITH_DEFAULT && arith != GCM_PRIM_ARITH_REFERENCE)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_ctx_set_primitive_arith: unknown mode %d", (int)arith);
+  ctx->prim_exact = arith == GCM_PRIM_ARITH_REFERENCE;
+  return GCM_OK;
+}
+
 // ------------------------------------------------------------------ mesh
 
 gcm_status gcm_mesh_field(gcm_ctx* ctx, const float* d_field, const gcm_grid* grid, float iso, float* d_pos,
@@ -695,6 +703,7 @@ gcm_status gcm_field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_
   p.ny = ny;
   p.nz = nz;
   p.out = d_out;
+  p.exact = ctx->prim_exact ? 1u : 0u;
   GCM_CUDA(ctx, gcm::launch_csg(p, (uint32_t)ctx->sm_count, static_cast<cudaStream_t>(stream)));
   count_launch(ctx, 1);
   return GCM_OK;

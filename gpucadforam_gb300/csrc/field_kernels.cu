@@ -52,55 +52,6 @@ __device__ __forceinline__ float tpms_sc(uint32_t type, float sX, float cX, floa
   }
 }
 
-// sin and cos for |x| <= pi/4: their Taylor series to degree 11 and 12
-// (truncation below 2e-9 there) in Horner form.
-__device__ __forceinline__ void sincos_taylor(float x, float* s, float* c) {
-  const float x2 = fm(x, x);
-  float ps = __fmaf_rn(x2, -2.5052108e-8f, 2.7557319e-6f);  // -1/11!, 1/9!
-  ps = __fmaf_rn(x2, ps, -1.9841270e-4f);                   // -1/7!
-  ps = __fmaf_rn(x2, ps, 8.3333333e-3f);                    // 1/5!
-  ps = __fmaf_rn(x2, ps, -1.6666667e-1f);                   // -1/3!
-  *s = __fmaf_rn(fm(x, x2), ps, x);
-  float pc = __fmaf_rn(x2, 2.0876757e-9f, -2.7557319e-7f);  // 1/12!, -1/10!
-  pc = __fmaf_rn(x2, pc, 2.4801587e-5f);                    // 1/8!
-  pc = __fmaf_rn(x2, pc, -1.3888889e-3f);                   // -1/6!
-  pc = __fmaf_rn(x2, pc, 4.1666667e-2f);                    // 1/4!
-  pc = __fmaf_rn(x2, pc, -0.5f);                            // -1/2!
-  *c = __fmaf_rn(x2, pc, 1.0f);
-}
-
-// sin and cos: the Taylor series above for |x| <= pi/4, else sincosf.
-__device__ __forceinline__ void sincos_small(float x, float* s, float* c) {
-  if (fabsf(x) <= 0.78539818f) sincos_taylor(x, s, c);
-  else sincosf(x, s, c);
-}
-
-// Euler basis rows, ZYX convention of src/Modelling.cu:401-407.
-__device__ __forceinline__ void euler_rows(float ax, float ay, float az, float R[9]) {
-  float sx, cx, sy, cy, sz, cz;
-  constexpr float kQuarter = 0.78539818f;
-  if (fabsf(ax) <= kQuarter && fabsf(ay) <= kQuarter && fabsf(az) <= kQuarter) {
-    // one test for the three angles (false for NaN, which takes the
-    // per-angle path): the same values as sincos_small gives each of them
-    sincos_taylor(ax, &sx, &cx);
-    sincos_taylor(ay, &sy, &cy);
-    sincos_taylor(az, &sz, &cz);
-  } else {
-    sincos_small(ax, &sx, &cx);
-    sincos_small(ay, &sy, &cy);
-    sincos_small(az, &sz, &cz);
-  }
-  R[0] = fm(cz, cy);
-  R[1] = fs(fm(fm(cz, sy), sx), fm(sz, cx));
-  R[2] = fa(fm(fm(cz, sy), cx), fm(sz, sx));
-  R[3] = fm(sz, cy);
-  R[4] = fa(fm(fm(sz, sy), sx), fm(cz, cx));
-  R[5] = fs(fm(fm(sz, sy), cx), fm(cz, sx));
-  R[6] = -sy;
-  R[7] = fm(cy, sx);
-  R[8] = fm(cy, cx);
-}
-
 // ---------------------------------------------------------------------------
 // Compensated FP32 arithmetic of the graded lattices.  The phase X of a 512^3
 // lattice reaches ~55 half-turns, where one float ulp is 4e-6 half-turns; so
@@ -843,7 +794,9 @@ struct PrimPre {
   uint32_t kind, op, flag, pad;
   float c[3];
   float p[6];
-  float R[9];      // rotated kinds
+  float R[9];      // rotated kinds: rows of the ZYX basis
+  float ang[3];    // rotated kinds: the Euler angles
+  float sy;        // rotated kinds: sin(angle y)
   float axis[3];   // cylinder: unit axis
   float end[3];    // cylinder: center + axis
   float w3[3];     // cylinder: end - center
@@ -852,6 +805,13 @@ struct PrimPre {
 
 __device__ __forceinline__ float sqf(float x) { return fm(x, x); }
 
+// Per primitive, the sample-independent values every thread of the reference
+// kernels computes for itself (src/Modelling.cu:264-270, 401-407).  The basis
+// rows are written in the reference's expression shapes (CUDA sinf/cosf,
+// plain operators) so that nvcc rounds and contracts them the same way.
+// EXACT: the axis length of a cylinder squares with powf as the reference
+// does; otherwise with correctly rounded products.
+template <bool EXACT>
 __device__ void prim_setup(const gcm_primitive& q, PrimPre& o) {
   o.kind = q.kind;
   o.op = q.op;
@@ -859,49 +819,98 @@ __device__ void prim_setup(const gcm_primitive& q, PrimPre& o) {
   for (int a = 0; a < 3; ++a) o.c[a] = q.center[a];
   for (int a = 0; a < 6; ++a) o.p[a] = q.p[a];
   if (q.kind == 1) {
-    const float am = __fsqrt_rn(fa(fa(sqf(q.v3[0]), sqf(q.v3[1])), sqf(q.v3[2])));
+    float am;
+    if constexpr (EXACT) am = sqrtf(powf(q.v3[0], 2) + powf(q.v3[1], 2) + powf(q.v3[2], 2));
+    else am = __fsqrt_rn(fa(fa(sqf(q.v3[0]), sqf(q.v3[1])), sqf(q.v3[2])));
     for (int a = 0; a < 3; ++a) {
       o.axis[a] = __fdiv_rn(q.v3[a], am);
       o.end[a] = fa(o.axis[a], q.center[a]);
-      o.w3[a] = fs(o.end[a], q.center[a]);
     }
-    o.dis = __fsqrt_rn(fa(fa(sqf(o.w3[0]), sqf(o.w3[1])), sqf(o.w3[2])));
+    for (int a = 0; a < 3; ++a) o.w3[a] = fs(o.end[a], q.center[a]);
+    if constexpr (EXACT) o.dis = sqrtf(powf(o.w3[0], 2) + powf(o.w3[1], 2) + powf(o.w3[2], 2));
+    else o.dis = __fsqrt_rn(fa(fa(sqf(o.w3[0]), sqf(o.w3[1])), sqf(o.w3[2])));
   } else if (q.kind >= 2) {
-    euler_rows(q.v3[0], q.v3[1], q.v3[2], o.R);
+    const float ax = q.v3[0], ay = q.v3[1], az = q.v3[2];
+    o.ang[0] = ax;
+    o.ang[1] = ay;
+    o.ang[2] = az;
+    o.R[0] = cosf(az) * cosf(ay);
+    o.R[1] = (cosf(az) * sinf(ay) * sinf(ax)) - (sinf(az) * cosf(ax));
+    o.R[2] = (cosf(az) * sinf(ay) * cosf(ax)) + (sinf(az) * sinf(ax));
+    o.R[3] = (sinf(az)) * cosf(ay);
+    o.R[4] = (sinf(az) * sinf(ay) * sinf(ax)) + (cosf(az) * cosf(ax));
+    o.R[5] = (sinf(az) * sinf(ay) * cosf(ax)) - (cosf(az) * sinf(ax));
+    o.R[6] = -1.0f * sinf(ay);
+    o.R[7] = cosf(ay) * sinf(ax);
+    o.R[8] = cosf(ay) * cosf(ax);
+    o.sy = sinf(ay);
   }
 }
 
-// Field of one primitive of kind K at scene point (X, Y, Z); src/Modelling.cu
-// kernels.  Kinds 7 and above are pyramid frustums.
+// Field of one primitive of kind K at sample offset t = index - origin (per
+// axis) and spacing sp, after the kernels of src/Modelling.cu, with the
+// rounding pattern of the reference's own build (nvcc default contraction):
+// the position t * sp - c is one fused multiply-add, the sums of products in
+// the basis rows, cross products and the cylinder's axial distance fuse their
+// first product, 1 - 2 products of a lerp (pyramid widths) fuse, and literals
+// such as 2.0 and 100 promote the cone height terms to double.  Every
+// operation is an explicit IEEE intrinsic, so the CPU oracle restates it bit
+// for bit.  Squares are correctly rounded products; the reference squares
+// with powf(v, 2), which differs from the rounded square in the last bit for
+// about 6% of floats, so these fields stay within a few ulp of the
+// reference's (prim_eval_exact reproduces it bit for bit).  Kinds 7 and
+// above are pyramid frustums.
+__device__ __forceinline__ void rotate_ref(const PrimPre& P, float x, float y, float z, float& a, float& b,
+                                           float& cc) {
+  a = __fmaf_rn(z, P.R[2], __fmaf_rn(x, P.R[0], fm(y, P.R[1])));
+  b = __fmaf_rn(z, P.R[5], __fmaf_rn(x, P.R[3], fm(y, P.R[4])));
+  // the reference's -1.0f * sinf(angle y) folds into y * R7 - x * sin(angle y)
+  cc = __fmaf_rn(z, P.R[8], __fmaf_rn(y, P.R[7], -fm(x, P.sy)));
+}
+
+// The cone height terms: g = y - h/2 and the slab max((g - h/2)*100,
+// -(g + h/2)*100), in double as the reference's literals make them.
+__device__ __forceinline__ float cone_slab(float b, float h) {
+  const float g = (float)__dsub_rn((double)b, (double)h / 2.0);
+  return (float)fmax(__dmul_rn(__dsub_rn((double)g, (double)h / 2.0), 100.0),
+                     -__dmul_rn(__dadd_rn((double)g, (double)h / 2.0), 100.0));
+}
+
 template <int K>
-__device__ __forceinline__ float prim_eval_k(const PrimPre& P, float X, float Y, float Z) {
+__device__ __forceinline__ float prim_eval_k(const PrimPre& P, float tx, float ty, float tz, const float sp[3]) {
   if constexpr (K == 0) {  // implicit_sphere_kernel :314-361
-    const float x = fs(X, P.c[0]), y = fs(Y, P.c[1]), z = fs(Z, P.c[2]);
-    const float r = P.p[0], t = P.p[1] * 0.5f;
+    const float x = __fmaf_rn(tx, sp[0], -P.c[0]), y = __fmaf_rn(ty, sp[1], -P.c[1]),
+                z = __fmaf_rn(tz, sp[2], -P.c[2]);
+    const float r = P.p[0], td = fm(P.p[1], 0.5f);
     const float d2 = fa(fa(sqf(x), sqf(y)), sqf(z));
-    if (P.flag) return fmaxf(-fs(d2, sqf(fs(r, t))), fs(d2, sqf(fa(r, t))));
+    if (P.flag) return fmaxf(-fs(d2, sqf(fs(r, td))), fs(d2, sqf(fa(r, td))));
     return fs(d2, sqf(r));
   } else if constexpr (K == 1) {  // distance_from_line_kernel :244-302
-    const float r = P.p[0], td = P.p[1] * 0.5f, tda = P.p[2] * 0.5f;
-    const float w1x = fs(X, P.c[0]), w1y = fs(Y, P.c[1]), w1z = fs(Z, P.c[2]);
-    const float w2x = fs(X, P.end[0]), w2y = fs(Y, P.end[1]), w2z = fs(Z, P.end[2]);
-    const float dx = fs(fm(w1y, w2z), fm(w1z, w2y)), dy = fs(fm(w1z, w2x), fm(w1x, w2z)),
-                dz = fs(fm(w1x, w2y), fm(w1y, w2x));
-    const float e = __fsqrt_rn(fa(fa(sqf(dx), sqf(dy)), sqf(dz)));
-    const float f = __fdiv_rn(e, P.dis);
-    const float g = fa(fa(fm(fs(X, P.c[0]), P.axis[0]), fm(fs(Y, P.c[1]), P.axis[1])), fm(fs(Z, P.c[2]), P.axis[2]));
+    const float r = P.p[0], td = fm(P.p[1], 0.5f), tda = fm(P.p[2], 0.5f);
+    float w1[3], w2[3];
+    const float t[3] = {tx, ty, tz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      w1[a] = __fmaf_rn(t[a], sp[a], -P.c[a]);
+      w2[a] = __fmaf_rn(t[a], sp[a], -P.end[a]);
+    }
+    const float dx = __fmaf_rn(w1[1], w2[2], -fm(w1[2], w2[1])), dy = __fmaf_rn(w1[2], w2[0], -fm(w1[0], w2[2])),
+                dz = __fmaf_rn(w1[0], w2[1], -fm(w1[1], w2[0]));
+    const float f = __fdiv_rn(__fsqrt_rn(fa(fa(sqf(dx), sqf(dy)), sqf(dz))), P.dis);
+    const float g = __fmaf_rn(w1[2], P.axis[2], __fmaf_rn(w1[0], P.axis[0], fm(w1[1], P.axis[1])));
     const float fld1 = fmaxf(fs(g, tda), -fa(g, tda));
     const float fld2 = P.flag ? fmaxf(fs(f, fa(r, td)), -fs(f, fs(r, td))) : fs(f, r);
     return fmaxf(fld1, fld2);
   } else {
-    const float x = fs(X, P.c[0]), y = fs(Y, P.c[1]), z = fs(Z, P.c[2]);
-    const float a = fa(fa(fm(x, P.R[0]), fm(y, P.R[1])), fm(z, P.R[2]));
-    const float b = fa(fa(fm(x, P.R[3]), fm(y, P.R[4])), fm(z, P.R[5]));
-    const float cc = fa(fa(fm(x, P.R[6]), fm(y, P.R[7])), fm(z, P.R[8]));
+    const float x = __fmaf_rn(tx, sp[0], -P.c[0]), y = __fmaf_rn(ty, sp[1], -P.c[1]),
+                z = __fmaf_rn(tz, sp[2], -P.c[2]);
+    float a, b, cc;
+    rotate_ref(P, x, y, z, a, b, cc);
     if constexpr (K == 2) {  // implicit_cuboid_kernel :375-421
-      return fmaxf(fmaxf(fs(fabsf(a), P.p[0] * 0.5f), fs(fabsf(b), P.p[1] * 0.5f)), fs(fabsf(cc), P.p[2] * 0.5f));
+      return fmaxf(fmaxf(fs(fabsf(a), fm(P.p[0], 0.5f)), fs(fabsf(b), fm(P.p[1], 0.5f))),
+                   fs(fabsf(cc), fm(P.p[2], 0.5f)));
     } else if constexpr (K == 3) {  // implicit_cuboid_shell_kernel :435-487
-      const float wx = P.p[0] * 0.5f, wy = P.p[1] * 0.5f, wz = P.p[2] * 0.5f, th = P.p[3];
+      const float wx = fm(P.p[0], 0.5f), wy = fm(P.p[1], 0.5f), wz = fm(P.p[2], 0.5f), th = P.p[3];
       const float f11 = fs(fabsf(a), wx), f12 = fs(fabsf(a), fs(wx, th));
       const float f21 = fs(fabsf(b), wy), f22 = fs(fabsf(b), fs(wy, th));
       return fmaxf(fmaxf(fmaxf(f11, f21), -fmaxf(f12, f22)), fs(fabsf(cc), wz));
@@ -911,28 +920,114 @@ __device__ __forceinline__ float prim_eval_k(const PrimPre& P, float X, float Y,
     } else if constexpr (K == 5) {  // implicit_cone_kernel :631-683
       const float br = P.p[0], hgt = P.p[1];
       const float k2 = sqf(__fdiv_rn(hgt, br));
-      const float g = (float)((double)b - (double)hgt / 2.0);
-      const float h = (float)fmax(((double)g - (double)hgt / 2.0) * 100.0, ((double)g + (double)hgt / 2.0) * 100.0 * -1.0);
-      const float f1 = fs(fm(fa(sqf(a), sqf(cc)), k2), sqf(fs(b, hgt)));
-      return fmaxf(f1, h);
+      const float f1 = __fmaf_rn(fa(sqf(a), sqf(cc)), k2, -sqf(fs(b, hgt)));
+      return fmaxf(f1, cone_slab(b, hgt));
     } else if constexpr (K == 6) {  // implicit_cone_frustum_kernel :698-750
       const float tr = P.p[0], brr = P.p[1], hgt = P.p[2];
-      const float rd = fm(__fdiv_rn(fs(hgt, b), hgt), fs(brr, tr));
-      const float g = (float)((double)b - (double)hgt / 2.0);
-      const float h = (float)fmax(((double)g - (double)hgt / 2.0) * 100.0, ((double)g + (double)hgt / 2.0) * 100.0 * -1.0);
-      const double rr = (double)fa(rd, tr);
-      const float f1 = (float)((double)fa(sqf(a), sqf(cc)) - rr * rr);
-      return fmaxf(f1, h);
+      const float rr = __fmaf_rn(__fdiv_rn(fs(hgt, b), hgt), fs(brr, tr), tr);
+      const float f1 = (float)__dsub_rn((double)fa(sqf(a), sqf(cc)), __dmul_rn((double)rr, (double)rr));
+      return fmaxf(f1, cone_slab(b, hgt));
     } else {  // implicit_pyramid_frustum_kernel :501-557
-      const float xwb = P.p[0] * 0.5f, xwt = P.p[1] * 0.5f, yh = P.p[2];
-      const float zwb = P.p[3] * 0.5f, zwt = P.p[4] * 0.5f;
+      const float xwb = fm(P.p[0], 0.5f), xwt = fm(P.p[1], 0.5f), yh = P.p[2];
+      const float zwb = fm(P.p[3], 0.5f), zwt = fm(P.p[4], 0.5f);
       const float ratio = __fdiv_rn(fs(yh, b), yh);
-      const float xw = fa(fm(ratio, fs(xwb, xwt)), xwt);
-      const float f1 = fs(fabsf(a), xw);
-      const float f2 = fs(fabsf(fs(b, __fdiv_rn(yh, 2.0f))), __fdiv_rn(yh, 2.0f));
-      const float zw = fa(fm(ratio, fs(zwb, zwt)), zwt);
-      const float f3 = fs(fabsf(cc), zw);
+      const float hy = fm(yh, 0.5f);
+      const float f1 = fs(fabsf(a), __fmaf_rn(ratio, fs(xwb, xwt), xwt));
+      const float f2 = fs(fabsf(fs(b, hy)), hy);
+      const float f3 = fs(fabsf(cc), __fmaf_rn(ratio, fs(zwb, zwt), zwt));
       return fmaxf(fmaxf(f1, f2), f3);
+    }
+  }
+}
+
+// The same fields bit for bit as the reference's kernels: written in their
+// expression shapes with plain float operators, CUDA powf / sqrtf / division
+// and default contraction, so that nvcc forms the same roundings and fused
+// multiply-adds as in the reference's own build.  The cone kinds evaluate the
+// basis per sample from the angles, as the reference does (their expressions
+// around powf round differently when the basis comes from memory), one sample
+// at a time (see csg_eval8).
+__device__ __forceinline__ void rotate_inline(const PrimPre& P, float x, float y, float z, float& a, float& b,
+                                              float& cc) {
+  const float ax = P.ang[0], ay = P.ang[1], az = P.ang[2];
+  const float px[3] = {(cosf(az) * cosf(ay)), (cosf(az) * sinf(ay) * sinf(ax)) - (sinf(az) * cosf(ax)),
+                       (cosf(az) * sinf(ay) * cosf(ax)) + (sinf(az) * sinf(ax))};
+  const float py[3] = {((sinf(az)) * cosf(ay)), (sinf(az) * sinf(ay) * sinf(ax)) + (cosf(az) * cosf(ax)),
+                       (sinf(az) * sinf(ay) * cosf(ax)) - (cosf(az) * sinf(ax))};
+  const float pz[3] = {(-1.0f * sinf(ay)), cosf(ay) * sinf(ax), cosf(ay) * cosf(ax)};
+  a = x * px[0] + y * px[1] + z * px[2];
+  b = x * py[0] + y * py[1] + z * py[2];
+  cc = x * pz[0] + y * pz[1] + z * pz[2];
+}
+
+template <int K>
+__device__ __forceinline__ float prim_eval_exact(const PrimPre& P, float tx, float ty, float tz, const float sp[3]) {
+  if constexpr (K == 0) {
+    const float x = tx * sp[0] - P.c[0], y = ty * sp[1] - P.c[1], z = tz * sp[2] - P.c[2];
+    const float r = P.p[0], td = P.p[1] / 2.0;
+    if (P.flag) {
+      const float f1 = powf(x, 2) + powf(y, 2) + powf(z, 2) - powf((r - td), 2);
+      const float f2 = powf(x, 2) + powf(y, 2) + powf(z, 2) - powf((r + td), 2);
+      return max(f1 * -1.0, f2);
+    }
+    return powf(x, 2) + powf(y, 2) + powf(z, 2) - powf((r), 2);
+  } else if constexpr (K == 1) {
+    const float x1 = tx * sp[0], y1 = ty * sp[1], z1 = tz * sp[2];
+    const float r = P.p[0], td = P.p[1] / 2.0, tda = P.p[2] / 2.0;
+    const float w1[3] = {x1 - P.c[0], y1 - P.c[1], z1 - P.c[2]};
+    const float w2[3] = {x1 - P.end[0], y1 - P.end[1], z1 - P.end[2]};
+    const float d[3] = {w1[1] * w2[2] - w1[2] * w2[1], w1[2] * w2[0] - w1[0] * w2[2], w1[0] * w2[1] - w1[1] * w2[0]};
+    const float e = sqrtf(powf(d[0], 2) + powf(d[1], 2) + powf(d[2], 2));
+    const float f = e / P.dis;
+    const float g = ((x1 - P.c[0]) * P.axis[0] + (y1 - P.c[1]) * P.axis[1] + (z1 - P.c[2]) * P.axis[2]);
+    const float fld1 = max(g - tda, (g + tda) * -1);
+    const float fld2 = P.flag ? (float)max((f - (r + td)), (f - (r - td)) * -1.0) : (f - (r));
+    return max(fld1, fld2);
+  } else {
+    const float x = tx * sp[0] - P.c[0], y = ty * sp[1] - P.c[1], z = tz * sp[2] - P.c[2];
+    float a, b, cc;
+    if constexpr (K == 5 || K == 6) {
+      rotate_inline(P, x, y, z, a, b, cc);
+    } else {
+      a = x * P.R[0] + y * P.R[1] + z * P.R[2];
+      b = x * P.R[3] + y * P.R[4] + z * P.R[5];
+      cc = __fmaf_rn(z, P.R[8], __fmaf_rn(y, P.R[7], -__fmul_rn(x, P.sy)));
+    }
+    if constexpr (K == 2) {
+      const float xw = P.p[0] / 2.0, yw = P.p[1] / 2.0, zw = P.p[2] / 2.0;
+      return max(max(fabs(a) - xw, fabs(b) - yw), fabs(cc) - zw);
+    } else if constexpr (K == 3) {
+      const float xw = P.p[0] / 2.0, yw = P.p[1] / 2.0, zw = P.p[2] / 2.0, th = P.p[3];
+      const float f11 = fabs(a) - xw, f12 = fabs(a) - (xw - th);
+      const float f21 = fabs(b) - yw, f22 = fabs(b) - (yw - th);
+      const float f3 = fabs(cc) - zw;
+      return max(max(max(f11, f21), (max(f12, f22)) * -1.0), f3);
+    } else if constexpr (K == 4) {
+      const float side = (P.p[0] - sqrtf(powf(a, 2) + powf(b, 2)));
+      return powf(cc, 2) - powf(P.p[1], 2) + powf(side, 2);
+    } else if constexpr (K == 5) {
+      const float br = P.p[0], h = P.p[1];
+      const float k2 = powf((h / br), 2);
+      const float g = (b - (h / 2.0));
+      const float hh = max((g - (h / 2.0)) * 100, (g + (h / 2.0)) * 100 * -1.0);
+      const float f1 = ((powf((a), 2) + powf((cc), 2)) * k2) - powf((b - h), 2);
+      return max(f1, hh);
+    } else if constexpr (K == 6) {
+      const float tr = P.p[0], brr = P.p[1], h = P.p[2];
+      const float rd = ((h - b) / h) * (brr - tr);
+      const float g = (b - (h / 2.0));
+      const float hh = max((g - (h / 2.0)) * 100, (g + (h / 2.0)) * 100 * -1.0);
+      const float f1 = ((powf((a), 2) + powf((cc), 2))) - pow((rd + tr), 2);
+      return max(f1, hh);
+    } else {
+      const float xwb = P.p[0] / 2.0, xwt = P.p[1] / 2.0, yh = P.p[2], zwb = P.p[3] / 2.0, zwt = P.p[4] / 2.0;
+      const float ratio = ((yh - b) / yh);
+      const float xw = (ratio * (xwb - xwt)) + xwt;
+      const float f1 = fabs(a) - xw;
+      const float f2 = fabs(b - (yh / 2)) - ((yh) / 2);
+      const float zw = (ratio * (zwb - zwt)) + zwt;
+      const float f3 = fabs(cc) - zw;
+      return max(max(f1, f2), f3);
     }
   }
 }
@@ -1197,15 +1292,26 @@ __device__ __forceinline__ float csg_fold(uint32_t op, float f, float g) {
   return op == 1 ? fmaxf(f, -g) : (op == 2 ? fmaxf(f, g) : fminf(f, g));
 }
 
-template <int K>
-__device__ __forceinline__ void csg_eval8(const PrimPre& P, uint32_t op, float X, float Y, const float (&Z)[kCsgTz],
-                                          float (&f)[kCsgTz]) {
+template <int K, bool EXACT>
+__device__ __forceinline__ void csg_eval8(const PrimPre& P, uint32_t op, float tX, float tY,
+                                          const float (&tZ)[kCsgTz], const float sp[3], float (&f)[kCsgTz]) {
+  if constexpr (!EXACT) {
 #pragma unroll
-  for (uint32_t q = 0; q < kCsgTz; ++q) f[q] = csg_fold(op, f[q], prim_eval_k<K>(P, X, Y, Z[q]));
+    for (uint32_t q = 0; q < kCsgTz; ++q) f[q] = csg_fold(op, f[q], prim_eval_k<K>(P, tX, tY, tZ[q], sp));
+  } else if constexpr (K == 5 || K == 6) {
+    // one sample per iteration: unrolled, the samples' shared terms change
+    // how nvcc contracts these expressions
+#pragma unroll 1
+    for (uint32_t q = 0; q < kCsgTz; ++q) f[q] = csg_fold(op, f[q], prim_eval_exact<K>(P, tX, tY, tZ[q], sp));
+  } else {
+#pragma unroll
+    for (uint32_t q = 0; q < kCsgTz; ++q) f[q] = csg_fold(op, f[q], prim_eval_exact<K>(P, tX, tY, tZ[q], sp));
+  }
 }
 
 }  // namespace
 
+template <bool EXACT>
 __global__ void __launch_bounds__(kCsgWarps * 32, 4) csg_kernel(CsgParams p) {
   extern __shared__ __align__(16) unsigned char csg_smem[];
   const uint32_t n = p.n;  // at most 256 (checked by the caller)
@@ -1215,7 +1321,7 @@ __global__ void __launch_bounds__(kCsgWarps * 32, 4) csg_kernel(CsgParams p) {
   uint8_t* s_perm = reinterpret_cast<uint8_t*>(s_run + n);
   uint8_t* s_list = s_perm + n;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  for (uint32_t i = tid; i < n; i += blockDim.x) prim_setup(p.prims[i], s_pre[i]);
+  for (uint32_t i = tid; i < n; i += blockDim.x) prim_setup<EXACT>(p.prims[i], s_pre[i]);
   __syncthreads();
   for (uint32_t i = tid; i < n; i += blockDim.x) {
     const uint32_t op = csg_op(s_pre[i].op), kind = min(s_pre[i].kind, 7u);
@@ -1266,15 +1372,16 @@ __global__ void __launch_bounds__(kCsgWarps * 32, 4) csg_kernel(CsgParams p) {
     __syncwarp();
     const uint32_t cnt = csg_cull_warp(s_pre, s_run, lu, n, list, lane);
     const uint32_t px = x0 + lane;
-    const float X = csg_coord(px, p.origin[0], p.spacing[0]);
-    float Z[kCsgTz];
+    // sample offsets index - origin; the primitives form their positions
+    const float tX = fs((float)px, p.origin[0]);
+    float tZ[kCsgTz];
 #pragma unroll
-    for (uint32_t q = 0; q < kCsgTz; ++q) Z[q] = csg_coord(z0 + q, p.origin[2], p.spacing[2]);
+    for (uint32_t q = 0; q < kCsgTz; ++q) tZ[q] = fs((float)(z0 + q), p.origin[2]);
 #pragma unroll 1
     for (uint32_t r = 0; r < kCsgTy; ++r) {
       const uint32_t py = y0 + r;
       if (py >= p.ny) break;  // warp-uniform
-      const float Y = csg_coord(py, p.origin[1], p.spacing[1]);
+      const float tY = fs((float)py, p.origin[1]);
       float f[kCsgTz];
 #pragma unroll
       for (uint32_t q = 0; q < kCsgTz; ++q) f[q] = INFINITY;
@@ -1282,14 +1389,14 @@ __global__ void __launch_bounds__(kCsgWarps * 32, 4) csg_kernel(CsgParams p) {
         const PrimPre& P = s_pre[list[j]];
         const uint32_t op = P.op;
         switch (P.kind) {
-          case 0: csg_eval8<0>(P, op, X, Y, Z, f); break;
-          case 1: csg_eval8<1>(P, op, X, Y, Z, f); break;
-          case 2: csg_eval8<2>(P, op, X, Y, Z, f); break;
-          case 3: csg_eval8<3>(P, op, X, Y, Z, f); break;
-          case 4: csg_eval8<4>(P, op, X, Y, Z, f); break;
-          case 5: csg_eval8<5>(P, op, X, Y, Z, f); break;
-          case 6: csg_eval8<6>(P, op, X, Y, Z, f); break;
-          default: csg_eval8<7>(P, op, X, Y, Z, f); break;
+          case 0: csg_eval8<0, EXACT>(P, op, tX, tY, tZ, p.spacing, f); break;
+          case 1: csg_eval8<1, EXACT>(P, op, tX, tY, tZ, p.spacing, f); break;
+          case 2: csg_eval8<2, EXACT>(P, op, tX, tY, tZ, p.spacing, f); break;
+          case 3: csg_eval8<3, EXACT>(P, op, tX, tY, tZ, p.spacing, f); break;
+          case 4: csg_eval8<4, EXACT>(P, op, tX, tY, tZ, p.spacing, f); break;
+          case 5: csg_eval8<5, EXACT>(P, op, tX, tY, tZ, p.spacing, f); break;
+          case 6: csg_eval8<6, EXACT>(P, op, tX, tY, tZ, p.spacing, f); break;
+          default: csg_eval8<7, EXACT>(P, op, tX, tY, tZ, p.spacing, f); break;
         }
       }
       if (px < p.nx) {
@@ -1471,7 +1578,8 @@ uint64_t csg_tiles(uint32_t nx, uint32_t ny, uint32_t nz) {
   return (t + kCsgWarps - 1) / kCsgWarps;  // CTAs that give every warp a tile
 }
 
-cudaError_t launch_csg(const CsgParams& p, uint32_t sm_count, cudaStream_t st) {
+template <bool EXACT>
+static cudaError_t launch_csg_form(const CsgParams& p, uint32_t sm_count, cudaStream_t st) {
   const size_t smem = (size_t)p.n * (sizeof(PrimPre) + kCsgWarps * (sizeof(float2) + 1) + sizeof(uint16_t) + 1);
   cudaError_t e = cudaSuccess;
   if (smem > 48 * 1024) {
@@ -1479,16 +1587,21 @@ cudaError_t launch_csg(const CsgParams& p, uint32_t sm_count, cudaStream_t st) {
     int dev = 0, optin = 0;
     e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(csg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(csg_kernel<EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     if (e != cudaSuccess) return e;
   }
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, csg_kernel, kCsgWarps * 32, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, csg_kernel<EXACT>, kCsgWarps * 32, smem);
   if (e != cudaSuccess) return e;
   const uint64_t want = csg_tiles(p.nx, p.ny, p.nz), cap = (uint64_t)sm_count * (uint64_t)(per_sm > 0 ? per_sm : 1);
   const uint32_t blocks = (uint32_t)(want < cap ? want : cap);
-  csg_kernel<<<blocks, kCsgWarps * 32, smem, st>>>(p);
+  csg_kernel<EXACT><<<blocks, kCsgWarps * 32, smem, st>>>(p);
   return cudaGetLastError();
+}
+
+cudaError_t launch_csg(const CsgParams& p, uint32_t sm_count, cudaStream_t st) {
+  return p.exact ? launch_csg_form<true>(p, sm_count, st) : launch_csg_form<false>(p, sm_count, st);
 }
 
 cudaError_t launch_normalise(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, unsigned int* enc, float lo,

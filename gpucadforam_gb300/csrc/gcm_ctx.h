@@ -22,6 +22,7 @@ struct gcm_ctx {
   int mesh_threads = GCM_MESH_THREADS;
   uint32_t tile_voxels = GCM_MESH_TILE_VOXELS;
   bool shape_set = false;  // the caller chose the launch shape (else per-form defaults)
+  bool prim_exact = false; // primitive fields in the reference's powf arithmetic
   std::atomic<uint64_t> launches{0};
   std::string last_error;
   // scratch (device): counts + counters + tile states

@@ -172,6 +172,7 @@ struct CsgParams {
   float origin[3], spacing[3];
   uint32_t nx, ny, nz;
   float* out;
+  uint32_t exact;  // GCM_PRIM_ARITH_REFERENCE: the reference's powf squares, bit for bit
 };
 
 // Launch wrappers (each kernel is launched from the file that defines it).

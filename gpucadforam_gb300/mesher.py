@@ -76,6 +76,11 @@ class Context:
     def reserve(self, max_points: int):
         self.check(self.lib.gcm_ctx_reserve(self.h, int(max_points)))
 
+    def set_primitive_arith(self, reference_exact: bool):
+        """CSG primitive fields bit for bit as the reference's kernels (powf
+        squares) instead of the default correctly rounded squares."""
+        self.check(self.lib.gcm_ctx_set_primitive_arith(self.h, 1 if reference_exact else 0))
+
     def set_launch_shape(self, threads: int, tile_voxels: int):
         self.check(self.lib.gcm_ctx_set_launch_shape(self.h, int(threads), int(tile_voxels)))
 

@@ -240,6 +240,19 @@ typedef struct gcm_frame {
   float spacing[3];
 } gcm_frame;
 
+/* Rounding of the primitive fields (the kernels of src/Modelling.cu:244-750).
+ * DEFAULT follows the reference build's operation order and fused
+ * multiply-adds with correctly rounded squares: within a few ulp of the
+ * reference's fields (its powf(v, 2) differs from the rounded square in the
+ * last bit for about 6% of floats).  REFERENCE squares with CUDA's powf as the
+ * reference does and reproduces its fields bit for bit, at about 4x the cost
+ * of the default on primitive-heavy scenes. */
+typedef enum gcm_prim_arith { GCM_PRIM_ARITH_DEFAULT = 0, GCM_PRIM_ARITH_REFERENCE = 1 } gcm_prim_arith;
+/* Selects the primitive arithmetic of this context's CSG calls
+ * (gcm_field_csg, gcm_mesh_csg).  No reference counterpart: the reference has
+ * only the powf form. */
+gcm_status gcm_ctx_set_primitive_arith(gcm_ctx* ctx, gcm_prim_arith arith);
+
 /* CSG field: f = op_n(... op_0(+inf, g_0) ..., g_n) with union = min,
  * subtract = max(f, -g), intersect = max(f, g).  d_prims is a device array. */
 gcm_status gcm_field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,

@@ -714,6 +714,100 @@ T primitive_at(uint32_t kind, uint32_t flag, const float* center, const float* v
   }
 }
 
+// The float primitive fields as the GPU evaluates them by default: sample
+// offset t = index - origin and spacing sp per axis; the reference build's
+// operation order and fused multiply-adds (position t * sp - c fused, sums of
+// products and cross products fusing their first product, lerps of the
+// pyramid widths fused, cone height terms in double) with correctly rounded
+// squares where the reference calls powf(v, 2).  The basis rows come from the
+// host's sinf/cosf, so rotated kinds agree with the GPU (CUDA sinf/cosf) only
+// to the trig's last bits.
+float primitive_f32(uint32_t kind, uint32_t flag, const float* c, const float* v3, const float* p, const float t[3],
+                    const float sp[3]) {
+  using std::fma;
+  auto sqr = [](float v) { return v * v; };
+  switch (kind) {
+    case 0: {
+      const float x = fma(t[0], sp[0], -c[0]), y = fma(t[1], sp[1], -c[1]), z = fma(t[2], sp[2], -c[2]);
+      const float r = p[0], td = p[1] * 0.5f;
+      const float d2 = (sqr(x) + sqr(y)) + sqr(z);
+      if (flag) return std::fmax(-(d2 - sqr(r - td)), d2 - sqr(r + td));
+      return d2 - sqr(r);
+    }
+    case 1: {
+      const float r = p[0], td = p[1] * 0.5f, tda = p[2] * 0.5f;
+      const float am = std::sqrt((sqr(v3[0]) + sqr(v3[1])) + sqr(v3[2]));
+      float ax[3], end[3], w1[3], w2[3], w3[3];
+      for (int k = 0; k < 3; ++k) {
+        ax[k] = v3[k] / am;
+        end[k] = ax[k] + c[k];
+      }
+      for (int k = 0; k < 3; ++k) {
+        w1[k] = fma(t[k], sp[k], -c[k]);
+        w2[k] = fma(t[k], sp[k], -end[k]);
+        w3[k] = end[k] - c[k];
+      }
+      const float dis = std::sqrt((sqr(w3[0]) + sqr(w3[1])) + sqr(w3[2]));
+      const float dx = fma(w1[1], w2[2], -(w1[2] * w2[1])), dy = fma(w1[2], w2[0], -(w1[0] * w2[2])),
+                  dz = fma(w1[0], w2[1], -(w1[1] * w2[0]));
+      const float f = std::sqrt((sqr(dx) + sqr(dy)) + sqr(dz)) / dis;
+      const float g = fma(w1[2], ax[2], fma(w1[0], ax[0], w1[1] * ax[1]));
+      const float fld1 = std::fmax(g - tda, -(g + tda));
+      const float fld2 = flag ? std::fmax(f - (r + td), -(f - (r - td))) : f - r;
+      return std::fmax(fld1, fld2);
+    }
+    default: {
+      const float x = fma(t[0], sp[0], -c[0]), y = fma(t[1], sp[1], -c[1]), z = fma(t[2], sp[2], -c[2]);
+      const float ax = v3[0], ay = v3[1], az = v3[2];
+      const float sx = std::sin(ax), cx = std::cos(ax), sy = std::sin(ay), cy = std::cos(ay), sz = std::sin(az),
+                  cz = std::cos(az);
+      const float R0 = cz * cy, R1 = fma(cz * sy, sx, -(sz * cx)), R2 = fma(cz * sy, cx, sz * sx);
+      const float R3 = sz * cy, R4 = fma(sz * sy, sx, cz * cx), R5 = fma(sz * sy, cx, -(cz * sx));
+      const float R7 = cy * sx, R8 = cy * cx;
+      const float a = fma(z, R2, fma(x, R0, y * R1));
+      const float b = fma(z, R5, fma(x, R3, y * R4));
+      const float cc = fma(z, R8, fma(y, R7, -(x * sy)));
+      auto slab = [](float bb, float h) {
+        const float g = (float)((double)bb - (double)h / 2.0);
+        return (float)std::fmax(((double)g - (double)h / 2.0) * 100.0, -(((double)g + (double)h / 2.0) * 100.0));
+      };
+      switch (kind) {
+        case 2:
+          return std::fmax(std::fmax(std::fabs(a) - p[0] * 0.5f, std::fabs(b) - p[1] * 0.5f),
+                           std::fabs(cc) - p[2] * 0.5f);
+        case 3: {
+          const float wx = p[0] * 0.5f, wy = p[1] * 0.5f, wz = p[2] * 0.5f, th = p[3];
+          const float f11 = std::fabs(a) - wx, f12 = std::fabs(a) - (wx - th);
+          const float f21 = std::fabs(b) - wy, f22 = std::fabs(b) - (wy - th);
+          return std::fmax(std::fmax(std::fmax(f11, f21), -std::fmax(f12, f22)), std::fabs(cc) - wz);
+        }
+        case 4: {
+          const float side = p[0] - std::sqrt(sqr(a) + sqr(b));
+          return (sqr(cc) - sqr(p[1])) + sqr(side);
+        }
+        case 5: {
+          const float k2 = sqr(p[1] / p[0]);
+          return std::fmax(fma(sqr(a) + sqr(cc), k2, -sqr(b - p[1])), slab(b, p[1]));
+        }
+        case 6: {
+          const float tr = p[0], br = p[1], h = p[2];
+          const float rr = fma((h - b) / h, br - tr, tr);
+          const float f1 = (float)((double)(sqr(a) + sqr(cc)) - (double)rr * (double)rr);
+          return std::fmax(f1, slab(b, h));
+        }
+        default: {
+          const float xwb = p[0] * 0.5f, xwt = p[1] * 0.5f, yh = p[2], zwb = p[3] * 0.5f, zwt = p[4] * 0.5f;
+          const float ratio = (yh - b) / yh, hy = yh * 0.5f;
+          const float f1 = std::fabs(a) - fma(ratio, xwb - xwt, xwt);
+          const float f2 = std::fabs(b - hy) - hy;
+          const float f3 = std::fabs(cc) - fma(ratio, zwb - zwt, zwt);
+          return std::fmax(std::fmax(f1, f2), f3);
+        }
+      }
+    }
+  }
+}
+
 template <class T>
 T csg_apply(T f, T g, uint32_t op) {
   switch (op) {
@@ -735,13 +829,18 @@ void csg_impl(const orc_prim* prims, uint32_t n, const float* origin, const floa
   for (int64_t ii = 0; ii < (int64_t)total; ++ii) {
     const uint64_t i = (uint64_t)ii;
     const uint32_t px = (uint32_t)(i % nx), py = (uint32_t)((i / nx) % ny), pz = (uint32_t)(i / ((uint64_t)nx * ny));
-    const T X = (T)(((float)px - origin[0]) * spacing[0]);
-    const T Y = (T)(((float)py - origin[1]) * spacing[1]);
-    const T Z = (T)(((float)pz - origin[2]) * spacing[2]);
+    const float t[3] = {(float)px - origin[0], (float)py - origin[1], (float)pz - origin[2]};
     T f = std::numeric_limits<T>::infinity();
     for (uint32_t k = 0; k < n; ++k) {
       const orc_prim& P = prims[k];
-      f = csg_apply<T>(f, primitive_at<T>(P.kind, P.flag, P.center, P.v3, P.p, X, Y, Z), P.op);
+      T g;
+      if constexpr (sizeof(T) == 4) {
+        g = primitive_f32(P.kind, P.flag, P.center, P.v3, P.p, t, spacing);
+      } else {
+        g = primitive_at<T>(P.kind, P.flag, P.center, P.v3, P.p, (T)t[0] * (T)spacing[0], (T)t[1] * (T)spacing[1],
+                            (T)t[2] * (T)spacing[2]);
+      }
+      f = csg_apply<T>(f, g, P.op);
     }
     out[i] = (Out)f;
   }
@@ -1423,11 +1522,12 @@ void orc_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t nz, float* 
 void orc_primitive(uint32_t kind, int nx, int ny, int nz, float dx, float dy, float dz, const float* center,
                    const float* v3, const float* p, uint32_t flag, float* out) {
   const float mx = (float)((nx - 1) / 2.0), my = (float)((ny - 1) / 2.0), mz = (float)((nz - 1) / 2.0);
+  const float sp[3] = {dx, dy, dz};
   for (int z = 0; z < nz; ++z)
     for (int y = 0; y < ny; ++y)
       for (int x = 0; x < nx; ++x) {
-        const float X = (x - mx) * dx, Y = (y - my) * dy, Z = (z - mz) * dz;
-        out[pidx(x, y, z, nx, ny)] = primitive_at<float>(kind, flag, center, v3, p, X, Y, Z);
+        const float t[3] = {x - mx, y - my, z - mz};
+        out[pidx(x, y, z, nx, ny)] = primitive_f32(kind, flag, center, v3, p, t, sp);
       }
 }
 

@@ -99,6 +99,27 @@ def test_cull_equals_full_fold_all_kinds(ctx, seed, n, shape, spacing):
     _same(got, _fold(ctx, prims, frame, shape))
 
 
+@pytest.mark.parametrize("seed,n,shape,spacing", [
+    (21, 48, (40, 52, 36), 1.0 / 50),
+    (22, 64, (64, 64, 64), -1.0 / 63),
+])
+def test_cull_equals_full_fold_reference_arith(seed, n, shape, spacing):
+    """The same with GCM_PRIM_ARITH_REFERENCE (powf squares, per-sample cone
+    bases): the enclosures still hold."""
+    from gpucadforam_gb300.mesher import Context, make_frame, primitives_to_device
+
+    c = Context(0)
+    try:
+        c.set_primitive_arith(True)
+        prims = _scene(seed, n)
+        origin = (0.0, 0.0, 0.0) if spacing > 0 else tuple(float(s) for s in shape[::-1])
+        frame = make_frame(origin, (spacing,) * 3)
+        got = c.csg_field(primitives_to_device(prims), len(prims), frame, shape)
+        _same(got, _fold(c, prims, frame, shape))
+    finally:
+        c.close()
+
+
 def test_cull_many_small_primitives(ctx):
     """256 small primitives (the most a scene may hold): most tiles keep only a few."""
     from gpucadforam_gb300.mesher import make_frame, primitives_to_device

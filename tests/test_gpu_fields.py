@@ -1,9 +1,10 @@
 """GPU parity of the field kernels, through the C ABI.
 
 Unit cells and primitives against the reference's own kernels (fixtures);
-graded lattices bit for bit against the oracle's restatement of the kernels'
-compensated float arithmetic and within 1e-5 relative of the FP64 oracle; CSG
-scenes against the FP32 and FP64 oracles.  Tolerances are written in each test.
+primitives bit for bit against the reference's own kernels; graded lattices bit
+for bit against the oracle's restatement of the kernels' compensated float
+arithmetic and within 1e-5 relative of the FP64 oracle; CSG scenes against the
+FP32 and FP64 oracles.  Tolerances are written in each test.
 """
 import numpy as np
 import pytest
@@ -43,18 +44,44 @@ def test_unit_cell_vs_reference(ctx, i):
     assert_field_close(got, FIELDS[f"sm103a/unit{i}"], k_rel=2, k_scale=4)
 
 
-@pytest.mark.parametrize("i", range(n_cases(FIELDS, "prim")))
-def test_primitive_vs_reference(ctx, i):
+def _prim_case(i):
     from gpucadforam_gb300.mesher import make_frame, primitives_to_device
 
     q = FIELDS[f"in/prim{i}"]
     nx, ny, nz = (int(v) for v in q[:3])
-    d = q[3:6]
     prim = dict(kind=int(q[6]), flag=int(q[7]), center=q[8:11], v3=q[11:14], p=q[14:20], op=0)
     origin = [np.float32((n - 1) / 2.0) for n in (nx, ny, nz)]  # the reference's centred frame
-    got = host(ctx.csg_field(primitives_to_device([prim]), 1, make_frame(origin, d), (nz, ny, nx)))
-    k_scale = 32 if prim["kind"] == 1 else 8
-    assert_field_close(got, FIELDS[f"sm103a/prim{i}"], k_scale=k_scale)
+    return primitives_to_device([prim]), make_frame(origin, q[3:6]), (nz, ny, nx), q
+
+
+@pytest.mark.parametrize("i", range(n_cases(FIELDS, "prim")))
+def test_primitive_vs_reference(ctx, i):
+    """Default arithmetic: the reference build's operation order and fused
+    multiply-adds with correctly rounded squares (the reference's powf(v, 2)
+    differs from them in the last bit for some floats): within 4 ulp of the
+    value plus 3 ulp of the field's scale."""
+    prims, frame, shape, q = _prim_case(i)
+    got = host(ctx.csg_field(prims, 1, frame, shape))
+    assert_field_close(got, FIELDS[f"sm103a/prim{i}"], k_rel=4, k_scale=3)
+    if int(q[6]) in (0, 1) or not q[11:14].any():
+        # no trig: the oracle restates the default arithmetic bit for bit
+        ref32 = O.primitive(int(q[6]), shape[::-1], q[3:6], q[8:11], q[11:14], q[14:20], int(q[7]))
+        assert got.tobytes() == ref32.tobytes()
+
+
+@pytest.mark.parametrize("i", range(n_cases(FIELDS, "prim")))
+def test_primitive_reference_arith_bit_exact(i):
+    """GCM_PRIM_ARITH_REFERENCE: the reference's own kernels' values, bit for bit."""
+    from gpucadforam_gb300.mesher import Context
+
+    prims, frame, shape, _ = _prim_case(i)
+    c = Context(0)
+    try:
+        c.set_primitive_arith(True)
+        got = host(c.csg_field(prims, 1, frame, shape))
+    finally:
+        c.close()
+    assert got.tobytes() == FIELDS[f"sm103a/prim{i}"].tobytes()
 
 
 @pytest.mark.parametrize("i", range(n_cases(FIELDS, "norm")))
@@ -164,8 +191,8 @@ def test_csg_scene_vs_oracle(ctx):
     h = np.float32(1.0 / (n - 1))
     got = host(ctx.csg_field(primitives_to_device(prims), len(prims), make_frame((0, 0, 0), (h, h, h)), (n, n, n)))
     ref32 = O.csg_field(prims, (n, n, n), (0, 0, 0), (h, h, h))
-    # spheres, z-axis cylinders and unrotated boxes use no trig: same IEEE
-    # operations in the same order, so the FP32 oracle matches bit for bit
+    # spheres, z-axis cylinders and unrotated boxes use no trig: the oracle
+    # restates the default arithmetic operation for operation
     assert got.tobytes() == ref32.tobytes()
     ref64 = O.csg_field(prims, (n, n, n), (0, 0, 0), (h, h, h), fp64=True)
     assert np.abs(got - ref64).max() < 1e-5 * max(1.0, float(np.abs(ref64).max()))
