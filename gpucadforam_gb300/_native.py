@@ -119,6 +119,9 @@ PROTOTYPES = {
     "gcm_mc_compact": (I32, [P, P, P, U64, P, P]),
     "gcm_mc_generate": (I32, [P, P, C.POINTER(GcmGrid), F32, P, U64, P, P, P, U64, P]),
     "gcm_normalise_band": (I32, [P, P, U32, U32, U32, F32, F32, P, P, C.POINTER(F32), P]),
+    "gcm_normalise_range": (I32, [P, P, P, U64, F32, F32, C.POINTER(F32), P]),
+    "gcm_lattice_mask": (I32, [P, P, P, P, U32, U32, U32, I32, I32, P]),
+    "gcm_svl_period_field": (I32, [P, P, U32, U32, U32, F32, F32, F32, F32, F32, F32, C.c_char, P]),
     "gcm_mesh_band": (I32, [P, P, P, C.POINTER(GcmGrid), F32, F32, F32, P, P, U64, C.POINTER(GcmCounts), P]),
     "gcm_mesh_band_async": (I32, [P, P, P, C.POINTER(GcmGrid), F32, F32, F32, P, P, U64, P, P]),
     "gcm_field_unit_cell": (I32, [P, U32, U32, U32, U32, P, P]),

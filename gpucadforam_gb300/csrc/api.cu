@@ -754,6 +754,42 @@ gcm_status gcm_normalise_band(gcm_ctx* ctx, const float* d_field, uint32_t nx, u
   return GCM_OK;
 }
 
+gcm_status gcm_normalise_range(gcm_ctx* ctx, const float* d_in, float* d_out, uint64_t n, float range_lo,
+                               float range_span, float* h_minmax, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_in || !d_out || n == 0) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_normalise_range: bad argument");
+  gcm_status s = ensure_scratch(ctx, 128);
+  if (s) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned int* enc = reinterpret_cast<unsigned int*>(static_cast<char*>(ctx->scratch) + 64);
+  GCM_CUDA(ctx, gcm::launch_normalise_range(d_in, d_out, n, enc, range_lo, range_span,
+                                             grid_blocks(ctx, (n + 3) / 4, 256, 4), st));
+  count_launch(ctx, 3);
+  if (h_minmax) {
+    unsigned int k[2];
+    GCM_CUDA(ctx, cudaMemcpyAsync(k, enc, sizeof(k), cudaMemcpyDeviceToHost, st));
+    GCM_CUDA(ctx, cudaStreamSynchronize(st));
+    for (int i = 0; i < 2; ++i) {
+      const unsigned int u = (k[i] & 0x80000000u) ? (k[i] & 0x7fffffffu) : ~k[i];
+      std::memcpy(&h_minmax[i], &u, 4);
+    }
+  }
+  return GCM_OK;
+}
+
+gcm_status gcm_lattice_mask(gcm_ctx* ctx, const gcm_csg_point* d_acc, const float* d_primitive, float* d_lattice,
+                            uint32_t nx, uint32_t ny, uint32_t nz, int fixed, int dynamic, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_lattice || nx == 0 || ny == 0 || nz == 0 || (fixed && !d_acc) || (!fixed && dynamic && !d_primitive))
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_lattice_mask: bad argument");
+  if (!fixed && !dynamic) return GCM_OK;  // the reference's kernel changes nothing then
+  const uint64_t n = (uint64_t)nx * ny * nz;
+  GCM_CUDA(ctx, gcm::launch_lattice_mask(d_acc, d_primitive, d_lattice, n, fixed != 0, grid_blocks(ctx, n, 256, 4),
+                                          static_cast<cudaStream_t>(stream)));
+  count_launch(ctx, 1);
+  return GCM_OK;
+}
+
 gcm_status gcm_test_lookback_stall(gcm_ctx* ctx, uint32_t ntiles, uint32_t stall_tile, uint64_t wait_ns,
                                    uint64_t* d_prefix_out, gcm_stream stream) {
   if (!ctx) return GCM_ERR_INVALID_ARGUMENT;

@@ -1512,6 +1512,50 @@ __global__ void __launch_bounds__(256) band_map_kernel(const float* f, uint32_t 
   }
 }
 
+// device_bufferthree (src/lattice_files/Gratings.cu:1071-1087): v -> a1 + b1 *
+// (v - min) / (max - min), with the min/max keys of minmax_kernel (whose
+// reduction starts from 0, like GPU_buffer_normalise_three's, :1539-1572); the
+// reference build fuses a1 + b1 * k.  Four samples per thread where the
+// buffers allow 16-byte accesses.
+__device__ __forceinline__ float range_map(float v, float a, float b, float a1, float b1) {
+  return __fmaf_rn(b1, __fdiv_rn(fs(v, a), fs(b, a)), a1);
+}
+
+__global__ void __launch_bounds__(256) range_map_kernel(const float* in, float* out, uint64_t n,
+                                                        const unsigned int* enc, float a1, float b1) {
+  const float a = key2f(enc[0]), b = key2f(enc[1]);
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+  if ((((uintptr_t)in | (uintptr_t)out) & 15u) == 0) {
+    const uint64_t n4 = n / 4;
+    for (uint64_t i = tid; i < n4; i += stride) {
+      float4 v = reinterpret_cast<const float4*>(in)[i];
+      v.x = range_map(v.x, a, b, a1, b1);
+      v.y = range_map(v.y, a, b, a1, b1);
+      v.z = range_map(v.z, a, b, a1, b1);
+      v.w = range_map(v.w, a, b, a1, b1);
+      reinterpret_cast<float4*>(out)[i] = v;
+    }
+    for (uint64_t i = 4 * n4 + tid; i < n; i += stride) out[i] = range_map(in[i], a, b, a1, b1);
+  } else {
+    for (uint64_t i = tid; i < n; i += stride) out[i] = range_map(in[i], a, b, a1, b1);
+  }
+}
+
+// primitive_field_kernel (src/lattice_files/Gratings.cu:1695-1725): a lattice
+// sample becomes FLT_MAX where the retained model does not hold it (fixed:
+// the record's sign val > -1, i.e. outside or never touched) or, otherwise,
+// where the live primitive field is >= 0 (dynamic); other samples keep their
+// value.  NaN primitive values keep the sample, as in the reference.
+__global__ void __launch_bounds__(256) lattice_mask_kernel(const gcm_csg_point* __restrict__ acc,
+                                                           const float* __restrict__ prim, float* lat, uint64_t n,
+                                                           uint32_t fixed) {
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = tid; i < n; i += stride) {
+    const bool out = fixed ? __ldg(&acc[i].val) > -1 : __ldg(prim + i) >= 0.0f;
+    if (out) lat[i] = FLT_MAX;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Launch wrappers.
 // ---------------------------------------------------------------------------
@@ -1602,6 +1646,22 @@ static cudaError_t launch_csg_form(const CsgParams& p, uint32_t sm_count, cudaSt
 
 cudaError_t launch_csg(const CsgParams& p, uint32_t sm_count, cudaStream_t st) {
   return p.exact ? launch_csg_form<true>(p, sm_count, st) : launch_csg_form<false>(p, sm_count, st);
+}
+
+cudaError_t launch_normalise_range(const float* in, float* out, uint64_t n, unsigned int* enc, float a1, float b1,
+                                   uint32_t blocks, cudaStream_t st) {
+  minmax_init_kernel<<<1, 1, 0, st>>>(enc);
+  minmax_kernel<<<blocks, 256, 0, st>>>(in, n, enc, enc + 1);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  range_map_kernel<<<blocks, 256, 0, st>>>(in, out, n, enc, a1, b1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lattice_mask(const gcm_csg_point* acc, const float* prim, float* lat, uint64_t n, bool fixed,
+                                uint32_t blocks, cudaStream_t st) {
+  lattice_mask_kernel<<<blocks, 256, 0, st>>>(acc, prim, lat, n, fixed ? 1u : 0u);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_normalise(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, unsigned int* enc, float lo,

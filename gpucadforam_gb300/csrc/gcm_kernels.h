@@ -213,6 +213,14 @@ cudaError_t launch_csg(const CsgParams& p, uint32_t sm_count, cudaStream_t st);
 cudaError_t launch_normalise(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, unsigned int* enc, float lo,
                              float hi, float* label, float* norm_field, uint32_t blocks, cudaStream_t st);
 
+// Min/max normalisation into [a1, a1 + b1] (in may equal out).
+cudaError_t launch_normalise_range(const float* in, float* out, uint64_t n, unsigned int* enc, float a1, float b1,
+                                   uint32_t blocks, cudaStream_t st);
+// Lattice samples outside the retained model (fixed) or the live primitive
+// (otherwise) become FLT_MAX.
+cudaError_t launch_lattice_mask(const gcm_csg_point* acc, const float* prim, float* lat, uint64_t n, bool fixed,
+                                uint32_t blocks, cudaStream_t st);
+
 size_t mesh_smem_bytes(uint32_t nx, uint32_t rows, int mode);
 // Folds one primitive field into a retained accumulator (gcm_csg_point per sample).
 cudaError_t launch_csg_retain(gcm_csg_point* acc, const float* f, uint32_t nx, uint32_t ny, uint32_t nz, float iso,

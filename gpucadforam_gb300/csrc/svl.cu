@@ -620,6 +620,45 @@ using namespace gcm;
 
 extern "C" {
 
+// set_period_kernel (src/lattice_files/Gratings.cu:818-860): the radial
+// period sqrt((u + 1)^2 + (v + 1)^2) of the two sample coordinates across the
+// rotation axis ('z': x and y, 'y': x and z, else z and y), each coordinate
+// (i - mean) * d.  Written in the reference's expression shapes (plain float
+// operators, powf, default contraction: (i - mean) * d + 1 is one fused
+// multiply-add), so that the values are the reference's own.
+__global__ void __launch_bounds__(256) svl_period_kernel(float* __restrict__ out, uint32_t nx, uint32_t ny,
+                                                         uint32_t nz, float dx, float dy, float dz, float mean_x,
+                                                         float mean_y, float mean_z, char axis) {
+  const uint64_t n = (uint64_t)nx * ny * nz, plane = (uint64_t)nx * ny;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const int xx = (int)(i % nx), yy = (int)((i % plane) / nx), zz = (int)(i / plane);
+    const float x = (xx - mean_x) * dx;
+    const float y = (yy - mean_y) * dy;
+    const float z = (zz - mean_z) * dz;
+    float period;
+    if (axis == 'z') period = sqrtf(powf(x + 1, 2) + powf(y + 1, 2));
+    else if (axis == 'y') period = sqrtf(powf(x + 1, 2) + powf(z + 1, 2));
+    else period = sqrtf(powf(z + 1, 2) + powf(y + 1, 2));
+    out[i] = period;
+  }
+}
+
+gcm_status gcm_svl_period_field(gcm_ctx* ctx, float* d_period, uint32_t nx, uint32_t ny, uint32_t nz, float dx,
+                                float dy, float dz, float mean_x, float mean_y, float mean_z, char axis,
+                                gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_period || nx == 0 || ny == 0 || nz == 0)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_svl_period_field: bad argument");
+  if (axis != 'x' && axis != 'y' && axis != 'z')
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_svl_period_field: axis must be 'x', 'y' or 'z'");
+  const uint64_t n = (uint64_t)nx * ny * nz;
+  svl_period_kernel<<<grid_blocks(ctx, n, 256, 4), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      d_period, nx, ny, nz, dx, dy, dz, mean_x, mean_y, mean_z, axis);
+  GCM_CUDA(ctx, cudaGetLastError());
+  count_launch(ctx, 1);
+  return GCM_OK;
+}
+
 gcm_status gcm_svl_coefficients(gcm_ctx* ctx, uint32_t unit_type, uint32_t unit_n, uint32_t range, float* d_coeff,
                                 gcm_stream stream) {
   if (!ctx) return GCM_ERR_INVALID_ARGUMENT;

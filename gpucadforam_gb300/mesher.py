@@ -180,6 +180,31 @@ class Context:
                                                _ptr(nf), mm, _stream(stream)))
         return label, nf, (mm[0], mm[1])
 
+    def normalise_range(self, field, range_lo, range_span, out=None, stream=None):
+        """Min/max map into [range_lo, range_lo + range_span] (in place when out is field)."""
+        if out is None:
+            out = torch.empty_like(field)
+        mm = (C.c_float * 2)()
+        self.check(self.lib.gcm_normalise_range(self.h, _ptr(field), _ptr(out), field.numel(), float(range_lo),
+                                                float(range_span), mm, _stream(stream)))
+        return out, (mm[0], mm[1])
+
+    def svl_period_field(self, shape_zyx, spacing, mean, axis="z", stream=None):
+        nz, ny, nx = shape_zyx
+        out = torch.empty((nz, ny, nx), dtype=torch.float32, device=f"cuda:{self.device}")
+        self.check(self.lib.gcm_svl_period_field(self.h, _ptr(out), nx, ny, nz, *(float(v) for v in spacing),
+                                                 *(float(v) for v in mean), axis.encode(), _stream(stream)))
+        return out
+
+    def lattice_mask(self, lattice, acc=None, primitive=None, fixed=False, dynamic=False, stream=None):
+        """In place: lattice samples outside the retained model (fixed) or the
+        live primitive (dynamic) become FLT_MAX."""
+        nz, ny, nx = lattice.shape
+        self.check(self.lib.gcm_lattice_mask(self.h, _ptr(acc) if acc is not None else None,
+                                             _ptr(primitive) if primitive is not None else None, _ptr(lattice),
+                                             nx, ny, nz, int(bool(fixed)), int(bool(dynamic)), _stream(stream)))
+        return lattice
+
     def lattice_struct(self, lat):  # noqa: D401 - also used unbound by Server
         return N.GcmLattice(lat.mode, lat.ctrl[0], lat.ctrl[1], lat.ctrl[2], _ptr(lat.period), _ptr(lat.euler),
                             _ptr(lat.thickness), _ptr(lat.types), (C.c_float * 3)(*lat.origin))

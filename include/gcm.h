@@ -145,6 +145,14 @@ gcm_status gcm_mc_generate(gcm_ctx* ctx, const float* d_field, const gcm_grid* g
  * samples forced to k = 0, label 0.  h_minmax (optional, syncs) gets min,max. */
 gcm_status gcm_normalise_band(gcm_ctx* ctx, const float* d_field, uint32_t nx, uint32_t ny, uint32_t nz, float band_lo,
                               float band_hi, float* d_label, float* d_norm_field, float* h_minmax, gcm_stream stream);
+/* GPU_buffer_normalise_three (src/lattice_files/Gratings.cu:1539-1572,
+ * device_bufferthree :1071-1087): min/max over the n values (the range always
+ * includes 0, as the reference's reduction starts from {0,0}), then
+ * v -> range_lo + range_span * (v - min) / (max - min).  d_in may equal d_out
+ * (the reference maps its period field in place).  h_minmax (optional, syncs)
+ * gets min, max. */
+gcm_status gcm_normalise_range(gcm_ctx* ctx, const float* d_in, float* d_out, uint64_t n, float range_lo,
+                               float range_span, float* h_minmax, gcm_stream stream);
 /* Band extraction: cube index from the label field (< iso), vertices from the
  * normalised field at the band edges with the reference's 0.0005 endpoint
  * snapping.  Replaces computeIsosurface_lattice / _latticeone with
@@ -287,6 +295,15 @@ gcm_status gcm_csg_retain(gcm_ctx* ctx, gcm_csg_point* d_acc, const float* d_fie
 gcm_status gcm_csg_retain_band(gcm_ctx* ctx, gcm_csg_point* d_acc, const float* d_lattice, uint32_t nx, uint32_t ny,
                                uint32_t nz, float iso, float band_lo, float band_hi, gcm_csg_op op,
                                gcm_stream stream);
+/* Gratings::primitive_field (src/lattice_files/Gratings.cu:1695-1735, called
+ * at src/main.cu:3394, 3978, 4402): restricts a lattice field to the model
+ * before it is normalised and meshed.  fixed: samples the retained model does
+ * not hold (record val > -1: outside or never touched) become FLT_MAX;
+ * otherwise, dynamic: samples where the live primitive field d_primitive is
+ * >= 0 become FLT_MAX; neither: nothing changes.  In place on d_lattice
+ * (nx*ny*nz samples, like d_acc and d_primitive). */
+gcm_status gcm_lattice_mask(gcm_ctx* ctx, const gcm_csg_point* d_acc, const float* d_primitive, float* d_lattice,
+                            uint32_t nx, uint32_t ny, uint32_t nz, int fixed, int dynamic, gcm_stream stream);
 /* Mesh of the accumulator, one fused pass (Isosurface::computeIsosurface,
  * src/Isosurface.cu:44-135, with classifyVoxel and
  * generateTriangles_lattice_kernel, src/MarchingCubes_kernel.cu:869-1052,
@@ -337,6 +354,16 @@ typedef struct gcm_svl_params {
   float end_res;            /* CG stop when r.d falls to end_res^2 (the reference: 0.01) */
 } gcm_svl_params;
 
+/* Gratings::period_data / set_period_kernel (src/lattice_files/Gratings.cu:
+ * 818-860, 1376-1389): the radial period field of the spatially variant
+ * lattice on the solve grid, sqrt((u + 1)^2 + (v + 1)^2) of the coordinates
+ * u, v across the rotation axis ('z': x and y; 'y': x and z; 'x': z and y),
+ * each (i - mean) * d.  The reference's round lattices pass mean = N/2.0 and
+ * then map the field in place with gcm_normalise_range(range_lo = N/10,
+ * range_span = N/4, integer divisions of N = nx; src/main.cu:3929-3931). */
+gcm_status gcm_svl_period_field(gcm_ctx* ctx, float* d_period, uint32_t nx, uint32_t ny, uint32_t nz, float dx,
+                                float dy, float dz, float mean_x, float mean_y, float mean_z, char axis,
+                                gcm_stream stream);
 /* Unit cell of TPMS unit_type (gcm_field_unit_cell) on unit_n^3 samples and its
  * Fourier coefficients c_m = (1/N) sum f e^{-2 pi i (i x/n + j y/n + k z/n)}
  * (what the reference takes from an R2C cuFFT scaled by 1/N,

@@ -72,6 +72,9 @@ def lib():
                                     F32P, C.c_int]
         L.orc_csg_field64.argtypes = [C.POINTER(OrcPrim), C.c_uint32, F32P, F32P, C.c_uint32, C.c_uint32,
                                       C.c_uint32, F64P, C.c_int]
+        L.orc_svl_period_field.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32, F32P, F32P, C.c_char, F32P]
+        L.orc_normalise_range.argtypes = [F32P, F32P, C.c_uint64, C.c_float, C.c_float, F32P]
+        L.orc_lattice_mask.argtypes = [C.c_void_p, C.c_void_p, F32P, C.c_uint64, C.c_int, C.c_int]
         L.orc_normalise_band.argtypes = [F32P, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, F32P, F32P, F32P]
         L.orc_write_obj.argtypes = [F32P, C.c_uint64, C.c_char_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.orc_write_obj.restype = C.c_int
@@ -283,6 +286,30 @@ def csg_field(prims, n, origin, spacing, threads=0, fp64=False):
         out = np.zeros(nx * ny * nz, np.float32)
         lib().orc_csg_field(arr, len(prims), _f3(origin), _f3(spacing), nx, ny, nz, out, threads)
     return out.reshape(nz, ny, nx)
+
+
+def svl_period_field(n, d, mean, axis="z"):
+    nx, ny, nz = n
+    out = np.zeros(nx * ny * nz, np.float32)
+    lib().orc_svl_period_field(nx, ny, nz, _f3(d), _f3(mean), axis.encode(), out)
+    return out.reshape(nz, ny, nx)
+
+
+def normalise_range(field, a1, b1):
+    f = np.ascontiguousarray(field, np.float32).reshape(-1)
+    out = np.empty_like(f)
+    mm = np.zeros(2, np.float32)
+    lib().orc_normalise_range(f, out, f.size, a1, b1, mm)
+    return out.reshape(np.shape(field)), mm
+
+
+def lattice_mask(lattice, acc=None, prim=None, fixed=False, dynamic=False):
+    lat = np.array(lattice, np.float32).reshape(-1)
+    a = None if acc is None else np.ascontiguousarray(acc)
+    q = None if prim is None else np.ascontiguousarray(prim, np.float32)
+    lib().orc_lattice_mask(None if a is None else a.ctypes.data, None if q is None else q.ctypes.data, lat, lat.size,
+                           int(bool(fixed)), int(bool(dynamic)))
+    return lat.reshape(np.shape(lattice))
 
 
 def normalise_band(field, lo, hi):

@@ -1560,6 +1560,53 @@ void orc_csg_field64(const orc_prim* prims, uint32_t n, const float* origin, con
 // (Min_reduction_lattice, :1439-1495), so the range always includes 0; then
 // device_bufferfour (:1089-1134) maps k = (v - min) / (max - min), labels the
 // band lo <= k <= hi with 1, and forces boundary samples to k = 0, label 0.
+// set_period_kernel (src/lattice_files/Gratings.cu:818-860): sqrt((u+1)^2 +
+// (v+1)^2) of the coordinates across the axis, x = (i - mean) * d; the
+// reference build fuses (i - mean) * d + 1.  Squares here are correctly
+// rounded (the reference's powf(v, 2) can differ in the last bit).
+void orc_svl_period_field(uint32_t nx, uint32_t ny, uint32_t nz, const float* d, const float* mean, char axis,
+                          float* out) {
+  for (uint32_t zz = 0; zz < nz; ++zz)
+    for (uint32_t yy = 0; yy < ny; ++yy)
+      for (uint32_t xx = 0; xx < nx; ++xx) {
+        const float x1 = std::fma((float)(int)xx - mean[0], d[0], 1.0f);
+        const float y1 = std::fma((float)(int)yy - mean[1], d[1], 1.0f);
+        const float z1 = std::fma((float)(int)zz - mean[2], d[2], 1.0f);
+        float s;
+        if (axis == 'z') s = x1 * x1 + y1 * y1;
+        else if (axis == 'y') s = x1 * x1 + z1 * z1;
+        else s = z1 * z1 + y1 * y1;
+        out[pidx(xx, yy, zz, nx, ny)] = std::sqrt(s);
+      }
+}
+
+// GPU_buffer_normalise_three (src/lattice_files/Gratings.cu:1539-1572) with
+// device_bufferthree (:1071-1087): min/max starting from {0,0}, then
+// a1 + b1 * (v - min) / (max - min), the reference build fusing a1 + b1 * k.
+void orc_normalise_range(const float* in, float* out, uint64_t n, float a1, float b1, float* minmax) {
+  float lo = 0.0f, hi = 0.0f;
+  for (uint64_t i = 0; i < n; ++i) {
+    lo = std::min(lo, in[i]);
+    hi = std::max(hi, in[i]);
+  }
+  for (uint64_t i = 0; i < n; ++i) out[i] = std::fma(b1, (in[i] - lo) / (hi - lo), a1);
+  if (minmax) {
+    minmax[0] = lo;
+    minmax[1] = hi;
+  }
+}
+
+// primitive_field_kernel (src/lattice_files/Gratings.cu:1695-1725).
+void orc_lattice_mask(const orc_csg_point* acc, const float* prim, float* lat, uint64_t n, int fixed, int dynamic) {
+  for (uint64_t i = 0; i < n; ++i) {
+    if (fixed) {
+      if ((float)acc[i].val > -1.0f) lat[i] = FLT_MAX;
+    } else if (dynamic) {
+      if (prim[i] >= 0.0f) lat[i] = FLT_MAX;
+    }
+  }
+}
+
 void orc_normalise_band(const float* field, int nx, int ny, int nz, float lo, float hi, float* label, float* nf,
                         float* minmax) {
   const uint64_t total = (uint64_t)nx * ny * nz;

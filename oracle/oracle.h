@@ -86,6 +86,15 @@ void orc_csg_field64(const orc_prim* prims, uint32_t n, const float* origin, con
 void orc_normalise_band(const float* field, int nx, int ny, int nz, float band_lo, float band_hi, float* label,
                         float* norm_field, float* minmax);
 
+// SVL period field (set_period_kernel), min/max range map
+// (GPU_buffer_normalise_three) and the lattice mask (primitive_field_kernel).
+void orc_svl_period_field(uint32_t nx, uint32_t ny, uint32_t nz, const float* d, const float* mean, char axis,
+                          float* out);
+void orc_normalise_range(const float* in, float* out, uint64_t n, float a1, float b1, float* minmax);
+struct orc_csg_point;
+void orc_lattice_mask(const struct orc_csg_point* acc, const float* prim, float* lat, uint64_t n, int fixed,
+                      int dynamic);
+
 // ---- .obj -----------------------------------------------------------------------------
 int orc_write_obj(const float* pos, uint64_t nverts, const char* path, uint64_t* nv_out, uint64_t* nf_out);
 

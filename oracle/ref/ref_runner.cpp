@@ -432,6 +432,74 @@ void run_normalise_four(Reader& r, Writer& w, CUmodule gr) {
   cuMemFree(d_in); cuMemFree(d_red); cuMemFree(d_label); cuMemFree(d_norm);
 }
 
+// kind 11: the SVL period field, Gratings::period_data (src/lattice_files/
+// Gratings.cu:1376-1389: set_period_kernel :818-860) then
+// GPU_buffer_normalise_three (:1539-1572: GPUScalar_normalise_kernel_lattice,
+// Min_reduction_lattice, device_bufferthree :1071-1087) in place, as
+// src/main.cu:3929-3931 calls them.  set_period_kernel synchronises inside its
+// bounds test, so jobs cover whole 1024-thread blocks (the runner refuses
+// others).  Writes the raw field, the min/max pair and the mapped field.
+void run_period(Reader& r, Writer& w, CUmodule gr) {
+  int nx = r.get<int32_t>(), ny = r.get<int32_t>(), nz = r.get<int32_t>();
+  float dx = r.get<float>(), dy = r.get<float>(), dz = r.get<float>();
+  float mx = r.get<float>(), my = r.get<float>(), mz = r.get<float>();
+  char axis = (char)r.get<uint32_t>();
+  float a1 = r.get<float>(), b1 = r.get<float>();
+  size_t P = (size_t)nx * ny * nz;
+  if (P % 1024) die("period jobs must fill whole 1024-thread blocks");
+  int n = (int)P;
+  int block_num = (int)blocks_for(P, 1024);
+  CUdeviceptr d_p = dalloc<float>(P), d_red = dalloc<float>(2 * (size_t)block_num);
+  {
+    CUfunction k = find_kernel(gr, "set_period_kernel");
+    void* a[] = {&d_p, &nx, &ny, &nz, &dx, &dy, &dz, &mx, &my, &mz, &axis};
+    launch(k, (unsigned)block_num, 1, 1, 1024, 1, 1, a);
+  }
+  w.arr(ddownload<float>(d_p, P));
+  {
+    CUfunction k = find_kernel(gr, "GPUScalar_normalise_kernel_lattice");
+    void* a[] = {&d_red, &d_p, &n};
+    launch(k, (unsigned)block_num, 1, 1, 1024, 1, 1, a);
+  }
+  {
+    CUfunction k = find_kernel(gr, "Min_reduction_lattice");
+    void* a[] = {&d_red, &block_num};
+    launch(k, 1, 1, 1, 1024, 1, 1, a);
+  }
+  float mm[2];
+  ck(cuMemcpyDtoH(mm, d_red, sizeof(mm)), "cuMemcpyDtoH");
+  {
+    CUfunction k = find_kernel(gr, "device_bufferthree");
+    void* a[] = {&d_p, &d_p, &n, &mm[0], &mm[1], &a1, &b1};
+    launch(k, (unsigned)block_num, 1, 1, 1024, 1, 1, a);
+  }
+  w.put<float>(mm[0]);
+  w.put<float>(mm[1]);
+  w.arr(ddownload<float>(d_p, P));
+  cuMemFree(d_p); cuMemFree(d_red);
+}
+
+// kind 12: Gratings::primitive_field (src/lattice_files/Gratings.cu:1695-1735):
+// primitive_field_kernel sets the lattice to FLT_MAX where the retained model
+// (fixed) or the live primitive field (dynamic) leaves a sample out.  Inputs:
+// the fixed / dynamic flags, the grid_points accumulator (16-byte records), the
+// primitive field and the lattice; writes the lattice after the kernel.
+void run_mask(Reader& r, Writer& w, CUmodule gr) {
+  uint32_t n = r.get<uint32_t>();
+  bool fixed = r.get<uint32_t>() != 0, dynamic = r.get<uint32_t>() != 0;
+  auto acc = r.arr<uint8_t>(16 * (size_t)n);
+  auto prim = r.arr<float>(n);
+  auto lat = r.arr<float>(n);
+  CUdeviceptr d_acc = dupload(acc), d_prim = dupload(prim), d_lat = dupload(lat);
+  float isoval = 0.0f;
+  unsigned int size = n;
+  CUfunction k = find_kernel(gr, "primitive_field_kernel");
+  void* a[] = {&d_acc, &d_prim, &d_lat, &isoval, &size, &fixed, &dynamic};
+  launch(k, (unsigned)blocks_for(n, 1024), 1, 1, 1024, 1, 1, a);
+  w.arr(ddownload<float>(d_lat, n));
+  cuMemFree(d_acc); cuMemFree(d_prim); cuMemFree(d_lat);
+}
+
 }  // namespace
 
 // kind 7: retained primitive editing.  A zeroed grid_points accumulator
@@ -784,6 +852,8 @@ int main(int argc, char** argv) {
       case 10: run_retain(r, w, mc, T, true); break;
       case 8: run_svl(r, w, gr, false); break;
       case 9: run_svl(r, w, gr, true); break;
+      case 11: run_period(r, w, gr); break;
+      case 12: run_mask(r, w, gr); break;
       default: die("unknown job kind");
     }
   }
