@@ -80,8 +80,9 @@ extern "C" gcm_status gcm_mesh_field_noalloc(const float* d_field, const gcm_gri
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
     return GCM_ERR_CUDA;
 
-  // Tile shape: whole voxel rows, about 2048 voxels, grown until the tile
-  // states fit the fixed array, within the shared-memory budget.
+  // Tile shape: whole voxel rows, about GCM_MESH_TILE_VOXELS (1024) voxels,
+  // grown until the tile states fit the fixed array, within the shared-memory
+  // budget (cubes up to 907^3 fit; 908^3 needs more tiles than the array holds).
   const uint32_t vx = grid->nx - 1, vy = grid->ny - 1, vz = grid->nz - 1;
   const size_t budget = std::min(kSmemBudget, (size_t)optin);
   uint32_t rows =

@@ -548,8 +548,10 @@ gcm_status gcm_write_obj(gcm_ctx* ctx, const float* d_pos, uint64_t nverts, cons
  * allocated or freed.  The caller passes the field, 16-byte aligned output
  * buffers and a device gcm_counts; works on the current device and is
  * stream-ordered (no host synchronisation).  Results equal gcm_mesh_field's.
- *  - Grids whose tile states do not fit the array (about 131 thousand tiles;
- *    512^3 and 1024^3 fit) return GCM_ERR_NOT_SUPPORTED before any launch.
+ *  - Grids whose tile states do not fit the array (at most 131,056 tiles of
+ *    whole voxel rows, grown to up to 96 KB of staged rows) return
+ *    GCM_ERR_NOT_SUPPORTED before any launch: cubes up to 907^3 fit, 908^3
+ *    and larger are refused.
  *  - Every call shares the array and clears the part it uses first; calls
  *    that overlap on the GPU (other streams, other host threads) race on it,
  *    so serialise them.
