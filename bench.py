@@ -272,19 +272,28 @@ def run_configs(ctx, steps, warmup, cpu=True):
             if ev:
                 ev[2].record(stream)
 
-        for _ in range(warmup):
-            step()
-        torch.cuda.synchronize()
-        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
-        for k in range(steps):
-            step(evs[k])
-        torch.cuda.synchronize()
-        f_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in evs)
-        m_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in evs)
+        # both extraction paths; the line's mesh_ms is the one the workload's
+        # own call takes by default (gcm_mesh_csg: sparse, lattices: fused)
+        times = {}
+        for path in ("fused", "sparse"):
+            ctx.set_mesh_path(path)
+            for _ in range(warmup):
+                step()
+            torch.cuda.synchronize()
+            evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+            for k in range(steps):
+                step(evs[k])
+            torch.cuda.synchronize()
+            times[path] = (statistics.mean(e[0].elapsed_time(e[1]) for e in evs),
+                           statistics.mean(e[1].elapsed_time(e[2]) for e in evs))
+        ctx.set_mesh_path("auto")
+        chosen = "sparse" if name == "C3" else "fused"
+        f_ms, m_ms = times[chosen]
         vox = (n - 1) ** 3
         alg = 4 * n ** 3 + 32 * cnt.total_verts
         r = {"workload": desc, "grid": [n, n, n], "verts": int(cnt.total_verts), "active_voxels": int(cnt.active_voxels),
-             "field_ms": f_ms, "mesh_ms": m_ms, "voxels_per_s": vox / ((f_ms + m_ms) / 1e3),
+             "field_ms": f_ms, "mesh_ms": m_ms, "mesh_path": chosen, "mesh_ms_fused": times["fused"][1],
+             "mesh_ms_sparse": times["sparse"][1], "voxels_per_s": vox / ((f_ms + m_ms) / 1e3),
              "tris_per_s": cnt.total_verts / 3 / ((f_ms + m_ms) / 1e3), "mesh_GBs": alg / (m_ms / 1e3) / 1e9,
              "mesh_frac_of_measured": alg / (m_ms / 1e3) / 1e9 / peak}
         if cpu:

@@ -111,6 +111,7 @@ PROTOTYPES = {
     "gcm_ctx_set_wait_limit": (I32, [P, U64]),
     "gcm_ctx_launch_count": (U64, [P]),
     "gcm_ctx_set_primitive_arith": (I32, [P, I32]),
+    "gcm_ctx_set_mesh_path": (I32, [P, I32]),
     "gcm_mesh_field": (I32, [P, P, C.POINTER(GcmGrid), F32, P, P, U64, C.POINTER(GcmCounts), P]),
     "gcm_mesh_field_async": (I32, [P, P, C.POINTER(GcmGrid), F32, P, P, U64, P, P]),
     "gcm_count_field": (I32, [P, P, C.POINTER(GcmGrid), F32, C.POINTER(GcmCounts), P]),

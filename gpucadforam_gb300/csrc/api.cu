@@ -167,11 +167,69 @@ gcm_status status_of(gcm_ctx* ctx, const gcm_counts& c) {
 
 // Core of every fused extraction.  counts_out: device pointer receiving the
 // counts (the context's scratch when null).  The caller zeroes nothing.
+// The sparse path of a plain extraction: window counts, their exclusive scan,
+// emission of the windows that hold triangles.  Scratch: [0, 64) counts,
+// [64, 68) scan tile counter, [72, 80) scan total, [128, ...) scan tile
+// states, then the window counts and their offsets.
+gcm_status mesh_sparse(gcm_ctx* ctx, const float* f, const gcm_grid* grid, float iso, float* pos, float* norm,
+                       uint64_t capacity, gcm_counts* counts_out, cudaStream_t st, gcm_counts** counts_used) {
+  const uint32_t vx = grid->nx - 1, vy = grid->ny - 1, vz = grid->nz - 1;
+  const uint64_t nwx = windows_per_row(vx), rows = (uint64_t)vy * vz, nwin = rows * nwx;
+  const uint64_t tile = scan_tile_elems(), scan_tiles = (nwin + tile - 1) / tile;
+  if (scan_tiles >= (1ull << 31)) return fail(ctx, GCM_ERR_NOT_SUPPORTED, "grid too large for the sparse path");
+  const size_t off_tris = (128 + scan_tiles * 8 + 15) & ~(size_t)15;
+  const size_t off_off = (off_tris + nwin * 4 + 15) & ~(size_t)15;
+  gcm_status s = ensure_scratch(ctx, off_off + nwin * 4);
+  if (s) return s;
+  char* b = static_cast<char*>(ctx->scratch);
+  gcm_counts* cnt = counts_out ? counts_out : reinterpret_cast<gcm_counts*>(b);
+  GCM_CUDA(ctx, cudaMemsetAsync(b, 0, 128 + scan_tiles * 8, st));
+  if (counts_out) GCM_CUDA(ctx, cudaMemsetAsync(counts_out, 0, sizeof(gcm_counts), st));
+  uint32_t* win_tris = reinterpret_cast<uint32_t*>(b + off_tris);
+  uint32_t* win_off = reinterpret_cast<uint32_t*>(b + off_off);
+  const uint32_t blocks = grid_blocks(ctx, rows * 32, 256, 8);
+  GCM_CUDA(ctx, launch_window_count(f, grid->nx, grid->ny, grid->nz, iso, win_tris, cnt, blocks, st));
+  ScanParams sp{};
+  sp.in = win_tris;
+  sp.out = win_off;
+  sp.n = nwin;
+  sp.ntiles = scan_tiles;
+  sp.tile_status = reinterpret_cast<uint64_t*>(b + 128);
+  sp.counter = reinterpret_cast<uint32_t*>(b + 64);
+  sp.total = reinterpret_cast<uint64_t*>(b + 72);
+  sp.status = &cnt->status;
+  sp.wait_ns = ctx->wait_ns;
+  GCM_CUDA(ctx, launch_scan(sp, (uint32_t)std::min<uint64_t>(scan_tiles, (uint64_t)ctx->sm_count * 8), st));
+  WindowEmitParams ep{};
+  ep.f = f;
+  ep.nx = grid->nx;
+  ep.ny = grid->ny;
+  ep.nz = grid->nz;
+  for (int a = 0; a < 3; ++a) {
+    ep.vs[a] = grid->voxel_size[a];
+    ep.gc[a] = grid->grid_center[a];
+  }
+  ep.iso = iso;
+  ep.win_tris = win_tris;
+  ep.win_off = win_off;
+  ep.pos = reinterpret_cast<float4*>(pos);
+  ep.norm = reinterpret_cast<float4*>(norm);
+  ep.capacity = capacity;
+  ep.status = &cnt->status;
+  GCM_CUDA(ctx, launch_window_emit(ep, blocks, st));
+  count_launch(ctx, 3);
+  if (counts_used) *counts_used = cnt;
+  return GCM_OK;
+}
+
 gcm_status mesh_core(gcm_ctx* ctx, const float* f, const float* gfield, const gcm_grid* grid, float iso, float lo,
                      float hi, int mode, uint32_t op, bool emit, float* pos, float* norm, uint64_t capacity,
-                     gcm_counts* counts_out, cudaStream_t st, gcm_counts** counts_used) {
+                     gcm_counts* counts_out, cudaStream_t st, gcm_counts** counts_used, bool sparse_scene = false) {
   if (((reinterpret_cast<uintptr_t>(pos) | reinterpret_cast<uintptr_t>(norm)) & 15u) != 0)
     return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "position and normal buffers must be 16-byte aligned");
+  if (mode == kMeshPlain && emit &&
+      (ctx->mesh_path == GCM_MESH_PATH_SPARSE || (ctx->mesh_path == GCM_MESH_PATH_AUTO && sparse_scene)))
+    return mesh_sparse(ctx, f, grid, iso, pos, norm, capacity, counts_out, st, counts_used);
   MeshPlan plan;
   gcm_status s = plan_mesh(ctx, grid, mode, &plan);
   if (s) return s;
@@ -309,6 +367,14 @@ gcm_status gcm_ctx_set_wait_limit(gcm_ctx* ctx, uint64_t ns) {
 
 uint64_t gcm_ctx_launch_count(const gcm_ctx* ctx) { return ctx ? ctx->launches.load() : 0; }
 
+gcm_status gcm_ctx_set_mesh_path(gcm_ctx* ctx, gcm_mesh_path path) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (path != GCM_MESH_PATH_AUTO && path != GCM_MESH_PATH_FUSED && path != GCM_MESH_PATH_SPARSE)
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_ctx_set_mesh_path: unknown path %d", (int)path);
+  ctx->mesh_path = path;
+  return GCM_OK;
+}
+
 gcm_status gcm_ctx_set_primitive_arith(gcm_ctx* ctx, gcm_prim_arith arith) {
   if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
   if (arith != GCM_PRIM_ARITH_DEFAULT && arith != GCM_PRIM_ARITH_REFERENCE)
@@ -351,10 +417,17 @@ gcm_status gcm_count_field(gcm_ctx* ctx, const float* d_field, const gcm_grid* g
   gcm_status s = check_grid(ctx, grid);
   if (s) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  gcm_counts* used = nullptr;
-  s = mesh_core(ctx, d_field, nullptr, grid, iso, 0, 0, kMeshPlain, 0, false, nullptr, nullptr, 0, nullptr, st, &used);
+  // the window count kernel: the same counts as the fused kernel's count
+  // pass, from one streaming read of the field
+  s = ensure_scratch(ctx, 128);
   if (s) return s;
-  return read_counts(ctx, used, h_counts, st);
+  gcm_counts* cnt = static_cast<gcm_counts*>(ctx->scratch);
+  GCM_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(gcm_counts), st));
+  const uint64_t rows = (uint64_t)(grid->ny - 1) * (grid->nz - 1);
+  GCM_CUDA(ctx, launch_window_count(d_field, grid->nx, grid->ny, grid->nz, iso, nullptr, cnt,
+                                    grid_blocks(ctx, rows * 32, 256, 8), st));
+  count_launch(ctx, 1);
+  return read_counts(ctx, cnt, h_counts, st);
 }
 
 gcm_status gcm_mesh_band(gcm_ctx* ctx, const float* d_label, const float* d_norm_field, const gcm_grid* grid, float iso,
@@ -724,7 +797,8 @@ gcm_status gcm_mesh_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_p
   if (s) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   gcm_counts* used = nullptr;
-  s = mesh_core(ctx, ctx->field_buf, nullptr, grid, iso, 0, 0, kMeshPlain, 0, true, d_pos, d_norm, capacity, nullptr, st, &used);
+  s = mesh_core(ctx, ctx->field_buf, nullptr, grid, iso, 0, 0, kMeshPlain, 0, true, d_pos, d_norm, capacity, nullptr, st, &used,
+                true);
   if (s) return s;
   return read_counts(ctx, used, h_counts, st);
 }

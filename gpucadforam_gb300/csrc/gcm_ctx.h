@@ -23,6 +23,7 @@ struct gcm_ctx {
   uint32_t tile_voxels = GCM_MESH_TILE_VOXELS;
   bool shape_set = false;  // the caller chose the launch shape (else per-form defaults)
   bool prim_exact = false; // primitive fields in the reference's powf arithmetic
+  int mesh_path = GCM_MESH_PATH_AUTO;
   std::atomic<uint64_t> launches{0};
   std::string last_error;
   // scratch (device): counts + counters + tile states

@@ -127,6 +127,23 @@ struct GenerateParams {
   uint32_t* status;
 };
 
+// Sparse path: windows of 31 voxels of a row, windows_per_row(nx - 1) per row.
+__host__ __device__ constexpr uint32_t windows_per_row(uint32_t vx) { return (vx + 30u) / 31u; }
+
+// Sparse path emission: window triangle counts and their exclusive scan.
+struct WindowEmitParams {
+  const float* f;
+  uint32_t nx, ny, nz;
+  float vs[3], gc[3];
+  float iso;
+  const uint32_t* win_tris;
+  const uint32_t* win_off;
+  float4* pos;
+  float4* norm;
+  uint64_t capacity;
+  uint32_t* status;
+};
+
 struct ScanParams {
   const uint32_t* in;
   uint32_t* out;
@@ -191,6 +208,10 @@ cudaError_t launch_compact(const uint32_t* occ, const uint32_t* scan, uint64_t n
                            cudaStream_t st);
 cudaError_t launch_generate(bool band, const GenerateParams& p, uint32_t blocks, cudaStream_t st);
 cudaError_t launch_scan(const ScanParams& p, uint32_t blocks, cudaStream_t st);
+// Sparse path: window counts (win_tris may be null: counts only), then emission.
+cudaError_t launch_window_count(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, float iso, uint32_t* win_tris,
+                                gcm_counts* counts, uint32_t blocks, cudaStream_t st);
+cudaError_t launch_window_emit(const WindowEmitParams& p, uint32_t blocks, cudaStream_t st);
 cudaError_t launch_lookback_stall(uint32_t ntiles, uint32_t stall, uint64_t wait_ns, uint64_t* tile_status,
                                   uint32_t* counter, uint64_t* prefix_out, uint32_t* status, uint32_t blocks,
                                   cudaStream_t st);

@@ -835,6 +835,276 @@ __global__ void __launch_bounds__(kScanThreads) scan_u32_kernel(ScanParams p) {
 uint32_t scan_tile_elems() { return kScanThreads * kScanItems; }
 
 // ----------------------------------------------------------------------------
+// Sparse path: windows of 32 consecutive voxels of a row, in voxel order
+// (window (row, wx) holds voxels wx*32 .. wx*32+31 of voxel row row = y + vy*z).
+// mc_window_count_kernel: a warp per row at a time, a lane per voxel, corners
+// read straight from the field (neighbouring lanes and rows share them through
+// L1 and L2); writes each window's triangle count and adds the active voxels
+// and vertices to the counts.  mc_window_emit_kernel: after an exclusive scan
+// of the window counts, a warp visits only the windows that hold triangles,
+// classifies them again and writes each lane's triangles at the window's offset
+// plus the lane's prefix: the reference's vertex order, with the same vertex
+// arithmetic as every other path.  No look-back and no tile staging, so a
+// surface that touches a few percent of the voxels costs little more than one
+// read of the field.
+// ----------------------------------------------------------------------------
+constexpr uint32_t kWinBatch = 4;  // windows a warp handles at once (independent loads in flight)
+// A window is 31 voxels of a row: its 32 lanes load 32 consecutive sample
+// columns, and lane l's voxel takes column l + 1 from the next lane (lane 31
+// only supplies that column).
+constexpr uint32_t kWinVox = 31;
+
+static_assert(windows_per_row(62) == 2 && windows_per_row(63) == 3, "windows of kWinVox voxels");
+
+// c[k] for a run-time k without local memory: three levels of selects.
+__device__ __forceinline__ float sel8(const float c[8], int k) {
+  const float a0 = (k & 1) ? c[1] : c[0], a1 = (k & 1) ? c[3] : c[2], a2 = (k & 1) ? c[5] : c[4],
+              a3 = (k & 1) ? c[7] : c[6];
+  const float b0 = (k & 2) ? a1 : a0, b1 = (k & 2) ? a3 : a2;
+  return (k & 4) ? b1 : b0;
+}
+
+// The four samples of column x of the voxel row at rb: (y, z), (y+1, z),
+// (y, z+1), (y+1, z+1).
+__device__ __forceinline__ float4 load_column(const float* __restrict__ f, uint64_t rb, uint32_t x, uint64_t sy,
+                                              uint64_t sz) {
+  const float* q = f + rb + x;
+  return make_float4(__ldg(q), __ldg(q + sy), __ldg(q + sz), __ldg(q + sy + sz));
+}
+
+// Inside bits of a column (bit i: component i < iso, the classify test).
+__device__ __forceinline__ uint32_t column_bits(float4 s, float iso) {
+  return (uint32_t)(s.x < iso) | ((uint32_t)(s.y < iso) << 1) | ((uint32_t)(s.z < iso) << 2) |
+         ((uint32_t)(s.w < iso) << 3);
+}
+
+// Cube index from the inside bits of columns x (m) and x + 1 (n): corners
+// 0 (x,y,z) 1 (x+1,y,z) 2 (x+1,y+1,z) 3 (x,y+1,z) 4 (x,y,z+1) 5 (x+1,y,z+1)
+// 6 (x+1,y+1,z+1) 7 (x,y+1,z+1): the order of cube_index8.  m's bits go to
+// corners 0, 3, 4, 7 and n's to 1, 2, 5, 6.
+__device__ __forceinline__ uint32_t cube_from_columns(uint32_t m, uint32_t n) {
+  return (m & 1u) | ((m & 6u) << 2) | ((m & 8u) << 4) | ((n & 3u) << 1) | ((n & 12u) << 3);
+}
+
+// One window batch of a row, classified: each lane's column samples and its
+// voxel's cube index (0 for lane 31 and past the row's end).
+struct WindowBatch {
+  float4 col[kWinBatch];
+  uint32_t ci[kWinBatch];
+};
+
+__device__ __forceinline__ void classify_batch(const float* __restrict__ f, uint64_t rb, const uint32_t* wx, uint32_t nb,
+                                               uint32_t vx, uint64_t sy, uint64_t sz, float iso, uint32_t lane,
+                                               WindowBatch& B) {
+#pragma unroll
+  for (uint32_t k = 0; k < kWinBatch; ++k) {
+    B.col[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const uint32_t x = wx[k] * kWinVox + lane;
+    if (k < nb && x <= vx) B.col[k] = load_column(f, rb, x, sy, sz);
+  }
+#pragma unroll
+  for (uint32_t k = 0; k < kWinBatch; ++k) {
+    const uint32_t x = wx[k] * kWinVox + lane;
+    const uint32_t m = column_bits(B.col[k], iso);
+    const uint32_t n = __shfl_down_sync(0xffffffffu, m, 1);
+    B.ci[k] = (k < nb && lane < kWinVox && x < vx) ? cube_from_columns(m, n) : 0u;
+  }
+}
+
+// Count pass: a warp task is one window column over up to kCountRows voxel
+// rows of one z-plane.  It loads each sample line of planes z and z + 1 once,
+// keeps its inside bits, and forms every row's column bits from two adjacent
+// lines.  Tasks run window column fastest, so the warps of a wave read one
+// contiguous slab of the field.
+constexpr uint32_t kCountRows = 8;
+
+template <bool WRITE>
+__global__ void __launch_bounds__(256) mc_window_count_kernel(const float* __restrict__ f, uint32_t nx, uint32_t ny,
+                                                              uint32_t nz, float iso, uint32_t* __restrict__ win_tris,
+                                                              gcm_counts* counts) {
+  __shared__ uint64_t s_tri[256];
+  load_tri_table_counted(s_tri);
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t vx = nx - 1, vy = ny - 1, vz = nz - 1, nwx = windows_per_row(vx);
+  const uint32_t nyb = (vy + kCountRows - 1) / kCountRows;
+  const uint64_t tasks = (uint64_t)vz * nyb * nwx, sy = nx, sz = (uint64_t)nx * ny;
+  const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  uint32_t active = 0;
+  uint64_t tris = 0;
+  for (uint64_t t = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; t < tasks; t += warps) {
+    const uint32_t wx = (uint32_t)(t % nwx);
+    const uint64_t rest = t / nwx;
+    const uint32_t yb = (uint32_t)(rest % nyb), z = (uint32_t)(rest / nyb);
+    const uint32_t y0 = yb * kCountRows, nr = min(kCountRows, vy - y0);
+    const uint32_t x = wx * kWinVox + lane;
+    const bool has = x <= vx, voxel = lane < kWinVox && x < vx;
+    const float* p0 = f + (uint64_t)y0 * sy + (uint64_t)z * sz + x;
+    uint32_t line[kCountRows + 1];  // bit 0: plane z, bit 2: plane z + 1
+#pragma unroll
+    for (uint32_t i = 0; i <= kCountRows; ++i) {
+      float a = 0.0f, b = 0.0f;
+      if (i <= nr && has) {
+        a = __ldg(p0 + i * sy);
+        b = __ldg(p0 + i * sy + sz);
+      }
+      line[i] = (uint32_t)(a < iso) | ((uint32_t)(b < iso) << 2);
+    }
+    uint32_t nt[kCountRows], task_tris = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < kCountRows; ++i) {
+      const uint32_t m = line[i] | (line[i + 1] << 1);
+      const uint32_t n = __shfl_down_sync(0xffffffffu, m, 1);
+      nt[i] = (voxel && i < nr) ? (uint32_t)(s_tri[cube_from_columns(m, n)] & 0xFu) : 0u;
+      active += nt[i] > 0;
+      task_tris += nt[i];
+    }
+    tris += task_tris;
+    if (WRITE) {
+      // the rows' window sums, then lane i stores row i's
+      uint32_t mine = 0;
+#pragma unroll
+      for (uint32_t i = 0; i < kCountRows; ++i) {
+        const uint32_t wsum = __reduce_add_sync(0xffffffffu, nt[i]);
+        if (lane == i) mine = wsum;
+      }
+      if (lane < nr) win_tris[((uint64_t)z * vy + y0 + lane) * nwx + wx] = mine;
+    }
+  }
+  const uint64_t wa = warp_sum_u64(active), wt = warp_sum_u64(tris);
+  if (lane == 0 && (wa | wt)) {
+    atomicAdd(reinterpret_cast<unsigned long long*>(&counts->active_voxels), (unsigned long long)wa);
+    atomicAdd(reinterpret_cast<unsigned long long*>(&counts->total_verts), 3ull * wt);
+  }
+}
+
+// Per warp of the emit kernel: the batch's voxels (corner values, cube
+// index, first output triangle) and its triangle list (window, lane and
+// triangle number per entry), so that every lane emits one triangle per step.
+constexpr uint32_t kEmitWarps = 4;
+constexpr uint32_t kEmitList = kWinBatch * 32u * 5u;
+struct EmitShared {
+  float4 corner[kWinBatch * 32u][2];
+  uint64_t first[kWinBatch * 32u];
+  uint8_t cube[kWinBatch * 32u];
+  uint16_t list[kEmitList];
+};
+
+__global__ void __launch_bounds__(kEmitWarps * 32, 8) mc_window_emit_kernel(WindowEmitParams p) {
+  __shared__ uint64_t s_tri[256];
+  __shared__ EmitShared s_em[kEmitWarps];
+  load_tri_table_counted(s_tri);
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u;
+  EmitShared& E = s_em[threadIdx.x >> 5];
+  const uint32_t nx = p.nx, ny = p.ny, vx = nx - 1, vy = ny - 1, nwx = windows_per_row(vx);
+  const uint64_t rows = (uint64_t)vy * (p.nz - 1), sy = nx, sz = (uint64_t)nx * ny;
+  const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+  const Frame fr{{p.vs[0], p.vs[1], p.vs[2]}, {p.gc[0], p.gc[1], p.gc[2]}};
+  bool dropped = false;
+  for (uint64_t row = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; row < rows; row += warps) {
+    const uint32_t y = (uint32_t)(row % vy), z = (uint32_t)(row / vy);
+    const uint64_t rb = (uint64_t)y * sy + (uint64_t)z * sz;
+    VoxelCorners V;
+    axis_corners(y, fr.gc[1], fr.vs[1], V.y0, V.y1);
+    axis_corners(z, fr.gc[2], fr.vs[2], V.z0, V.z1);
+    for (uint32_t g0 = 0; g0 < nwx; g0 += 32u) {
+      const uint32_t wl = g0 + lane;
+      uint32_t todo = __ballot_sync(0xffffffffu, wl < nwx && __ldg(p.win_tris + row * nwx + wl) != 0u);
+      while (todo) {
+        // the next (up to) kWinBatch windows that hold triangles, all at once
+        uint32_t wx[kWinBatch];
+        uint32_t nb = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kWinBatch; ++k) {
+          wx[k] = 0;
+          if (todo) {
+            wx[k] = g0 + (uint32_t)(__ffs(todo) - 1);
+            todo &= todo - 1;
+            nb = k + 1;
+          }
+        }
+        uint64_t off[kWinBatch];
+#pragma unroll
+        for (uint32_t k = 0; k < kWinBatch; ++k) off[k] = k < nb ? __ldg(p.win_off + row * nwx + wx[k]) : 0ull;
+        WindowBatch B;
+        classify_batch(p.f, rb, wx, nb, vx, sy, sz, p.iso, lane, B);
+        // list the batch's triangles; stage each active voxel's corners
+        __syncwarp();  // the previous batch's entries are read
+        uint32_t listed = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kWinBatch; ++k) {
+          const uint32_t nt = (uint32_t)(s_tri[B.ci[k]] & 0xFu);
+          const CountPlanes cp = count_planes(nt);
+          const uint32_t excl = planes_excl(cp), slot = k * 32u + lane;
+          // the x + 1 column: the next lane's
+          float4 n4;
+          n4.x = __shfl_down_sync(0xffffffffu, B.col[k].x, 1);
+          n4.y = __shfl_down_sync(0xffffffffu, B.col[k].y, 1);
+          n4.z = __shfl_down_sync(0xffffffffu, B.col[k].z, 1);
+          n4.w = __shfl_down_sync(0xffffffffu, B.col[k].w, 1);
+          if (nt) {
+            // kCorner order: 0 (x,y,z) 1 (x+1,y,z) 2 (x+1,y+1,z) 3 (x,y+1,z) | 4..7 at z+1
+            E.corner[slot][0] = make_float4(B.col[k].x, n4.x, n4.y, B.col[k].y);
+            E.corner[slot][1] = make_float4(B.col[k].z, n4.z, n4.w, B.col[k].w);
+            E.first[slot] = off[k] + excl;
+            E.cube[slot] = (uint8_t)B.ci[k];
+            for (uint32_t j = 0; j < nt; ++j) E.list[listed + excl + j] = (uint16_t)((slot << 3) | j);
+          }
+          listed += planes_total(cp);
+        }
+        __syncwarp();
+        for (uint32_t u = lane; u < listed; u += 32u) {
+          const uint32_t ent = E.list[u], slot = ent >> 3, j = ent & 7u;
+          const uint32_t k = slot >> 5, l = slot & 31u;
+          const float4 ca = E.corner[slot][0], cb = E.corner[slot][1];
+          const float c[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
+          const uint64_t tri_row = s_tri[E.cube[slot]];
+          uint32_t wxk = wx[0];
+#pragma unroll
+          for (uint32_t q = 1; q < kWinBatch; ++q) wxk = (k == q) ? wx[q] : wxk;
+          const uint32_t x = wxk * kWinVox + l;
+          axis_corners(x, fr.gc[0], fr.vs[0], V.x0, V.x1);
+          float3 v[3];
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            const int e = (int)tri_edge_dev(tri_row, 3u * j + m);
+            const int ka = edge_a(e), kb = edge_b(e);
+            const uint32_t ba = (uint32_t)(corner_x(ka) | (corner_y(ka) << 1) | (corner_z(ka) << 2));
+            const uint32_t bb = (uint32_t)(corner_x(kb) | (corner_y(kb) << 1) | (corner_z(kb) << 2));
+            v[m] = edge_point_plain_v(sel8(c, ka), sel8(c, kb), corner_sel(V, ba), corner_sel(V, bb), p.iso);
+          }
+          const float3 n = normal_of(v[0], v[1], v[2]);
+          const uint64_t idx = 3ull * (E.first[slot] + j);
+          if (idx + 3 > p.capacity) {
+            dropped = true;
+            continue;
+          }
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            __stcs(p.pos + idx + m, make_float4(v[m].x, v[m].y, v[m].z, 1.0f));
+            __stcs(p.norm + idx + m, make_float4(n.x, n.y, n.z, 0.0f));
+          }
+        }
+      }
+    }
+  }
+  if (dropped) set_status(p.status, kStatusOverflow);
+}
+
+cudaError_t launch_window_count(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, float iso, uint32_t* win_tris,
+                                gcm_counts* counts, uint32_t blocks, cudaStream_t st) {
+  if (win_tris) mc_window_count_kernel<true><<<blocks, 256, 0, st>>>(f, nx, ny, nz, iso, win_tris, counts);
+  else mc_window_count_kernel<false><<<blocks, 256, 0, st>>>(f, nx, ny, nz, iso, nullptr, counts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_window_emit(const WindowEmitParams& p, uint32_t blocks, cudaStream_t st) {
+  mc_window_emit_kernel<<<blocks, kEmitWarps * 32, 0, st>>>(p);
+  return cudaGetLastError();
+}
+
+// ----------------------------------------------------------------------------
 // Test kernel for the bounded look-back: one warp per CTA, tiles of aggregate 1,
 // tile `stall` never publishes.
 // ----------------------------------------------------------------------------

@@ -76,6 +76,10 @@ class Context:
     def reserve(self, max_points: int):
         self.check(self.lib.gcm_ctx_reserve(self.h, int(max_points)))
 
+    def set_mesh_path(self, path: str):
+        """'auto' (sparse for CSG scenes), 'fused' or 'sparse' plain extraction."""
+        self.check(self.lib.gcm_ctx_set_mesh_path(self.h, {"auto": 0, "fused": 1, "sparse": 2}[path]))
+
     def set_primitive_arith(self, reference_exact: bool):
         """CSG primitive fields bit for bit as the reference's kernels (powf
         squares) instead of the default correctly rounded squares."""

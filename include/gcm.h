@@ -95,6 +95,18 @@ gcm_status gcm_ctx_reserve(gcm_ctx* ctx, uint64_t max_points);
  * look-back).  Default 2e9.  A wait that runs out sets
  * GCM_ERR_DEVICE_TIMEOUT and the kernel returns. */
 gcm_status gcm_ctx_set_wait_limit(gcm_ctx* ctx, uint64_t ns);
+/* Extraction path of plain meshes (gcm_mesh_field, gcm_mesh_field_async,
+ * gcm_mesh_lattice*, gcm_mesh_csg).  FUSED: one pass over tiles of whole
+ * voxel rows with a decoupled look-back (best for dense surfaces, such as
+ * graded lattices).  SPARSE: count the triangles of every 32-voxel window,
+ * scan, and emit only the windows that hold triangles (best when the surface
+ * touches a few percent of the voxels, such as primitive scenes).  AUTO
+ * (default): SPARSE for gcm_mesh_csg, FUSED otherwise.  Every path writes the
+ * same vertices in the same order.  No reference counterpart: the reference
+ * runs classify, two thrust scans, compaction and generate
+ * (src/Isosurface.cu:401-486). */
+typedef enum gcm_mesh_path { GCM_MESH_PATH_AUTO = 0, GCM_MESH_PATH_FUSED = 1, GCM_MESH_PATH_SPARSE = 2 } gcm_mesh_path;
+gcm_status gcm_ctx_set_mesh_path(gcm_ctx* ctx, gcm_mesh_path path);
 /* Number of kernel launches this context has issued (for accounting). */
 uint64_t gcm_ctx_launch_count(const gcm_ctx* ctx);
 int gcm_abi_version(void);

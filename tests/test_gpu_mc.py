@@ -17,13 +17,17 @@ pytestmark = pytest.mark.gpu
 MC = golden("golden_mc.npz")
 
 
-@pytest.fixture(scope="module", params=[(256, 2048), (128, 1024)], ids=["256x2048", "128x1024"])
+@pytest.fixture(scope="module", params=[(256, 2048), (128, 1024), "sparse"], ids=["256x2048", "128x1024", "sparse"])
 def ctx(request):
-    """Every case runs through two launch shapes of the fused kernel."""
+    """Every case runs through two launch shapes of the fused kernel and
+    through the sparse (window) path."""
     from gpucadforam_gb300.mesher import Context
 
     c = Context(0)
-    c.set_launch_shape(*request.param)
+    if request.param == "sparse":
+        c.set_mesh_path("sparse")
+    else:
+        c.set_launch_shape(*request.param)
     yield c
     c.close()
 
