@@ -1,7 +1,8 @@
 """Recipe that compiles the reference's own hot-path CUDA files for the parity harness.
 
-Test infrastructure only.  It reads the reference sources where they lie
-(``/root/reference/src``), never copies them, and writes only into
+Test infrastructure only.  It reads the reference sources where they lie (the
+``src`` directory of a reference checkout: ``GCM_REFERENCE_SRC``, by default
+``/root/reference/src``), never copies them, and writes only into
 ``oracle/_ref/`` (git-ignored; it travels to the GPU machine with the rest of the
 working tree).  Outputs:
 
@@ -39,7 +40,7 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 REPO = os.path.dirname(ORACLE)
-REF_SRC = "/root/reference/src"
+REF_SRC = os.environ.get("GCM_REFERENCE_SRC", "/root/reference/src")
 OUT = os.path.join(ORACLE, "_ref")
 
 # (name, reference source file relative to src/)
