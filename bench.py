@@ -537,6 +537,62 @@ def run_reference(args):
 # ----------------------------------------------------------------------------- GPU
 
 
+def run_reference_cuda(field, local, reps=5):
+    """The reference's own plain marching-cubes kernels (classifyVoxel_new,
+    compactVoxels, generateTriangles_lattice_kernel_3 of
+    src/MarchingCubes_kernel.cu:3207-3249, 1594-1608, 3041-3170, compiled for
+    sm_103a from its sources into oracle/_ref/) timed on this GPU on the bench
+    field, in a subprocess (oracle/ref/time_ref.py) with its own clock samples.
+
+    A reported baseline beside ``kernels_ms``, never the bench value.  The
+    field is shifted by +3 with the isovalue at 3, because the reference's
+    generate kernel indexes cubes by (f < iso) && (f > 0); its two thrust scans
+    run between the kernels on the host in the timing harness and are not
+    counted, which favours the reference."""
+    import shutil
+    import tempfile
+
+    import torch
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    ref_dir = os.path.join(here, "oracle", "_ref")
+    need = [os.path.join(ref_dir, "ref_mc_sm103a.fatbin"), os.path.join(here, "tests", "golden", "ref_tables.bin")]
+    missing = [os.path.relpath(p, here) for p in need if not os.path.exists(p)]
+    if missing:
+        return {"unavailable": "reference device code not built here: missing " + ", ".join(missing)}
+    n = field.shape[0]
+    work = tempfile.mkdtemp(prefix="gcm_ref_cuda_")
+    try:
+        path = os.path.join(work, "field.bin")
+        (field + 3.0).cpu().numpy().tofile(path)
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local)
+        clocks.start()
+        time.sleep(0.3)
+        r = subprocess.run([sys.executable, os.path.join(here, "oracle", "ref", "time_ref.py"), "--grid", str(n),
+                            "--reps", str(reps), "--field", path, "--work", work],
+                           capture_output=True, text=True, timeout=600,
+                           env=dict(os.environ, CUDA_VISIBLE_DEVICES=os.environ.get("CUDA_VISIBLE_DEVICES", str(local))))
+        clk = clocks.stop()
+    except (OSError, subprocess.SubprocessError) as e:
+        return {"unavailable": f"reference timing did not run: {type(e).__name__}: {e}"}
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+    if r.returncode != 0:
+        tail = (r.stderr or r.stdout).strip().splitlines()[-1:] or ["no output"]
+        return {"unavailable": f"reference timing exited {r.returncode}: {tail[0][:200]}"}
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    ms = d["reference_ms"]
+    return {"classify_ms": ms["classifyVoxel_new"], "compact_ms": ms["compactVoxels"],
+            "generate_ms": ms["generateTriangles_lattice_kernel_3"], "total_ms": ms["sum_without_scans"],
+            "scans": "thrust exclusive scans not counted (run on the host between the timed kernels)",
+            "reps": d["reps"], "statistic": "median over reps", "verts": d["verts_reference"],
+            "gcm_mesh_ms_same_field": d["gcm_fused_ms"], "verts_gcm": d["verts_gcm"],
+            "speedup_mesh": d["speedup"], "algorithmic_bytes": d["algorithmic_bytes"],
+            "reference_GBs": d["reference_GBs"], "field": f"bench field + 3, iso 3, {n}^3",
+            "clocks": clk}
+
+
 def run_batched(ctx, steps, warmup, n_inst=256, seed=SEED + 2):
     """Config C4: n_inst graded lattices (sides U{32..256}, one type and one
     period U[8,48] per instance, thickness and rotation graded on an 8^3 control
@@ -856,6 +912,11 @@ def run_gcm(args):
     if not args.no_rows:
         rows = run_rows(ctx, args.steps, args.warmup, cpu=(rank == 0 and not args.no_cpu))
 
+    reference_cuda = None
+    if rank == 0 and not args.no_reference_cuda:
+        ctx.check(ctx.lib.gcm_field_lattice(ctx.h, C.byref(s), n, n, n, C.c_void_p(field.data_ptr()), cs))
+        reference_cuda = run_reference_cuda(field, local)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         r = cpu_sample(os.cpu_count() or 1, planes=args.cpu_planes)
@@ -871,6 +932,7 @@ def run_gcm(args):
                 "active_voxels": cnt.active_voxels,
                 "kernels_ms": {"lattice_rows_kernel": statistics.mean(field_ms),
                                "mc_mesh_kernel": statistics.mean(mc_ms)},
+                "reference_cuda": reference_cuda,
                 "roofline": {"bound": "hbm", "kernel": "mc_mesh_kernel", "achieved": achieved, "peak": peak,
                              "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                              "algorithmic_bytes": mc_bytes, "traffic": traffic},
@@ -898,6 +960,8 @@ def main():
     ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--no-rows", action="store_true", help="skip the retained-CSG, band and .obj lines")
     ap.add_argument("--batch-instances", type=int, default=256)
+    ap.add_argument("--no-reference-cuda", action="store_true",
+                    help="skip timing the reference's own marching-cubes kernels on this GPU")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -10,7 +10,11 @@ isovalue moved to 3: the reference's plain generate kernel takes its cube index
 as (f < iso) && (f > 0) (src/MarchingCubes_kernel.cu:3041-3170), so it needs a
 positive field to agree with its classify kernel.
 
-    python oracle/ref/time_ref.py [--grid 512] [--reps 5]
+    python oracle/ref/time_ref.py [--grid 512] [--reps 5] [--field FILE]
+
+``--field`` takes the field (grid^3 float32, x fastest, already shifted by +3)
+from a file instead of evaluating it with the oracle; the bench writes its own
+device field there, which is bit-identical to the oracle's.
 
 Prints one JSON line: per-kernel median times of the reference (classify,
 compaction, generate; its two thrust scans cannot be launched by name and are
@@ -59,13 +63,20 @@ def main():
     ap.add_argument("--grid", type=int, default=512)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--work", default=None, help="scratch directory for the 4 P-byte job file (default: a temp dir)")
+    ap.add_argument("--field", default=None, help="raw float32 field file (grid^3 samples, shifted by +3)")
     args = ap.parse_args()
-    import oracle as O
 
     n = args.grid
-    period, euler, thick, types = controls()
-    f = O.lattice_field((n, n, n), 0, (16, 16, 16), period, euler, thick, types, origin=((n - 1) / 2,) * 3)
-    f = (f + np.float32(3.0)).astype(np.float32)
+    if args.field:
+        f = np.fromfile(args.field, np.float32)
+        assert f.size == n ** 3, (f.size, n)
+        f = f.reshape(n, n, n)
+    else:
+        import oracle as O
+
+        period, euler, thick, types = controls()
+        f = O.lattice_field((n, n, n), 0, (16, 16, 16), period, euler, thick, types, origin=((n - 1) / 2,) * 3)
+        f = (f + np.float32(3.0)).astype(np.float32)
     iso = 3.0
     work = args.work or tempfile.mkdtemp(prefix="gcm_time_ref_")
     os.makedirs(work, exist_ok=True)
@@ -113,6 +124,7 @@ def main():
     print(json.dumps({
         "grid": n, "voxels": int(nvox), "active_voxels": int(active), "verts_reference": int(total),
         "verts_gcm": int(cnt.total_verts),
+        "reps": int(reps), "reference_ms_per_rep": t.tolist(),
         "reference_ms": {"classifyVoxel_new": float(med[0]), "compactVoxels": float(med[1]),
                          "generateTriangles_lattice_kernel_3": float(med[2]), "sum_without_scans": ref_ms},
         "gcm_fused_ms": ours,
