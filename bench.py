@@ -745,12 +745,44 @@ def serve_stream(arrivals, reqs, lanes, pool_bytes=64 << 30, host_bytes=16 << 30
             "device_pool_peak_gb": st["device_pool_peak"] / 1e9}
 
 
+def d2h_copy_rate(streams, total=2 << 30, reps=3):
+    """Device -> pinned host copy rate (GB/s) of `total` bytes split over
+    `streams` streams: the ceiling of a served stream whose meshes all go to
+    host memory."""
+    import torch
+
+    src = torch.empty(total, dtype=torch.uint8, device="cuda")
+    dst = torch.empty(total, dtype=torch.uint8).pin_memory()
+    cuts = [total * i // streams for i in range(streams + 1)]
+    ss = [torch.cuda.Stream() for _ in range(streams)]
+
+    def go():
+        for i, st in enumerate(ss):
+            with torch.cuda.stream(st):
+                dst[cuts[i]:cuts[i + 1]].copy_(src[cuts[i]:cuts[i + 1]], non_blocking=True)
+        torch.cuda.synchronize()
+
+    go()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        go()
+    dt = (time.perf_counter() - t0) / reps
+    del src, dst
+    return total / dt / 1e9
+
+
 def run_served(duration_s=4.0, rate=200.0, lanes=6, seed=SEED + 3):
     arrivals, reqs, resident = served_requests(seed, duration_s, rate)
     served = serve_stream(arrivals, reqs, lanes)
     plain = serve_stream(arrivals, reqs, 1)
     sat_served = serve_stream(arrivals, reqs, lanes, saturate=True)
     sat_plain = serve_stream(arrivals, reqs, 1, saturate=True)
+    # the copy floor: every mesh (32 B per vertex) crosses to pinned host memory
+    rates = {"1_stream": d2h_copy_rate(1), f"{lanes}_streams": d2h_copy_rate(lanes)}
+    best = max(rates.values())
+    mesh_bytes = 32 * sat_served["verts"]
+    floor = {"d2h_GBs": rates, "mesh_bytes": int(mesh_bytes),
+             "copy_bound_meshes_per_s": sat_served["completed"] / (mesh_bytes / (best * 1e9)) if mesh_bytes else None}
     return {"workload": f"Poisson {rate:g} req/s for {duration_s:g} s, edges log-U[64,512], 70% graded TPMS "
                         f"(blend grading, 8 resident 8^3 grading fields) / 30% CSG (8-64 primitives), 64 GB pool, "
                         f"meshes copied to pinned host memory",
@@ -758,7 +790,8 @@ def run_served(duration_s=4.0, rate=200.0, lanes=6, seed=SEED + 3):
             "saturation_meshes_per_s": sat_served["meshes_per_s"],
             "saturation_plain_meshes_per_s": sat_plain["meshes_per_s"],
             "saturation_speedup": (sat_served["meshes_per_s"] / sat_plain["meshes_per_s"]
-                                   if sat_plain["meshes_per_s"] else None)}
+                                   if sat_plain["meshes_per_s"] else None),
+            "copy_floor": floor}
 
 
 def run_gcm(args):

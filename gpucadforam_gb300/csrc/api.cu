@@ -53,6 +53,8 @@ gcm_status ensure_scratch(gcm_ctx* ctx, size_t bytes) {
   // Growing allocates; under stream capture cudaMalloc fails and the error is
   // returned, so callers that capture reserve first (gcm_ctx_reserve).
   if (bytes <= ctx->scratch_bytes) return GCM_OK;
+  if (ctx->lent)
+    return fail(ctx, GCM_ERR_OUT_OF_MEMORY, "lent scratch of %zu bytes, %zu needed", ctx->scratch_bytes, bytes);
   if (ctx->scratch) cudaFree(ctx->scratch);
   ctx->scratch = nullptr;
   ctx->scratch_bytes = 0;
@@ -64,6 +66,7 @@ gcm_status ensure_scratch(gcm_ctx* ctx, size_t bytes) {
 
 gcm_status ensure_buffer(gcm_ctx* ctx, float** buf, size_t* have, size_t bytes) {
   if (bytes <= *have) return GCM_OK;
+  if (ctx->lent) return fail(ctx, GCM_ERR_OUT_OF_MEMORY, "lent buffer of %zu bytes, %zu needed", *have, bytes);
   if (*buf) cudaFree(*buf);
   *buf = nullptr;
   *have = 0;
@@ -171,15 +174,31 @@ gcm_status status_of(gcm_ctx* ctx, const gcm_counts& c) {
 // emission of the windows that hold triangles.  Scratch: [0, 64) counts,
 // [64, 68) scan tile counter, [72, 80) scan total, [128, ...) scan tile
 // states, then the window counts and their offsets.
+struct SparseLayout {
+  uint64_t rows, nwin, scan_tiles;
+  size_t off_tris, off_off, bytes;
+};
+
+SparseLayout sparse_layout(const gcm_grid* grid) {
+  SparseLayout L;
+  const uint32_t vx = grid->nx - 1, vy = grid->ny - 1, vz = grid->nz - 1;
+  L.rows = (uint64_t)vy * vz;
+  L.nwin = L.rows * windows_per_row(vx);
+  const uint64_t tile = scan_tile_elems();
+  L.scan_tiles = (L.nwin + tile - 1) / tile;
+  L.off_tris = (128 + L.scan_tiles * 8 + 15) & ~(size_t)15;
+  L.off_off = (L.off_tris + L.nwin * 4 + 15) & ~(size_t)15;
+  L.bytes = L.off_off + L.nwin * 4;
+  return L;
+}
+
 gcm_status mesh_sparse(gcm_ctx* ctx, const float* f, const gcm_grid* grid, float iso, float* pos, float* norm,
                        uint64_t capacity, gcm_counts* counts_out, cudaStream_t st, gcm_counts** counts_used) {
-  const uint32_t vx = grid->nx - 1, vy = grid->ny - 1, vz = grid->nz - 1;
-  const uint64_t nwx = windows_per_row(vx), rows = (uint64_t)vy * vz, nwin = rows * nwx;
-  const uint64_t tile = scan_tile_elems(), scan_tiles = (nwin + tile - 1) / tile;
+  const SparseLayout SL = sparse_layout(grid);
+  const uint64_t rows = SL.rows, nwin = SL.nwin, scan_tiles = SL.scan_tiles;
   if (scan_tiles >= (1ull << 31)) return fail(ctx, GCM_ERR_NOT_SUPPORTED, "grid too large for the sparse path");
-  const size_t off_tris = (128 + scan_tiles * 8 + 15) & ~(size_t)15;
-  const size_t off_off = (off_tris + nwin * 4 + 15) & ~(size_t)15;
-  gcm_status s = ensure_scratch(ctx, off_off + nwin * 4);
+  const size_t off_tris = SL.off_tris, off_off = SL.off_off;
+  gcm_status s = ensure_scratch(ctx, SL.bytes);
   if (s) return s;
   char* b = static_cast<char*>(ctx->scratch);
   gcm_counts* cnt = counts_out ? counts_out : reinterpret_cast<gcm_counts*>(b);
@@ -269,6 +288,14 @@ gcm_status mesh_core(gcm_ctx* ctx, const float* f, const float* gfield, const gc
   s = launch_mesh_kernel(ctx, mode, emit, p, plan, st);
   if (counts_used) *counts_used = cnt;
   return s;
+}
+
+size_t extraction_scratch_bytes(gcm_ctx* ctx, const gcm_grid* grid, bool sparse) {
+  if (!grid || grid->nx < 2 || grid->ny < 2 || grid->nz < 2) return 0;
+  if (sparse) return std::max<size_t>(128, sparse_layout(grid).bytes);
+  MeshPlan plan;
+  if (plan_mesh(ctx, grid, kMeshPlain, &plan) != GCM_OK) return 0;
+  return 128 + plan.ntiles * sizeof(uint64_t);
 }
 
 gcm_status read_counts(gcm_ctx* ctx, const gcm_counts* d, gcm_counts* h, cudaStream_t st) {

@@ -48,7 +48,7 @@ struct gcm_batch {
   std::vector<uint64_t> field_off;  // floats, 16-byte aligned starts
   gcm::BatchLattice* d_lat = nullptr;
   uint32_t n_params = 0;  // instances evaluated by the batched field kernel
-  uint64_t param_rows = 0;
+  uint64_t param_groups = 0;  // row groups of those instances
   bool params_wide = false;  // some instance has more than GCM_BATCH_WARP_CX control columns
   std::vector<uint32_t> blend_ids;  // instances evaluated one by one (blend mode)
   float* blend_buf = nullptr;
@@ -142,10 +142,10 @@ gcm_status make_plan(gcm_batch* b, int threads, uint32_t tile_voxels) {
 gcm_status launch_fields(gcm_batch* b, cudaStream_t st) {
   gcm_ctx* ctx = b->ctx;
   if (b->n_params) {
-    // about 8 rows per warp (8 warps per CTA): many CTAs rather than one
-    // resident wave, so the block scheduler balances the SMs
-    const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((b->param_rows + 63) / 64, 1u << 26));
-    GCM_CUDA(ctx, launch_lattice_batch(b->d_lat, b->n_params, b->param_rows, blocks, b->params_wide, st));
+    // about 2 row groups per warp (8 warps per CTA): many CTAs rather than
+    // one resident wave, so the block scheduler balances the SMs
+    const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((b->param_groups + 15) / 16, 1u << 26));
+    GCM_CUDA(ctx, launch_lattice_batch(b->d_lat, b->n_params, b->param_groups, blocks, b->params_wide, st));
     count_launch(ctx, b->params_wide ? 2 : 1);
   }
   for (uint32_t i : b->blend_ids) {
@@ -305,8 +305,9 @@ gcm_status gcm_batch_create(gcm_ctx* ctx, const gcm_batch_instance* h_instances,
     p.ny = g.ny;
     p.nz = g.nz;
     if (L.cx > GCM_BATCH_WARP_CX) b->params_wide = true;
-    bl.row_begin = b->param_rows;
-    b->param_rows += (uint64_t)g.ny * g.nz;
+    bl.group_begin = b->param_groups;
+    bl.group_rows = batch_group_rows(L.cx);
+    b->param_groups += ((uint64_t)g.ny * g.nz + bl.group_rows - 1) / bl.group_rows;
     lat.push_back(bl);
     lat_inst.push_back(i);
   }

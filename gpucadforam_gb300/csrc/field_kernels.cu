@@ -285,49 +285,95 @@ __device__ __forceinline__ float axis_weight(const AxisCell& k, uint32_t c, int 
 // literal 3.14 are double and rounded to float at the trig call, type 5 takes
 // its first factor through the double cos, type 4 sums double squares.
 // ---------------------------------------------------------------------------
+//
+// Every double operation and every trig call depends on one axis only, so it
+// runs once per column (x, per thread) or once per row (y and z, in shared
+// memory), not per sample: a sample is then a few float products and one
+// store, with the same values.  A CTA takes items of W columns x kUnitRows
+// rows (W = nx rounded up to 32, at most 256), 256 / W rows at a time.
+constexpr uint32_t kUnitRows = 32;
+
+namespace {
+
+// The per-axis factors of one TPMS type: t0, t1 floats, d the double cos of
+// type 5 (x axis only).
+struct UnitAxis {
+  float t0, t1;
+  double d;
+};
+
+__device__ __forceinline__ UnitAxis unit_axis(uint32_t type, uint32_t i, uint32_t n, bool want_double) {
+  const float v = (float)(((i * 1.0) / (double)(n - 1) - 0.5) / 0.5);
+  const float a = (float)(3.14 * v);
+  UnitAxis u{0.0f, 0.0f, 0.0};
+  switch (type) {
+    case 0: u.t0 = cosf(a); u.t1 = sinf(a); break;
+    case 1: u.t0 = cosf(a); break;
+    case 2: u.t0 = cosf(v); u.t1 = cosf(fm(2.0f, v)); break;
+    case 3: u.t0 = cosf(a); u.t1 = cosf((float)(2 * 3.14 * v)); break;
+    case 4: u.t0 = v; break;
+    case 5:
+      u.t0 = cosf(a);
+      u.t1 = sinf(a);
+      if (want_double) u.d = cos(3.14 * v);
+      break;
+    default: break;
+  }
+  return u;
+}
+
+__device__ __forceinline__ float unit_value(uint32_t type, const UnitAxis& X, float y0, float y1, float z0,
+                                            float z1) {
+  switch (type) {
+    case 0: return fa(fa(fm(X.t0, y1), fm(y0, z1)), fm(z0, X.t1));
+    case 1: return fa(fa(X.t0, y0), z0);
+    case 2: return fs(fm(4.0f, fm(fm(X.t0, y0), z0)), fa(fa(fm(X.t1, y1), fm(y1, z1)), fm(z1, X.t1)));
+    case 3: return fs(fm(2.0f, fa(fa(fm(X.t0, y0), fm(y0, z0)), fm(z0, X.t0))), fa(fa(X.t1, y1), z1));
+    case 4: {
+      const double x2 = (double)fm(X.t0, X.t0), y2 = (double)y0 * (double)y0, z2 = (double)z0 * (double)z0;
+      const double xd2 = (double)X.t0 * (double)X.t0;
+      return (float)fmin(fmin(x2 + y2, y2 + z2), z2 + xd2);
+    }
+    case 5: {
+      // cos(3.14 x) is the double cos, so the product runs in double left to right
+      const double prod = X.d * (double)y0 * (double)z0;
+      const float sss = fm(fm(X.t1, y1), z1);
+      return (float)(prod - (double)sss);
+    }
+    default: return 0.0f;
+  }
+}
+
+}  // namespace
+
 __global__ void __launch_bounds__(256) unit_cell_kernel(uint32_t type, uint32_t nx, uint32_t ny, uint32_t nz,
                                                         float* out) {
-  const uint64_t total = (uint64_t)nx * ny * nz;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t x = (uint32_t)(i % nx), y = (uint32_t)((i / nx) % ny), z = (uint32_t)(i / ((uint64_t)nx * ny));
-    const float xx = (float)(((x * 1.0) / (double)(nx - 1) - 0.5) / 0.5);
-    const float yy = (float)(((y * 1.0) / (double)(ny - 1) - 0.5) / 0.5);
-    const float zz = (float)(((z * 1.0) / (double)(nz - 1) - 0.5) / 0.5);
-    float aa = 0.0f;
-    switch (type) {
-      case 0:
-        aa = fa(fa(fm(cosf((float)(3.14 * xx)), sinf((float)(3.14 * yy))),
-                   fm(cosf((float)(3.14 * yy)), sinf((float)(3.14 * zz)))),
-                fm(cosf((float)(3.14 * zz)), sinf((float)(3.14 * xx))));
-        break;
-      case 1: aa = fa(fa(cosf((float)(3.14 * xx)), cosf((float)(3.14 * yy))), cosf((float)(3.14 * zz))); break;
-      case 2:
-        aa = fs(fm(4.0f, fm(fm(cosf(xx), cosf(yy)), cosf(zz))),
-                fa(fa(fm(cosf(fm(2.0f, xx)), cosf(fm(2.0f, yy))), fm(cosf(fm(2.0f, yy)), cosf(fm(2.0f, zz)))),
-                   fm(cosf(fm(2.0f, zz)), cosf(fm(2.0f, xx)))));
-        break;
-      case 3: {
-        const float cx = cosf((float)(3.14 * xx)), cy = cosf((float)(3.14 * yy)), cz = cosf((float)(3.14 * zz));
-        aa = fs(fm(2.0f, fa(fa(fm(cx, cy), fm(cy, cz)), fm(cz, cx))),
-                fa(fa(cosf((float)(2 * 3.14 * xx)), cosf((float)(2 * 3.14 * yy))), cosf((float)(2 * 3.14 * zz))));
-        break;
-      }
-      case 4: {
-        const double x2 = (double)fm(xx, xx), y2 = (double)yy * (double)yy, z2 = (double)zz * (double)zz;
-        const double xd2 = (double)xx * (double)xx;
-        aa = (float)fmin(fmin(x2 + y2, y2 + z2), z2 + xd2);
-        break;
-      }
-      case 5: {
-        // cos(3.14 x) is the double cos, so the product runs in double left to right
-        const double prod = cos(3.14 * xx) * (double)cosf((float)(3.14 * yy)) * (double)cosf((float)(3.14 * zz));
-        const float sss = fm(fm(sinf((float)(3.14 * xx)), sinf((float)(3.14 * yy))), sinf((float)(3.14 * zz)));
-        aa = (float)(prod - (double)sss);
-        break;
-      }
-      default: aa = 0.0f;
+  __shared__ float4 s_row[kUnitRows];  // per row of the item: y factors, z factors
+  const uint32_t W = nx >= 256 ? 256 : (nx + 31) & ~31u;
+  const uint32_t RS = 256 / W;  // rows in flight
+  const uint32_t xl = threadIdx.x % W, rsub = threadIdx.x / W;
+  const uint64_t rows = (uint64_t)ny * nz;
+  const uint64_t xchunks = (nx + W - 1) / W, rgroups = (rows + kUnitRows - 1) / kUnitRows;
+  const uint64_t items = xchunks * rgroups;
+  for (uint64_t it = blockIdx.x; it < items; it += gridDim.x) {
+    const uint32_t x = (uint32_t)(it % xchunks) * W + xl;
+    const uint64_t row0 = (it / xchunks) * kUnitRows;
+    const uint32_t nr = rows - row0 < kUnitRows ? (uint32_t)(rows - row0) : kUnitRows;
+    __syncthreads();  // the previous item's rows are read
+    if (threadIdx.x < nr) {
+      const uint64_t row = row0 + threadIdx.x;
+      const UnitAxis Y = unit_axis(type, (uint32_t)(row % ny), ny, false);
+      const UnitAxis Z = unit_axis(type, (uint32_t)(row / ny), nz, false);
+      s_row[threadIdx.x] = make_float4(Y.t0, Y.t1, Z.t0, Z.t1);
     }
-    out[i] = aa;
+    __syncthreads();
+    if (rsub >= RS || x >= nx) continue;
+    const UnitAxis X = unit_axis(type, x, nx, true);
+    float* o = out + row0 * nx + x;
+    for (uint32_t r = rsub; r < nr; r += RS) {
+      const float4 q = s_row[r];
+      o[(uint64_t)r * nx] = unit_value(type, X, q.x, q.y, q.z, q.w);
+    }
   }
 }
 
@@ -685,53 +731,65 @@ __global__ void __launch_bounds__(256) lattice_blend_kernel(LatticeParams p) {
 }
 
 // Batched graded lattices (GCM_GRADE_PARAMS): the sample rows of all
-// instances form one sequence; a warp takes one row (the rows of these grids
-// are short) and stages that row's cell records in its own slice of shared
-// memory as lattice_rows_kernel does.  Same values as the single-grid kernels.
+// instances form one sequence of row groups (BatchLattice); a warp takes one
+// group at a time.  A staged group holds up to 32 / cx rows of one instance:
+// lane (r, col) stages control column col of row r, so every lane has a column
+// to interpolate, and the cell records go into the warp's own slice of shared
+// memory as in lattice_rows_kernel.  The group's samples are then one run
+// (its rows are consecutive in the output), two per lane per step, so short
+// rows leave no lanes idle at their ends.  Same values as the single-grid
+// kernels.
 constexpr uint32_t kWarpCx = GCM_BATCH_WARP_CX;  // control columns staged per warp
+constexpr uint32_t kGroupRows = 8;                // rows of a group, at most
 
-// STAGED: the rows of instances with at most kWarpCx control columns (the
-// other rows are skipped); the other form takes the wider ones.
+// STAGED: the groups of instances with at most kWarpCx control columns (the
+// other groups are skipped); the other form takes the wider ones, a row each.
 template <bool STAGED>
 __global__ void __launch_bounds__(256, 4) lattice_params_batch_kernel(const BatchLattice* inst, uint32_t n_inst,
-                                                                   uint64_t total_rows) {
-  __shared__ float4 s_rec[8][kRecWords * kWarpCx];  // per warp: the row's cell records
+                                                                   uint64_t total_groups) {
+  __shared__ float4 s_rec[8][kRecWords * kWarpCx];  // per warp: the group's cell records
+  __shared__ float2 s_q[8][kGroupRows];             // per warp: the (y, z) phase coordinates of each row
   __shared__ float4 s_tab[kAngleRows];
   load_angle_table(s_tab);
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
-  uint32_t lo = 0;  // instance of the warp's row: rows only increase, so search only when it moves on
-  for (uint64_t row = (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib; row < total_rows; row += warps) {
-    if (lo + 1 < n_inst && inst[lo + 1].row_begin <= row) {
-      uint32_t a = lo + 1, b = n_inst - 1;  // last instance with row_begin <= row
+  uint32_t lo = 0;  // instance of the warp's group: groups only increase, so search only when it moves on
+  for (uint64_t grp = (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib; grp < total_groups; grp += warps) {
+    if (lo + 1 < n_inst && inst[lo + 1].group_begin <= grp) {
+      uint32_t a = lo + 1, b = n_inst - 1;  // last instance with group_begin <= grp
       while (a < b) {
         const uint32_t mid = (a + b + 1) / 2;
-        if (inst[mid].row_begin <= row) a = mid;
+        if (inst[mid].group_begin <= grp) a = mid;
         else b = mid - 1;
       }
       lo = a;
     }
     const LatticeParams& p = inst[lo].p;
     if ((p.cx <= kWarpCx) != STAGED) continue;  // warp-uniform
-    const uint32_t local = (uint32_t)(row - inst[lo].row_begin);
-    const uint32_t y = local % p.ny, z = local / p.ny;
+    const uint32_t R = inst[lo].group_rows;
+    const uint32_t rows = p.ny * p.nz;
+    const uint32_t row0 = (uint32_t)(grp - inst[lo].group_begin) * R;
+    const uint32_t nr = min(R, rows - row0);
     const uint32_t c[3] = {p.cx, p.cy, p.cz};
     const uint32_t nc = p.cx * p.cy * p.cz;
     const float* arr[5] = {p.period, p.euler, p.euler ? p.euler + nc : nullptr,
                            p.euler ? p.euler + 2 * nc : nullptr, p.thickness};
-    const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
-    __syncwarp();
+    __syncwarp();  // the warp's previous group is read
     if (STAGED) {
-      // one control column per lane (at most kWarpCx = 32 of them); a cell's
-      // second column is the next lane's (a single column is its own)
-      const bool has_col = lane < p.cx;
-      const int col = has_col ? (int)lane : 0;
+      // lane = r * cx + col; a cell's second column is the next lane's (a
+      // single column is its own)
+      const uint32_t cells = row_cells(p.cx);
+      const uint32_t r = lane / p.cx, col = lane - r * p.cx;
+      const bool has_col = r < nr;
+      const uint32_t row = row0 + (has_col ? r : 0);
+      const uint32_t y = row % p.ny, z = row / p.ny;
+      const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
       PF u[4];
 #pragma unroll
-      for (uint32_t k = 0; k < 4; ++k) u[k] = column_pf(arr[k], col, ky, kz, c);
-      const float tu = column_yz(arr[4], col, ky, kz, c);
-      const uint32_t t0 = __ldg(p.type + cidx(col, ky.nearest, kz.nearest, c));
+      for (uint32_t k = 0; k < 4; ++k) u[k] = column_pf(arr[k], (int)col, ky, kz, c);
+      const float tu = column_yz(arr[4], (int)col, ky, kz, c);
+      const uint32_t t0 = __ldg(p.type + cidx((int)col, ky.nearest, kz.nearest, c));
       PF v[4];
 #pragma unroll
       for (uint32_t k = 0; k < 4; ++k)
@@ -744,8 +802,8 @@ __global__ void __launch_bounds__(256, 4) lattice_params_batch_kernel(const Batc
         tv = tu;
         t1 = t0;
       }
-      if (lane < row_cells(p.cx)) {
-        float4* w = &s_rec[wib][kRecWords * lane];
+      if (has_col && col < cells) {
+        float4* w = &s_rec[wib][kRecWords * (r * cells + col)];
 #pragma unroll
         for (uint32_t k = 0; k < 4; ++k) {
           const PF d = pf_diff(v[k], u[k]);
@@ -753,30 +811,50 @@ __global__ void __launch_bounds__(256, 4) lattice_params_batch_kernel(const Batc
         }
         w[4] = make_float4(tu, fs(tv, tu), __uint_as_float(t0), __uint_as_float(t1));
       }
-    }
-    __syncwarp();
-    float* out = p.out + (uint64_t)local * p.nx;
-    if (STAGED) {
-      const float2 qyz = make_float2(fs((float)y, p.origin[1]), fs((float)z, p.origin[2]));
-      for (uint32_t x0 = lane; x0 < p.nx; x0 += 64) {  // two samples per lane per step
-        const uint32_t x1 = x0 + 32;
-        const AxisCell k0 = locate1(x0, c[0], p.scale[0]);
-        const float q0 = fs((float)x0, p.origin[0]);
-        if (x0 - lane + 32 < p.nx) {  // warp-uniform: the second segment holds samples
-          const AxisCell k1 = locate1(min(x1, p.nx - 1), c[0], p.scale[0]);
-          const float v0 = record_sample(s_rec[wib], k0, q0, qyz, s_tab);
-          const float v1 = record_sample(s_rec[wib], k1, fs((float)x1, p.origin[0]), qyz, s_tab);
-          out[x0] = v0;
-          if (x1 < p.nx) out[x1] = v1;
+      if (has_col && col == 0) s_q[wib][r] = make_float2(fs((float)y, p.origin[1]), fs((float)z, p.origin[2]));
+      __syncwarp();
+      // the group's samples as one run: sample j is row j / nx, column j % nx
+      float* out = p.out + (uint64_t)row0 * p.nx;
+      const uint32_t total = nr * p.nx, stride = cells * kRecWords;
+      uint32_t ra = 0, xa = lane;  // row and column of sample j = j0 (j0 = lane + 64 k)
+      while (xa >= p.nx) {
+        xa -= p.nx;
+        ++ra;
+      }
+      for (uint32_t j0 = lane; j0 < total; j0 += 64) {
+        uint32_t rb = ra, xb = xa + 32;  // sample j0 + 32
+        while (xb >= p.nx) {
+          xb -= p.nx;
+          ++rb;
+        }
+        const AxisCell k0 = locate1(xa, c[0], p.scale[0]);
+        const float v0 = record_sample(&s_rec[wib][ra * stride], k0, fs((float)xa, p.origin[0]), s_q[wib][ra], s_tab);
+        if (j0 + 32 < total) {
+          const AxisCell k1 = locate1(xb, c[0], p.scale[0]);
+          const float v1 =
+              record_sample(&s_rec[wib][rb * stride], k1, fs((float)xb, p.origin[0]), s_q[wib][rb], s_tab);
+          out[j0] = v0;
+          out[j0 + 32] = v1;
         } else {
-          out[x0] = record_sample(s_rec[wib], k0, q0, qyz, s_tab);
+          out[j0] = v0;
+        }
+        xa = xb + 32;  // sample j0 + 64
+        ra = rb;
+        while (xa >= p.nx) {
+          xa -= p.nx;
+          ++ra;
         }
       }
     } else {
-      for (uint32_t x = lane; x < p.nx; x += 32) {
-        const AxisCell kx = locate1(x, c[0], p.scale[0]);
-        const float q[3] = {fs((float)x, p.origin[0]), fs((float)y, p.origin[1]), fs((float)z, p.origin[2])};
-        out[x] = params_sample(arr, p.type, kx, ky, kz, c, q, s_tab);
+      for (uint32_t r = 0; r < nr; ++r) {
+        const uint32_t row = row0 + r, y = row % p.ny, z = row / p.ny;
+        const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
+        float* out = p.out + (uint64_t)row * p.nx;
+        for (uint32_t x = lane; x < p.nx; x += 32) {
+          const AxisCell kx = locate1(x, c[0], p.scale[0]);
+          const float q[3] = {fs((float)x, p.origin[0]), fs((float)y, p.origin[1]), fs((float)z, p.origin[2])};
+          out[x] = params_sample(arr, p.type, kx, ky, kz, c, q, s_tab);
+        }
       }
     }
   }
@@ -1606,13 +1684,13 @@ cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t pr
   return cudaGetLastError();
 }
 
-cudaError_t launch_lattice_batch(const BatchLattice* inst, uint32_t n_inst, uint64_t total_rows, uint32_t blocks,
+cudaError_t launch_lattice_batch(const BatchLattice* inst, uint32_t n_inst, uint64_t total_groups, uint32_t blocks,
                                  bool any_wide, cudaStream_t st) {
-  lattice_params_batch_kernel<true><<<blocks, 256, 0, st>>>(inst, n_inst, total_rows);
+  lattice_params_batch_kernel<true><<<blocks, 256, 0, st>>>(inst, n_inst, total_groups);
   if (any_wide) {
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    lattice_params_batch_kernel<false><<<blocks, 256, 0, st>>>(inst, n_inst, total_rows);
+    lattice_params_batch_kernel<false><<<blocks, 256, 0, st>>>(inst, n_inst, total_groups);
   }
   return cudaGetLastError();
 }

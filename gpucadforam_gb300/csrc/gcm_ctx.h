@@ -34,6 +34,10 @@ struct gcm_ctx {
   size_t field_bytes = 0;
   float* blend_buf = nullptr;
   size_t blend_bytes = 0;
+  // scratch and blend buffer lent by an owner for one request (the server
+  // lends ranges of its device pool): never grown or freed by the context; a
+  // call that needs more fails with GCM_ERR_OUT_OF_MEMORY
+  bool lent = false;
   // pinned host staging for count readback
   gcm_counts* h_pinned = nullptr;
   // .obj welding buffers (grown on demand)
@@ -51,6 +55,9 @@ gcm_status ensure_buffer(gcm_ctx* ctx, float** buf, size_t* have, size_t bytes);
 gcm_status read_counts(gcm_ctx* ctx, const gcm_counts* d, gcm_counts* h, cudaStream_t st);
 void count_launch(gcm_ctx* ctx, uint64_t n);
 uint32_t grid_blocks(gcm_ctx* ctx, uint64_t work, uint32_t threads, uint32_t per_sm = 8);
+// Scratch bytes one plain extraction of `grid` takes (gcm_count_field, then
+// gcm_mesh_field[_async] on the fused or the sparse path); 0 for a bad grid.
+size_t extraction_scratch_bytes(gcm_ctx* ctx, const gcm_grid* grid, bool sparse);
 
 }  // namespace gcm
 

@@ -178,10 +178,24 @@ struct LatticeParams {
 
 // One graded lattice of a batch (GCM_GRADE_PARAMS), its sample rows starting
 // at row_begin of the batch's row sequence.
+#define GCM_BATCH_WARP_CX 32  // control columns a warp stages per row
+
+// One instance of the batched field kernel: its sample rows are taken in
+// groups of `group_rows` consecutive rows (32 / cx for a staged instance, at
+// most 8; 1 for a wide one); group_begin is the first group's index in the
+// batch's group sequence.
 struct BatchLattice {
   LatticeParams p;
-  uint64_t row_begin;
+  uint64_t group_begin;
+  uint32_t group_rows;
+  uint32_t pad;
 };
+// Rows per group of an instance with cx control columns.
+inline uint32_t batch_group_rows(uint32_t cx) {
+  if (cx > GCM_BATCH_WARP_CX) return 1;
+  const uint32_t r = GCM_BATCH_WARP_CX / cx;
+  return r > 8 ? 8 : r;
+}
 
 struct CsgParams {
   const gcm_primitive* prims;
@@ -224,8 +238,7 @@ cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t pr
                            uint32_t sm_count, cudaStream_t st);
 // Batched lattice fields: one launch for instances with at most
 // GCM_BATCH_WARP_CX control columns, a second one only when some are wider.
-#define GCM_BATCH_WARP_CX 32
-cudaError_t launch_lattice_batch(const BatchLattice* inst, uint32_t n_inst, uint64_t total_rows, uint32_t blocks,
+cudaError_t launch_lattice_batch(const BatchLattice* inst, uint32_t n_inst, uint64_t total_groups, uint32_t blocks,
                                  bool any_wide, cudaStream_t st);
 // CSG field over tiles of 32 x 8 x 8 samples, one tile per warp at a time;
 // csg_tiles is the CTA count that gives every warp a tile.

@@ -5,11 +5,16 @@
 // takes the next request as soon as device memory for it can be reserved
 // from the server's pool, so requests that arrive while others run are
 // admitted as lanes and memory free up and their kernels overlap on the GPU.
-// Memory is admitted exactly (two passes): the field is reserved and
-// evaluated, a counting pass gives the vertex total, then the mesh buffers
-// are reserved and the fused pass writes them.  With a host pool the mesh is
-// copied to pinned host memory and its device memory returned at once, so the
-// result's latency is arrival -> mesh on the host.
+// Memory is admitted exactly (two passes): one pool range holds the
+// request's field, device counts, extraction scratch and blend buffer (lent to
+// the lane's context, so lanes never allocate or free device memory while
+// others run); the field is evaluated, a counting pass gives the vertex total
+// (the one readback before the mesh), then the mesh buffers are reserved and
+// the mesh pass, its counts and the copies to pinned host memory are enqueued
+// together and synchronised once.  Lattices take the fused extraction, CSG
+// scenes (sparse surfaces) the windowed one.  With a host pool the mesh's
+// device memory is returned at once, so the result's latency is arrival ->
+// mesh on the host.
 //
 // Faults are injected on the host only (tests): failing pool reservations,
 // a slow lane, a lane that dies after taking a request (the request goes back
@@ -29,6 +34,7 @@
 #include <vector>
 
 #include "../../include/gcm.h"
+#include "gcm_ctx.h"
 #include "pool.h"
 
 namespace {
@@ -53,6 +59,8 @@ struct Job {
 };
 
 uint64_t field_bytes(const gcm_grid& g) { return (uint64_t)g.nx * g.ny * g.nz * sizeof(float); }
+size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
+constexpr size_t kCountsBytes = 64;  // a request's device counts, before its scratch
 
 }  // namespace
 
@@ -110,67 +118,90 @@ struct gcm_server {
   }
 
   void lane_main(uint32_t lane);
-  gcm_status run_job(uint32_t lane, gcm_ctx* ctx, cudaStream_t st, Job* j);
+  gcm_status run_job(uint32_t lane, gcm_ctx* ctx, cudaStream_t st, gcm_counts* h_counts, Job* j);
 };
 
-gcm_status gcm_server::run_job(uint32_t lane, gcm_ctx* ctx, cudaStream_t st, Job* j) {
+gcm_status gcm_server::run_job(uint32_t lane, gcm_ctx* ctx, cudaStream_t st, gcm_counts* h_counts, Job* j) {
   const gcm_request& r = j->req;
   const gcm_grid& g = r.grid;
-  // 1. field
-  const float* field = nullptr;
-  size_t foff = 0, fbytes = 0;
-  bool has_field = false;
-  auto drop_field = [&] {
-    if (has_field) dpool.release(foff, fbytes);
-    has_field = false;
+  // CSG scenes are sparse surfaces: the windowed extraction path
+  const bool sparse = r.kind == GCM_REQUEST_CSG;
+  ctx->mesh_path = sparse ? GCM_MESH_PATH_SPARSE : GCM_MESH_PATH_AUTO;
+  // 1. one pool range for the request's working memory: [field | counts |
+  //    scratch | blend buffer], lent to the lane's context, so that no lane
+  //    allocates or frees device memory while the others run
+  const size_t fb = r.kind == GCM_REQUEST_FIELD ? 0 : align16(field_bytes(g));
+  const size_t sb = align16(gcm::extraction_scratch_bytes(ctx, &g, sparse));
+  const uint64_t nc = r.kind == GCM_REQUEST_LATTICE && r.lattice.mode == GCM_GRADE_BLEND
+                          ? (uint64_t)r.lattice.cx * r.lattice.cy * r.lattice.cz
+                          : 0;
+  const size_t bb = align16((size_t)nc * GCM_BLEND_WORDS * sizeof(float));
+  if (sb == 0) return GCM_ERR_INVALID_ARGUMENT;
+  const size_t wbytes = fb + kCountsBytes + sb + bb;
+  if (wbytes > dpool.size()) return GCM_ERR_REJECTED;  // can never be admitted
+  size_t woff = 0;
+  bool has_work = false;
+  auto drop_work = [&] {
+    ctx->scratch = nullptr;
+    ctx->scratch_bytes = 0;
+    ctx->blend_buf = nullptr;
+    ctx->blend_bytes = 0;
+    if (has_work) dpool.release(woff, wbytes);
+    has_work = false;
   };
-  if (r.kind == GCM_REQUEST_FIELD) {
-    field = r.d_field;
-  } else {
-    fbytes = field_bytes(g);
-    int tries = 0;
-    while (!dalloc(fbytes, &foff, j)) {
-      if (j->cancel.load()) return GCM_ERR_CANCELLED;
-      if (stopping) return GCM_ERR_CANCELLED;
-      if (++tries >= 4) return GCM_ERR_OUT_OF_MEMORY;
-    }
-    has_field = true;
-    float* f = reinterpret_cast<float*>(dbase + foff);
+  int tries = 0;
+  while (!dalloc(wbytes, &woff, j)) {
+    if (j->cancel.load() || stopping) return GCM_ERR_CANCELLED;
+    if (++tries >= 4) return GCM_ERR_OUT_OF_MEMORY;
+  }
+  has_work = true;
+  char* w = dbase + woff;
+  gcm_counts* d_counts = reinterpret_cast<gcm_counts*>(w + fb);
+  ctx->scratch = w + fb + kCountsBytes;
+  ctx->scratch_bytes = sb;
+  ctx->blend_buf = bb ? reinterpret_cast<float*>(w + fb + kCountsBytes + sb) : nullptr;
+  ctx->blend_bytes = bb;
+  const float* field = r.d_field;
+  if (r.kind != GCM_REQUEST_FIELD) {
+    float* f = reinterpret_cast<float*>(w);
     const gcm_status s = r.kind == GCM_REQUEST_LATTICE
                              ? gcm_field_lattice(ctx, &r.lattice, g.nx, g.ny, g.nz, f, st)
                              : gcm_field_csg(ctx, r.d_prims, r.n_prims, &r.frame, g.nx, g.ny, g.nz, f, st);
     if (s) {
-      drop_field();
+      cudaStreamSynchronize(st);
+      drop_work();
       return s;
     }
     field = f;
   }
   if (j->cancel.load()) {
-    drop_field();
+    cudaStreamSynchronize(st);
+    drop_work();
     return GCM_ERR_CANCELLED;
   }
-  // 2. exact size
+  // 2. exact size: the one readback before the mesh, which admission needs
   gcm_counts c{};
   gcm_status s = gcm_count_field(ctx, field, &g, r.iso, &c, st);
   if (s) {
-    drop_field();
+    cudaStreamSynchronize(st);
+    drop_work();
     return s;
   }
   j->verts = c.total_verts;
   j->active = c.active_voxels;
   const size_t obytes = (size_t)std::max<uint64_t>(c.total_verts, 1) * 32;
-  if (obytes + fbytes > dpool.size()) {
-    drop_field();
+  if (obytes + wbytes > dpool.size()) {
+    drop_work();
     return GCM_ERR_REJECTED;
   }
-  int tries = 0;
+  tries = 0;
   while (!dalloc(obytes, &j->out_off, j)) {
     if (j->cancel.load() || stopping) {
-      drop_field();
+      drop_work();
       return GCM_ERR_CANCELLED;
     }
     if (++tries >= 4) {
-      drop_field();
+      drop_work();
       return GCM_ERR_OUT_OF_MEMORY;
     }
   }
@@ -178,26 +209,35 @@ gcm_status gcm_server::run_job(uint32_t lane, gcm_ctx* ctx, cudaStream_t st, Job
   j->out_bytes = obytes;
   float* pos = reinterpret_cast<float*>(dbase + j->out_off);
   float* norm = pos + 4 * std::max<uint64_t>(c.total_verts, 1);
-  // 3. mesh
-  s = gcm_mesh_field(ctx, field, &g, r.iso, pos, norm, c.total_verts, &c, st);
-  drop_field();
-  if (s) return s;
-  // 4. copy out
+  // host range before the mesh is enqueued, so that the mesh and its copies
+  // run back to back on the stream with one synchronisation at the end
   if (hbase) {
-    const size_t hbytes = obytes;
     if (!hpool.alloc_wait(
-            hbytes, &j->host_off, [&] { return stopping || j->cancel.load(); }, 60000))
+            obytes, &j->host_off, [&] { return stopping || j->cancel.load(); }, 60000)) {
+      drop_work();
       return j->cancel.load() ? GCM_ERR_CANCELLED : GCM_ERR_OUT_OF_MEMORY;
+    }
     j->has_host = true;
-    j->host_bytes = hbytes;
+    j->host_bytes = obytes;
+  }
+  // 3. mesh, counts and (with a host pool) the copies, then one synchronisation
+  s = gcm_mesh_field_async(ctx, field, &g, r.iso, pos, norm, c.total_verts, d_counts, st);
+  cudaError_t e = s ? cudaSuccess : cudaMemcpyAsync(h_counts, d_counts, sizeof(gcm_counts), cudaMemcpyDeviceToHost, st);
+  if (!s && hbase) {
     const size_t half = (size_t)c.total_verts * 16;
     char* h = hbase + j->host_off;
-    cudaError_t e = cudaMemcpyAsync(h, pos, half, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, pos, half, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h + half, norm, half, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  }
+  const cudaError_t es = cudaStreamSynchronize(st);
+  drop_work();
+  if (s) return s;
+  if (e != cudaSuccess || es != cudaSuccess) return GCM_ERR_CUDA;
+  if (h_counts->status == GCM_ERR_DEVICE_TIMEOUT) return GCM_ERR_DEVICE_TIMEOUT;
+  if (h_counts->status != 0 || h_counts->total_verts != c.total_verts) return GCM_ERR_CUDA;
+  if (hbase) {
     dpool.release(j->out_off, j->out_bytes);
     j->has_out = false;
-    if (e != cudaSuccess) return GCM_ERR_CUDA;
   }
   (void)lane;
   return GCM_OK;
@@ -207,12 +247,16 @@ void gcm_server::lane_main(uint32_t lane) {
   cudaSetDevice(cfg.device);
   gcm_ctx* ctx = nullptr;
   cudaStream_t st = nullptr;
-  if (gcm_ctx_create(cfg.device, &ctx) != GCM_OK || cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+  gcm_counts* h_counts = nullptr;
+  if (gcm_ctx_create(cfg.device, &ctx) != GCM_OK || cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMallocHost(reinterpret_cast<void**>(&h_counts), sizeof(gcm_counts)) != cudaSuccess) {
+    if (st) cudaStreamDestroy(st);
     if (ctx) gcm_ctx_destroy(ctx);
     alive.fetch_sub(1);
     cv_done.notify_all();
     return;
   }
+  ctx->lent = true;  // each request lends the context its scratch from the pool
   while (true) {
     Job* j = nullptr;
     {
@@ -236,7 +280,7 @@ void gcm_server::lane_main(uint32_t lane) {
       std::this_thread::sleep_for(std::chrono::milliseconds(cfg.fault_param));
     j->lane = lane;
     j->t_start = now();
-    gcm_status s = j->cancel.load() ? GCM_ERR_CANCELLED : run_job(lane, ctx, st, j);
+    gcm_status s = j->cancel.load() ? GCM_ERR_CANCELLED : run_job(lane, ctx, st, h_counts, j);
     if (s != GCM_OK && j->has_out) {
       dpool.release(j->out_off, j->out_bytes);
       j->has_out = false;
@@ -248,7 +292,8 @@ void gcm_server::lane_main(uint32_t lane) {
     finish(j, s);
   }
   if (st) cudaStreamDestroy(st);
-  gcm_ctx_destroy(ctx);
+  cudaFreeHost(h_counts);
+  gcm_ctx_destroy(ctx);  // holds no lent range between requests
   const uint32_t left = alive.fetch_sub(1) - 1;
   if (left == 0) {
     // nothing can serve the queue any more: fail what is left
