@@ -209,30 +209,30 @@ gcm_status gcm_server::run_job(uint32_t lane, gcm_ctx* ctx, cudaStream_t st, gcm
   j->out_bytes = obytes;
   float* pos = reinterpret_cast<float*>(dbase + j->out_off);
   float* norm = pos + 4 * std::max<uint64_t>(c.total_verts, 1);
-  // host range before the mesh is enqueued, so that the mesh and its copies
-  // run back to back on the stream with one synchronisation at the end
-  if (hbase) {
-    if (!hpool.alloc_wait(
-            obytes, &j->host_off, [&] { return stopping || j->cancel.load(); }, 60000)) {
-      drop_work();
-      return j->cancel.load() ? GCM_ERR_CANCELLED : GCM_ERR_OUT_OF_MEMORY;
-    }
-    j->has_host = true;
-    j->host_bytes = obytes;
-  }
-  // 3. mesh, counts and (with a host pool) the copies, then one synchronisation
+  // 3. mesh and its counts enqueued; the host range is reserved while the
+  //    mesh runs, then the copies follow on the stream and one
+  //    synchronisation ends the request
   s = gcm_mesh_field_async(ctx, field, &g, r.iso, pos, norm, c.total_verts, d_counts, st);
   cudaError_t e = s ? cudaSuccess : cudaMemcpyAsync(h_counts, d_counts, sizeof(gcm_counts), cudaMemcpyDeviceToHost, st);
-  if (!s && hbase) {
-    const size_t half = (size_t)c.total_verts * 16;
-    char* h = hbase + j->host_off;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h, pos, half, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h + half, norm, half, cudaMemcpyDeviceToHost, st);
+  gcm_status host_fail = GCM_OK;
+  if (!s && e == cudaSuccess && hbase) {
+    if (hpool.alloc_wait(
+            obytes, &j->host_off, [&] { return stopping || j->cancel.load(); }, 60000)) {
+      j->has_host = true;
+      j->host_bytes = obytes;
+      const size_t half = (size_t)c.total_verts * 16;
+      char* h = hbase + j->host_off;
+      e = cudaMemcpyAsync(h, pos, half, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(h + half, norm, half, cudaMemcpyDeviceToHost, st);
+    } else {
+      host_fail = j->cancel.load() ? GCM_ERR_CANCELLED : GCM_ERR_OUT_OF_MEMORY;
+    }
   }
   const cudaError_t es = cudaStreamSynchronize(st);
   drop_work();
   if (s) return s;
   if (e != cudaSuccess || es != cudaSuccess) return GCM_ERR_CUDA;
+  if (host_fail) return host_fail;
   if (h_counts->status == GCM_ERR_DEVICE_TIMEOUT) return GCM_ERR_DEVICE_TIMEOUT;
   if (h_counts->status != 0 || h_counts->total_verts != c.total_verts) return GCM_ERR_CUDA;
   if (hbase) {
