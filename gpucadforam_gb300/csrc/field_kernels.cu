@@ -290,8 +290,10 @@ __device__ __forceinline__ float axis_weight(const AxisCell& k, uint32_t c, int 
 // runs once per column (x, per thread) or once per row (y and z, in shared
 // memory), not per sample: a sample is then a few float products and one
 // store, with the same values.  A CTA takes items of W columns x kUnitRows
-// rows (W = nx rounded up to 32, at most 256), 256 / W rows at a time.
-constexpr uint32_t kUnitRows = 32;
+// rows (W = nx rounded up to 32, at most 256), 256 / W rows at a time; the
+// grid is a multiple of the column chunks, so a CTA keeps one chunk and forms
+// its column factors once.
+constexpr uint32_t kUnitRows = 64;
 
 namespace {
 
@@ -346,17 +348,22 @@ __device__ __forceinline__ float unit_value(uint32_t type, const UnitAxis& X, fl
 
 }  // namespace
 
+__host__ __device__ inline uint32_t unit_cell_width(uint32_t nx) { return nx >= 256 ? 256 : (nx + 31) & ~31u; }
+
 __global__ void __launch_bounds__(256) unit_cell_kernel(uint32_t type, uint32_t nx, uint32_t ny, uint32_t nz,
                                                         float* out) {
   __shared__ float4 s_row[kUnitRows];  // per row of the item: y factors, z factors
-  const uint32_t W = nx >= 256 ? 256 : (nx + 31) & ~31u;
+  const uint32_t W = unit_cell_width(nx);
   const uint32_t RS = 256 / W;  // rows in flight
   const uint32_t xl = threadIdx.x % W, rsub = threadIdx.x / W;
   const uint64_t rows = (uint64_t)ny * nz;
   const uint64_t xchunks = (nx + W - 1) / W, rgroups = (rows + kUnitRows - 1) / kUnitRows;
   const uint64_t items = xchunks * rgroups;
+  // gridDim.x is a multiple of xchunks: the CTA's column chunk never changes
+  const uint32_t x = (uint32_t)(blockIdx.x % xchunks) * W + xl;
+  const bool has_x = rsub < RS && x < nx;
+  const UnitAxis X = unit_axis(type, has_x ? x : 0, nx, true);
   for (uint64_t it = blockIdx.x; it < items; it += gridDim.x) {
-    const uint32_t x = (uint32_t)(it % xchunks) * W + xl;
     const uint64_t row0 = (it / xchunks) * kUnitRows;
     const uint32_t nr = rows - row0 < kUnitRows ? (uint32_t)(rows - row0) : kUnitRows;
     __syncthreads();  // the previous item's rows are read
@@ -367,8 +374,7 @@ __global__ void __launch_bounds__(256) unit_cell_kernel(uint32_t type, uint32_t 
       s_row[threadIdx.x] = make_float4(Y.t0, Y.t1, Z.t0, Z.t1);
     }
     __syncthreads();
-    if (rsub >= RS || x >= nx) continue;
-    const UnitAxis X = unit_axis(type, x, nx, true);
+    if (!has_x) continue;
     float* o = out + row0 * nx + x;
     for (uint32_t r = rsub; r < nr; r += RS) {
       const float4 q = s_row[r];
@@ -1639,7 +1645,12 @@ __global__ void __launch_bounds__(256) lattice_mask_kernel(const gcm_csg_point* 
 // ---------------------------------------------------------------------------
 cudaError_t launch_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t nz, float* out, uint32_t blocks,
                              cudaStream_t st) {
-  unit_cell_kernel<<<blocks, 256, 0, st>>>(type, nx, ny, nz, out);
+  // a whole number of column chunks per grid (at least one of each)
+  const uint64_t W = unit_cell_width(nx), xchunks = (nx + W - 1) / W;
+  const uint64_t items = xchunks * (((uint64_t)ny * nz + kUnitRows - 1) / kUnitRows);
+  uint64_t g = std::min<uint64_t>(std::max<uint64_t>(blocks, xchunks), items);
+  g = std::max<uint64_t>(g / xchunks, 1) * xchunks;
+  unit_cell_kernel<<<(uint32_t)std::min<uint64_t>(g, 1ull << 30), 256, 0, st>>>(type, nx, ny, nz, out);
   return cudaGetLastError();
 }
 

@@ -776,43 +776,63 @@ __global__ void __launch_bounds__(128) mc_generate_kernel(GenerateParams p) {
 // wrap-around output like thrust's scan over uint, 64-bit running total.
 // ----------------------------------------------------------------------------
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 16;
+constexpr int kScanRounds = 4;  // 128-element rounds per warp and tile
+constexpr uint32_t kScanWarpElems = 32 * 4 * kScanRounds;
 
-__global__ void __launch_bounds__(kScanThreads) scan_u32_kernel(ScanParams p) {
+namespace {
+
+__device__ __forceinline__ uint64_t warp_inclusive_u64(uint64_t x, uint32_t lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t nb = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += nb;
+  }
+  return x;
+}
+
+}  // namespace
+
+// Exclusive scan of 32-bit values with 64-bit running sums (the tile prefixes
+// and the total are 64-bit; each output is the prefix modulo 2^32, as a
+// 32-bit scan's would be).  Tiles of kScanThreads * 16 elements are claimed in
+// order from a counter and chained by the decoupled look-back.  Each warp
+// scans a contiguous segment of 512 elements in four rounds of 128: lane l
+// holds elements 4l .. 4l + 3 of a round (one 16-byte load and store when
+// VEC: both arrays 16-byte aligned), so every access is coalesced.
+template <bool VEC>
+__global__ void __launch_bounds__(kScanThreads, 4) scan_u32_kernel(ScanParams p) {
   __shared__ uint32_t sh_tile;
   __shared__ uint64_t sh_warp[kScanThreads / 32];
   __shared__ uint64_t sh_prefix;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   while (true) {
     if (tid == 0) sh_tile = atomicAdd(p.counter, 1u);
-    __syncthreads();
+    __syncthreads();  // also: every warp has read the previous tile's sh_warp and sh_prefix
     const uint64_t t = sh_tile;
     if (t >= p.ntiles) break;
-    const uint64_t base = t * (uint64_t)(kScanThreads * kScanItems) + (uint64_t)tid * kScanItems;
-    uint32_t v[kScanItems];
-    uint64_t local = 0;
+    const uint64_t seg = t * (uint64_t)(kScanThreads / 32 * kScanWarpElems) + (uint64_t)warp * kScanWarpElems;
+    uint4 v[kScanRounds];
+    uint64_t inc[kScanRounds], warp_total = 0;
 #pragma unroll
-    for (int i = 0; i < kScanItems; ++i) {
-      v[i] = (base + i < p.n) ? p.in[base + i] : 0u;
-      local += v[i];
+    for (int k = 0; k < kScanRounds; ++k) {
+      const uint64_t i = seg + (uint64_t)k * 128 + 4u * lane;
+      if (VEC && i + 3 < p.n) {
+        v[k] = __ldcs(reinterpret_cast<const uint4*>(p.in + i));
+      } else {
+        v[k].x = i < p.n ? p.in[i] : 0u;
+        v[k].y = i + 1 < p.n ? p.in[i + 1] : 0u;
+        v[k].z = i + 2 < p.n ? p.in[i + 2] : 0u;
+        v[k].w = i + 3 < p.n ? p.in[i + 3] : 0u;
+      }
+      const uint64_t s4 = (uint64_t)v[k].x + v[k].y + v[k].z + v[k].w;
+      inc[k] = warp_inclusive_u64(s4, lane);
+      warp_total += __shfl_sync(0xffffffffu, inc[k], 31);
     }
-    // block-exclusive prefix of `local`
-    uint64_t inc = local;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint64_t nb = __shfl_up_sync(0xffffffffu, inc, o);
-      if (lane >= (uint32_t)o) inc += nb;
-    }
-    if (lane == 31) sh_warp[warp] = inc;
+    if (lane == 31) sh_warp[warp] = warp_total;
     __syncthreads();
     if (warp == 0) {
-      uint64_t wv = lane < (uint32_t)(kScanThreads / 32) ? sh_warp[lane] : 0;
-      uint64_t winc = wv;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint64_t nb = __shfl_up_sync(0xffffffffu, winc, o);
-        if (lane >= (uint32_t)o) winc += nb;
-      }
+      const uint64_t wv = lane < (uint32_t)(kScanThreads / 32) ? sh_warp[lane] : 0;
+      const uint64_t winc = warp_inclusive_u64(wv, lane);
       const uint64_t tile_total = __shfl_sync(0xffffffffu, winc, 31);
       if (lane < (uint32_t)(kScanThreads / 32)) sh_warp[lane] = winc - wv;
       const uint64_t excl = lookback_exclusive(p.tile_status, t, tile_total, p.wait_ns, p.status);
@@ -822,17 +842,31 @@ __global__ void __launch_bounds__(kScanThreads) scan_u32_kernel(ScanParams p) {
       }
     }
     __syncthreads();
-    uint64_t run = sh_prefix + sh_warp[warp] + (inc - local);
+    uint64_t run = sh_prefix + sh_warp[warp];
 #pragma unroll
-    for (int i = 0; i < kScanItems; ++i) {
-      if (base + i < p.n) p.out[base + i] = (uint32_t)run;
-      run += v[i];
+    for (int k = 0; k < kScanRounds; ++k) {
+      const uint64_t i = seg + (uint64_t)k * 128 + 4u * lane;
+      const uint64_t s4 = (uint64_t)v[k].x + v[k].y + v[k].z + v[k].w;
+      const uint64_t e = run + inc[k] - s4;
+      uint4 o;
+      o.x = (uint32_t)e;
+      o.y = (uint32_t)(e + v[k].x);
+      o.z = (uint32_t)(e + v[k].x + v[k].y);
+      o.w = (uint32_t)(e + v[k].x + v[k].y + v[k].z);
+      if (VEC && i + 3 < p.n) {
+        __stcs(reinterpret_cast<uint4*>(p.out + i), o);
+      } else {
+        if (i < p.n) p.out[i] = o.x;
+        if (i + 1 < p.n) p.out[i + 1] = o.y;
+        if (i + 2 < p.n) p.out[i + 2] = o.z;
+        if (i + 3 < p.n) p.out[i + 3] = o.w;
+      }
+      run += __shfl_sync(0xffffffffu, inc[k], 31);
     }
-    __syncthreads();
   }
 }
 
-uint32_t scan_tile_elems() { return kScanThreads * kScanItems; }
+uint32_t scan_tile_elems() { return kScanThreads / 32 * kScanWarpElems; }
 
 // ----------------------------------------------------------------------------
 // Sparse path: windows of 32 consecutive voxels of a row, in voxel order
@@ -1286,7 +1320,10 @@ cudaError_t launch_generate(bool band, const GenerateParams& p, uint32_t blocks,
 }
 
 cudaError_t launch_scan(const ScanParams& p, uint32_t blocks, cudaStream_t st) {
-  scan_u32_kernel<<<blocks, kScanThreads, 0, st>>>(p);
+  if (((reinterpret_cast<uintptr_t>(p.in) | reinterpret_cast<uintptr_t>(p.out)) & 15u) == 0)
+    scan_u32_kernel<true><<<blocks, kScanThreads, 0, st>>>(p);
+  else
+    scan_u32_kernel<false><<<blocks, kScanThreads, 0, st>>>(p);
   return cudaGetLastError();
 }
 
