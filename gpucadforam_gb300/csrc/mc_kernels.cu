@@ -966,10 +966,15 @@ __global__ void __launch_bounds__(256) mc_window_count_kernel(const float* __res
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
   uint32_t active = 0;
   uint64_t tris = 0;
-  for (uint64_t t = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; t < tasks; t += warps) {
-    const uint32_t wx = (uint32_t)(t % nwx);
-    const uint64_t rest = t / nwx;
-    const uint32_t yb = (uint32_t)(rest % nyb), z = (uint32_t)(rest / nyb);
+  // task t = wx + nwx * (yb + nyb * z), stepped by `warps` as a mixed-radix
+  // counter (no divisions in the loop)
+  uint64_t t = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint32_t wx = (uint32_t)(t % nwx), yb = (uint32_t)((t / nwx) % nyb);
+  uint64_t zz = t / nwx / nyb;
+  const uint32_t dwx = (uint32_t)(warps % nwx), dyb = (uint32_t)((warps / nwx) % nyb);
+  const uint64_t dz = warps / nwx / nyb;
+  for (; t < tasks; t += warps) {
+    const uint32_t z = (uint32_t)zz;
     const uint32_t y0 = yb * kCountRows, nr = min(kCountRows, vy - y0);
     const uint32_t x = wx * kWinVox + lane;
     const bool has = x <= vx, voxel = lane < kWinVox && x < vx;
@@ -1004,6 +1009,13 @@ __global__ void __launch_bounds__(256) mc_window_count_kernel(const float* __res
       }
       if (lane < nr) win_tris[((uint64_t)z * vy + y0 + lane) * nwx + wx] = mine;
     }
+    wx += dwx;
+    uint32_t carry = wx >= nwx;
+    if (carry) wx -= nwx;
+    yb += dyb + carry;
+    carry = yb >= nyb;
+    if (carry) yb -= nyb;
+    zz += dz + carry;
   }
   const uint64_t wa = warp_sum_u64(active), wt = warp_sum_u64(tris);
   if (lane == 0 && (wa | wt)) {
@@ -1036,8 +1048,14 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 8) mc_window_emit_kernel(Wind
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
   const Frame fr{{p.vs[0], p.vs[1], p.vs[2]}, {p.gc[0], p.gc[1], p.gc[2]}};
   bool dropped = false;
-  for (uint64_t row = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; row < rows; row += warps) {
-    const uint32_t y = (uint32_t)(row % vy), z = (uint32_t)(row / vy);
+  // row = y + vy * z, stepped by `warps` without divisions in the loop
+  uint64_t row = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  uint32_t yy = (uint32_t)(row % vy);
+  uint64_t zz = row / vy;
+  const uint32_t dyy = (uint32_t)(warps % vy);
+  const uint64_t dzz = warps / vy;
+  for (; row < rows; row += warps, yy += dyy, zz += dzz + (yy >= vy ? 1u : 0u), yy -= yy >= vy ? vy : 0u) {
+    const uint32_t y = yy, z = (uint32_t)zz;
     const uint64_t rb = (uint64_t)y * sy + (uint64_t)z * sz;
     VoxelCorners V;
     axis_corners(y, fr.gc[1], fr.vs[1], V.y0, V.y1);
