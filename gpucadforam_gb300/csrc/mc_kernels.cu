@@ -990,22 +990,37 @@ __global__ void __launch_bounds__(256) mc_window_count_kernel(const float* __res
       line[i] = (uint32_t)(a < iso) | ((uint32_t)(b < iso) << 2);
     }
     uint32_t nt[kCountRows], task_tris = 0;
+    // a task whose lines all lie on one side of the isovalue (every column,
+    // both planes) has cube indices 0 or 255 only: no triangles
+    uint32_t lor = 0, land = 5u;
 #pragma unroll
-    for (uint32_t i = 0; i < kCountRows; ++i) {
-      const uint32_t m = line[i] | (line[i + 1] << 1);
-      const uint32_t n = __shfl_down_sync(0xffffffffu, m, 1);
-      nt[i] = (voxel && i < nr) ? (uint32_t)(s_tri[cube_from_columns(m, n)] & 0xFu) : 0u;
-      active += nt[i] > 0;
-      task_tris += nt[i];
+    for (uint32_t i = 0; i <= kCountRows; ++i) {
+      lor |= line[i];
+      land &= line[i];
+    }
+    const bool mixed = __ballot_sync(0xffffffffu, lor != 0u) != 0u && __ballot_sync(0xffffffffu, land != 5u) != 0u;
+#pragma unroll
+    for (uint32_t i = 0; i < kCountRows; ++i) nt[i] = 0;
+    if (mixed) {
+#pragma unroll
+      for (uint32_t i = 0; i < kCountRows; ++i) {
+        const uint32_t m = line[i] | (line[i + 1] << 1);
+        const uint32_t n = __shfl_down_sync(0xffffffffu, m, 1);
+        nt[i] = (voxel && i < nr) ? (uint32_t)(s_tri[cube_from_columns(m, n)] & 0xFu) : 0u;
+        active += nt[i] > 0;
+        task_tris += nt[i];
+      }
     }
     tris += task_tris;
     if (WRITE) {
       // the rows' window sums, then lane i stores row i's
       uint32_t mine = 0;
+      if (mixed) {
 #pragma unroll
-      for (uint32_t i = 0; i < kCountRows; ++i) {
-        const uint32_t wsum = __reduce_add_sync(0xffffffffu, nt[i]);
-        if (lane == i) mine = wsum;
+        for (uint32_t i = 0; i < kCountRows; ++i) {
+          const uint32_t wsum = __reduce_add_sync(0xffffffffu, nt[i]);
+          if (lane == i) mine = wsum;
+        }
       }
       if (lane < nr) win_tris[((uint64_t)z * vy + y0 + lane) * nwx + wx] = mine;
     }
