@@ -140,18 +140,22 @@ def test_batch_with_wide_control_grid(ctx):
         b.close()
 
 
-@pytest.mark.parametrize("cw", [(1, 1, 1), (2, 2, 2), (32, 3, 2), (31, 1, 4)])
-def test_batch_staged_control_grid_edges(ctx, cw):
-    """The staged batched field form holds one control column per lane and
-    takes each cell's second column from the next lane: a single column (its
-    own), two columns, and 31 or 32 columns (every lane holding one) must
-    give each instance its one-at-a-time mesh bit for bit."""
+@pytest.mark.parametrize("shape", [(36, 30, 75), (37, 29, 5), (13, 11, 33)])
+@pytest.mark.parametrize("cw", [(1, 1, 1), (2, 2, 2), (3, 4, 2), (5, 2, 3), (7, 3, 2), (32, 3, 2), (31, 1, 4)])
+def test_batch_staged_control_grid_edges(ctx, cw, shape):
+    """The staged batched field form takes groups of 32 / cx sample rows (at
+    most 8) per warp, one control column per lane, each cell's second column
+    from the next lane, and runs a group's samples as one sequence.  A single
+    column (its own), groups that leave lanes without a column (3, 5 and 7
+    columns), 31 or 32 columns (a row per group), row counts that leave a
+    partial last group, and rows shorter than a warp (5 and 33 samples, so one
+    lane's samples span several rows) must give each instance its
+    one-at-a-time mesh bit for bit."""
     from gpucadforam_gb300.mesher import Batch, Lattice, random_batch_lattices
 
     lats, shapes = random_batch_lattices(2, seed=0xD4A + 11, dims=(24, 56))
-    rng = np.random.default_rng(sum(cw))
+    rng = np.random.default_rng(sum(cw) + shape[2])
     nc = int(np.prod(cw))
-    shape = (36, 30, 75)
     lats.insert(1, Lattice.from_numpy(0, cw, rng.uniform(12, 40, nc).astype(np.float32),
                                       rng.uniform(-np.pi / 4, np.pi / 4, 3 * nc).astype(np.float32),
                                       rng.uniform(-0.6, 0.6, nc).astype(np.float32),
