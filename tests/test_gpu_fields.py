@@ -44,6 +44,22 @@ def test_unit_cell_vs_reference(ctx, i):
     assert_field_close(got, FIELDS[f"sm103a/unit{i}"], k_rel=2, k_scale=4)
 
 
+@pytest.mark.parametrize("shape", [(300, 7, 9), (5, 40, 33), (257, 65, 3), (96, 130, 2)])
+@pytest.mark.parametrize("t", range(6))
+def test_unit_cell_layouts_vs_oracle(ctx, shape, t):
+    """The unit-cell kernel forms its double coordinate factors once per
+    column (per thread) and once per sample row (in shared memory), over
+    column chunks of up to 256 and items of 64 rows: several chunks with a
+    ragged last one (300, 257), rows narrower than a warp (5), row counts
+    that leave a partial item, and planes of 2 and 3 samples must give the
+    per-sample values.  The oracle computes every sample on its own with
+    the host's trig, so the tolerance is the oracle's against the reference
+    kernels plus the kernel's own."""
+    nx, ny, nz = shape
+    got = host(ctx.unit_cell(t, nx, ny, nz))
+    assert_field_close(got, O.unit_cell(t, nx, ny, nz), k_rel=6, k_scale=12)
+
+
 def _prim_case(i):
     from gpucadforam_gb300.mesher import make_frame, primitives_to_device
 
