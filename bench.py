@@ -783,6 +783,17 @@ def run_served(duration_s=4.0, rate=200.0, lanes=6, seed=SEED + 3):
     mesh_bytes = 32 * sat_served["verts"]
     floor = {"d2h_GBs": rates, "mesh_bytes": int(mesh_bytes),
              "copy_bound_meshes_per_s": sat_served["completed"] / (mesh_bytes / (best * 1e9)) if mesh_bytes else None}
+    # the same streams with every mesh left in the device pool (a consumer on
+    # the GPU takes the result): the GPU's own service rate, no copy floor
+    dev_served = serve_stream(arrivals, reqs, lanes, host_bytes=0)
+    dev_plain = serve_stream(arrivals, reqs, 1, host_bytes=0)
+    dev_sat = serve_stream(arrivals, reqs, lanes, host_bytes=0, saturate=True)
+    dev_sat_plain = serve_stream(arrivals, reqs, 1, host_bytes=0, saturate=True)
+    device = {"served": dev_served, "plain_one_lane": dev_plain,
+              "saturation_meshes_per_s": dev_sat["meshes_per_s"],
+              "saturation_plain_meshes_per_s": dev_sat_plain["meshes_per_s"],
+              "saturation_speedup": (dev_sat["meshes_per_s"] / dev_sat_plain["meshes_per_s"]
+                                     if dev_sat_plain["meshes_per_s"] else None)}
     return {"workload": f"Poisson {rate:g} req/s for {duration_s:g} s, edges log-U[64,512], 70% graded TPMS "
                         f"(blend grading, 8 resident 8^3 grading fields) / 30% CSG (8-64 primitives), 64 GB pool, "
                         f"meshes copied to pinned host memory",
@@ -791,7 +802,7 @@ def run_served(duration_s=4.0, rate=200.0, lanes=6, seed=SEED + 3):
             "saturation_plain_meshes_per_s": sat_plain["meshes_per_s"],
             "saturation_speedup": (sat_served["meshes_per_s"] / sat_plain["meshes_per_s"]
                                    if sat_plain["meshes_per_s"] else None),
-            "copy_floor": floor}
+            "copy_floor": floor, "device_resident": device}
 
 
 def run_gcm(args):
