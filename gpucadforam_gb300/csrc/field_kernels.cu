@@ -647,92 +647,156 @@ __device__ __forceinline__ PF blend_k(const float* __restrict__ rec, uint32_t r,
 
 }  // namespace
 
+namespace {
+
+// One sample row of the blend form: its control cells along y and z, the
+// corner rows' phase coordinates and the y/z part of the trilinear weights.
+struct BlendRow {
+  AxisCell ky, kz;
+  int gy[2], gz[2];
+  float qy[2], qz[2], wyz[4];
+};
+
+__device__ __forceinline__ BlendRow blend_row(const LatticeParams& p, const uint32_t c[3], uint32_t y, uint32_t z) {
+  BlendRow R;
+  R.ky = locate1(y, c[1], p.scale[1]);
+  R.kz = locate1(z, c[2], p.scale[2]);
+  R.gy[0] = c[1] > 1 ? R.ky.i0 : 0;
+  R.gy[1] = c[1] > 1 ? R.ky.i0 + 1 : 0;
+  R.gz[0] = c[2] > 1 ? R.kz.i0 : 0;
+  R.gz[1] = c[2] > 1 ? R.kz.i0 + 1 : 0;
+#pragma unroll
+  for (int d = 0; d < 2; ++d) {
+    R.qy[d] = fs((float)y, c[1] > 1 ? fm((float)R.gy[d], p.anchor[1]) : 0.0f);
+    R.qz[d] = fs((float)z, c[2] > 1 ? fm((float)R.gz[d], p.anchor[2]) : 0.0f);
+  }
+#pragma unroll
+  for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+      R.wyz[2 * dz + dy] = fm(axis_weight(R.ky, c[1], dy), axis_weight(R.kz, c[2], dz));
+  return R;
+}
+
+// The staged record of corner row (dy, dz) = corner and control column xc:
+// M_r0 pairs (3), K_r pairs (3), thickness, type.
+__device__ __forceinline__ void blend_stage(const LatticeParams& p, const uint32_t c[3], const BlendRow& R,
+                                            uint32_t corner, uint32_t xc, float4* w) {
+  const int dy = corner & 1, dz = corner >> 1;
+  const int gyc = dy ? R.gy[1] : R.gy[0], gzc = dz ? R.gz[1] : R.gz[0];
+  const float qyc = dy ? R.qy[1] : R.qy[0], qzc = dz ? R.qz[1] : R.qz[0];
+  const float* rec = p.blend + GCM_BLEND_WORDS * (uint64_t)cidx((int)xc, gyc, gzc, c);
+  float m[6];
+#pragma unroll
+  for (uint32_t r = 0; r < 3; ++r) {
+    m[2 * r] = __ldg(rec + 6 * r);
+    m[2 * r + 1] = __ldg(rec + 6 * r + 1);
+  }
+  const PF K0 = blend_k(rec, 0, qyc, qzc), K1 = blend_k(rec, 1, qyc, qzc), K2 = blend_k(rec, 2, qyc, qzc);
+  w[0] = make_float4(m[0], m[1], m[2], m[3]);
+  w[1] = make_float4(m[4], m[5], K0.h, K0.l);
+  w[2] = make_float4(K1.h, K1.l, K2.h, K2.l);
+  w[3] = make_float4(__ldg(rec + 18), __ldg(rec + 19), 0.0f, 0.0f);
+}
+
+// One sample: the weighted sum of the 8 corner lattices.  rec(corner, xc)
+// gives the staged record, or null for the unstaged form (read from p.blend).
+template <typename Rec>
+__device__ __forceinline__ float blend_sample(const LatticeParams& p, const uint32_t c[3], const BlendRow& R,
+                                              uint32_t x, Rec rec) {
+  const AxisCell kx = locate1(x, c[0], p.scale[0]);
+  const int gx[2] = {c[0] > 1 ? kx.i0 : 0, c[0] > 1 ? kx.i0 + 1 : 0};
+  float acc = 0.0f;
+#pragma unroll 1
+  for (int corner = 0; corner < 8; ++corner) {
+    // selects rather than run-time array indices keep R in registers
+    const int dx = corner & 1, dy = (corner >> 1) & 1, dz = corner >> 2;
+    const float wyz = dz ? (dy ? R.wyz[3] : R.wyz[2]) : (dy ? R.wyz[1] : R.wyz[0]);
+    const int gxc = dx ? gx[1] : gx[0], gyc = dy ? R.gy[1] : R.gy[0], gzc = dz ? R.gz[1] : R.gz[0];
+    const float qyc = dy ? R.qy[1] : R.qy[0], qzc = dz ? R.qz[1] : R.qz[0];
+    const float w = fm(axis_weight(kx, c[0], dx), wyz);
+    if (w == 0.0f) continue;
+    const float q0 = fs((float)x, c[0] > 1 ? fm((float)gxc, p.anchor[0]) : 0.0f);
+    PF M0, M1, M2, K0, K1, K2;
+    float thick;
+    uint32_t type;
+    const float4* s = rec(2 * dz + dy, gxc);
+    if (s) {
+      const float4 a = s[0], b = s[1], e = s[2], f = s[3];
+      M0 = {a.x, a.y};
+      M1 = {a.z, a.w};
+      M2 = {b.x, b.y};
+      K0 = {b.z, b.w};
+      K1 = {e.x, e.y};
+      K2 = {e.z, e.w};
+      thick = f.x;
+      type = __float_as_uint(f.y);
+    } else {
+      const float* g = p.blend + GCM_BLEND_WORDS * (uint64_t)cidx(gxc, gyc, gzc, c);
+      M0 = {__ldg(g + 0), __ldg(g + 1)};
+      M1 = {__ldg(g + 6), __ldg(g + 7)};
+      M2 = {__ldg(g + 12), __ldg(g + 13)};
+      K0 = blend_k(g, 0, qyc, qzc);
+      K1 = blend_k(g, 1, qyc, qzc);
+      K2 = blend_k(g, 2, qyc, qzc);
+      thick = __ldg(g + 18);
+      type = __float_as_uint(__ldg(g + 19));
+    }
+    const float r[3] = {pf_reduce(pf_add(pf_mulf(M0, q0), K0)), pf_reduce(pf_add(pf_mulf(M1, q0), K1)),
+                        pf_reduce(pf_add(pf_mulf(M2, q0), K2))};
+    acc = fmaf_(w, tpms_of_phase(type, r, thick), acc);
+  }
+  return acc;
+}
+
+}  // namespace
+
+// BLEND mode, CTA per sample row: the row's records staged by the whole CTA
+// (control grids up to kBlendCx columns), else read from the setup buffer.
 __global__ void __launch_bounds__(256) lattice_blend_kernel(LatticeParams p) {
-  // per (y, z) corner row of the current sample row and control column:
-  // M_r0 pairs (3), K_r pairs (3), thickness, type
   __shared__ float4 s_rec[4][kBlendCx][4];
   const uint32_t c[3] = {p.cx, p.cy, p.cz};
   const bool staged = p.cx <= kBlendCx;
   const uint32_t rows = p.ny * p.nz;
   for (uint32_t row = blockIdx.x; row < rows; row += gridDim.x) {
-    const uint32_t y = row % p.ny, z = row / p.ny;
-    const AxisCell ky = locate1(y, c[1], p.scale[1]), kz = locate1(z, c[2], p.scale[2]);
-    const int gy[2] = {c[1] > 1 ? ky.i0 : 0, c[1] > 1 ? ky.i0 + 1 : 0};
-    const int gz[2] = {c[2] > 1 ? kz.i0 : 0, c[2] > 1 ? kz.i0 + 1 : 0};
-    float wyz[4], qy[2], qz[2];
-#pragma unroll
-    for (int d = 0; d < 2; ++d) {
-      qy[d] = fs((float)y, c[1] > 1 ? fm((float)gy[d], p.anchor[1]) : 0.0f);
-      qz[d] = fs((float)z, c[2] > 1 ? fm((float)gz[d], p.anchor[2]) : 0.0f);
-    }
-#pragma unroll
-    for (int dz = 0; dz < 2; ++dz)
-#pragma unroll
-      for (int dy = 0; dy < 2; ++dy) wyz[2 * dz + dy] = fm(axis_weight(ky, c[1], dy), axis_weight(kz, c[2], dz));
+    const BlendRow R = blend_row(p, c, row % p.ny, row / p.ny);
     if (staged) {
       __syncthreads();  // the previous row's records are read
-      for (uint32_t i = threadIdx.x; i < 4 * p.cx; i += blockDim.x) {
-        const uint32_t corner = i / p.cx, xc = i % p.cx;
-        const int dy = corner & 1, dz = corner >> 1;
-        const float* rec = p.blend + GCM_BLEND_WORDS * (uint64_t)cidx((int)xc, gy[dy], gz[dz], c);
-        float m[6];
-#pragma unroll
-        for (uint32_t r = 0; r < 3; ++r) {
-          m[2 * r] = __ldg(rec + 6 * r);
-          m[2 * r + 1] = __ldg(rec + 6 * r + 1);
-        }
-        const PF K0 = blend_k(rec, 0, qy[dy], qz[dz]), K1 = blend_k(rec, 1, qy[dy], qz[dz]),
-                 K2 = blend_k(rec, 2, qy[dy], qz[dz]);
-        float4* w = s_rec[corner][xc];
-        w[0] = make_float4(m[0], m[1], m[2], m[3]);
-        w[1] = make_float4(m[4], m[5], K0.h, K0.l);
-        w[2] = make_float4(K1.h, K1.l, K2.h, K2.l);
-        w[3] = make_float4(__ldg(rec + 18), __ldg(rec + 19), 0.0f, 0.0f);
-      }
+      for (uint32_t i = threadIdx.x; i < 4 * p.cx; i += blockDim.x)
+        blend_stage(p, c, R, i / p.cx, i % p.cx, s_rec[i / p.cx][i % p.cx]);
       __syncthreads();
     }
     float* out = p.out + (uint64_t)row * p.nx;
-    for (uint32_t x = threadIdx.x; x < p.nx; x += blockDim.x) {
-      const AxisCell kx = locate1(x, c[0], p.scale[0]);
-      const int gx[2] = {c[0] > 1 ? kx.i0 : 0, c[0] > 1 ? kx.i0 + 1 : 0};
-      float acc = 0.0f;
-#pragma unroll 1
-      for (int corner = 0; corner < 8; ++corner) {
-        const int dx = corner & 1, dy = (corner >> 1) & 1, dz = corner >> 2;
-        const float w = fm(axis_weight(kx, c[0], dx), wyz[2 * dz + dy]);
-        if (w == 0.0f) continue;
-        const float q0 = fs((float)x, c[0] > 1 ? fm((float)gx[dx], p.anchor[0]) : 0.0f);
-        PF M0, M1, M2, K0, K1, K2;
-        float thick;
-        uint32_t type;
-        if (staged) {
-          const float4* s = s_rec[2 * dz + dy][gx[dx]];
-          const float4 a = s[0], b = s[1], e = s[2], f = s[3];
-          M0 = {a.x, a.y};
-          M1 = {a.z, a.w};
-          M2 = {b.x, b.y};
-          K0 = {b.z, b.w};
-          K1 = {e.x, e.y};
-          K2 = {e.z, e.w};
-          thick = f.x;
-          type = __float_as_uint(f.y);
-        } else {
-          const float* rec = p.blend + GCM_BLEND_WORDS * (uint64_t)cidx(gx[dx], gy[dy], gz[dz], c);
-          M0 = {__ldg(rec + 0), __ldg(rec + 1)};
-          M1 = {__ldg(rec + 6), __ldg(rec + 7)};
-          M2 = {__ldg(rec + 12), __ldg(rec + 13)};
-          K0 = blend_k(rec, 0, qy[dy], qz[dz]);
-          K1 = blend_k(rec, 1, qy[dy], qz[dz]);
-          K2 = blend_k(rec, 2, qy[dy], qz[dz]);
-          thick = __ldg(rec + 18);
-          type = __float_as_uint(__ldg(rec + 19));
-        }
-        const float r[3] = {pf_reduce(pf_add(pf_mulf(M0, q0), K0)), pf_reduce(pf_add(pf_mulf(M1, q0), K1)),
-                            pf_reduce(pf_add(pf_mulf(M2, q0), K2))};
-        acc = fmaf_(w, tpms_of_phase(type, r, thick), acc);
-      }
-      out[x] = acc;
-    }
+    for (uint32_t x = threadIdx.x; x < p.nx; x += blockDim.x)
+      out[x] = blend_sample(p, c, R, x, [&](int corner, int xc) -> const float4* {
+        return staged ? s_rec[corner][xc] : nullptr;
+      });
+  }
+}
+
+// BLEND mode, warp per sample row: each warp stages its row's records in its
+// own slice of shared memory (warp syncs only, no CTA barrier) for control
+// grids up to kBlendWarpCx columns.  Same values as lattice_blend_kernel.
+constexpr uint32_t kBlendWarps = 8;
+constexpr uint32_t kBlendWarpCx = 24;  // 8 warps x 4 corner rows x 24 columns x 64 B = 48 KB
+
+__global__ void __launch_bounds__(kBlendWarps * 32) lattice_blend_warp_kernel(LatticeParams p) {
+  extern __shared__ float4 s_blend[];
+  const uint32_t c[3] = {p.cx, p.cy, p.cz};
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  float4* rec = s_blend + (size_t)warp * 4u * p.cx * 4u;  // [corner][xc][4]
+  const uint32_t rows = p.ny * p.nz;
+  const uint32_t nw = gridDim.x * kBlendWarps;
+  for (uint32_t row = blockIdx.x * kBlendWarps + warp; row < rows; row += nw) {
+    const BlendRow R = blend_row(p, c, row % p.ny, row / p.ny);
+    __syncwarp();  // the previous row's records are read
+    for (uint32_t i = lane; i < 4 * p.cx; i += 32) blend_stage(p, c, R, i / p.cx, i % p.cx, rec + 4u * i);
+    __syncwarp();
+    float* out = p.out + (uint64_t)row * p.nx;
+    for (uint32_t x = lane; x < p.nx; x += 32)
+      out[x] = blend_sample(p, c, R, x, [&](int corner, int xc) -> const float4* {
+        return rec + 4u * ((uint32_t)corner * p.cx + (uint32_t)xc);
+      });
   }
 }
 
@@ -1682,7 +1746,14 @@ cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t pr
     if (e != cudaSuccess) return e;
     LatticeParams q = p;
     q.blend = blend_buf;
-    lattice_blend_kernel<<<blocks, 256, 0, st>>>(q);
+    if (p.cx <= kBlendWarpCx) {
+      // a sample row per warp; many CTAs, so the block scheduler balances the SMs
+      const uint64_t rows = (uint64_t)p.ny * p.nz;
+      const uint32_t wblocks = (uint32_t)std::min<uint64_t>((rows + kBlendWarps - 1) / kBlendWarps, 1u << 26);
+      lattice_blend_warp_kernel<<<wblocks, kBlendWarps * 32, (size_t)kBlendWarps * 4 * p.cx * 4 * sizeof(float4), st>>>(q);
+    } else {
+      lattice_blend_kernel<<<blocks, 256, 0, st>>>(q);
+    }
   } else {
     switch (lattice_rows_per_warp(p.cx, p.ny * p.nz, sm_count)) {
       case 8: launch_rows<8>(p, st); break;

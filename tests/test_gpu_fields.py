@@ -140,6 +140,35 @@ def test_graded_lattice_vs_oracle(ctx, mode, shape):
 
 
 @pytest.mark.parametrize("shape,ctrl", [
+    ((20, 18, 40), (1, 1, 1)),        # one control point: a single lattice
+    ((30, 26, 61), (3, 2, 5)),        # warp per row, few columns
+    ((24, 20, 100), (24, 4, 4)),      # warp per row at its widest (24 columns)
+    ((20, 16, 90), (25, 3, 3)),       # CTA per row, records staged by the CTA
+    ((10, 8, 300), (140, 2, 2)),      # CTA per row, records read from the setup buffer
+])
+def test_blend_lattice_kernel_forms_vs_oracle(ctx, shape, ctrl):
+    """The blend grading runs as a warp per sample row (control grids up to 24
+    columns) or a CTA per row (staged up to 128 columns, else unstaged); every
+    form equals the oracle bit for bit and the FP64 oracle within 1e-5."""
+    from gpucadforam_gb300.mesher import Lattice
+
+    nz, ny, nx = shape
+    rng = np.random.default_rng(sum(shape) + sum(ctrl) + 1)
+    n = ctrl[0] * ctrl[1] * ctrl[2]
+    period = rng.uniform(16, 64, n).astype(np.float32)
+    euler = rng.uniform(-np.pi / 4, np.pi / 4, 3 * n).astype(np.float32)
+    thick = rng.uniform(-0.6, 0.6, n).astype(np.float32)
+    types = rng.choice(np.array([0, 1, 2, 3, 5], np.uint8), n)
+    origin = ((nx - 1) / 2, (ny - 1) / 2, (nz - 1) / 2)
+    lat = Lattice.from_numpy(1, ctrl, period, euler, thick, types, origin)
+    got = host(ctx.lattice_field(lat, shape))
+    ref32 = O.lattice_field((nx, ny, nz), 1, ctrl, period, euler, thick, types, origin)
+    assert got.tobytes() == ref32.tobytes()
+    ref64 = O.lattice_field((nx, ny, nz), 1, ctrl, period, euler, thick, types, origin, fp64=True)
+    assert_rel_close(got, ref64, 1e-5)
+
+
+@pytest.mark.parametrize("shape,ctrl", [
     ((200, 200, 64), (16, 16, 16)),   # 40,000 sample rows: 8 rows per warp
     ((150, 150, 64), (16, 16, 16)),   # 22,500 rows: 4 per warp
     ((110, 110, 70), (16, 16, 16)),   # 12,100 rows: 2 per warp; rows of 70 end on a single-sample step
