@@ -17,9 +17,11 @@ from a file instead of evaluating it with the oracle; the bench writes its own
 device field there, which is bit-identical to the oracle's.
 
 Prints one JSON line: per-kernel median times of the reference (classify,
-compaction, generate; its two thrust scans cannot be launched by name and are
-left out, which favours the reference), this project's fused kernel on the same
-field, and both as achieved GB/s of the algorithmic bytes 4 P + 32 V.
+compaction, generate, launched by name from its compiled code; its thrust
+exclusive scan, which cannot be launched by name, is timed by ref_scan.cu making
+the same thrust call on as many voxels, and counted twice as the reference
+scans twice), this project's fused kernel on the same field, and both as
+achieved GB/s of the algorithmic bytes 4 P + 32 V.
 """
 import argparse
 import ctypes as C
@@ -58,6 +60,15 @@ def build_runner():
     return exe
 
 
+def build_scan():
+    """The reference's thrust scan call, compiled with nvcc (ref_scan.cu)."""
+    exe = os.path.join(REF_DIR, "ref_scan")
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    subprocess.run([os.path.join(cuda, "bin", "nvcc"), "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+                    "-std=c++17", os.path.join(HERE, "ref_scan.cu"), "-o", exe], check=True)
+    return exe
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--grid", type=int, default=512)
@@ -93,6 +104,14 @@ def main():
     kind, nvox, active, total, reps = struct.unpack_from("<IIIII", b, 0)
     t = np.frombuffer(b, np.float32, 3 * reps, 20).reshape(reps, 3)
     med = np.median(t, axis=0)
+    # the reference's two thrust scans per extraction (vertex counts and
+    # occupancy), each over all voxels
+    scan_ms = None
+    try:
+        r = subprocess.run([build_scan(), str(nvox), str(args.reps)], check=True, capture_output=True, text=True)
+        scan_ms = float(r.stdout.split()[1])
+    except (OSError, subprocess.SubprocessError, ValueError, IndexError) as e:
+        print(f"thrust scan not timed: {e}", file=sys.stderr)
 
     # this project's fused kernel, same field and isovalue
     import torch
@@ -126,7 +145,9 @@ def main():
         "verts_gcm": int(cnt.total_verts),
         "reps": int(reps), "reference_ms_per_rep": t.tolist(),
         "reference_ms": {"classifyVoxel_new": float(med[0]), "compactVoxels": float(med[1]),
-                         "generateTriangles_lattice_kernel_3": float(med[2]), "sum_without_scans": ref_ms},
+                         "generateTriangles_lattice_kernel_3": float(med[2]), "sum_without_scans": ref_ms,
+                         "thrust_exclusive_scan": scan_ms,
+                         "sum_with_scans": ref_ms + 2 * scan_ms if scan_ms is not None else None},
         "gcm_fused_ms": ours,
         "algorithmic_bytes": alg,
         "reference_GBs": alg / ref_ms / 1e6, "gcm_GBs": (4 * P + 32 * int(cnt.total_verts)) / ours / 1e6,
