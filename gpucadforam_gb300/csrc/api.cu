@@ -696,6 +696,10 @@ static gcm_status lattice_params(gcm_ctx* ctx, const gcm_lattice* L, uint32_t nx
   if (L->cx == 0 || L->cy == 0 || L->cz == 0) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "lattice: empty control grid");
   if (L->mode > 1) return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "lattice: unknown grading mode %u", L->mode);
   if ((uint64_t)L->cx * L->cy * L->cz > (1u << 24)) return fail(ctx, GCM_ERR_NOT_SUPPORTED, "control grid too large");
+  // the field kernels count sample rows (ny * nz) and step through them in 32 bits
+  if ((uint64_t)ny * nz >= (1ull << 31))
+    return fail(ctx, GCM_ERR_NOT_SUPPORTED, "lattice grid has %llu sample rows (ny * nz), at most 2^31 - 1",
+                (unsigned long long)ny * nz);
   *p = LatticeParams{};
   p->mode = L->mode;
   p->cx = L->cx;

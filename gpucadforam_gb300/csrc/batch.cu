@@ -278,6 +278,10 @@ gcm_status gcm_batch_create(gcm_ctx* ctx, const gcm_batch_instance* h_instances,
       delete b;
       return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_batch_create: instance %u is invalid", i);
     }
+    if ((uint64_t)g.ny * g.nz >= (1ull << 31)) {  // the field kernel counts sample rows in 32 bits
+      delete b;
+      return fail(ctx, GCM_ERR_NOT_SUPPORTED, "gcm_batch_create: instance %u has too many sample rows", i);
+    }
     b->field_off[i] = off;
     off += ((uint64_t)g.nx * g.ny * g.nz + 3) / 4 * 4;
     if (L.mode == GCM_GRADE_BLEND) {

@@ -310,3 +310,25 @@ def test_mesh_lattice_async_equals_sync(ctx):
         dc = host(d_counts)
         assert int(dc[0]) == c.active_voxels and int(dc[1]) == c.total_verts and int(dc[2]) == 0
         assert host(pos).tobytes() == p.tobytes() and host(norm).tobytes() == n.tobytes()
+
+
+def test_lattice_grids_with_too_many_sample_rows_are_refused(ctx):
+    """The lattice field kernels count sample rows (ny * nz) in 32 bits: a grid
+    of 2^31 rows or more is refused before anything launches or allocates,
+    by the single-grid call and by a batch."""
+    import ctypes as C
+
+    from gpucadforam_gb300 import _native as N
+    from gpucadforam_gb300.mesher import Batch, Lattice
+
+    lat = Lattice.from_numpy(0, (1, 1, 1), np.array([16.0], np.float32))
+    s = ctx.lattice_struct(lat)
+    dummy = torch.empty(16, device="cuda")
+    rc = ctx.lib.gcm_field_lattice(ctx.h, C.byref(s), 2, 65536, 32768, C.c_void_p(dummy.data_ptr()), None)
+    assert rc == N.GCM_ERR_NOT_SUPPORTED
+    with pytest.raises(N.GcmError) as e:
+        Batch(ctx, [lat, lat], [(16, 16, 16), (32768, 65536, 2)])
+    assert e.value.code == N.GCM_ERR_NOT_SUPPORTED
+    # a small grid on the same context still evaluates (12 samples into the 16-float buffer)
+    rc = ctx.lib.gcm_field_lattice(ctx.h, C.byref(s), 2, 2, 3, C.c_void_p(dummy.data_ptr()), None)
+    assert rc == N.GCM_OK
