@@ -160,6 +160,7 @@ PROTOTYPES = {
     "gcm_mesh_field_noalloc": (I32, [P, C.POINTER(GcmGrid), F32, P, P, U64, P, P]),
     "gcm_mesh_csg": (I32, [P, P, U32, C.POINTER(GcmFrame), C.POINTER(GcmGrid), F32, P, P, U64,
                            C.POINTER(GcmCounts), P]),
+    "gcm_mesh_csg_async": (I32, [P, P, U32, C.POINTER(GcmFrame), C.POINTER(GcmGrid), F32, P, P, U64, P, P]),
 }
 
 

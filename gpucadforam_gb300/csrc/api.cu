@@ -193,7 +193,8 @@ SparseLayout sparse_layout(const gcm_grid* grid) {
 }
 
 gcm_status mesh_sparse(gcm_ctx* ctx, const float* f, const gcm_grid* grid, float iso, float* pos, float* norm,
-                       uint64_t capacity, gcm_counts* counts_out, cudaStream_t st, gcm_counts** counts_used) {
+                       uint64_t capacity, gcm_counts* counts_out, cudaStream_t st, gcm_counts** counts_used,
+                       TileStates tiles = {}) {
   const SparseLayout SL = sparse_layout(grid);
   const uint64_t rows = SL.rows, nwin = SL.nwin, scan_tiles = SL.scan_tiles;
   if (scan_tiles >= (1ull << 31)) return fail(ctx, GCM_ERR_NOT_SUPPORTED, "grid too large for the sparse path");
@@ -207,7 +208,7 @@ gcm_status mesh_sparse(gcm_ctx* ctx, const float* f, const gcm_grid* grid, float
   uint32_t* win_tris = reinterpret_cast<uint32_t*>(b + off_tris);
   uint32_t* win_off = reinterpret_cast<uint32_t*>(b + off_off);
   const uint32_t blocks = grid_blocks(ctx, rows * 32, 256, 8);
-  GCM_CUDA(ctx, launch_window_count(f, grid->nx, grid->ny, grid->nz, iso, win_tris, cnt, blocks, st));
+  GCM_CUDA(ctx, launch_window_count(f, grid->nx, grid->ny, grid->nz, iso, win_tris, cnt, blocks, st, tiles));
   ScanParams sp{};
   sp.in = win_tris;
   sp.out = win_off;
@@ -243,12 +244,13 @@ gcm_status mesh_sparse(gcm_ctx* ctx, const float* f, const gcm_grid* grid, float
 
 gcm_status mesh_core(gcm_ctx* ctx, const float* f, const float* gfield, const gcm_grid* grid, float iso, float lo,
                      float hi, int mode, uint32_t op, bool emit, float* pos, float* norm, uint64_t capacity,
-                     gcm_counts* counts_out, cudaStream_t st, gcm_counts** counts_used, bool sparse_scene = false) {
+                     gcm_counts* counts_out, cudaStream_t st, gcm_counts** counts_used, bool sparse_scene = false,
+                     TileStates tiles = {}) {
   if (((reinterpret_cast<uintptr_t>(pos) | reinterpret_cast<uintptr_t>(norm)) & 15u) != 0)
     return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "position and normal buffers must be 16-byte aligned");
   if (mode == kMeshPlain && emit &&
       (ctx->mesh_path == GCM_MESH_PATH_SPARSE || (ctx->mesh_path == GCM_MESH_PATH_AUTO && sparse_scene)))
-    return mesh_sparse(ctx, f, grid, iso, pos, norm, capacity, counts_out, st, counts_used);
+    return mesh_sparse(ctx, f, grid, iso, pos, norm, capacity, counts_out, st, counts_used, tiles);
   MeshPlan plan;
   gcm_status s = plan_mesh(ctx, grid, mode, &plan);
   if (s) return s;
@@ -790,9 +792,10 @@ gcm_status gcm_mesh_lattice_async(gcm_ctx* ctx, const gcm_lattice* lattice, cons
                    d_counts, st, nullptr);
 }
 
-gcm_status gcm_field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
-                         uint32_t nx, uint32_t ny, uint32_t nz, float* d_out, gcm_stream stream) {
-  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+// The CSG field; with tile_state, also each sample tile's state against iso.
+static gcm_status field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
+                            uint32_t nx, uint32_t ny, uint32_t nz, float* d_out, uint8_t* tile_state, float iso,
+                            cudaStream_t st) {
   if (!d_prims || !frame || !d_out || n_prims == 0 || nx == 0 || ny == 0 || nz == 0)
     return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_field_csg: bad argument");
   if (n_prims > 256) return fail(ctx, GCM_ERR_NOT_SUPPORTED, "gcm_field_csg: at most 256 primitives");
@@ -808,9 +811,40 @@ gcm_status gcm_field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_
   p.nz = nz;
   p.out = d_out;
   p.exact = ctx->prim_exact ? 1u : 0u;
-  GCM_CUDA(ctx, gcm::launch_csg(p, (uint32_t)ctx->sm_count, static_cast<cudaStream_t>(stream)));
+  p.tile_state = tile_state;
+  p.iso = iso;
+  GCM_CUDA(ctx, gcm::launch_csg(p, (uint32_t)ctx->sm_count, st));
   count_launch(ctx, 1);
   return GCM_OK;
+}
+
+gcm_status gcm_field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
+                         uint32_t nx, uint32_t ny, uint32_t nz, float* d_out, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  return field_csg(ctx, d_prims, n_prims, frame, nx, ny, nz, d_out, nullptr, 0.0f, static_cast<cudaStream_t>(stream));
+}
+
+// Field into the context's buffer with its tile states, then the extraction:
+// on the windowed path the count pass skips the tasks whose tiles all lie on
+// one side of the isovalue without reading their samples.
+static gcm_status mesh_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
+                           const gcm_grid* grid, float iso, float* d_pos, float* d_norm, uint64_t capacity,
+                           gcm_counts* d_counts, cudaStream_t st, gcm_counts** used) {
+  gcm_status s = check_grid(ctx, grid);
+  if (s) return s;
+  const uint64_t n = (uint64_t)grid->nx * grid->ny * grid->nz;
+  const uint32_t tx = (grid->nx + GCM_CSG_TILE_X - 1) / GCM_CSG_TILE_X;
+  const uint32_t ty = (grid->ny + GCM_CSG_TILE_Y - 1) / GCM_CSG_TILE_Y;
+  const uint64_t tiles = (uint64_t)tx * ty * ((grid->nz + GCM_CSG_TILE_Z - 1) / GCM_CSG_TILE_Z);
+  // the field, then the tile states after it (16-byte aligned)
+  const size_t field_bytes = (n * sizeof(float) + 15) & ~(size_t)15;
+  s = ensure_buffer(ctx, &ctx->field_buf, &ctx->field_bytes, field_bytes + tiles);
+  if (s) return s;
+  uint8_t* tile_state = reinterpret_cast<uint8_t*>(ctx->field_buf) + field_bytes;
+  s = field_csg(ctx, d_prims, n_prims, frame, grid->nx, grid->ny, grid->nz, ctx->field_buf, tile_state, iso, st);
+  if (s) return s;
+  return mesh_core(ctx, ctx->field_buf, nullptr, grid, iso, 0, 0, kMeshPlain, 0, true, d_pos, d_norm, capacity, d_counts,
+                   st, used, true, TileStates{tile_state, tx, ty});
 }
 
 gcm_status gcm_mesh_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
@@ -819,19 +853,21 @@ gcm_status gcm_mesh_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_p
   if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
   if (!h_counts || (capacity && (!d_pos || !d_norm)))
     return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_mesh_csg: NULL counts or outputs");
-  gcm_status s = check_grid(ctx, grid);
-  if (s) return s;
-  const uint64_t n = (uint64_t)grid->nx * grid->ny * grid->nz;
-  s = ensure_buffer(ctx, &ctx->field_buf, &ctx->field_bytes, n * sizeof(float));
-  if (s) return s;
-  s = gcm_field_csg(ctx, d_prims, n_prims, frame, grid->nx, grid->ny, grid->nz, ctx->field_buf, stream);
-  if (s) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   gcm_counts* used = nullptr;
-  s = mesh_core(ctx, ctx->field_buf, nullptr, grid, iso, 0, 0, kMeshPlain, 0, true, d_pos, d_norm, capacity, nullptr, st, &used,
-                true);
+  gcm_status s = mesh_csg(ctx, d_prims, n_prims, frame, grid, iso, d_pos, d_norm, capacity, nullptr, st, &used);
   if (s) return s;
   return read_counts(ctx, used, h_counts, st);
+}
+
+gcm_status gcm_mesh_csg_async(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
+                              const gcm_grid* grid, float iso, float* d_pos, float* d_norm, uint64_t capacity,
+                              gcm_counts* d_counts, gcm_stream stream) {
+  if (!ctx) return GCM_ERR_INVALID_ARGUMENT;
+  if (!d_counts || (capacity && (!d_pos || !d_norm)))
+    return fail(ctx, GCM_ERR_INVALID_ARGUMENT, "gcm_mesh_csg_async: NULL counts or outputs");
+  return mesh_csg(ctx, d_prims, n_prims, frame, grid, iso, d_pos, d_norm, capacity, d_counts,
+                  static_cast<cudaStream_t>(stream), nullptr);
 }
 
 gcm_status gcm_normalise_band(gcm_ctx* ctx, const float* d_field, uint32_t nx, uint32_t ny, uint32_t nz, float lo,

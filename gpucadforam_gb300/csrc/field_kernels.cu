@@ -1381,8 +1381,9 @@ __device__ __forceinline__ float warp_max(float v) {
 // tile, from their enclosures lu[] (x = L, y = U).  run_end[i] is the end of
 // the run of equal operations starting at i.  Returns the count; the indices
 // go to list[].
+// flo_out, fhi_out: an enclosure of the folded field over the tile.
 __device__ uint32_t csg_cull_warp(const PrimPre* pre, const uint16_t* run_end, const float2* lu, uint32_t n,
-                                  uint8_t* list, uint32_t lane) {
+                                  uint8_t* list, uint32_t lane, float& flo_out, float& fhi_out) {
   float flo = INFINITY, fhi = INFINITY;  // the running field starts at +inf
   uint32_t cnt = 0;
   const uint32_t below = (1u << lane) - 1u;
@@ -1428,11 +1429,13 @@ __device__ uint32_t csg_cull_warp(const PrimPre* pre, const uint16_t* run_end, c
     i = j;
   }
   __syncwarp();
+  flo_out = flo;
+  fhi_out = fhi;
   return cnt;
 }
 
 // A warp's tile: 32 samples along x (one per lane) by 8 rows (y) by 8 planes (z).
-constexpr uint32_t kCsgTx = 32, kCsgTy = 8, kCsgTz = 8, kCsgWarps = 8;
+constexpr uint32_t kCsgTx = GCM_CSG_TILE_X, kCsgTy = GCM_CSG_TILE_Y, kCsgTz = GCM_CSG_TILE_Z, kCsgWarps = 8;
 
 __device__ __forceinline__ float csg_coord(uint32_t i, float o, float s) { return fm(fs((float)i, o), s); }
 
@@ -1518,7 +1521,11 @@ __global__ void __launch_bounds__(kCsgWarps * 32, 4) csg_kernel(CsgParams p) {
       }
     }
     __syncwarp();
-    const uint32_t cnt = csg_cull_warp(s_pre, s_run, lu, n, list, lane);
+    float flo, fhi;
+    const uint32_t cnt = csg_cull_warp(s_pre, s_run, lu, n, list, lane, flo, fhi);
+    // every sample of the tile lies in [flo, fhi] (NaN bounds compare false: mixed)
+    if (p.tile_state && lane == 0)
+      p.tile_state[t] = fhi < p.iso ? kTileInside : (flo >= p.iso ? kTileOutside : kTileMixed);
     const uint32_t px = x0 + lane;
     // sample offsets index - origin; the primitives form their positions
     const float tX = fs((float)px, p.origin[0]);

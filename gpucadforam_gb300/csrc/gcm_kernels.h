@@ -197,13 +197,29 @@ inline uint32_t batch_group_rows(uint32_t cx) {
   return r > 8 ? 8 : r;
 }
 
+// Sample tile of one warp of the CSG field kernel: 32 along x, 8 rows, 8 planes.
+#define GCM_CSG_TILE_X 32
+#define GCM_CSG_TILE_Y 8
+#define GCM_CSG_TILE_Z 8
+// Per-tile state the CSG field kernel can record for the extraction: whether
+// every sample of the tile is inside (f < iso), outside, or unknown.
+enum : uint8_t { kTileMixed = 0, kTileInside = 1, kTileOutside = 2 };
+
 struct CsgParams {
   const gcm_primitive* prims;
   uint32_t n;
   float origin[3], spacing[3];
   uint32_t nx, ny, nz;
   float* out;
-  uint32_t exact;  // GCM_PRIM_ARITH_REFERENCE: the reference's powf squares, bit for bit
+  uint32_t exact;        // GCM_PRIM_ARITH_REFERENCE: the reference's powf squares, bit for bit
+  uint8_t* tile_state;   // optional: one kTile* per sample tile, tile index bx + tx * (by + ty * bz)
+  float iso;             // the isovalue tile_state is judged against
+};
+
+// Tile states for the window count kernel (null state: none).
+struct TileStates {
+  const uint8_t* state;
+  uint32_t tx, ty;  // tiles along x and y
 };
 
 // Launch wrappers (each kernel is launched from the file that defines it).
@@ -224,7 +240,7 @@ cudaError_t launch_generate(bool band, const GenerateParams& p, uint32_t blocks,
 cudaError_t launch_scan(const ScanParams& p, uint32_t blocks, cudaStream_t st);
 // Sparse path: window counts (win_tris may be null: counts only), then emission.
 cudaError_t launch_window_count(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, float iso, uint32_t* win_tris,
-                                gcm_counts* counts, uint32_t blocks, cudaStream_t st);
+                                gcm_counts* counts, uint32_t blocks, cudaStream_t st, TileStates tiles = {});
 cudaError_t launch_window_emit(const WindowEmitParams& p, uint32_t blocks, cudaStream_t st);
 cudaError_t launch_lookback_stall(uint32_t ntiles, uint32_t stall, uint64_t wait_ns, uint64_t* tile_status,
                                   uint32_t* counter, uint64_t* prefix_out, uint32_t* status, uint32_t blocks,

@@ -955,7 +955,7 @@ constexpr uint32_t kCountRows = 8;
 template <bool WRITE>
 __global__ void __launch_bounds__(256) mc_window_count_kernel(const float* __restrict__ f, uint32_t nx, uint32_t ny,
                                                               uint32_t nz, float iso, uint32_t* __restrict__ win_tris,
-                                                              gcm_counts* counts) {
+                                                              gcm_counts* counts, TileStates tiles) {
   __shared__ uint64_t s_tri[256];
   load_tri_table_counted(s_tri);
   __syncthreads();
@@ -979,11 +979,27 @@ __global__ void __launch_bounds__(256) mc_window_count_kernel(const float* __res
     const uint32_t x = wx * kWinVox + lane;
     const bool has = x <= vx, voxel = lane < kWinVox && x < vx;
     const float* p0 = f + (uint64_t)y0 * sy + (uint64_t)z * sz + x;
+    // With tile states from the field kernel: the task's samples (columns
+    // 31 wx .. 31 wx + 31, lines y0 .. y0 + nr, planes z and z + 1) lie in at
+    // most 2 x 2 x 2 tiles; if all of them are inside, or all outside, every
+    // cube index is 0 or 255 and the samples need not be read.
+    bool known = false;
+    if (tiles.state) {
+      const uint32_t xs = wx * kWinVox, xe = min(xs + kWinVox, vx);
+      const uint32_t bx = (lane & 1u) ? xe / GCM_CSG_TILE_X : xs / GCM_CSG_TILE_X;
+      const uint32_t by = (lane & 2u) ? (y0 + nr) / GCM_CSG_TILE_Y : y0 / GCM_CSG_TILE_Y;
+      const uint32_t bz = (lane & 4u) ? (z + 1) / GCM_CSG_TILE_Z : z / GCM_CSG_TILE_Z;
+      const uint32_t st = __ldg(tiles.state + bx + (uint64_t)tiles.tx * (by + (uint64_t)tiles.ty * bz));
+      // both collectives run on every lane; only then are their results combined
+      const uint32_t st0 = __shfl_sync(0xffffffffu, st, 0);
+      const bool same = __all_sync(0xffffffffu, st == st0);
+      known = same && st0 != kTileMixed;
+    }
     uint32_t line[kCountRows + 1];  // bit 0: plane z, bit 2: plane z + 1
 #pragma unroll
     for (uint32_t i = 0; i <= kCountRows; ++i) {
       float a = 0.0f, b = 0.0f;
-      if (i <= nr && has) {
+      if (!known && i <= nr && has) {
         a = __ldg(p0 + i * sy);
         b = __ldg(p0 + i * sy + sz);
       }
@@ -998,7 +1014,8 @@ __global__ void __launch_bounds__(256) mc_window_count_kernel(const float* __res
       lor |= line[i];
       land &= line[i];
     }
-    const bool mixed = __ballot_sync(0xffffffffu, lor != 0u) != 0u && __ballot_sync(0xffffffffu, land != 5u) != 0u;
+    const bool mixed = !known && __ballot_sync(0xffffffffu, lor != 0u) != 0u &&
+                       __ballot_sync(0xffffffffu, land != 5u) != 0u;
 #pragma unroll
     for (uint32_t i = 0; i < kCountRows; ++i) nt[i] = 0;
     if (mixed) {
@@ -1160,9 +1177,9 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 8) mc_window_emit_kernel(Wind
 }
 
 cudaError_t launch_window_count(const float* f, uint32_t nx, uint32_t ny, uint32_t nz, float iso, uint32_t* win_tris,
-                                gcm_counts* counts, uint32_t blocks, cudaStream_t st) {
-  if (win_tris) mc_window_count_kernel<true><<<blocks, 256, 0, st>>>(f, nx, ny, nz, iso, win_tris, counts);
-  else mc_window_count_kernel<false><<<blocks, 256, 0, st>>>(f, nx, ny, nz, iso, nullptr, counts);
+                                gcm_counts* counts, uint32_t blocks, cudaStream_t st, TileStates tiles) {
+  if (win_tris) mc_window_count_kernel<true><<<blocks, 256, 0, st>>>(f, nx, ny, nz, iso, win_tris, counts, tiles);
+  else mc_window_count_kernel<false><<<blocks, 256, 0, st>>>(f, nx, ny, nz, iso, nullptr, counts, tiles);
   return cudaGetLastError();
 }
 

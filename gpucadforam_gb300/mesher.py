@@ -335,6 +335,14 @@ class Context:
         n = int(c.total_verts)
         return pos[:n], norm[:n], Counts(c.active_voxels, c.total_verts, c.status)
 
+    def mesh_csg_async(self, prims_dev, n_prims, frame, shape_zyx, iso, pos, norm, d_counts, voxel_size=(1, 1, 1),
+                       grid_center=(0, 0, 0), stream=None):
+        """gcm_mesh_csg_async: counts into the int64[4] device tensor d_counts."""
+        g = make_grid(shape_zyx, voxel_size, grid_center)
+        self.check(self.lib.gcm_mesh_csg_async(self.h, _ptr(prims_dev), n_prims, C.byref(frame), C.byref(g), float(iso),
+                                               _ptr(pos), _ptr(norm), int(pos.shape[0]), _ptr(d_counts),
+                                               _stream(stream)))
+
     def mesh_csg(self, prims_dev, n_prims, frame, shape_zyx, iso, voxel_size=(1, 1, 1), grid_center=(0, 0, 0),
                  pos=None, norm=None, stream=None, allow_overflow=False):
         g = make_grid(shape_zyx, voxel_size, grid_center)

@@ -277,9 +277,20 @@ gcm_status gcm_ctx_set_primitive_arith(gcm_ctx* ctx, gcm_prim_arith arith);
  * subtract = max(f, -g), intersect = max(f, g).  d_prims is a device array. */
 gcm_status gcm_field_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
                          uint32_t nx, uint32_t ny, uint32_t nz, float* d_out, gcm_stream stream);
+/* Field + extraction of a CSG scene in one call (the context keeps the field).
+ * The field kernel records, per 32 x 8 x 8 sample tile, whether an enclosure
+ * of the folded field lies wholly below or above iso; the windowed extraction
+ * (the default for CSG, GCM_MESH_PATH_AUTO) then reads only the samples of
+ * tiles that can hold the surface.  The same vertices as gcm_field_csg
+ * followed by gcm_mesh_field. */
 gcm_status gcm_mesh_csg(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
                         const gcm_grid* grid, float iso, float* d_pos, float* d_norm, uint64_t capacity_verts,
                         gcm_counts* h_counts, gcm_stream stream);
+/* The same with the counts written to device memory, without a host
+ * synchronisation. */
+gcm_status gcm_mesh_csg_async(gcm_ctx* ctx, const gcm_primitive* d_prims, uint32_t n_prims, const gcm_frame* frame,
+                              const gcm_grid* grid, float iso, float* d_pos, float* d_norm, uint64_t capacity_verts,
+                              gcm_counts* d_counts, gcm_stream stream);
 
 /* ------------------------------------------------- retained CSG accumulation */
 

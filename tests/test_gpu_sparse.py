@@ -92,3 +92,50 @@ def test_sparse_overflow_like_fused(ctxs, short):
     assert ca.total_verts == cb.total_verts == total and ca.status == cb.status != 0
     assert torch.equal(pa.view(torch.int32), pb.view(torch.int32))
     assert torch.equal(na.view(torch.int32), nb.view(torch.int32))
+
+
+@pytest.mark.parametrize("seed,n_prims,shape,spacing,iso", [
+    (31, 40, (70, 45, 97), 1.0 / 64, 0.0),      # ragged: partial tiles on every axis
+    (32, 64, (64, 64, 64), -1.0 / 63, 0.0),     # mirrored frame
+    (33, 24, (9, 130, 33), 1.0 / 100, 0.02),    # thin grid, an isovalue above 0
+    (34, 48, (50, 40, 60), 1.0 / 55, -0.03),    # an isovalue below 0
+])
+def test_csg_tile_states_change_nothing(ctxs, seed, n_prims, shape, spacing, iso):
+    """gcm_mesh_csg records per sample tile whether the folded field's
+    enclosure lies wholly below or above iso, and its count pass skips tasks
+    whose tiles all agree.  Every primitive kind, subtract and intersect runs,
+    mirrored frames and isovalues off zero: the same mesh as the field meshed
+    on the fused path, and gcm_mesh_csg_async the same as gcm_mesh_csg."""
+    from gpucadforam_gb300.mesher import Context, make_frame, primitives_to_device
+    from tests.test_gpu_csg_cull import _scene
+
+    fused, _ = ctxs
+    prims = _scene(seed, n_prims)
+    for i in range(min(4, n_prims)):
+        prims[i]["op"] = 2 if i % 2 else 1  # leading subtract and intersect runs
+    nz, ny, nx = shape
+    origin = (0.0, 0.0, 0.0) if spacing > 0 else tuple(float(v) for v in (nx, ny, nz))
+    frame = make_frame(origin, (spacing,) * 3)
+    d_prims = primitives_to_device(prims)
+    vs = (abs(spacing),) * 3
+    field = fused.csg_field(d_prims, len(prims), frame, shape)
+    ref = fused.mesh_field(field, iso, vs, (0, 0, 0))
+    auto = Context(0)
+    try:
+        pos = torch.empty((max(ref[2].total_verts, 1), 4), device="cuda")
+        norm = torch.empty_like(pos)
+        cnt = auto.mesh_csg(d_prims, len(prims), frame, shape, iso, vs, (0, 0, 0), pos=pos, norm=norm)
+        assert cnt.total_verts == ref[2].total_verts and cnt.active_voxels == ref[2].active_voxels
+        k = cnt.total_verts
+        assert torch.equal(pos[:k].view(torch.int32), ref[0].view(torch.int32))
+        assert torch.equal(norm[:k].view(torch.int32), ref[1].view(torch.int32))
+        pos2 = torch.full_like(pos, -5.0)
+        norm2 = torch.full_like(norm, -5.0)
+        d_counts = torch.zeros(4, dtype=torch.int64, device="cuda")
+        auto.mesh_csg_async(d_prims, len(prims), frame, shape, iso, pos2, norm2, d_counts, vs, (0, 0, 0))
+        torch.cuda.synchronize()
+        c = d_counts.cpu().numpy().view(np.uint64)
+        assert int(c[1]) == k and int(c[0]) == cnt.active_voxels
+        assert torch.equal(pos2[:k], pos[:k]) and torch.equal(norm2[:k], norm[:k])
+    finally:
+        auto.close()
