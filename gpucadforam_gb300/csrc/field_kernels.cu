@@ -441,6 +441,9 @@ __global__ void __launch_bounds__(256) lattice_prep_kernel(LatticeParams p, floa
 constexpr uint32_t kBlendCx = 128;        // control columns staged per row (BLEND)
 constexpr uint32_t kRowWarps = 8;         // warps per CTA of lattice_rows_kernel
 constexpr size_t kRowSmem = 48 * 1024;    // shared memory of one such CTA, at most
+// control grids too wide for that: one row per warp in opt-in shared memory,
+// up to this much per CTA (about 250 control columns)
+constexpr size_t kRowSmemWide = 160 * 1024;
 constexpr uint32_t kRecWords = 5;         // 16-byte words of one cell record
 
 // Cells of a row: cx - 1 (one for a single control column).
@@ -1726,23 +1729,36 @@ cudaError_t launch_unit_cell(uint32_t type, uint32_t nx, uint32_t ny, uint32_t n
 }
 
 // Rows per warp for lattice_rows_kernel: the most of {8, 4, 2, 1} whose slices
-// fit kRowSmem and that still leave 32 warps of row groups per SM; 0 when not
-// even one row's slice fits (the unstaged kernel then runs).
+// fit kRowSmem and that still leave 32 warps of row groups per SM; 1 when one
+// row's slices fit kRowSmemWide (opt-in shared memory); 0 when not even that
+// (the unstaged kernel then runs).
 uint32_t lattice_rows_per_warp(uint32_t cx, uint32_t rows, uint32_t sm_count) {
   for (uint32_t R = 8; R >= 1; R /= 2) {
     if (row_smem_bytes(R, cx) > kRowSmem) continue;
     if (R == 1 || (uint64_t)(rows + R - 1) / R >= (uint64_t)sm_count * 32) return R;
   }
+  if (row_smem_bytes(1, cx) <= kRowSmemWide) return 1;  // a wide control grid, opt-in shared memory
   return 0;
 }
 
 template <uint32_t R>
-static void launch_rows(const LatticeParams& p, cudaStream_t st) {
+static cudaError_t launch_rows(const LatticeParams& p, cudaStream_t st) {
   const uint64_t groups = ((uint64_t)p.ny * p.nz + R - 1) / R;
   // at most 2^26 CTAs, so the kernel's 32-bit warp stride cannot wrap (the
   // group loop covers the rest)
   const uint32_t blocks = (uint32_t)std::min<uint64_t>((groups + kRowWarps - 1) / kRowWarps, 1u << 26);
-  lattice_rows_kernel<R><<<blocks, kRowWarps * 32, row_smem_bytes(R, p.cx), st>>>(p);
+  const size_t smem = row_smem_bytes(R, p.cx);
+  if (smem > kRowSmem) {
+    // every caller sets the same value (the kernel's full opt-in limit)
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(lattice_rows_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e != cudaSuccess) return e;
+  }
+  lattice_rows_kernel<R><<<blocks, kRowWarps * 32, smem, st>>>(p);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t prep_blocks, uint32_t blocks,
@@ -1763,10 +1779,10 @@ cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t pr
     }
   } else {
     switch (lattice_rows_per_warp(p.cx, p.ny * p.nz, sm_count)) {
-      case 8: launch_rows<8>(p, st); break;
-      case 4: launch_rows<4>(p, st); break;
-      case 2: launch_rows<2>(p, st); break;
-      case 1: launch_rows<1>(p, st); break;
+      case 8: return launch_rows<8>(p, st);
+      case 4: return launch_rows<4>(p, st);
+      case 2: return launch_rows<2>(p, st);
+      case 1: return launch_rows<1>(p, st);
       default: lattice_params_kernel<<<blocks, 256, 0, st>>>(p);
     }
   }

@@ -9,7 +9,9 @@ Cases (the kernel each one launches ``reps`` times after one warm-up call):
 * ``lattice_rows``   lattice_rows_kernel: the graded TPMS lattice of a 16^3
                      control grid (periods U[16, 64], Euler angles U[-pi/4, pi/4],
                      thickness U[-0.6, 0.6], types gyroid/diamond/Schwarz-P);
-* ``lattice_params`` lattice_params_kernel: the same with a 96 x 8 x 8 control
+* ``lattice_wide``   lattice_rows_kernel with one row per warp in opt-in shared
+                     memory: the same with a 96 x 8 x 8 control grid;
+* ``lattice_params`` lattice_params_kernel: the same with a 320 x 4 x 4 control
                      grid, wider than the row kernel stages;
 * ``lattice_blend``  lattice_prep_kernel + lattice_blend_kernel: the 16^3 grid
                      in the blend grading;
@@ -55,7 +57,8 @@ def _timed(fn, reps):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["unit_cell", "lattice_rows", "lattice_params", "lattice_blend", "staged_mc"])
+    ap.add_argument("case", choices=["unit_cell", "lattice_rows", "lattice_wide", "lattice_params", "lattice_blend",
+                                     "staged_mc"])
     ap.add_argument("--n", type=int, default=320)
     ap.add_argument("--reps", type=int, default=3)
     args = ap.parse_args(argv)
@@ -76,9 +79,9 @@ def main(argv=None):
 
     if args.case == "unit_cell":
         info["ms"] = _timed(lambda: ctx.unit_cell(0, n, n, n), args.reps)
-    elif args.case in ("lattice_rows", "lattice_params", "lattice_blend"):
-        lat = lattice(1 if args.case == "lattice_blend" else 0, (96, 8, 8) if args.case == "lattice_params" else
-                      (16, 16, 16))
+    elif args.case in ("lattice_rows", "lattice_wide", "lattice_params", "lattice_blend"):
+        ctrl = {"lattice_wide": (96, 8, 8), "lattice_params": (min(320, n), 4, 4)}.get(args.case, (16, 16, 16))
+        lat = lattice(1 if args.case == "lattice_blend" else 0, ctrl)
         out = torch.empty(shape, dtype=torch.float32, device="cuda")
         s = ctx.lattice_struct(lat)
         import ctypes as C

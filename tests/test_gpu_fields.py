@@ -174,7 +174,8 @@ def test_blend_lattice_kernel_forms_vs_oracle(ctx, shape, ctrl):
     ((110, 110, 70), (16, 16, 16)),   # 12,100 rows: 2 per warp; rows of 70 end on a single-sample step
     ((40, 40, 100), (16, 16, 16)),    # 1,600 rows: 1 per warp; a ragged second segment
     ((24, 20, 300), (64, 4, 4)),      # 64 control columns: one row's records per warp fit
-    ((12, 10, 500), (200, 3, 3)),     # 200 control columns: the unstaged kernel
+    ((12, 10, 500), (200, 3, 3)),     # 200 control columns: one row per warp in opt-in shared memory
+    ((6, 5, 700), (300, 2, 2)),       # 300 control columns: the unstaged kernel
 ])
 def test_graded_lattice_kernel_forms_vs_oracle(ctx, shape, ctrl):
     """Each staged form of the PARAMS field kernel (rows per warp picked from

@@ -7,7 +7,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("case", ["unit_cell", "lattice_rows", "lattice_params", "lattice_blend", "staged_mc"])
+@pytest.mark.parametrize("case", ["unit_cell", "lattice_rows", "lattice_wide", "lattice_params", "lattice_blend",
+                                  "staged_mc"])
 def test_kernel_case_runs(case, capsys):
     from gpucadforam_gb300 import kernel_cases
 
