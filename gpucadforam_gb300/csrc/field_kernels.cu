@@ -779,9 +779,11 @@ __global__ void __launch_bounds__(256) lattice_blend_kernel(LatticeParams p) {
 
 // BLEND mode, warp per sample row: each warp stages its row's records in its
 // own slice of shared memory (warp syncs only, no CTA barrier) for control
-// grids up to kBlendWarpCx columns.  Same values as lattice_blend_kernel.
+// grids up to kBlendWarpCxWide columns (opt-in shared memory above
+// kBlendWarpCx).  Same values as lattice_blend_kernel.
 constexpr uint32_t kBlendWarps = 8;
-constexpr uint32_t kBlendWarpCx = 24;  // 8 warps x 4 corner rows x 24 columns x 64 B = 48 KB
+constexpr uint32_t kBlendWarpCx = 24;      // 8 warps x 4 corner rows x 24 columns x 64 B = 48 KB
+constexpr uint32_t kBlendWarpCxWide = 80;  // the same in opt-in shared memory: 160 KB
 
 __global__ void __launch_bounds__(kBlendWarps * 32) lattice_blend_warp_kernel(LatticeParams p) {
   extern __shared__ float4 s_blend[];
@@ -1769,11 +1771,21 @@ cudaError_t launch_lattice(const LatticeParams& p, float* blend_buf, uint32_t pr
     if (e != cudaSuccess) return e;
     LatticeParams q = p;
     q.blend = blend_buf;
-    if (p.cx <= kBlendWarpCx) {
+    if (p.cx <= kBlendWarpCxWide) {
       // a sample row per warp; many CTAs, so the block scheduler balances the SMs
       const uint64_t rows = (uint64_t)p.ny * p.nz;
       const uint32_t wblocks = (uint32_t)std::min<uint64_t>((rows + kBlendWarps - 1) / kBlendWarps, 1u << 26);
-      lattice_blend_warp_kernel<<<wblocks, kBlendWarps * 32, (size_t)kBlendWarps * 4 * p.cx * 4 * sizeof(float4), st>>>(q);
+      const size_t smem = (size_t)kBlendWarps * 4 * p.cx * 4 * sizeof(float4);
+      if (p.cx > kBlendWarpCx) {
+        // every caller sets the same value (the kernel's full opt-in limit)
+        int dev = 0, optin = 0;
+        e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (e == cudaSuccess)
+          e = cudaFuncSetAttribute(lattice_blend_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        if (e != cudaSuccess) return e;
+      }
+      lattice_blend_warp_kernel<<<wblocks, kBlendWarps * 32, smem, st>>>(q);
     } else {
       lattice_blend_kernel<<<blocks, 256, 0, st>>>(q);
     }

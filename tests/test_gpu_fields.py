@@ -142,14 +142,17 @@ def test_graded_lattice_vs_oracle(ctx, mode, shape):
 @pytest.mark.parametrize("shape,ctrl", [
     ((20, 18, 40), (1, 1, 1)),        # one control point: a single lattice
     ((30, 26, 61), (3, 2, 5)),        # warp per row, few columns
-    ((24, 20, 100), (24, 4, 4)),      # warp per row at its widest (24 columns)
-    ((20, 16, 90), (25, 3, 3)),       # CTA per row, records staged by the CTA
+    ((24, 20, 100), (24, 4, 4)),      # warp per row, widest in the default shared memory (24 columns)
+    ((20, 16, 90), (25, 3, 3)),       # warp per row in opt-in shared memory
+    ((12, 10, 120), (80, 2, 2)),      # warp per row at its widest (80 columns)
+    ((10, 8, 140), (81, 2, 2)),       # CTA per row, records staged by the CTA
     ((10, 8, 300), (140, 2, 2)),      # CTA per row, records read from the setup buffer
 ])
 def test_blend_lattice_kernel_forms_vs_oracle(ctx, shape, ctrl):
-    """The blend grading runs as a warp per sample row (control grids up to 24
-    columns) or a CTA per row (staged up to 128 columns, else unstaged); every
-    form equals the oracle bit for bit and the FP64 oracle within 1e-5."""
+    """The blend grading runs as a warp per sample row (control grids up to 80
+    columns, above 24 in opt-in shared memory) or a CTA per row (staged up to
+    128 columns, else unstaged); every form equals the oracle bit for bit and
+    the FP64 oracle within 1e-5."""
     from gpucadforam_gb300.mesher import Lattice
 
     nz, ny, nx = shape
