@@ -920,21 +920,25 @@ __device__ __forceinline__ uint32_t cube_from_columns(uint32_t m, uint32_t n) {
   return (m & 1u) | ((m & 6u) << 2) | ((m & 8u) << 4) | ((n & 3u) << 1) | ((n & 12u) << 3);
 }
 
-// One window batch of a row, classified: each lane's column samples and its
-// voxel's cube index (0 for lane 31 and past the row's end).
+// One window batch, classified: each lane's column samples and its voxel's
+// cube index per window.
 struct WindowBatch {
   float4 col[kWinBatch];
   uint32_t ci[kWinBatch];
 };
 
-__device__ __forceinline__ void classify_batch(const float* __restrict__ f, uint64_t rb, const uint32_t* wx, uint32_t nb,
-                                               uint32_t vx, uint64_t sy, uint64_t sz, float iso, uint32_t lane,
-                                               WindowBatch& B) {
+
+// One window batch, classified: window k of voxel row rbk[k] (its first
+// sample), each lane's column samples and its voxel's cube index (0 for lane
+// 31 and past the row's end).
+__device__ __forceinline__ void classify_batch(const float* __restrict__ f, const uint64_t* rbk,
+                                                    const uint32_t* wx, uint32_t nb, uint32_t vx, uint64_t sy,
+                                                    uint64_t sz, float iso, uint32_t lane, WindowBatch& B) {
 #pragma unroll
   for (uint32_t k = 0; k < kWinBatch; ++k) {
     B.col[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const uint32_t x = wx[k] * kWinVox + lane;
-    if (k < nb && x <= vx) B.col[k] = load_column(f, rb, x, sy, sz);
+    if (k < nb && x <= vx) B.col[k] = load_column(f, rbk[k], x, sy, sz);
   }
 #pragma unroll
   for (uint32_t k = 0; k < kWinBatch; ++k) {
@@ -1080,39 +1084,65 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 8) mc_window_emit_kernel(Wind
   const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
   const Frame fr{{p.vs[0], p.vs[1], p.vs[2]}, {p.gc[0], p.gc[1], p.gc[2]}};
   bool dropped = false;
-  // row = y + vy * z, stepped by `warps` without divisions in the loop
+  // The warp's stream of windows that hold triangles: its voxel rows
+  // row = y + vy * z (stepped by `warps` without divisions), in each row the
+  // groups of 32 windows, in each group the windows whose count is not zero.
+  // A batch takes the next kWinBatch windows of the stream, across rows, so
+  // that rows with one or two such windows still fill the emission lanes.
   uint64_t row = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   uint32_t yy = (uint32_t)(row % vy);
   uint64_t zz = row / vy;
   const uint32_t dyy = (uint32_t)(warps % vy);
   const uint64_t dzz = warps / vy;
-  for (; row < rows; row += warps, yy += dyy, zz += dzz + (yy >= vy ? 1u : 0u), yy -= yy >= vy ? vy : 0u) {
-    const uint32_t y = yy, z = (uint32_t)zz;
-    const uint64_t rb = (uint64_t)y * sy + (uint64_t)z * sz;
-    VoxelCorners V;
-    axis_corners(y, fr.gc[1], fr.vs[1], V.y0, V.y1);
-    axis_corners(z, fr.gc[2], fr.vs[2], V.z0, V.z1);
-    for (uint32_t g0 = 0; g0 < nwx; g0 += 32u) {
-      const uint32_t wl = g0 + lane;
-      uint32_t todo = __ballot_sync(0xffffffffu, wl < nwx && __ldg(p.win_tris + row * nwx + wl) != 0u);
-      while (todo) {
-        // the next (up to) kWinBatch windows that hold triangles, all at once
-        uint32_t wx[kWinBatch];
-        uint32_t nb = 0;
+  uint32_t g0 = 0, todo = 0;  // the current group and its windows not yet taken (warp-uniform)
+  auto load_group = [&]() {
+    const uint32_t wl = g0 + lane;
+    todo = __ballot_sync(0xffffffffu, row < rows && wl < nwx && __ldg(p.win_tris + row * nwx + wl) != 0u);
+  };
+  auto next_group = [&]() {
+    g0 += 32u;
+    if (g0 >= nwx) {
+      g0 = 0;
+      row += warps;
+      yy += dyy;
+      const uint32_t carry = yy >= vy ? 1u : 0u;
+      zz += dzz + carry;
+      if (carry) yy -= vy;
+    }
+    load_group();
+  };
+  load_group();
+  while (true) {
+    // the next (up to) kWinBatch windows that hold triangles, all at once
+    uint32_t wx[kWinBatch], wy[kWinBatch], wz[kWinBatch];
+    uint64_t wrow[kWinBatch];
+    uint32_t nb = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kWinBatch; ++k) {
+      while (todo == 0u && row < rows) next_group();
+      wx[k] = 0;
+      wy[k] = 0;
+      wz[k] = 0;
+      wrow[k] = 0;
+      if (todo) {
+        wx[k] = g0 + (uint32_t)(__ffs(todo) - 1);
+        wy[k] = yy;
+        wz[k] = (uint32_t)zz;
+        wrow[k] = row;
+        todo &= todo - 1;
+        nb = k + 1;
+      }
+    }
+    if (nb == 0) break;  // the stream is exhausted
+    {
+        uint64_t off[kWinBatch], rbk[kWinBatch];
 #pragma unroll
         for (uint32_t k = 0; k < kWinBatch; ++k) {
-          wx[k] = 0;
-          if (todo) {
-            wx[k] = g0 + (uint32_t)(__ffs(todo) - 1);
-            todo &= todo - 1;
-            nb = k + 1;
-          }
+          off[k] = k < nb ? __ldg(p.win_off + wrow[k] * nwx + wx[k]) : 0ull;
+          rbk[k] = (uint64_t)wy[k] * sy + (uint64_t)wz[k] * sz;
         }
-        uint64_t off[kWinBatch];
-#pragma unroll
-        for (uint32_t k = 0; k < kWinBatch; ++k) off[k] = k < nb ? __ldg(p.win_off + row * nwx + wx[k]) : 0ull;
         WindowBatch B;
-        classify_batch(p.f, rb, wx, nb, vx, sy, sz, p.iso, lane, B);
+        classify_batch(p.f, rbk, wx, nb, vx, sy, sz, p.iso, lane, B);
         // list the batch's triangles; stage each active voxel's corners
         __syncwarp();  // the previous batch's entries are read
         uint32_t listed = 0;
@@ -1144,11 +1174,18 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 8) mc_window_emit_kernel(Wind
           const float4 ca = E.corner[slot][0], cb = E.corner[slot][1];
           const float c[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
           const uint64_t tri_row = s_tri[E.cube[slot]];
-          uint32_t wxk = wx[0];
+          uint32_t wxk = wx[0], wyk = wy[0], wzk = wz[0];
 #pragma unroll
-          for (uint32_t q = 1; q < kWinBatch; ++q) wxk = (k == q) ? wx[q] : wxk;
+          for (uint32_t q = 1; q < kWinBatch; ++q) {
+            wxk = (k == q) ? wx[q] : wxk;
+            wyk = (k == q) ? wy[q] : wyk;
+            wzk = (k == q) ? wz[q] : wzk;
+          }
           const uint32_t x = wxk * kWinVox + l;
+          VoxelCorners V;
           axis_corners(x, fr.gc[0], fr.vs[0], V.x0, V.x1);
+          axis_corners(wyk, fr.gc[1], fr.vs[1], V.y0, V.y1);
+          axis_corners(wzk, fr.gc[2], fr.vs[2], V.z0, V.z1);
           float3 v[3];
 #pragma unroll
           for (int m = 0; m < 3; ++m) {
@@ -1170,7 +1207,6 @@ __global__ void __launch_bounds__(kEmitWarps * 32, 8) mc_window_emit_kernel(Wind
             __stcs(p.norm + idx + m, make_float4(n.x, n.y, n.z, 0.0f));
           }
         }
-      }
     }
   }
   if (dropped) set_status(p.status, kStatusOverflow);
