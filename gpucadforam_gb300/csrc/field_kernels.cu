@@ -557,7 +557,7 @@ __device__ __forceinline__ float params_sample(const float* const arr[5], const 
 
 // CTAs per SM the register budget of lattice_rows_kernel is sized for.
 #ifndef GCM_LATTICE_ROWS_MIN_CTAS
-#define GCM_LATTICE_ROWS_MIN_CTAS 4
+#define GCM_LATTICE_ROWS_MIN_CTAS 5
 #endif
 
 template <uint32_t R>
