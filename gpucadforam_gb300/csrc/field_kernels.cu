@@ -785,7 +785,7 @@ constexpr uint32_t kBlendWarps = 8;
 constexpr uint32_t kBlendWarpCx = 24;      // 8 warps x 4 corner rows x 24 columns x 64 B = 48 KB
 constexpr uint32_t kBlendWarpCxWide = 80;  // the same in opt-in shared memory: 160 KB
 
-__global__ void __launch_bounds__(kBlendWarps * 32) lattice_blend_warp_kernel(LatticeParams p) {
+__global__ void __launch_bounds__(kBlendWarps * 32, 6) lattice_blend_warp_kernel(LatticeParams p) {
   extern __shared__ float4 s_blend[];
   const uint32_t c[3] = {p.cx, p.cy, p.cz};
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -820,7 +820,7 @@ constexpr uint32_t kGroupRows = 8;                // rows of a group, at most
 // STAGED: the groups of instances with at most kWarpCx control columns (the
 // other groups are skipped); the other form takes the wider ones, a row each.
 template <bool STAGED>
-__global__ void __launch_bounds__(256, 4) lattice_params_batch_kernel(const BatchLattice* inst, uint32_t n_inst,
+__global__ void __launch_bounds__(256, 5) lattice_params_batch_kernel(const BatchLattice* inst, uint32_t n_inst,
                                                                    uint64_t total_groups) {
   __shared__ float4 s_rec[8][kRecWords * kWarpCx];  // per warp: the group's cell records
   __shared__ float2 s_q[8][kGroupRows];             // per warp: the (y, z) phase coordinates of each row
