@@ -800,7 +800,7 @@ __device__ __forceinline__ uint64_t warp_inclusive_u64(uint64_t x, uint32_t lane
 // holds elements 4l .. 4l + 3 of a round (one 16-byte load and store when
 // VEC: both arrays 16-byte aligned), so every access is coalesced.
 template <bool VEC>
-__global__ void __launch_bounds__(kScanThreads, 4) scan_u32_kernel(ScanParams p) {
+__global__ void __launch_bounds__(kScanThreads, 6) scan_u32_kernel(ScanParams p) {
   __shared__ uint32_t sh_tile;
   __shared__ uint64_t sh_warp[kScanThreads / 32];
   __shared__ uint64_t sh_prefix;
